@@ -1,0 +1,322 @@
+#!/usr/bin/env python3
+"""Benchmark of the GB300 concrete-fft hot path.
+
+Headline workload: negacyclic u64 polynomial products, N = 2048 (folded to a
+1024-point c64 unordered FFT), 8192 products per launch, A uniform u64, B
+signed digits uniform in [-2^7, 2^7) pre-transformed and resident on the
+device (one operand per product).  One step = one launch over 8192 products.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
+
+--impl reference times the reference's algorithm on the host cores (the CPU
+restatement under oracle/: the Rust crate cannot be built here) on the same
+workload, using every host thread.  Prints one JSON line.
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+PKG = os.path.join(ROOT, "concrete-fft_gb300")
+
+N_POLY = 2048
+COUNT = 8192
+BASE_SEED = 2  # the workload's index in the benchmark table
+BYTES_PER_PRODUCT = 3 * N_POLY * 8  # A + Bhat + out: 16 KiB each
+METRIC = "N=2048 negacyclic u64 polymul/s"
+
+
+def fp64_ops_per_transform(n, base_n, algo):
+    """FP64 instructions (DADD/DMUL/DFMA, one each) of one unordered transform
+    of n points with the given base, counted from the butterfly code."""
+    core = {2: 4, 4: 16, 8: 56, 16: 168}
+    ops = 0
+    m = n
+    while m > base_n:  # outer levels: core + (r-1) twiddle products of 4 ops
+        r = 2 if m == 2 * base_n else (4 if m == 4 * base_n else 8)
+        ops += (n // r) * (core[r] + 4 * (r - 1))
+        m //= r
+    R = 2 << (algo // 2)
+    rem, passes = base_n, 0
+    while rem > R:
+        rem //= R
+        passes += 1
+    ops += passes * (n // R) * (core[R] + 4 * (R - 1))
+    ops += (n // rem) * core[rem]
+    return ops
+
+
+def fp64_ops_per_product(N, base_n, algo):
+    n = N // 2
+    return 2 * fp64_ops_per_transform(n, base_n, algo) + 3 * 4 * n  # twist, pointwise, untwist
+
+
+class ClockSampler:
+    """nvidia-smi sampling during the timed region (SM clock, throttle reasons)."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.Q,
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except OSError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *exc):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx = float(f[2])
+            except ValueError:
+                continue
+            for name, v in zip(names, f[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(name)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": mx, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def measured_peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            return json.load(f), "measured"
+    except (OSError, ValueError):
+        return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0}, "fallback"
+
+
+def profiled_traffic(name):
+    """DRAM bytes per launch from a committed ncu summary (profiles/<name>.json), if any."""
+    try:
+        with open(os.path.join(ROOT, "profiles", name + ".json")) as f:
+            return json.load(f)
+    except (OSError, ValueError):
+        return None
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", str(rank)))
+    return rank, world, local
+
+
+def make_inputs(count, seed):
+    import numpy as np
+    rng = np.random.default_rng(seed)
+    a = rng.integers(0, 2 ** 64, (count, N_POLY), dtype=np.uint64)
+    b = rng.integers(-2 ** 7, 2 ** 7, (count, N_POLY), dtype=np.int64)
+    return a, b
+
+
+def cpu_product_rate(threads, seconds, seed):
+    """Products/s of the oracle's restatement of the reference pipeline on the host cores."""
+    for p in (os.path.join(ROOT, "oracle"),):
+        sys.path.insert(0, p)
+    import numpy as np
+    import pyoracle
+    sample = 256 if threads == 1 else max(256, 64 * threads)
+    a, b = make_inputs(sample, seed + 1000)
+    bhat = pyoracle.u64_prepare(N_POLY, 6, 1024, b)
+    pyoracle.u64_product(N_POLY, 6, 1024, a[:threads], bhat[:threads], nthreads=threads)  # warm
+    done, t0 = 0, time.perf_counter()
+    while True:
+        pyoracle.u64_product(N_POLY, 6, 1024, a, bhat, nthreads=threads)
+        done += sample
+        el = time.perf_counter() - t0
+        if el >= seconds:
+            break
+    return done / el, done, el
+
+
+def run_reference(args):
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return
+    threads = os.cpu_count() or 1
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import pyoracle
+    import numpy as np
+    sample = max(256, 32 * threads)
+    a, b = make_inputs(sample, BASE_SEED)
+    bhat = pyoracle.u64_prepare(N_POLY, 6, 1024, b)
+    for _ in range(args.warmup):
+        pyoracle.u64_product(N_POLY, 6, 1024, a[:threads], bhat[:threads], nthreads=threads)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        pyoracle.u64_product(N_POLY, 6, 1024, a, bhat, nthreads=threads)
+    el = time.perf_counter() - t0
+    value = args.steps * sample / el
+    print(json.dumps({
+        "impl": "reference", "metric": METRIC, "value": value, "unit": "products/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * el / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic (seeded numpy PCG64)",
+        "config": {"workload": "u64 negacyclic product N=2048, unordered Dif16 base 1024 (CPU)",
+                   "products_per_step": sample, "threads": threads},
+        "cpu_baseline": {"value": value, "unit": "products/s", "cores": threads, "kind": "port",
+                         "sample": "%d products per step of the N=2048 workload" % sample},
+        "e2e": {"value": value, "unit": "products/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }))
+
+
+def run_gb300(args):
+    import numpy as np
+    import torch
+    rank, world, local = dist_env()
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    sys.path.insert(0, PKG)
+    import concrete_fft as cf
+    lib = cf.load()
+    cf.check(lib.cfft_device_check())
+
+    plan = cf.product.U64ProductPlan(N_POLY, measure_seconds=0.002)
+    algo, base_n = plan.algo()
+    a_np, b_np = make_inputs(COUNT, BASE_SEED + rank)
+    a = torch.from_numpy(a_np.view(np.int64)).cuda()
+    b = torch.from_numpy(b_np).cuda()
+    bhat = torch.empty((COUNT, N_POLY // 2), dtype=torch.complex128, device="cuda")
+    plan.prepare_operand(b, bhat)
+    out = torch.empty_like(a)
+    stream = torch.cuda.current_stream()
+
+    def barrier():
+        torch.cuda.synchronize()
+        if world > 1:
+            torch.distributed.barrier()
+            torch.cuda.synchronize()
+
+    for _ in range(args.warmup):
+        plan.product(a, bhat, out)
+    barrier()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    with ClockSampler(local) as clk:
+        e0.record(stream)
+        for _ in range(args.steps):
+            plan.product(a, bhat, out)
+        e1.record(stream)
+        barrier()
+    ms = e0.elapsed_time(e1)
+    if world > 1:
+        t = torch.tensor([ms], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms = float(t.item())
+    per_launch_s = ms * 1e-3 / args.steps
+    value = world * COUNT * args.steps / (ms * 1e-3)
+
+    # end to end: pinned host A in, pinned host result out, through the C ABI host entry point
+    ha = torch.from_numpy(a_np.view(np.int64)).pin_memory()
+    hout = torch.empty_like(ha).pin_memory()
+    for _ in range(max(1, args.warmup // 2)):
+        plan.product(ha, bhat, hout)
+    barrier()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        plan.product(ha, bhat, hout)
+    e2e_s = time.perf_counter() - t0
+    if world > 1:
+        t = torch.tensor([e2e_s], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        e2e_s = float(t.item())
+    e2e = world * COUNT * args.steps / e2e_s
+    ok = bool(np.array_equal(hout.numpy(), out.cpu().numpy()))
+
+    peaks, peak_kind = measured_peaks()
+    achieved_gbs = BYTES_PER_PRODUCT * COUNT / per_launch_s / 1e9
+    traffic = profiled_traffic("u64_product_n2048")
+    import ctypes
+    r = ctypes.c_double()
+    cf.check(lib.cfft_diag_fp64_peak(ctypes.byref(r)))
+    fp64_peak = r.value
+    fp64_ops = fp64_ops_per_product(N_POLY, base_n, int(algo))
+    fp64_achieved = fp64_ops * COUNT / per_launch_s
+
+    if rank != 0:
+        return
+    cpu = None
+    if world == 1 and not args.no_cpu_baseline:
+        threads = os.cpu_count() or 1
+        rate, done, el = cpu_product_rate(threads, args.cpu_seconds, BASE_SEED)
+        cpu = {"value": rate, "unit": "products/s", "cores": threads, "kind": "port",
+               "sample": "%d products (N=2048) in %.1f s on %d host threads" % (done, el, threads)}
+    line = {
+        "metric": METRIC, "value": value, "unit": "products/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded numpy PCG64)",
+        "config": {"workload": "u64 negacyclic product N=2048 (1024-point unordered c64 FFT), 8192 products "
+                               "per launch, distinct resident Bhat per product",
+                   "base_algo": algo.name, "base_n": base_n, "products_per_step": COUNT,
+                   "l2": "inputs 384 MiB > L2 (no flush needed)", "parallelism": "replicas" if world > 1 else "1 GPU"},
+        "roofline": {"bound": "hbm", "achieved": achieved_gbs, "peak": peaks.get("hbm_gbs"), "unit": "GB/s",
+                     "frac": achieved_gbs / peaks.get("hbm_gbs"), "peak_kind": peak_kind,
+                     "traffic": traffic.get("dram_bytes_per_launch") if traffic else None,
+                     "algorithmic_bytes_per_launch": BYTES_PER_PRODUCT * COUNT,
+                     "fp64": {"achieved_ops_per_s": fp64_achieved, "peak_ops_per_s": fp64_peak,
+                              "frac": fp64_achieved / fp64_peak, "ops_per_product": fp64_ops,
+                              "note": "binding roof: FP64 pipe (DFMA/DADD/DMUL issue rate, measured live)"}},
+        "cpu_baseline": cpu,
+        "e2e": {"value": e2e, "unit": "products/s", "h2d_bytes_per_step": COUNT * N_POLY * 8,
+                "d2h_bytes_per_step": COUNT * N_POLY * 8, "matches_device_result": ok},
+        "clocks": clk.summary(),
+        "gpu_launches": args.steps,
+    }
+    print(json.dumps(line))
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
+    ap.add_argument("--cpu-seconds", type=float, default=5.0)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_gb300(args)
+
+
+if __name__ == "__main__":
+    main()

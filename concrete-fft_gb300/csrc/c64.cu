@@ -1,0 +1,585 @@
+// c64.cu -- ordered::Plan and unordered::Plan on the GPU (c64 transforms).
+//
+// Execution: transforms (or, above 4096 points, the sub-transforms below the
+// top unordered levels) are loaded into one CTA's shared memory, run through
+// the reference's passes there and written back; unordered levels of larger
+// transforms run in place in global memory first (forward) or last (inverse).
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <chrono>
+#include <cstring>
+#include <vector>
+
+#include "cfft_internal.h"
+#include "runtime.h"
+#include "stockham.cuh"
+
+using namespace cfft;
+
+namespace cfft {
+
+__global__ void __launch_bounds__(256) c64_smem_fwd_kernel(double2* data, int count, int tpc, DevLevels L, int d0,
+                                                           int base_algo, const double2* __restrict__ w) {
+  extern __shared__ double2 smem[];
+  const int log2sub = L.log2n[d0];
+  const long first = (long)blockIdx.x * tpc;
+  const int nch = (int)min((long)tpc, (long)count - first);
+  double2* x = smem;
+  double2* y = smem + ((long)tpc << log2sub);
+  double2* g = data + (first << log2sub);
+  const int npts = nch << log2sub;
+  const int tid = threadIdx.x, nth = blockDim.x;
+  for (int i = tid; i < npts; i += nth) x[i] = g[i];
+  __syncthreads();
+  const double2* r = unordered_smem<true>(L, d0, base_algo, nch, x, y, w, tid, nth);
+  for (int i = tid; i < npts; i += nth) g[i] = r[i];
+}
+
+__global__ void __launch_bounds__(256) c64_smem_inv_kernel(double2* data, int count, int tpc, DevLevels L, int d0,
+                                                           int base_algo, const double2* __restrict__ w) {
+  extern __shared__ double2 smem[];
+  const int log2sub = L.log2n[d0];
+  const long first = (long)blockIdx.x * tpc;
+  const int nch = (int)min((long)tpc, (long)count - first);
+  double2* x = smem;
+  double2* y = smem + ((long)tpc << log2sub);
+  double2* g = data + (first << log2sub);
+  const int npts = nch << log2sub;
+  const int tid = threadIdx.x, nth = blockDim.x;
+  for (int i = tid; i < npts; i += nth) x[i] = g[i];
+  __syncthreads();
+  const double2* r = unordered_smem<false>(L, d0, base_algo, nch, x, y, w, tid, nth);
+  for (int i = tid; i < npts; i += nth) g[i] = r[i];
+}
+
+// One unordered level in place in global memory, over every chunk of 2^log2nl points.
+template <bool FWD>
+__global__ void __launch_bounds__(256) c64_level_kernel(double2* data, long total, int log2r, int log2nl,
+                                                        const double2* __restrict__ wl) {
+  const int lm = log2nl - log2r;
+  for (long g = (long)blockIdx.x * blockDim.x + threadIdx.x; g < total; g += (long)gridDim.x * blockDim.x) {
+    double2* zc = data + ((g >> lm) << log2nl);
+    const int i = (int)(g & ((1L << lm) - 1));
+    if (log2r == 1) outer_group<2, FWD>(zc, lm, i, wl);
+    else if (log2r == 2) outer_group<4, FWD>(zc, lm, i, wl);
+    else outer_group<8, FWD>(zc, lm, i, wl);
+  }
+}
+
+__device__ __forceinline__ unsigned bit_rev_dev(int nbits, unsigned i) {
+  return nbits == 0 ? 0u : (__brev(i) >> (32 - nbits));
+}
+// src/unordered.rs:1046-1059
+__device__ __forceinline__ unsigned bit_rev_twice_dev(int nbits, int base_nbits, unsigned i) {
+  const unsigned i_rev = bit_rev_dev(nbits, i);
+  const unsigned mask = (1u << base_nbits) - 1u;
+  return (i_rev & ~mask) | bit_rev_dev(base_nbits, i_rev & mask);
+}
+__device__ __forceinline__ unsigned bit_rev_twice_inv_dev(int nbits, int base_nbits, unsigned i) {
+  const unsigned mask = (1u << base_nbits) - 1u;
+  return bit_rev_dev(nbits, (i & ~mask) | bit_rev_dev(base_nbits, i & mask));
+}
+
+// standard[i] = permuted[bit_rev_twice(i)] (to_standard) or the scatter back.
+template <bool TO_STD>
+__global__ void c64_permute_kernel(const double2* __restrict__ src, double2* __restrict__ dst, long total, int nbits,
+                                   int base_nbits) {
+  const long mask = (1L << nbits) - 1;
+  for (long g = (long)blockIdx.x * blockDim.x + threadIdx.x; g < total; g += (long)gridDim.x * blockDim.x) {
+    const long b = g & ~mask;
+    const unsigned i = (unsigned)(g & mask);
+    const unsigned j = bit_rev_twice_dev(nbits, base_nbits, i);
+    if (TO_STD) dst[g] = src[b + j];
+    else dst[b + j] = src[g];
+  }
+}
+
+// src/unordered.rs:844-900
+__global__ void c64_monomial_kernel(double2* __restrict__ buf, const double2* __restrict__ tw, int nbits,
+                                    int base_nbits, unsigned long long degree) {
+  const unsigned n = 1u << nbits;
+  const unsigned long long mask = n - 1;
+  const int ratio_log = nbits - base_nbits;
+  for (unsigned j = blockIdx.x * blockDim.x + threadIdx.x; j < n; j += gridDim.x * blockDim.x) {
+    unsigned long long idx;
+    if (ratio_log == 0) idx = j;
+    else if (ratio_log == 1) idx = j < n / 2 ? 2ull * j : 2ull * (j - n / 2) + 1;
+    else idx = bit_rev_twice_inv_dev(nbits, base_nbits, j);
+    buf[j] = tw[(idx * degree) & mask];
+  }
+}
+
+}  // namespace cfft
+
+// ============================================================ plan object
+struct C64Plan {
+  size_t n = 0, base_n = 0;
+  int base_algo = 0;
+  bool unordered = false;
+  LevelDesc lv{};
+  DevLevels dlv{};
+  double2* d_w = nullptr;
+  double2* d_winv = nullptr;
+  double2* d_mono = nullptr;
+  int device = 0;
+  int d0 = 0;        // first level handled in shared memory
+  int threads = 128;  // CTA size of the shared-memory kernel
+  int tpc = 1;       // sub-transforms per CTA
+};
+
+struct cfft_ordered_plan {
+  C64Plan p;
+};
+struct cfft_unordered_plan {
+  C64Plan p;
+};
+
+namespace {
+
+DevLevels to_dev(const LevelDesc& l) {
+  DevLevels d;
+  std::memset(&d, 0, sizeof(d));
+  d.nlevels = l.nlevels;
+  for (int i = 0; i <= kMaxLevels; ++i) {
+    d.log2n[i] = l.log2n[i];
+    d.w_off[i] = l.w_off[i];
+  }
+  for (int i = 0; i < kMaxLevels; ++i) {
+    d.log2r[i] = l.log2r[i];
+    d.winv_off[i] = l.winv_off[i];
+  }
+  return d;
+}
+
+void default_launch(C64Plan& p) {
+  const int log2sub = p.lv.log2n[p.d0];
+  const size_t sub = size_t(1) << log2sub;
+  const size_t pts = std::max<size_t>(sub, 1024);
+  p.tpc = (int)(pts / sub);
+  p.threads = (int)std::min<size_t>(256, std::max<size_t>(64, pts / 8));
+}
+
+size_t smem_bytes(const C64Plan& p) { return (size_t)2 * p.tpc * (size_t(1) << p.lv.log2n[p.d0]) * sizeof(double2); }
+
+void free_plan(C64Plan& p) {
+  if (p.d_w) cudaFree(p.d_w);
+  if (p.d_winv) cudaFree(p.d_winv);
+  if (p.d_mono) cudaFree(p.d_mono);
+  p.d_w = p.d_winv = p.d_mono = nullptr;
+}
+
+bool g_attr_done = false;
+cfft_status ensure_attrs() {
+  if (g_attr_done) return CFFT_OK;
+  const int max_smem = 2 * (1 << kSmemLog2Max) * (int)sizeof(double2);
+  CFFT_CUDA_TRY(cudaFuncSetAttribute(c64_smem_fwd_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, max_smem));
+  CFFT_CUDA_TRY(cudaFuncSetAttribute(c64_smem_inv_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, max_smem));
+  g_attr_done = true;
+  return CFFT_OK;
+}
+
+cfft_status build_plan(C64Plan& p, size_t n, size_t base_n, int algo, bool unordered) {
+  p.n = n;
+  p.base_n = base_n;
+  p.base_algo = algo;
+  p.unordered = unordered;
+  CFFT_CUDA_TRY(cudaGetDevice(&p.device));
+  cfft_status st = ensure_attrs();
+  if (st != CFFT_OK) return st;
+  p.lv = make_levels(n, base_n);
+  p.dlv = to_dev(p.lv);
+  // first level whose sub-transforms fit in shared memory
+  p.d0 = 0;
+  while (p.lv.log2n[p.d0] > kSmemLog2Max) ++p.d0;
+  default_launch(p);
+  const size_t len = n + base_n;
+  std::vector<c64h> w(len), wi(len);
+  unordered_twiddles(n, base_n, algo_radix(algo), w.data(), wi.data());
+  st = upload((const double2*)w.data(), len, &p.d_w);
+  if (st == CFFT_OK) st = upload((const double2*)wi.data(), len, &p.d_winv);
+  if (st == CFFT_OK && unordered) {
+    std::vector<c64h> mono(n);
+    monomial_twiddles(n, mono.data());
+    st = upload((const double2*)mono.data(), n, &p.d_mono);
+  }
+  if (st != CFFT_OK) free_plan(p);
+  return st;
+}
+
+cfft_status run_plan(const C64Plan& p, double* buf, size_t batch, bool fwd, cudaStream_t stream) {
+  if (batch == 0) return CFFT_OK;
+  if (buf == nullptr) return fail(CFFT_ERR_INVALID_ARGUMENT, "null buffer");
+  if (p.n == 1) return CFFT_OK;
+  double2* data = (double2*)buf;
+  const int log2n = p.lv.log2n[0];
+  const int log2sub = p.lv.log2n[p.d0];
+  const long nsub = (long)batch << (log2n - log2sub);
+  if (nsub > 0x7fffffffL * (long)p.tpc) return fail(CFFT_ERR_INVALID_SIZE, "batch too large");
+  const int blocks = (int)((nsub + p.tpc - 1) / p.tpc);
+  const size_t smem = smem_bytes(p);
+  const int nsm = sm_count();
+  if (fwd) {
+    for (int l = 0; l < p.d0; ++l) {
+      const long total = ((long)batch << log2n) >> p.lv.log2r[l];
+      const int grid = (int)std::min<long>((total + 255) / 256, (long)nsm * 16);
+      c64_level_kernel<true><<<grid, 256, 0, stream>>>(data, total, p.lv.log2r[l], p.lv.log2n[l], p.d_w + p.lv.w_off[l]);
+      CFFT_CHECK_LAUNCH();
+    }
+    c64_smem_fwd_kernel<<<blocks, p.threads, smem, stream>>>(data, (int)nsub, p.tpc, p.dlv, p.d0, p.base_algo, p.d_w);
+    CFFT_CHECK_LAUNCH();
+  } else {
+    c64_smem_inv_kernel<<<blocks, p.threads, smem, stream>>>(data, (int)nsub, p.tpc, p.dlv, p.d0, p.base_algo,
+                                                              p.d_winv);
+    CFFT_CHECK_LAUNCH();
+    for (int l = p.d0 - 1; l >= 0; --l) {
+      const long total = ((long)batch << log2n) >> p.lv.log2r[l];
+      const int grid = (int)std::min<long>((total + 255) / 256, (long)nsm * 16);
+      c64_level_kernel<false>
+          <<<grid, 256, 0, stream>>>(data, total, p.lv.log2r[l], p.lv.log2n[l], p.d_winv + p.lv.winv_off[l]);
+      CFFT_CHECK_LAUNCH();
+    }
+  }
+  return CFFT_OK;
+}
+
+cfft_status run_host(const C64Plan& p, double* buf, size_t batch, bool fwd) {
+  if (buf == nullptr) return fail(CFFT_ERR_INVALID_ARGUMENT, "null buffer");
+  const size_t bytes = batch * p.n * sizeof(double2);
+  void* d = nullptr;
+  cudaStream_t s;
+  cfft_status st = host_staging(bytes, &d, &s);
+  if (st != CFFT_OK) return st;
+  CFFT_CUDA_TRY(cudaMemcpyAsync(d, buf, bytes, cudaMemcpyHostToDevice, s));
+  st = run_plan(p, (double*)d, batch, fwd, s);
+  if (st != CFFT_OK) return st;
+  CFFT_CUDA_TRY(cudaMemcpyAsync(buf, d, bytes, cudaMemcpyDeviceToHost, s));
+  CFFT_CUDA_TRY(cudaStreamSynchronize(s));
+  return CFFT_OK;
+}
+
+// Average device time of one forward call over `batch` transforms (events on a private stream).
+double time_forward(const C64Plan& p, double2* scratch, size_t batch, double seconds) {
+  cudaStream_t s;
+  cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking);
+  cudaEvent_t e0, e1;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  run_plan(p, (double*)scratch, batch, true, s);  // warm-up
+  int reps = 1;
+  double per = 0.0;
+  for (;;) {
+    cudaEventRecord(e0, s);
+    for (int i = 0; i < reps; ++i) run_plan(p, (double*)scratch, batch, true, s);
+    cudaEventRecord(e1, s);
+    cudaEventSynchronize(e1);
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, e0, e1);
+    per = ms * 1e-3 / reps;
+    if (ms * 1e-3 >= std::max(seconds, 1e-3) || reps >= (1 << 20)) break;
+    reps *= 2;
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  cudaStreamDestroy(s);
+  return per;
+}
+
+// Method::Measure for one ordered size: the reference times its 8 algorithms
+// (src/ordered.rs:99-180); here each algorithm, and then CTA shapes for the
+// winner, are timed on the GPU over a batch large enough to fill every SM.
+cfft_status measure_ordered(size_t n, double seconds, double2* scratch, size_t batch, int* best_algo,
+                            int* best_threads, int* best_tpc, double* best_time) {
+  double best = 1e30;
+  *best_algo = 0;
+  for (int algo = 0; algo < 8; ++algo) {
+    C64Plan p;
+    cfft_status st = build_plan(p, n, n, algo, false);
+    if (st != CFFT_OK) return st;
+    const double t = time_forward(p, scratch, batch, seconds);
+    if (t < best) {
+      best = t;
+      *best_algo = algo;
+      *best_threads = p.threads;
+      *best_tpc = p.tpc;
+    }
+    free_plan(p);
+  }
+  *best_time = best;
+  return CFFT_OK;
+}
+
+cfft_status alloc_measure_scratch(size_t n, double2** scratch, size_t* batch) {
+  *batch = std::max<size_t>(1, (size_t(1) << 22) / n);  // 64 MiB of c64
+  CFFT_CUDA_TRY(cudaMalloc((void**)scratch, *batch * n * sizeof(double2)));
+  CFFT_CUDA_TRY(cudaMemset(*scratch, 0, *batch * n * sizeof(double2)));
+  return CFFT_OK;
+}
+
+// CTA-shape sweep for a fixed algorithm (the "threads per transform and
+// transforms per CTA" part of the autotuner).
+void tune_launch(C64Plan& p, double2* scratch, size_t batch, double seconds) {
+  const int log2sub = p.lv.log2n[p.d0];
+  const size_t sub = size_t(1) << log2sub;
+  double best = time_forward(p, scratch, batch, seconds);
+  int bt = p.threads, bp = p.tpc;
+  for (size_t pts : {size_t(512), size_t(1024), size_t(2048), size_t(4096)}) {
+    if (pts < sub) continue;
+    for (int th : {64, 128, 256}) {
+      C64Plan q = p;
+      q.tpc = (int)(pts / sub);
+      q.threads = th;
+      if (smem_bytes(q) > (size_t)2 * (1 << kSmemLog2Max) * sizeof(double2)) continue;
+      const double t = time_forward(q, scratch, batch, seconds);
+      if (t < best) {
+        best = t;
+        bt = th;
+        bp = q.tpc;
+      }
+    }
+  }
+  p.threads = bt;
+  p.tpc = bp;
+}
+
+bool valid_algo(int a) { return a >= 0 && a <= 7; }
+
+}  // namespace
+
+// ================================================================= C ABI
+extern "C" {
+
+cfft_status cfft_ordered_plan_create(size_t n, cfft_algo algo, cfft_ordered_plan** out) {
+  if (!out) return fail(CFFT_ERR_INVALID_ARGUMENT, "null output pointer");
+  *out = nullptr;
+  if (!is_pow2(n)) return fail(CFFT_ERR_INVALID_SIZE, "ordered plan: n must be a power of two");
+  if (ilog2(n) >= 11) return fail(CFFT_ERR_INVALID_SIZE, "ordered plan: n must be at most 1024");
+  if (!valid_algo(algo)) return fail(CFFT_ERR_INVALID_ARGUMENT, "unknown FftAlgo");
+  auto* plan = new cfft_ordered_plan();
+  cfft_status st = build_plan(plan->p, n, n, algo, false);
+  if (st != CFFT_OK) {
+    delete plan;
+    return st;
+  }
+  *out = plan;
+  return CFFT_OK;
+}
+
+cfft_status cfft_ordered_plan_create_measure(size_t n, double seconds, cfft_ordered_plan** out) {
+  if (!out) return fail(CFFT_ERR_INVALID_ARGUMENT, "null output pointer");
+  *out = nullptr;
+  if (!is_pow2(n) || ilog2(n) >= 11) return fail(CFFT_ERR_INVALID_SIZE, "ordered plan: n must be 2^k, k <= 10");
+  if (n == 1) return cfft_ordered_plan_create(n, CFFT_DIF2, out);
+  double2* scratch = nullptr;
+  size_t batch = 0;
+  cfft_status st = alloc_measure_scratch(n, &scratch, &batch);
+  int algo = 0, th = 128, tpc = 1;
+  double t = 0;
+  if (st == CFFT_OK) st = measure_ordered(n, seconds, scratch, batch, &algo, &th, &tpc, &t);
+  if (st == CFFT_OK) st = cfft_ordered_plan_create(n, (cfft_algo)algo, out);
+  if (st == CFFT_OK) tune_launch((*out)->p, scratch, batch, seconds);
+  if (scratch) cudaFree(scratch);
+  return st;
+}
+
+void cfft_ordered_plan_destroy(cfft_ordered_plan* plan) {
+  if (!plan) return;
+  free_plan(plan->p);
+  delete plan;
+}
+size_t cfft_ordered_fft_size(const cfft_ordered_plan* plan) { return plan ? plan->p.n : 0; }
+cfft_algo cfft_ordered_algo(const cfft_ordered_plan* plan) { return (cfft_algo)(plan ? plan->p.base_algo : 0); }
+size_t cfft_ordered_scratch_bytes(const cfft_ordered_plan*) { return 0; }
+
+cfft_status cfft_ordered_fwd(const cfft_ordered_plan* plan, double* buf, size_t batch, void* stream) {
+  if (!plan) return fail(CFFT_ERR_INVALID_ARGUMENT, "null plan");
+  return run_plan(plan->p, buf, batch, true, (cudaStream_t)stream);
+}
+cfft_status cfft_ordered_inv(const cfft_ordered_plan* plan, double* buf, size_t batch, void* stream) {
+  if (!plan) return fail(CFFT_ERR_INVALID_ARGUMENT, "null plan");
+  return run_plan(plan->p, buf, batch, false, (cudaStream_t)stream);
+}
+cfft_status cfft_ordered_fwd_host(const cfft_ordered_plan* plan, double* buf, size_t batch) {
+  if (!plan) return fail(CFFT_ERR_INVALID_ARGUMENT, "null plan");
+  return run_host(plan->p, buf, batch, true);
+}
+cfft_status cfft_ordered_inv_host(const cfft_ordered_plan* plan, double* buf, size_t batch) {
+  if (!plan) return fail(CFFT_ERR_INVALID_ARGUMENT, "null plan");
+  return run_host(plan->p, buf, batch, false);
+}
+
+cfft_status cfft_unordered_plan_create(size_t n, cfft_algo base_algo, size_t base_n, cfft_unordered_plan** out) {
+  if (!out) return fail(CFFT_ERR_INVALID_ARGUMENT, "null output pointer");
+  *out = nullptr;
+  if (!is_pow2(n)) return fail(CFFT_ERR_INVALID_SIZE, "unordered plan: n must be a power of two");
+  if (ilog2(n) > 20) return fail(CFFT_ERR_INVALID_SIZE, "unordered plan: n must be at most 2^20");
+  if (!is_pow2(base_n)) return fail(CFFT_ERR_INVALID_ARGUMENT, "base_n must be a power of two");
+  if (base_n > n) return fail(CFFT_ERR_INVALID_ARGUMENT, "base_n must not exceed n");
+  if (base_n != n && base_n < 32) return fail(CFFT_ERR_INVALID_ARGUMENT, "base_n must be >= 32 when base_n != n");
+  if (ilog2(base_n) > 10) return fail(CFFT_ERR_INVALID_ARGUMENT, "base_n must be at most 1024");
+  if (!valid_algo(base_algo)) return fail(CFFT_ERR_INVALID_ARGUMENT, "unknown FftAlgo");
+  auto* plan = new cfft_unordered_plan();
+  cfft_status st = build_plan(plan->p, n, base_n, base_algo, true);
+  if (st != CFFT_OK) {
+    delete plan;
+    return st;
+  }
+  *out = plan;
+  return CFFT_OK;
+}
+
+// src/unordered.rs:540-640: n <= 256 measures the ordered algorithms at n;
+// otherwise bases 512 and 1024 (those <= n), each with its fastest ordered
+// algorithm, timed on the full unordered forward transform.
+cfft_status cfft_unordered_plan_create_measure(size_t n, double seconds, cfft_unordered_plan** out) {
+  if (!out) return fail(CFFT_ERR_INVALID_ARGUMENT, "null output pointer");
+  *out = nullptr;
+  if (!is_pow2(n) || ilog2(n) > 20) return fail(CFFT_ERR_INVALID_SIZE, "unordered plan: n must be 2^k, k <= 20");
+  double2* scratch = nullptr;
+  size_t batch = 0;
+  cfft_status st = alloc_measure_scratch(n, &scratch, &batch);
+  if (st != CFFT_OK) return st;
+  int best_algo = 0;
+  size_t best_base = n;
+  if (n <= 256) {
+    int th, tpc;
+    double t;
+    st = measure_ordered(n, seconds, scratch, batch, &best_algo, &th, &tpc, &t);
+  } else {
+    double best = 1e30;
+    for (size_t base : {size_t(512), size_t(1024)}) {
+      if (n < base) break;
+      double2* bs = nullptr;
+      size_t bb = 0;
+      st = alloc_measure_scratch(base, &bs, &bb);
+      if (st != CFFT_OK) break;
+      int algo = 0, th, tpc;
+      double t;
+      st = measure_ordered(base, seconds, bs, bb, &algo, &th, &tpc, &t);
+      cudaFree(bs);
+      if (st != CFFT_OK) break;
+      C64Plan p;
+      st = build_plan(p, n, base, algo, true);
+      if (st != CFFT_OK) break;
+      const double tu = time_forward(p, scratch, batch, seconds);
+      free_plan(p);
+      if (tu < best) {
+        best = tu;
+        best_algo = algo;
+        best_base = base;
+      }
+    }
+  }
+  if (st == CFFT_OK) st = cfft_unordered_plan_create(n, (cfft_algo)best_algo, best_base, out);
+  if (st == CFFT_OK) tune_launch((*out)->p, scratch, batch, seconds);
+  cudaFree(scratch);
+  return st;
+}
+
+void cfft_unordered_plan_destroy(cfft_unordered_plan* plan) {
+  if (!plan) return;
+  free_plan(plan->p);
+  delete plan;
+}
+size_t cfft_unordered_fft_size(const cfft_unordered_plan* plan) { return plan ? plan->p.n : 0; }
+void cfft_unordered_algo(const cfft_unordered_plan* plan, cfft_algo* base_algo, size_t* base_n) {
+  if (!plan) return;
+  if (base_algo) *base_algo = (cfft_algo)plan->p.base_algo;
+  if (base_n) *base_n = plan->p.base_n;
+}
+size_t cfft_unordered_scratch_bytes(const cfft_unordered_plan*) { return 0; }
+
+cfft_status cfft_unordered_fwd(const cfft_unordered_plan* plan, double* buf, size_t batch, void* stream) {
+  if (!plan) return fail(CFFT_ERR_INVALID_ARGUMENT, "null plan");
+  return run_plan(plan->p, buf, batch, true, (cudaStream_t)stream);
+}
+cfft_status cfft_unordered_inv(const cfft_unordered_plan* plan, double* buf, size_t batch, void* stream) {
+  if (!plan) return fail(CFFT_ERR_INVALID_ARGUMENT, "null plan");
+  return run_plan(plan->p, buf, batch, false, (cudaStream_t)stream);
+}
+cfft_status cfft_unordered_fwd_host(const cfft_unordered_plan* plan, double* buf, size_t batch) {
+  if (!plan) return fail(CFFT_ERR_INVALID_ARGUMENT, "null plan");
+  return run_host(plan->p, buf, batch, true);
+}
+cfft_status cfft_unordered_inv_host(const cfft_unordered_plan* plan, double* buf, size_t batch) {
+  if (!plan) return fail(CFFT_ERR_INVALID_ARGUMENT, "null plan");
+  return run_host(plan->p, buf, batch, false);
+}
+
+cfft_status cfft_unordered_fwd_monomial(const cfft_unordered_plan* plan, size_t degree, double* buf, void* stream) {
+  if (!plan || !buf) return fail(CFFT_ERR_INVALID_ARGUMENT, "null argument");
+  if (degree >= plan->p.n) return fail(CFFT_ERR_INVALID_ARGUMENT, "degree must be < fft size");
+  const int nbits = ilog2(plan->p.n), bb = ilog2(plan->p.base_n);
+  const int blocks = (int)std::min<size_t>((plan->p.n + 255) / 256, 1024);
+  c64_monomial_kernel<<<blocks, 256, 0, (cudaStream_t)stream>>>((double2*)buf, plan->p.d_mono, nbits, bb,
+                                                                 (unsigned long long)degree);
+  CFFT_CHECK_LAUNCH();
+  return CFFT_OK;
+}
+
+cfft_status cfft_unordered_fwd_monomial_host(const cfft_unordered_plan* plan, size_t degree, double* buf) {
+  if (!plan || !buf) return fail(CFFT_ERR_INVALID_ARGUMENT, "null argument");
+  const size_t bytes = plan->p.n * sizeof(double2);
+  void* d;
+  cudaStream_t s;
+  cfft_status st = host_staging(bytes, &d, &s);
+  if (st != CFFT_OK) return st;
+  st = cfft_unordered_fwd_monomial(plan, degree, (double*)d, s);
+  if (st != CFFT_OK) return st;
+  CFFT_CUDA_TRY(cudaMemcpyAsync(buf, d, bytes, cudaMemcpyDeviceToHost, s));
+  CFFT_CUDA_TRY(cudaStreamSynchronize(s));
+  return CFFT_OK;
+}
+
+static cfft_status permute(const cfft_unordered_plan* plan, const double* src, double* dst, size_t batch,
+                           cudaStream_t stream, bool to_std) {
+  if (!plan || !src || !dst) return fail(CFFT_ERR_INVALID_ARGUMENT, "null argument");
+  if (src == dst) return fail(CFFT_ERR_INVALID_ARGUMENT, "permutation is out of place: src and dst must differ");
+  if (batch == 0) return CFFT_OK;
+  const long total = (long)(batch * plan->p.n);
+  const int nbits = ilog2(plan->p.n), bb = ilog2(plan->p.base_n);
+  const int grid = (int)std::min<long>((total + 255) / 256, (long)sm_count() * 16);
+  if (to_std)
+    c64_permute_kernel<true><<<grid, 256, 0, stream>>>((const double2*)src, (double2*)dst, total, nbits, bb);
+  else
+    c64_permute_kernel<false><<<grid, 256, 0, stream>>>((const double2*)src, (double2*)dst, total, nbits, bb);
+  CFFT_CHECK_LAUNCH();
+  return CFFT_OK;
+}
+
+cfft_status cfft_unordered_to_standard(const cfft_unordered_plan* plan, const double* permuted, double* standard,
+                                       size_t batch, void* stream) {
+  return permute(plan, permuted, standard, batch, (cudaStream_t)stream, true);
+}
+cfft_status cfft_unordered_from_standard(const cfft_unordered_plan* plan, const double* standard, double* permuted,
+                                         size_t batch, void* stream) {
+  return permute(plan, standard, permuted, batch, (cudaStream_t)stream, false);
+}
+
+static cfft_status permute_host(const cfft_unordered_plan* plan, const double* src, double* dst, size_t batch,
+                                bool to_std) {
+  if (!plan || !src || !dst) return fail(CFFT_ERR_INVALID_ARGUMENT, "null argument");
+  const size_t bytes = batch * plan->p.n * sizeof(double2);
+  void* d;
+  cudaStream_t s;
+  cfft_status st = host_staging(2 * bytes, &d, &s);
+  if (st != CFFT_OK) return st;
+  double* din = (double*)d;
+  double* dout = (double*)((char*)d + bytes);
+  CFFT_CUDA_TRY(cudaMemcpyAsync(din, src, bytes, cudaMemcpyHostToDevice, s));
+  st = permute(plan, din, dout, batch, s, to_std);
+  if (st != CFFT_OK) return st;
+  CFFT_CUDA_TRY(cudaMemcpyAsync(dst, dout, bytes, cudaMemcpyDeviceToHost, s));
+  CFFT_CUDA_TRY(cudaStreamSynchronize(s));
+  return CFFT_OK;
+}
+cfft_status cfft_unordered_to_standard_host(const cfft_unordered_plan* plan, const double* permuted, double* standard,
+                                            size_t batch) {
+  return permute_host(plan, permuted, standard, batch, true);
+}
+cfft_status cfft_unordered_from_standard_host(const cfft_unordered_plan* plan, const double* standard,
+                                              double* permuted, size_t batch) {
+  return permute_host(plan, standard, permuted, batch, false);
+}
+
+}  // extern "C"

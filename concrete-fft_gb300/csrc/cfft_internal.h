@@ -1,0 +1,53 @@
+// cfft_internal.h -- host-side internals shared by the library's translation units.
+#pragma once
+#include <cstddef>
+#include <cstdint>
+#include <string>
+#include <vector>
+
+#include "../../include/cfft.h"
+
+namespace cfft {
+
+struct c64h {
+  double re, im;
+};
+
+// ---- twiddle generation (twiddles.cpp; host, no FMA contraction) ----
+void sincospi64(double a, double* s, double* c);
+// src/fft_simd.rs:298-321: 2n entries each
+void init_wt(int r, size_t n, c64h* w, c64h* w_inv);
+// src/unordered.rs:349-389 (complex_per_reg = 1 layout): n + base_n entries each
+void unordered_twiddles(size_t n, size_t base_n, int base_r, c64h* w, c64h* w_inv);
+// src/unordered.rs:694-699: monomial twiddles exp(-2 pi i k / n)
+void monomial_twiddles(size_t n, c64h* tw);
+// src/fft128/mod.rs:1805-1828: n entries each
+void f128_twiddles(size_t n, double* re0, double* re1, double* im0, double* im1);
+
+inline bool is_pow2(size_t n) { return n != 0 && (n & (n - 1)) == 0; }
+inline int ilog2(size_t n) {
+  int l = 0;
+  while ((size_t(1) << l) < n) ++l;
+  return l;
+}
+inline int algo_radix(int algo) { return 2 << (algo / 2); }
+inline int outer_radix(size_t n, size_t base_n) { return n == 2 * base_n ? 2 : (n == 4 * base_n ? 4 : 8); }
+
+// Level structure of an unordered plan: sizes n_0 = n > n_1 > ... > n_L = base_n.
+constexpr int kMaxLevels = 8;
+struct LevelDesc {
+  int nlevels;                 // L
+  int log2n[kMaxLevels + 1];   // log2 of n_l, l = 0..L (n_L = base_n)
+  int log2r[kMaxLevels];       // outer radix of level l
+  int w_off[kMaxLevels + 1];   // forward table offset of level l (l = L: base table)
+  int winv_off[kMaxLevels];    // inverse table offset of level l (the base table is at 0)
+};
+LevelDesc make_levels(size_t n, size_t base_n);
+
+void set_error(const std::string& msg);
+
+// The largest (sub)transform kept entirely in one CTA's shared memory
+// (data + ping-pong scratch, 16 B per point each: 128 KiB at 4096 points).
+constexpr int kSmemLog2Max = 12;
+
+}  // namespace cfft

@@ -1,0 +1,345 @@
+// f128.cu -- fft128::Plan (double-double negacyclic FFT) and the u128 product.
+//
+// A transform of up to 4096 points (32 bytes each in split re0/re1/im0/im1
+// form) is held by one CTA in shared memory and runs every radix-2 stage
+// there, in place, one barrier per stage.  Larger transforms run their widest
+// stages in global memory (forward: first, inverse: last) until the remaining
+// blocks fit a CTA.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <vector>
+
+#include "cfft_internal.h"
+#include "f128_device.cuh"
+#include "runtime.h"
+
+using namespace cfft;
+
+namespace cfft {
+
+constexpr int kF128SmemLog2 = 12;  // 4096 points x 32 B = 128 KiB
+
+template <bool FWD>
+__global__ void __launch_bounds__(256) f128_smem_kernel(F128Arrays g, int log2n, int log2c, long nblocks, F128Tw tw) {
+  extern __shared__ double sm[];
+  const int c = 1 << log2c;
+  F128Arrays s{sm, sm + c, sm + 2 * c, sm + 3 * c};
+  const int tid = threadIdx.x, nth = blockDim.x;
+  const long per_transform = 1L << (log2n - log2c);
+  for (long blk = blockIdx.x; blk < nblocks; blk += gridDim.x) {
+    const long off = blk << log2c;
+    const long sb = blk % per_transform;  // sub-block index inside its transform
+    for (int i = tid; i < c; i += nth) {
+      s.re0[i] = g.re0[off + i];
+      s.re1[i] = g.re1[off + i];
+      s.im0[i] = g.im0[off + i];
+      s.im1[i] = g.im1[off + i];
+    }
+    __syncthreads();
+    f128_stages_smem<FWD>(s, log2n, log2c, sb, tw, tid, nth);
+    for (int i = tid; i < c; i += nth) {
+      g.re0[off + i] = s.re0[i];
+      g.re1[off + i] = s.re1[i];
+      g.im0[off + i] = s.im0[i];
+      g.im1[off + i] = s.im1[i];
+    }
+    __syncthreads();
+  }
+}
+
+// One stage (half-size 2^log2t) over every transform of the batch, in global memory.
+template <bool FWD>
+__global__ void __launch_bounds__(256) f128_stage_kernel(F128Arrays g, int log2n, int log2t, long total, F128Tw tw) {
+  const long m = 1L << (log2n - 1 - log2t);
+  for (long b = (long)blockIdx.x * blockDim.x + threadIdx.x; b < total; b += (long)gridDim.x * blockDim.x) {
+    const long tr = b >> (log2n - 1);                 // transform index
+    const long bb = b & ((1L << (log2n - 1)) - 1);    // butterfly within transform
+    const long i = bb >> log2t;
+    const long j = (tr << log2n) + (i << (log2t + 1)) + (bb & ((1L << log2t) - 1));
+    if (FWD) f128_fwd_bfly(g, j, 1L << log2t, tw, m + i);
+    else f128_inv_bfly(g, j, 1L << log2t, tw, m + i);
+  }
+}
+
+// u128 product: the fft128 pipeline of src/fft128/mod.rs:1998-2058 fused.
+// a, out: N coefficients as (lo, hi) u64 pairs; bhat: 4 arrays of n = N/2 f64.
+__global__ void __launch_bounds__(256) u128_product_kernel(const uint64_t* __restrict__ a,
+                                                          const double* __restrict__ bhat, long bhat_stride,
+                                                          uint64_t* __restrict__ out, long count, int log2n,
+                                                          F128Tw tw, double factor) {
+  extern __shared__ double sm[];
+  const int n = 1 << log2n;
+  F128Arrays s{sm, sm + n, sm + 2 * n, sm + 3 * n};
+  const int tid = threadIdx.x, nth = blockDim.x;
+  for (long prod = blockIdx.x; prod < count; prod += gridDim.x) {
+    const uint64_t* ap = a + prod * 4L * n;
+    for (int j = tid; j < 2 * n; j += nth) {
+      // coefficient j -> re (j < n) or im (j >= n) of point j mod n
+      const uint64_t lo = __ldcs(ap + 2 * j), hi = __ldcs(ap + 2 * j + 1);
+      const double xh = i128_to_f64_rne(lo, hi);
+      uint64_t tl, th;
+      double fr;
+      trunc_mod128(xh, tl, th, fr);
+      const uint64_t rl = lo - tl;
+      const uint64_t rh = hi - th - (lo < tl ? 1 : 0);
+      const double xl = i128_to_f64_rne(rl, rh);
+      if (j < n) {
+        s.re0[j] = xh;
+        s.re1[j] = xl;
+      } else {
+        s.im0[j - n] = xh;
+        s.im1[j - n] = xl;
+      }
+    }
+    __syncthreads();
+    f128_stages_smem<true>(s, log2n, log2n, 0, tw, tid, nth);
+    const double* bp = bhat + prod * bhat_stride;
+    for (int k = tid; k < n; k += nth) {
+      f128 pr, pi;
+      cplx_mul(f128{s.re0[k], s.re1[k]}, f128{s.im0[k], s.im1[k]}, f128{__ldg(bp + k), __ldg(bp + n + k)},
+               f128{__ldg(bp + 2 * n + k), __ldg(bp + 3 * n + k)}, pr, pi);
+      s.re0[k] = __dmul_rn(pr.hi, factor);
+      s.re1[k] = __dmul_rn(pr.lo, factor);
+      s.im0[k] = __dmul_rn(pi.hi, factor);
+      s.im1[k] = __dmul_rn(pi.lo, factor);
+    }
+    __syncthreads();
+    f128_stages_smem<false>(s, log2n, log2n, 0, tw, tid, nth);
+    uint64_t* op = out + prod * 4L * n;
+    for (int j = tid; j < 2 * n; j += nth) {
+      uint64_t rl, rh;
+      if (j < n) round_half_up_mod128(s.re0[j], s.re1[j], rl, rh);
+      else round_half_up_mod128(s.im0[j - n], s.im1[j - n], rl, rh);
+      __stcs(op + 2 * j, rl);
+      __stcs(op + 2 * j + 1, rh);
+    }
+    __syncthreads();
+  }
+}
+
+// Bhat for small digits: f128(b, 0), fold, forward.
+__global__ void __launch_bounds__(256) u128_prepare_kernel(const int64_t* __restrict__ b, double* __restrict__ bhat,
+                                                          long count, int log2n, F128Tw tw) {
+  extern __shared__ double sm[];
+  const int n = 1 << log2n;
+  F128Arrays s{sm, sm + n, sm + 2 * n, sm + 3 * n};
+  const int tid = threadIdx.x, nth = blockDim.x;
+  for (long prod = blockIdx.x; prod < count; prod += gridDim.x) {
+    const int64_t* bp = b + prod * 2L * n;
+    for (int j = tid; j < n; j += nth) {
+      s.re0[j] = i64_to_f64_rne(bp[j]);
+      s.re1[j] = 0.0;
+      s.im0[j] = i64_to_f64_rne(bp[j + n]);
+      s.im1[j] = 0.0;
+    }
+    __syncthreads();
+    f128_stages_smem<true>(s, log2n, log2n, 0, tw, tid, nth);
+    double* op = bhat + prod * 4L * n;
+    for (int k = tid; k < n; k += nth) {
+      op[k] = s.re0[k];
+      op[n + k] = s.re1[k];
+      op[2 * n + k] = s.im0[k];
+      op[3 * n + k] = s.im1[k];
+    }
+    __syncthreads();
+  }
+}
+
+}  // namespace cfft
+
+struct cfft_f128_plan {
+  size_t n = 0;
+  double* d_tw = nullptr;  // 4 arrays of n
+  F128Tw tw() const { return F128Tw{d_tw, d_tw + n, d_tw + 2 * n, d_tw + 3 * n}; }
+};
+
+struct cfft_u128_product_plan {
+  size_t N = 0;
+  cfft_f128_plan f;
+};
+
+namespace {
+
+bool g_f128_attr = false;
+cfft_status f128_attrs() {
+  if (g_f128_attr) return CFFT_OK;
+  const int max_smem = 4 * (1 << kF128SmemLog2) * (int)sizeof(double);
+  CFFT_CUDA_TRY(cudaFuncSetAttribute(f128_smem_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, max_smem));
+  CFFT_CUDA_TRY(cudaFuncSetAttribute(f128_smem_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, max_smem));
+  CFFT_CUDA_TRY(cudaFuncSetAttribute(u128_product_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, max_smem));
+  CFFT_CUDA_TRY(cudaFuncSetAttribute(u128_prepare_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, max_smem));
+  g_f128_attr = true;
+  return CFFT_OK;
+}
+
+cfft_status build_f128(cfft_f128_plan* p, size_t n) {
+  cfft_status st = f128_attrs();
+  if (st != CFFT_OK) return st;
+  p->n = n;
+  std::vector<double> tw(4 * n);
+  f128_twiddles(n, tw.data(), tw.data() + n, tw.data() + 2 * n, tw.data() + 3 * n);
+  return upload(tw.data(), 4 * n, &p->d_tw);
+}
+
+int f128_threads(int log2c) { return std::min(256, std::max(64, (1 << log2c) / 8)); }
+
+cfft_status run_f128(const cfft_f128_plan* p, double* re0, double* re1, double* im0, double* im1, size_t batch,
+                     bool fwd, cudaStream_t stream) {
+  if (!p || !re0 || !re1 || !im0 || !im1) return fail(CFFT_ERR_INVALID_ARGUMENT, "null argument");
+  if (batch == 0) return CFFT_OK;
+  const int log2n = ilog2(p->n);
+  const int log2c = std::min(log2n, kF128SmemLog2);
+  F128Arrays g{re0, re1, im0, im1};
+  const F128Tw tw = p->tw();
+  const long nblocks = (long)batch << (log2n - log2c);
+  const int threads = f128_threads(log2c);
+  const size_t smem = (size_t)4 * (size_t(1) << log2c) * sizeof(double);
+  int per_sm = 1;
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fwd ? (const void*)f128_smem_kernel<true>
+                                                              : (const void*)f128_smem_kernel<false>,
+                                                threads, smem);
+  const int grid = (int)std::max<long>(1, std::min<long>(nblocks, (long)sm_count() * std::max(per_sm, 1)));
+  const long total = (long)batch << (log2n - 1);
+  const int sgrid = (int)std::min<long>((total + 255) / 256, (long)sm_count() * 16);
+  if (fwd) {
+    for (int lt = log2n - 1; lt >= log2c; --lt) {
+      f128_stage_kernel<true><<<sgrid, 256, 0, stream>>>(g, log2n, lt, total, tw);
+      CFFT_CHECK_LAUNCH();
+    }
+    f128_smem_kernel<true><<<grid, threads, smem, stream>>>(g, log2n, log2c, nblocks, tw);
+    CFFT_CHECK_LAUNCH();
+  } else {
+    f128_smem_kernel<false><<<grid, threads, smem, stream>>>(g, log2n, log2c, nblocks, tw);
+    CFFT_CHECK_LAUNCH();
+    for (int lt = log2c; lt <= log2n - 1; ++lt) {
+      f128_stage_kernel<false><<<sgrid, 256, 0, stream>>>(g, log2n, lt, total, tw);
+      CFFT_CHECK_LAUNCH();
+    }
+  }
+  return CFFT_OK;
+}
+
+cfft_status run_f128_host(const cfft_f128_plan* p, double* re0, double* re1, double* im0, double* im1, size_t batch,
+                          bool fwd) {
+  if (!p || !re0 || !re1 || !im0 || !im1) return fail(CFFT_ERR_INVALID_ARGUMENT, "null argument");
+  const size_t bytes = batch * p->n * sizeof(double);
+  void* d;
+  cudaStream_t s;
+  cfft_status st = host_staging(4 * bytes, &d, &s);
+  if (st != CFFT_OK) return st;
+  double* dd[4];
+  double* hh[4] = {re0, re1, im0, im1};
+  for (int i = 0; i < 4; ++i) {
+    dd[i] = (double*)((char*)d + i * bytes);
+    CFFT_CUDA_TRY(cudaMemcpyAsync(dd[i], hh[i], bytes, cudaMemcpyHostToDevice, s));
+  }
+  st = run_f128(p, dd[0], dd[1], dd[2], dd[3], batch, fwd, s);
+  if (st != CFFT_OK) return st;
+  for (int i = 0; i < 4; ++i) CFFT_CUDA_TRY(cudaMemcpyAsync(hh[i], dd[i], bytes, cudaMemcpyDeviceToHost, s));
+  CFFT_CUDA_TRY(cudaStreamSynchronize(s));
+  return CFFT_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+cfft_status cfft_f128_plan_create(size_t n, cfft_f128_plan** out) {
+  if (!out) return fail(CFFT_ERR_INVALID_ARGUMENT, "null output pointer");
+  *out = nullptr;
+  if (!is_pow2(n) || n < 32) return fail(CFFT_ERR_INVALID_SIZE, "fft128 plan: n must be a power of two >= 32");
+  if (ilog2(n) > 16) return fail(CFFT_ERR_INVALID_SIZE, "fft128 plan: n must be at most 65536");
+  auto* p = new cfft_f128_plan();
+  cfft_status st = build_f128(p, n);
+  if (st != CFFT_OK) {
+    if (p->d_tw) cudaFree(p->d_tw);
+    delete p;
+    return st;
+  }
+  *out = p;
+  return CFFT_OK;
+}
+
+void cfft_f128_plan_destroy(cfft_f128_plan* plan) {
+  if (!plan) return;
+  if (plan->d_tw) cudaFree(plan->d_tw);
+  delete plan;
+}
+size_t cfft_f128_fft_size(const cfft_f128_plan* plan) { return plan ? plan->n : 0; }
+
+cfft_status cfft_f128_fwd(const cfft_f128_plan* p, double* re0, double* re1, double* im0, double* im1, size_t batch,
+                          void* stream) {
+  return run_f128(p, re0, re1, im0, im1, batch, true, (cudaStream_t)stream);
+}
+cfft_status cfft_f128_inv(const cfft_f128_plan* p, double* re0, double* re1, double* im0, double* im1, size_t batch,
+                          void* stream) {
+  return run_f128(p, re0, re1, im0, im1, batch, false, (cudaStream_t)stream);
+}
+cfft_status cfft_f128_fwd_host(const cfft_f128_plan* p, double* re0, double* re1, double* im0, double* im1,
+                               size_t batch) {
+  return run_f128_host(p, re0, re1, im0, im1, batch, true);
+}
+cfft_status cfft_f128_inv_host(const cfft_f128_plan* p, double* re0, double* re1, double* im0, double* im1,
+                               size_t batch) {
+  return run_f128_host(p, re0, re1, im0, im1, batch, false);
+}
+
+cfft_status cfft_u128_product_plan_create(size_t N, cfft_u128_product_plan** out) {
+  if (!out) return fail(CFFT_ERR_INVALID_ARGUMENT, "null output pointer");
+  *out = nullptr;
+  if (!is_pow2(N) || N < 64 || ilog2(N) > kF128SmemLog2 + 1)
+    return fail(CFFT_ERR_INVALID_SIZE, "u128 product: N must be a power of two in [64, 8192]");
+  auto* p = new cfft_u128_product_plan();
+  p->N = N;
+  cfft_status st = build_f128(&p->f, N / 2);
+  if (st != CFFT_OK) {
+    if (p->f.d_tw) cudaFree(p->f.d_tw);
+    delete p;
+    return st;
+  }
+  *out = p;
+  return CFFT_OK;
+}
+
+void cfft_u128_product_plan_destroy(cfft_u128_product_plan* plan) {
+  if (!plan) return;
+  if (plan->f.d_tw) cudaFree(plan->f.d_tw);
+  delete plan;
+}
+size_t cfft_u128_product_poly_size(const cfft_u128_product_plan* plan) { return plan ? plan->N : 0; }
+
+cfft_status cfft_u128_prepare_operand(const cfft_u128_product_plan* p, const int64_t* b, double* bhat4, size_t count,
+                                      void* stream) {
+  if (!p || !b || !bhat4) return fail(CFFT_ERR_INVALID_ARGUMENT, "null argument");
+  if (count == 0) return CFFT_OK;
+  const int log2n = ilog2(p->f.n);
+  const int threads = f128_threads(log2n);
+  const size_t smem = 4 * p->f.n * sizeof(double);
+  int per_sm = 1;
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, u128_prepare_kernel, threads, smem);
+  const int grid = (int)std::max<long>(1, std::min<long>((long)count, (long)sm_count() * std::max(per_sm, 1)));
+  u128_prepare_kernel<<<grid, threads, smem, (cudaStream_t)stream>>>(b, bhat4, (long)count, log2n, p->f.tw());
+  CFFT_CHECK_LAUNCH();
+  return CFFT_OK;
+}
+
+cfft_status cfft_u128_product(const cfft_u128_product_plan* p, const uint64_t* a, const double* bhat4,
+                              size_t bhat_stride, uint64_t* out, size_t count, void* stream) {
+  if (!p || !a || !bhat4 || !out) return fail(CFFT_ERR_INVALID_ARGUMENT, "null argument");
+  if (bhat_stride != 0 && bhat_stride != 2 * p->N)
+    return fail(CFFT_ERR_INVALID_ARGUMENT, "bhat_stride must be 0 or 2N");
+  if (count == 0) return CFFT_OK;
+  const int log2n = ilog2(p->f.n);
+  const int threads = f128_threads(log2n);
+  const size_t smem = 4 * p->f.n * sizeof(double);
+  int per_sm = 1;
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, u128_product_kernel, threads, smem);
+  const int grid = (int)std::max<long>(1, std::min<long>((long)count, (long)sm_count() * std::max(per_sm, 1)));
+  u128_product_kernel<<<grid, threads, smem, (cudaStream_t)stream>>>(
+      a, bhat4, (long)bhat_stride, out, (long)count, log2n, p->f.tw(), 2.0 / (double)p->N);
+  CFFT_CHECK_LAUNCH();
+  return CFFT_OK;
+}
+
+}  // extern "C"

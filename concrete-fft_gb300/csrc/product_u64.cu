@@ -1,0 +1,326 @@
+// product_u64.cu -- fused negacyclic u64 polynomial product on unordered::Plan.
+//
+// One CTA computes one product at a time (grid-stride over the batch): it
+// reads N u64 coefficients and N/2 resident Fourier coefficients, writes N u64
+// results, and keeps every intermediate in shared memory, so a product costs
+// exactly 48 KiB of HBM traffic at N = 2048 (24 bytes per coefficient).
+//
+// Pipeline (the way the reference's caller uses unordered::Plan; the crate
+// itself has no product code):
+//   z_j = tau^j * (a_j + i a_{j+N/2}),  tau = exp(i pi / N),  a read as i64
+//   Z = fwd(z)                      unordered forward, permuted order
+//   P_k = Bhat_k * Z_k              Bhat = fwd of the twisted operand, resident
+//   p = inv(P)                      unordered inverse, standard order
+//   t_j = (conj(tau^j) / (N/2)) * p_j
+//   c_j = floor(Re t_j + 1/2) mod 2^64,  c_{j+N/2} = floor(Im t_j + 1/2) mod 2^64
+// Every complex product is the reference's FMA form (cmul); conversions are
+// exact integer-pipe routines, so the result is bit-identical to the oracle's
+// CPU restatement of the same pipeline.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstring>
+#include <vector>
+
+#include "cfft_internal.h"
+#include "runtime.h"
+#include "stockham.cuh"
+
+using namespace cfft;
+
+namespace cfft {
+
+template <int THREADS>
+__global__ void __launch_bounds__(THREADS) u64_product_kernel(const uint64_t* __restrict__ a,
+                                                             const double2* __restrict__ bhat, long bhat_stride,
+                                                             uint64_t* __restrict__ out, long count, DevLevels L,
+                                                             int base_algo, const double2* __restrict__ w,
+                                                             const double2* __restrict__ winv,
+                                                             const double2* __restrict__ tw,
+                                                             const double2* __restrict__ itw) {
+  extern __shared__ double2 smem[];
+  const int log2n = L.log2n[0];
+  const int n = 1 << log2n;
+  double2* x = smem;
+  double2* y = smem + n;
+  const int tid = threadIdx.x;
+  for (long prod = blockIdx.x; prod < count; prod += gridDim.x) {
+    const uint64_t* ap = a + (prod << (log2n + 1));
+    for (int j = tid; j < n; j += THREADS) {
+      const c64 v{i64_to_f64_rne((int64_t)__ldcs(ap + j)), i64_to_f64_rne((int64_t)__ldcs(ap + j + n))};
+      st(x + j, cmul(ldg(tw + j), v));
+    }
+    __syncthreads();
+    double2* r = unordered_smem<true>(L, 0, base_algo, 1, x, y, w, tid, THREADS);
+    const double2* bp = bhat + prod * bhat_stride;
+    for (int k = tid; k < n; k += THREADS) st(r + k, cmul(ldg(bp + k), ld(r + k)));
+    __syncthreads();
+    double2* o = (r == x) ? y : x;
+    double2* s = unordered_smem<false>(L, 0, base_algo, 1, r, o, winv, tid, THREADS);
+    uint64_t* op = out + (prod << (log2n + 1));
+    for (int j = tid; j < n; j += THREADS) {
+      const c64 t = cmul(ldg(itw + j), ld(s + j));
+      __stcs(op + j, round_half_up_mod64(t.re));
+      __stcs(op + j + n, round_half_up_mod64(t.im));
+    }
+    __syncthreads();
+  }
+}
+
+// Bhat = fwd(tau^j * (b_j + i b_{j+N/2})) for small signed digits b.
+template <int THREADS>
+__global__ void __launch_bounds__(THREADS) u64_prepare_kernel(const int64_t* __restrict__ b,
+                                                             double2* __restrict__ bhat, long count, DevLevels L,
+                                                             int base_algo, const double2* __restrict__ w,
+                                                             const double2* __restrict__ tw) {
+  extern __shared__ double2 smem[];
+  const int log2n = L.log2n[0];
+  const int n = 1 << log2n;
+  double2* x = smem;
+  double2* y = smem + n;
+  const int tid = threadIdx.x;
+  for (long prod = blockIdx.x; prod < count; prod += gridDim.x) {
+    const int64_t* bp = b + (prod << (log2n + 1));
+    for (int j = tid; j < n; j += THREADS) {
+      const c64 v{i64_to_f64_rne(bp[j]), i64_to_f64_rne(bp[j + n])};
+      st(x + j, cmul(ldg(tw + j), v));
+    }
+    __syncthreads();
+    const double2* r = unordered_smem<true>(L, 0, base_algo, 1, x, y, w, tid, THREADS);
+    double2* op = bhat + (prod << log2n);
+    for (int k = tid; k < n; k += THREADS) op[k] = r[k];
+    __syncthreads();
+  }
+}
+
+}  // namespace cfft
+
+struct cfft_u64_product_plan {
+  size_t N = 0, n = 0, base_n = 0;
+  int base_algo = 0;
+  LevelDesc lv{};
+  DevLevels dlv{};
+  double2 *d_w = nullptr, *d_winv = nullptr, *d_tw = nullptr, *d_itw = nullptr;
+  int threads = 128;
+  int blocks_per_sm = 0;  // 0: enough CTAs for every product (capped at SM count x occupancy)
+};
+
+namespace {
+
+constexpr int kProdThreads = 128;
+
+void free_u64(cfft_u64_product_plan* p) {
+  if (p->d_w) cudaFree(p->d_w);
+  if (p->d_winv) cudaFree(p->d_winv);
+  if (p->d_tw) cudaFree(p->d_tw);
+  if (p->d_itw) cudaFree(p->d_itw);
+}
+
+DevLevels dev_levels(const LevelDesc& l) {
+  DevLevels d;
+  std::memset(&d, 0, sizeof(d));
+  d.nlevels = l.nlevels;
+  for (int i = 0; i <= kMaxLevels; ++i) {
+    d.log2n[i] = l.log2n[i];
+    d.w_off[i] = l.w_off[i];
+  }
+  for (int i = 0; i < kMaxLevels; ++i) {
+    d.log2r[i] = l.log2r[i];
+    d.winv_off[i] = l.winv_off[i];
+  }
+  return d;
+}
+
+bool g_u64_attr = false;
+cfft_status u64_attrs() {
+  if (g_u64_attr) return CFFT_OK;
+  const int max_smem = 2 * (1 << kSmemLog2Max) * (int)sizeof(double2);
+  CFFT_CUDA_TRY(cudaFuncSetAttribute(u64_product_kernel<kProdThreads>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     max_smem));
+  CFFT_CUDA_TRY(cudaFuncSetAttribute(u64_prepare_kernel<kProdThreads>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     max_smem));
+  g_u64_attr = true;
+  return CFFT_OK;
+}
+
+int grid_for(const void* kernel, int threads, size_t smem, long count) {
+  int per_sm = 0;
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, threads, smem);
+  per_sm = std::max(per_sm, 1);
+  const long cap = (long)sm_count() * per_sm;
+  return (int)std::max<long>(1, std::min<long>(count, cap));
+}
+
+}  // namespace
+
+extern "C" {
+
+cfft_status cfft_u64_product_plan_create(size_t N, cfft_algo base_algo, size_t base_n, cfft_u64_product_plan** out) {
+  if (!out) return fail(CFFT_ERR_INVALID_ARGUMENT, "null output pointer");
+  *out = nullptr;
+  if (!is_pow2(N) || N < 64 || ilog2(N) > kSmemLog2Max + 1)
+    return fail(CFFT_ERR_INVALID_SIZE, "u64 product: N must be a power of two in [64, 8192]");
+  const size_t n = N / 2;
+  if (!is_pow2(base_n) || base_n > n || (base_n != n && base_n < 32) || ilog2(base_n) > 10)
+    return fail(CFFT_ERR_INVALID_ARGUMENT, "u64 product: invalid base_n");
+  if (base_algo < 0 || base_algo > 7) return fail(CFFT_ERR_INVALID_ARGUMENT, "unknown FftAlgo");
+  cfft_status st = u64_attrs();
+  if (st != CFFT_OK) return st;
+  auto* p = new cfft_u64_product_plan();
+  p->N = N;
+  p->n = n;
+  p->base_n = base_n;
+  p->base_algo = base_algo;
+  p->lv = make_levels(n, base_n);
+  p->dlv = dev_levels(p->lv);
+  std::vector<c64h> w(n + base_n), wi(n + base_n), tw(n), itw(n);
+  unordered_twiddles(n, base_n, algo_radix(base_algo), w.data(), wi.data());
+  const double inv_n = 1.0 / (double)n;
+  for (size_t j = 0; j < n; ++j) {
+    double s, c;
+    sincospi64((double)j / (double)N, &s, &c);
+    tw[j] = c64h{c, s};
+    itw[j] = c64h{c * inv_n, -s * inv_n};  // exact: inv_n is a power of two
+  }
+  st = upload((const double2*)w.data(), n + base_n, &p->d_w);
+  if (st == CFFT_OK) st = upload((const double2*)wi.data(), n + base_n, &p->d_winv);
+  if (st == CFFT_OK) st = upload((const double2*)tw.data(), n, &p->d_tw);
+  if (st == CFFT_OK) st = upload((const double2*)itw.data(), n, &p->d_itw);
+  if (st != CFFT_OK) {
+    free_u64(p);
+    delete p;
+    return st;
+  }
+  *out = p;
+  return CFFT_OK;
+}
+
+void cfft_u64_product_plan_destroy(cfft_u64_product_plan* plan) {
+  if (!plan) return;
+  free_u64(plan);
+  delete plan;
+}
+
+size_t cfft_u64_product_poly_size(const cfft_u64_product_plan* plan) { return plan ? plan->N : 0; }
+void cfft_u64_product_algo(const cfft_u64_product_plan* plan, cfft_algo* base_algo, size_t* base_n) {
+  if (!plan) return;
+  if (base_algo) *base_algo = (cfft_algo)plan->base_algo;
+  if (base_n) *base_n = plan->base_n;
+}
+
+cfft_status cfft_u64_prepare_operand(const cfft_u64_product_plan* plan, const int64_t* b, double* bhat, size_t count,
+                                     void* stream) {
+  if (!plan || !b || !bhat) return fail(CFFT_ERR_INVALID_ARGUMENT, "null argument");
+  if (count == 0) return CFFT_OK;
+  const size_t smem = 2 * plan->n * sizeof(double2);
+  const int grid = grid_for((const void*)u64_prepare_kernel<kProdThreads>, kProdThreads, smem, (long)count);
+  u64_prepare_kernel<kProdThreads><<<grid, kProdThreads, smem, (cudaStream_t)stream>>>(
+      b, (double2*)bhat, (long)count, plan->dlv, plan->base_algo, plan->d_w, plan->d_tw);
+  CFFT_CHECK_LAUNCH();
+  return CFFT_OK;
+}
+
+cfft_status cfft_u64_product(const cfft_u64_product_plan* plan, const uint64_t* a, const double* bhat,
+                             size_t bhat_stride, uint64_t* out, size_t count, void* stream) {
+  if (!plan || !a || !bhat || !out) return fail(CFFT_ERR_INVALID_ARGUMENT, "null argument");
+  if (bhat_stride != 0 && bhat_stride != plan->n)
+    return fail(CFFT_ERR_INVALID_ARGUMENT, "bhat_stride must be 0 or N/2");
+  if (count == 0) return CFFT_OK;
+  const size_t smem = 2 * plan->n * sizeof(double2);
+  const int grid = grid_for((const void*)u64_product_kernel<kProdThreads>, kProdThreads, smem, (long)count);
+  u64_product_kernel<kProdThreads><<<grid, kProdThreads, smem, (cudaStream_t)stream>>>(
+      a, (const double2*)bhat, (long)bhat_stride, out, (long)count, plan->dlv, plan->base_algo, plan->d_w,
+      plan->d_winv, plan->d_tw, plan->d_itw);
+  CFFT_CHECK_LAUNCH();
+  return CFFT_OK;
+}
+
+// Method::Measure for the product: every (base_algo, base_n) the reference's
+// unordered measurement considers for n = N/2 (src/unordered.rs:553-640: the
+// ordered algorithms at n when n <= 256, else bases 512 and 1024), timed on
+// the fused product kernel itself over a batch that fills every SM.
+cfft_status cfft_u64_product_plan_create_measure(size_t N, double seconds, cfft_u64_product_plan** out) {
+  if (!out) return fail(CFFT_ERR_INVALID_ARGUMENT, "null output pointer");
+  *out = nullptr;
+  if (!is_pow2(N) || N < 64 || ilog2(N) > kSmemLog2Max + 1)
+    return fail(CFFT_ERR_INVALID_SIZE, "u64 product: N must be a power of two in [64, 8192]");
+  const size_t n = N / 2;
+  std::vector<size_t> bases;
+  if (n <= 256) bases.push_back(n);
+  else
+    for (size_t b : {size_t(512), size_t(1024)})
+      if (b <= n) bases.push_back(b);
+  const size_t count = (size_t)sm_count() * 8;
+  uint64_t *da = nullptr, *dout = nullptr;
+  double* dbhat = nullptr;
+  CFFT_CUDA_TRY(cudaMalloc(&da, count * N * sizeof(uint64_t)));
+  CFFT_CUDA_TRY(cudaMalloc(&dout, count * N * sizeof(uint64_t)));
+  CFFT_CUDA_TRY(cudaMalloc(&dbhat, count * n * sizeof(double2)));
+  CFFT_CUDA_TRY(cudaMemset(da, 0, count * N * sizeof(uint64_t)));
+  CFFT_CUDA_TRY(cudaMemset(dbhat, 0, count * n * sizeof(double2)));
+  cudaStream_t s;
+  CFFT_CUDA_TRY(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
+  cudaEvent_t e0, e1;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  double best = 1e30;
+  int best_algo = 0;
+  size_t best_base = bases.front();
+  cfft_status st = CFFT_OK;
+  for (size_t base : bases) {
+    for (int algo = 0; algo < 8 && st == CFFT_OK; ++algo) {
+      cfft_u64_product_plan* p = nullptr;
+      st = cfft_u64_product_plan_create(N, (cfft_algo)algo, base, &p);
+      if (st != CFFT_OK) break;
+      cfft_u64_product(p, da, dbhat, n, dout, count, s);  // warm-up
+      int reps = 1;
+      double per = 0;
+      for (;;) {
+        cudaEventRecord(e0, s);
+        for (int r = 0; r < reps; ++r) cfft_u64_product(p, da, dbhat, n, dout, count, s);
+        cudaEventRecord(e1, s);
+        cudaEventSynchronize(e1);
+        float ms = 0;
+        cudaEventElapsedTime(&ms, e0, e1);
+        per = ms / reps;
+        if (ms * 1e-3 >= std::max(seconds, 1e-3) || reps >= 4096) break;
+        reps *= 2;
+      }
+      if (per < best) {
+        best = per;
+        best_algo = algo;
+        best_base = base;
+      }
+      cfft_u64_product_plan_destroy(p);
+    }
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  cudaStreamDestroy(s);
+  cudaFree(da);
+  cudaFree(dout);
+  cudaFree(dbhat);
+  if (st != CFFT_OK) return st;
+  return cfft_u64_product_plan_create(N, (cfft_algo)best_algo, best_base, out);
+}
+
+cfft_status cfft_u64_product_host(const cfft_u64_product_plan* plan, const uint64_t* a, const double* bhat,
+                                  size_t bhat_stride, uint64_t* out, size_t count) {
+  if (!plan || !a || !bhat || !out) return fail(CFFT_ERR_INVALID_ARGUMENT, "null argument");
+  if (count == 0) return CFFT_OK;
+  const size_t bytes = count * plan->N * sizeof(uint64_t);
+  void* d;
+  cudaStream_t s;
+  cfft_status st = host_staging(2 * bytes, &d, &s);
+  if (st != CFFT_OK) return st;
+  uint64_t* da = (uint64_t*)d;
+  uint64_t* dout = (uint64_t*)((char*)d + bytes);
+  CFFT_CUDA_TRY(cudaMemcpyAsync(da, a, bytes, cudaMemcpyHostToDevice, s));
+  st = cfft_u64_product(plan, da, bhat, bhat_stride, dout, count, s);
+  if (st != CFFT_OK) return st;
+  CFFT_CUDA_TRY(cudaMemcpyAsync(out, dout, bytes, cudaMemcpyDeviceToHost, s));
+  CFFT_CUDA_TRY(cudaStreamSynchronize(s));
+  return CFFT_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,50 @@
+// runtime.h -- host runtime helpers shared by the CUDA translation units.
+#pragma once
+#include <cuda_runtime.h>
+
+#include <cstdio>
+#include <string>
+
+#include "cfft_internal.h"
+
+#define CFFT_CUDA_TRY(expr)                                                                  \
+  do {                                                                                       \
+    cudaError_t err__ = (expr);                                                              \
+    if (err__ != cudaSuccess) {                                                              \
+      ::cfft::set_error(std::string(#expr) + ": " + cudaGetErrorString(err__));              \
+      return err__ == cudaErrorMemoryAllocation ? CFFT_ERR_OUT_OF_MEMORY : CFFT_ERR_CUDA;    \
+    }                                                                                        \
+  } while (0)
+
+#define CFFT_CHECK_LAUNCH()                                                                  \
+  do {                                                                                       \
+    cudaError_t err__ = cudaGetLastError();                                                  \
+    if (err__ != cudaSuccess) {                                                              \
+      ::cfft::set_error(std::string("kernel launch: ") + cudaGetErrorString(err__));         \
+      return CFFT_ERR_CUDA;                                                                  \
+    }                                                                                        \
+  } while (0)
+
+namespace cfft {
+
+inline cfft_status fail(cfft_status s, const std::string& msg) {
+  set_error(msg);
+  return s;
+}
+
+// Device-resident copy of a host table.
+template <class T>
+cfft_status upload(const T* host, size_t count, T** dev) {
+  *dev = nullptr;
+  if (count == 0) return CFFT_OK;
+  CFFT_CUDA_TRY(cudaMalloc((void**)dev, count * sizeof(T)));
+  CFFT_CUDA_TRY(cudaMemcpy(*dev, host, count * sizeof(T), cudaMemcpyHostToDevice));
+  return CFFT_OK;
+}
+
+int sm_count();
+
+// Persistent scratch for the *_host convenience entry points (one per thread).
+cfft_status host_staging(size_t bytes, void** dev_ptr, cudaStream_t* stream);
+
+}  // namespace cfft

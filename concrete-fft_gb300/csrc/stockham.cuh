@@ -1,0 +1,248 @@
+// stockham.cuh -- the reference's transform structure, executed by one CTA.
+//
+// A CTA owns `nchunks` independent transforms of 2^log2n points stored back to
+// back in shared memory and runs the reference's passes over all of them at
+// once: every pass is a loop of radix-R butterflies over the CTA's threads,
+// ping-ponging between two shared buffers, with one barrier per pass.  The
+// unordered outer passes (radix 2/4/8 over the whole transform, src/
+// unordered.rs:222-293) run in place before (forward) or after (inverse) the
+// ordered base transforms.
+#pragma once
+#include "cfft_device.cuh"
+
+namespace cfft {
+
+template <int R>
+struct Log2;
+template <>
+struct Log2<2> {
+  static constexpr int v = 1;
+};
+template <>
+struct Log2<4> {
+  static constexpr int v = 2;
+};
+template <>
+struct Log2<8> {
+  static constexpr int v = 3;
+};
+template <>
+struct Log2<16> {
+  static constexpr int v = 4;
+};
+
+// One generic Stockham pass of radix R at stride s = 2^log2s
+// (src/dif4.rs:118-168 for DIF, src/dit4.rs:94-140 for DIT, same for radix 2/8/16).
+// DIF: in[k] = src[k*n/R + p*s + q], dst[R*s*p + k*s + q] = w_k * core(in)_k.
+// DIT: in[k] = w_k * src[R*s*p + k*s + q], dst[k*n/R + p*s + q] = core(in)_k.
+// w is the second half of the init_wt table: w_k = w[R*s*p + k].
+template <int R, bool FWD, bool DIT>
+__device__ __forceinline__ void stockham_pass(int log2n, int log2s, int nchunks, const double2* src, double2* dst,
+                                              const double2* __restrict__ w, int tid, int nth) {
+  constexpr int LR = Log2<R>::v;
+  const int lper = log2n - LR;  // log2(n / R): butterflies per chunk
+  const int total = nchunks << lper;
+  const int smask = (1 << log2s) - 1;
+  for (int b = tid; b < total; b += nth) {
+    const int c = b >> lper;
+    const int bb = b & ((1 << lper) - 1);
+    const int p = bb >> log2s;
+    const int q = bb & smask;
+    const double2* sc = src + (c << log2n);
+    double2* dc = dst + (c << log2n);
+    const double2* tw = w + (p << (log2s + LR));
+    c64 v[R];
+    if (!DIT) {
+#pragma unroll
+      for (int k = 0; k < R; ++k) v[k] = ld(sc + (k << lper) + (p << log2s) + q);
+      Core<R, FWD>::run(v);
+      double2* o = dc + (p << (log2s + LR)) + q;
+      st(o, v[0]);
+#pragma unroll
+      for (int k = 1; k < R; ++k) st(o + (k << log2s), cmul(ldg(tw + k), v[k]));
+    } else {
+      const double2* i0 = sc + (p << (log2s + LR)) + q;
+      v[0] = ld(i0);
+#pragma unroll
+      for (int k = 1; k < R; ++k) v[k] = cmul(ldg(tw + k), ld(i0 + (k << log2s)));
+      Core<R, FWD>::run(v);
+#pragma unroll
+      for (int k = 0; k < R; ++k) st(dc + (k << lper) + (p << log2s) + q, v[k]);
+    }
+  }
+}
+
+// End butterfly of size M at stride n/M, in place (src/dif4.rs:195-244 and twins).
+template <int M, bool FWD>
+__device__ __forceinline__ void end_pass(int log2n, int nchunks, double2* x, int tid, int nth) {
+  constexpr int LM = Log2<M>::v;
+  const int log2s = log2n - LM;
+  const int total = nchunks << log2s;
+  const int smask = (1 << log2s) - 1;
+  for (int g = tid; g < total; g += nth) {
+    double2* xc = x + ((g >> log2s) << log2n) + (g & smask);
+    c64 v[M];
+#pragma unroll
+    for (int k = 0; k < M; ++k) v[k] = ld(xc + (k << log2s));
+    Core<M, FWD>::run(v);
+#pragma unroll
+    for (int k = 0; k < M; ++k) st(xc + (k << log2s), v[k]);
+  }
+}
+
+template <int R, bool FWD>
+__device__ __forceinline__ void end_dispatch(int lm, int log2n, int nchunks, double2* x, int tid, int nth) {
+  if (lm == 1) end_pass<2, FWD>(log2n, nchunks, x, tid, nth);
+  if constexpr (R >= 4) {
+    if (lm == 2) end_pass<4, FWD>(log2n, nchunks, x, tid, nth);
+  }
+  if constexpr (R >= 8) {
+    if (lm == 3) end_pass<8, FWD>(log2n, nchunks, x, tid, nth);
+  }
+  if constexpr (R >= 16) {
+    if (lm == 4) end_pass<16, FWD>(log2n, nchunks, x, tid, nth);
+  }
+}
+
+// The ordered transform of src/dif{R}.rs / src/dit{R}.rs (recursion e.g.
+// src/dif4.rs:285-303): DIF runs radix-R passes at s = 1, R, R^2, ... while the
+// remaining size exceeds R, then the end butterfly of the remaining size; DIT
+// runs the end butterfly first at the largest stride, then the passes in
+// reverse.  Returns the buffer (x or y) that holds the result.
+template <int R, bool FWD, bool DIT>
+__device__ double2* stockham_smem(int log2n, int nchunks, double2* x, double2* y, const double2* __restrict__ w,
+                                  int tid, int nth) {
+  constexpr int LR = Log2<R>::v;
+  if (log2n == 0) return x;
+  int lm = log2n, npass = 0;
+  while (lm > LR) {
+    lm -= LR;
+    ++npass;
+  }
+  double2* cur = x;
+  double2* oth = y;
+  if (!DIT) {
+    for (int i = 0; i < npass; ++i) {
+      stockham_pass<R, FWD, false>(log2n, i * LR, nchunks, cur, oth, w, tid, nth);
+      __syncthreads();
+      double2* t = cur;
+      cur = oth;
+      oth = t;
+    }
+    end_dispatch<R, FWD>(lm, log2n, nchunks, cur, tid, nth);
+    __syncthreads();
+  } else {
+    end_dispatch<R, FWD>(lm, log2n, nchunks, cur, tid, nth);
+    __syncthreads();
+    for (int i = npass - 1; i >= 0; --i) {
+      stockham_pass<R, FWD, true>(log2n, i * LR, nchunks, cur, oth, w, tid, nth);
+      __syncthreads();
+      double2* t = cur;
+      cur = oth;
+      oth = t;
+    }
+  }
+  return cur;
+}
+
+template <bool FWD>
+__device__ double2* ordered_dispatch(int algo, int log2n, int nchunks, double2* x, double2* y,
+                                     const double2* __restrict__ w, int tid, int nth) {
+  switch (algo) {
+    case 0: return stockham_smem<2, FWD, false>(log2n, nchunks, x, y, w, tid, nth);
+    case 1: return stockham_smem<2, FWD, true>(log2n, nchunks, x, y, w, tid, nth);
+    case 2: return stockham_smem<4, FWD, false>(log2n, nchunks, x, y, w, tid, nth);
+    case 3: return stockham_smem<4, FWD, true>(log2n, nchunks, x, y, w, tid, nth);
+    case 4: return stockham_smem<8, FWD, false>(log2n, nchunks, x, y, w, tid, nth);
+    case 5: return stockham_smem<8, FWD, true>(log2n, nchunks, x, y, w, tid, nth);
+    case 6: return stockham_smem<16, FWD, false>(log2n, nchunks, x, y, w, tid, nth);
+    default: return stockham_smem<16, FWD, true>(log2n, nchunks, x, y, w, tid, nth);
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Unordered outer passes (src/unordered.rs:222-293).  A level of size
+// nl = 2^log2nl splits each chunk into r slices of m = nl/r points.  Forward:
+// butterfly inputs z[k*m + i], outputs (twiddled after the core) stored to
+// slot bitrev(k); inverse: inputs read from slot bitrev(k), twiddled before the
+// core, outputs to z[k*m + i].  Level twiddles: w_k = wl[(r-1)*i + k-1].
+template <int R>
+__device__ __forceinline__ int slot(int k) {
+  if constexpr (R == 2) return k;
+  if constexpr (R == 4) return ((k & 1) << 1) | (k >> 1);
+  return ((k & 1) << 2) | (k & 2) | (k >> 2);
+}
+
+template <int R, bool FWD>
+__device__ __forceinline__ void outer_group(double2* zc, int lm, int i, const double2* __restrict__ wl) {
+  c64 v[R];
+  const double2* tw = wl + (R - 1) * i - 1;  // tw[k] = w_k, k >= 1
+  if (FWD) {
+#pragma unroll
+    for (int k = 0; k < R; ++k) v[k] = ld(zc + (k << lm) + i);
+    Core<R, true>::run(v);
+#pragma unroll
+    for (int k = 1; k < R; ++k) v[k] = cmul(ldg(tw + k), v[k]);
+#pragma unroll
+    for (int k = 0; k < R; ++k) st(zc + (slot<R>(k) << lm) + i, v[k]);
+  } else {
+    v[0] = ld(zc + i);
+#pragma unroll
+    for (int k = 1; k < R; ++k) v[k] = cmul(ldg(tw + k), ld(zc + (slot<R>(k) << lm) + i));
+    Core<R, false>::run(v);
+#pragma unroll
+    for (int k = 0; k < R; ++k) st(zc + (k << lm) + i, v[k]);
+  }
+}
+
+// One level over `nchunks` chunks of 2^log2nl points stored back to back.
+template <bool FWD>
+__device__ __forceinline__ void outer_level(int log2r, int log2nl, int nchunks, double2* z,
+                                            const double2* __restrict__ wl, int tid, int nth) {
+  const int lm = log2nl - log2r;
+  const int total = nchunks << lm;
+  for (int g = tid; g < total; g += nth) {
+    double2* zc = z + ((g >> lm) << log2nl);
+    const int i = g & ((1 << lm) - 1);
+    if (log2r == 1) outer_group<2, FWD>(zc, lm, i, wl);
+    else if (log2r == 2) outer_group<4, FWD>(zc, lm, i, wl);
+    else outer_group<8, FWD>(zc, lm, i, wl);
+  }
+}
+
+// Device copy of the level structure (see LevelDesc in cfft_internal.h).
+struct DevLevels {
+  int nlevels;
+  int log2n[9];
+  int log2r[8];
+  int w_off[9];
+  int winv_off[8];
+};
+
+// Unordered transform of `nchunks` (sub)transforms of size n_{d0} held in x:
+// fwd_depth (src/unordered.rs:392-439) or inv_depth (:442-489) from level d0.
+// w: the plan's forward table (forward) or inverse table (inverse).
+template <bool FWD>
+__device__ double2* unordered_smem(const DevLevels& L, int d0, int base_algo, int nchunks, double2* x, double2* y,
+                                   const double2* __restrict__ w, int tid, int nth) {
+  const int log2base = L.log2n[L.nlevels];
+  const int log2sub = L.log2n[d0];
+  const int nbase = nchunks << (log2sub - log2base);
+  if (FWD) {
+    for (int l = d0; l < L.nlevels; ++l) {
+      outer_level<true>(L.log2r[l], L.log2n[l], nchunks << (log2sub - L.log2n[l]), x, w + L.w_off[l], tid, nth);
+      __syncthreads();
+    }
+    return ordered_dispatch<true>(base_algo, log2base, nbase, x, y, w + L.w_off[L.nlevels] + (1 << log2base), tid,
+                                  nth);
+  } else {
+    double2* r = ordered_dispatch<false>(base_algo, log2base, nbase, x, y, w + (1 << log2base), tid, nth);
+    for (int l = L.nlevels - 1; l >= d0; --l) {
+      outer_level<false>(L.log2r[l], L.log2n[l], nchunks << (log2sub - L.log2n[l]), r, w + L.winv_off[l], tid, nth);
+      __syncthreads();
+    }
+    return r;
+  }
+}
+
+}  // namespace cfft

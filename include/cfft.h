@@ -1,0 +1,189 @@
+/*
+ * cfft.h -- C ABI of the GB300 implementation of concrete-fft's FFT hot path.
+ *
+ * One shared library, libcfft_gb300.so (sm_103a).  Every entry point takes
+ * plain pointers, sizes and a CUDA stream passed as `void*` (a cudaStream_t,
+ * NULL = the legacy default stream), and returns a cfft_status.  The reference
+ * crate (zama-ai/concrete-fft v0.5.1) panics where this ABI returns an error
+ * code; cfft_last_error() gives the message.
+ *
+ * Buffers: a "c64" buffer is interleaved (re, im) f64 pairs, 16 bytes per
+ * point, the memory layout of num_complex::Complex64.  Batched calls process
+ * `batch` transforms stored back to back.  Functions without a `_host` suffix
+ * take DEVICE pointers and are asynchronous on `stream`; `_host` functions take
+ * host pointers, copy in and out and return when the result is in host memory
+ * (the shape of the reference's slice API, `fwd(&self, buf: &mut [c64], ..)`).
+ *
+ * Results: the transforms are bit-identical to the reference's output for the
+ * same algorithm, size and base size (the GPU executes the reference's exact
+ * operation sequence in IEEE FP64, with the reference's twiddle tables).
+ *
+ * Plans are immutable after creation and may be shared across threads, like
+ * the reference's `Plan: Clone + Send + Sync`.
+ */
+#ifndef CFFT_H
+#define CFFT_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum cfft_status {
+  CFFT_OK = 0,
+  CFFT_ERR_INVALID_SIZE = -1,      /* not a power of two, or outside the plan's range */
+  CFFT_ERR_INVALID_ARGUMENT = -2,  /* null pointer, unknown algorithm, bad base size */
+  CFFT_ERR_LENGTH_MISMATCH = -3,   /* buffer length differs from the plan's size */
+  CFFT_ERR_CUDA = -4,              /* a CUDA call failed (message in cfft_last_error) */
+  CFFT_ERR_OUT_OF_MEMORY = -5,     /* device allocation failed */
+  CFFT_ERR_NO_DEVICE = -6,         /* no usable sm_103 device */
+  CFFT_ERR_TIMEOUT = -7            /* a bounded device wait expired */
+} cfft_status;
+
+/* ordered::FftAlgo (src/ordered.rs:28-45), same discriminant order. */
+typedef enum cfft_algo {
+  CFFT_DIF2 = 0,
+  CFFT_DIT2 = 1,
+  CFFT_DIF4 = 2,
+  CFFT_DIT4 = 3,
+  CFFT_DIF8 = 4,
+  CFFT_DIT8 = 5,
+  CFFT_DIF16 = 6,
+  CFFT_DIT16 = 7
+} cfft_algo;
+
+/* Human-readable text of the last error on any thread (never NULL). */
+const char* cfft_last_error(void);
+/* Library version string. */
+const char* cfft_version(void);
+/* 0 when a device of compute capability 10.3 is usable, else a cfft_status. */
+cfft_status cfft_device_check(void);
+
+/* ======================================================= ordered::Plan ====
+ * Replaces src/ordered.rs:187-373.  Sizes: powers of two, 1 <= n <= 1024
+ * (the reference asserts n.trailing_zeros() < 11, src/ordered.rs:244). */
+typedef struct cfft_ordered_plan cfft_ordered_plan;
+
+/* Plan::new(n, Method::UserProvided(algo)) -- src/ordered.rs:242-278 */
+cfft_status cfft_ordered_plan_create(size_t n, cfft_algo algo, cfft_ordered_plan** out);
+/* Plan::new(n, Method::Measure(duration)) -- src/ordered.rs:99-180: times every
+ * algorithm on the GPU for about `seconds_per_algo` each and keeps the fastest. */
+cfft_status cfft_ordered_plan_create_measure(size_t n, double seconds_per_algo, cfft_ordered_plan** out);
+void cfft_ordered_plan_destroy(cfft_ordered_plan* plan);
+/* Plan::fft_size -- src/ordered.rs:291 */
+size_t cfft_ordered_fft_size(const cfft_ordered_plan* plan);
+/* Plan::algo -- src/ordered.rs:305 */
+cfft_algo cfft_ordered_algo(const cfft_ordered_plan* plan);
+/* Plan::fft_scratch -- src/ordered.rs:320-322: bytes of caller scratch a call
+ * needs.  The GPU path keeps its scratch in shared memory: always 0. */
+size_t cfft_ordered_scratch_bytes(const cfft_ordered_plan* plan);
+/* Plan::fwd / Plan::inv -- src/ordered.rs:342-373, batched, in place, unnormalised. */
+cfft_status cfft_ordered_fwd(const cfft_ordered_plan* plan, double* buf, size_t batch, void* stream);
+cfft_status cfft_ordered_inv(const cfft_ordered_plan* plan, double* buf, size_t batch, void* stream);
+cfft_status cfft_ordered_fwd_host(const cfft_ordered_plan* plan, double* buf, size_t batch);
+cfft_status cfft_ordered_inv_host(const cfft_ordered_plan* plan, double* buf, size_t batch);
+
+/* ===================================================== unordered::Plan ====
+ * Replaces src/unordered.rs:496-1036.  Any power-of-two n up to 2^20 with a
+ * base (internal ordered) size base_n <= 1024, base_n >= 32 unless base_n == n
+ * (src/unordered.rs:660-670). */
+typedef struct cfft_unordered_plan cfft_unordered_plan;
+
+/* Plan::new(n, Method::UserProvided { base_algo, base_n }) -- src/unordered.rs:659-747 */
+cfft_status cfft_unordered_plan_create(size_t n, cfft_algo base_algo, size_t base_n, cfft_unordered_plan** out);
+/* Plan::new(n, Method::Measure(duration)) -- src/unordered.rs:540-640: GPU timing
+ * of bases 512/1024 (n > 256) or every ordered algorithm (n <= 256). */
+cfft_status cfft_unordered_plan_create_measure(size_t n, double seconds_per_algo, cfft_unordered_plan** out);
+void cfft_unordered_plan_destroy(cfft_unordered_plan* plan);
+/* Plan::fft_size -- src/unordered.rs:770 */
+size_t cfft_unordered_fft_size(const cfft_unordered_plan* plan);
+/* Plan::algo -- src/unordered.rs:793: (base_algo, base_n) */
+void cfft_unordered_algo(const cfft_unordered_plan* plan, cfft_algo* base_algo, size_t* base_n);
+/* Plan::fft_scratch -- src/unordered.rs:798-800 (0: scratch is on chip or plan-owned) */
+size_t cfft_unordered_scratch_bytes(const cfft_unordered_plan* plan);
+/* Plan::fwd -- src/unordered.rs:826-839: standard order in, permuted order out. */
+cfft_status cfft_unordered_fwd(const cfft_unordered_plan* plan, double* buf, size_t batch, void* stream);
+/* Plan::inv -- src/unordered.rs:927-940: permuted order in, standard order out. */
+cfft_status cfft_unordered_inv(const cfft_unordered_plan* plan, double* buf, size_t batch, void* stream);
+cfft_status cfft_unordered_fwd_host(const cfft_unordered_plan* plan, double* buf, size_t batch);
+cfft_status cfft_unordered_inv_host(const cfft_unordered_plan* plan, double* buf, size_t batch);
+/* Plan::fwd_monomial -- src/unordered.rs:844-900: FFT of X^degree, permuted order. */
+cfft_status cfft_unordered_fwd_monomial(const cfft_unordered_plan* plan, size_t degree, double* buf, void* stream);
+cfft_status cfft_unordered_fwd_monomial_host(const cfft_unordered_plan* plan, size_t degree, double* buf);
+/* serialize_fourier_buffer's element order -- src/unordered.rs:951-970:
+ * standard[i] = permuted[bit_rev_twice(i)], batch buffers, out of place. */
+cfft_status cfft_unordered_to_standard(const cfft_unordered_plan* plan, const double* permuted, double* standard,
+                                       size_t batch, void* stream);
+/* deserialize_fourier_buffer's element order -- src/unordered.rs:981-1036. */
+cfft_status cfft_unordered_from_standard(const cfft_unordered_plan* plan, const double* standard, double* permuted,
+                                         size_t batch, void* stream);
+cfft_status cfft_unordered_to_standard_host(const cfft_unordered_plan* plan, const double* permuted,
+                                            double* standard, size_t batch);
+cfft_status cfft_unordered_from_standard_host(const cfft_unordered_plan* plan, const double* standard,
+                                              double* permuted, size_t batch);
+
+/* ======================================================== fft128::Plan ====
+ * Replaces src/fft128/mod.rs:1832-1960.  n a power of two, 32 <= n <= 8192.
+ * Split double-double storage: four f64 arrays (re0, re1, im0, im1), each
+ * batch * n long; forward output is in bit-reversed order, inverse is
+ * unnormalised. */
+typedef struct cfft_f128_plan cfft_f128_plan;
+cfft_status cfft_f128_plan_create(size_t n, cfft_f128_plan** out);
+void cfft_f128_plan_destroy(cfft_f128_plan* plan);
+size_t cfft_f128_fft_size(const cfft_f128_plan* plan);
+cfft_status cfft_f128_fwd(const cfft_f128_plan* plan, double* re0, double* re1, double* im0, double* im1,
+                          size_t batch, void* stream);
+cfft_status cfft_f128_inv(const cfft_f128_plan* plan, double* re0, double* re1, double* im0, double* im1,
+                          size_t batch, void* stream);
+cfft_status cfft_f128_fwd_host(const cfft_f128_plan* plan, double* re0, double* re1, double* im0, double* im1,
+                               size_t batch);
+cfft_status cfft_f128_inv_host(const cfft_f128_plan* plan, double* re0, double* re1, double* im0, double* im1,
+                               size_t batch);
+
+/* ================================================ negacyclic products ====
+ * The reference's caller (TFHE-rs) builds polynomial products mod X^N + 1 on
+ * unordered::Plan (u64 torus) and fft128::Plan (u128 torus); the crate itself
+ * has no product code.  These entry points fuse that whole pipeline into one
+ * kernel: fold N coefficients into N/2 complex points, twist, forward FFT,
+ * pointwise product with a device-resident Fourier operand, inverse FFT,
+ * untwist, exact rounding back to the integer ring.
+ *
+ * u64: coefficients are read as i64, rounded with floor(x + 1/2) and reduced
+ * mod 2^64.  N a power of two, 64 <= N <= 8192.  bhat holds N/2 c64 per
+ * operand in the plan's permuted order; `bhat_stride` is 0 (one operand shared
+ * by all products) or N/2 (one operand per product). */
+typedef struct cfft_u64_product_plan cfft_u64_product_plan;
+cfft_status cfft_u64_product_plan_create(size_t N, cfft_algo base_algo, size_t base_n, cfft_u64_product_plan** out);
+cfft_status cfft_u64_product_plan_create_measure(size_t N, double seconds_per_algo, cfft_u64_product_plan** out);
+void cfft_u64_product_plan_destroy(cfft_u64_product_plan* plan);
+size_t cfft_u64_product_poly_size(const cfft_u64_product_plan* plan);
+void cfft_u64_product_algo(const cfft_u64_product_plan* plan, cfft_algo* base_algo, size_t* base_n);
+/* b: `count` polynomials of N signed digits -> bhat: count * N/2 c64. */
+cfft_status cfft_u64_prepare_operand(const cfft_u64_product_plan* plan, const int64_t* b, double* bhat, size_t count,
+                                     void* stream);
+/* out[i] = a[i] * B_i mod (X^N + 1), i < count; a, out: count * N u64. */
+cfft_status cfft_u64_product(const cfft_u64_product_plan* plan, const uint64_t* a, const double* bhat,
+                             size_t bhat_stride, uint64_t* out, size_t count, void* stream);
+/* Host buffers for a and out (bhat stays device-resident). */
+cfft_status cfft_u64_product_host(const cfft_u64_product_plan* plan, const uint64_t* a, const double* bhat,
+                                  size_t bhat_stride, uint64_t* out, size_t count);
+
+/* u128: coefficients as little-endian (lo, hi) u64 pairs read as i128,
+ * double-double arithmetic around fft128::Plan(N/2), floor(x + 1/2) mod 2^128.
+ * 64 <= N <= 8192.  bhat holds 4 arrays of N/2 f64 (re0, re1, im0, im1) per
+ * operand; bhat_stride is 0 or 2N (doubles). */
+typedef struct cfft_u128_product_plan cfft_u128_product_plan;
+cfft_status cfft_u128_product_plan_create(size_t N, cfft_u128_product_plan** out);
+void cfft_u128_product_plan_destroy(cfft_u128_product_plan* plan);
+size_t cfft_u128_product_poly_size(const cfft_u128_product_plan* plan);
+cfft_status cfft_u128_prepare_operand(const cfft_u128_product_plan* plan, const int64_t* b, double* bhat4,
+                                      size_t count, void* stream);
+cfft_status cfft_u128_product(const cfft_u128_product_plan* plan, const uint64_t* a, const double* bhat4,
+                              size_t bhat_stride, uint64_t* out, size_t count, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* CFFT_H */

@@ -1,0 +1,21 @@
+/*
+ * cfft_diag.h -- diagnostics of libcfft_gb300.so (no counterpart in the
+ * reference crate, which has no device).
+ */
+#ifndef CFFT_DIAG_H
+#define CFFT_DIAG_H
+#include "cfft.h"
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Measures the device's FP64 issue rate: independent DFMA chains on every SM,
+ * timed with CUDA events.  Writes FP64 instructions per second (one DFMA, DADD
+ * or DMUL each) to *ops_per_second.  The FFT kernels of this library are bound
+ * by this rate on GB300, where FP64 runs at 1/64 of the FP32 rate. */
+cfft_status cfft_diag_fp64_peak(double* ops_per_second);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

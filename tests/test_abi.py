@@ -1,0 +1,62 @@
+"""The C ABI library without a GPU: it loads, exports every declared symbol,
+and rejects invalid arguments before touching the device."""
+import ctypes
+import os
+import re
+
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def declared_functions():
+    txt = "".join(open(os.path.join(ROOT, "include", h)).read() for h in sorted(os.listdir(os.path.join(ROOT, "include")))
+                  if h.endswith(".h"))
+    txt = re.sub(r"/\*.*?\*/", "", txt, flags=re.S)
+    return sorted(set(re.findall(r"\b(cfft_\w+)\s*\(", txt)))
+
+
+def test_every_declared_symbol_is_exported(cfft_lib):
+    names = declared_functions()
+    assert len(names) >= 40
+    for name in names:
+        assert hasattr(cfft_lib, name), name
+
+
+def test_python_signatures_cover_the_header(cfft_lib):
+    import concrete_fft
+    assert sorted(concrete_fft.EXPORTED) == declared_functions()
+
+
+def test_argument_errors_without_device(cfft_lib):
+    h = ctypes.c_void_p()
+    L = cfft_lib
+    assert L.cfft_ordered_plan_create(3, 0, ctypes.byref(h)) == -1           # not a power of two
+    assert L.cfft_ordered_plan_create(2048, 0, ctypes.byref(h)) == -1        # n > 1024 (ordered.rs:244)
+    assert L.cfft_ordered_plan_create(1024, 9, ctypes.byref(h)) == -2        # unknown FftAlgo
+    assert L.cfft_ordered_plan_create(1024, 0, None) == -2
+    assert L.cfft_unordered_plan_create(1024, 2, 16, ctypes.byref(h)) == -2  # base < 32 and != n
+    assert L.cfft_unordered_plan_create(1024, 2, 2048, ctypes.byref(h)) == -2
+    assert L.cfft_unordered_plan_create(1000, 2, 32, ctypes.byref(h)) == -1
+    assert L.cfft_f128_plan_create(16, ctypes.byref(h)) == -1                # n < 32 (fft128/mod.rs:1866)
+    assert L.cfft_u64_product_plan_create(2048, 6, 4096, ctypes.byref(h)) == -2
+    assert L.cfft_u64_product_plan_create(100, 6, 32, ctypes.byref(h)) == -1
+    assert L.cfft_u128_product_plan_create(16384, ctypes.byref(h)) == -1
+    assert b"power of two" in L.cfft_last_error()
+
+
+def test_no_device_is_reported(cfft_lib):
+    import torch
+    if torch.cuda.is_available():
+        pytest.skip("a device is present")
+    assert cfft_lib.cfft_device_check() == -6
+
+
+def test_library_has_no_oracle_dependency():
+    """The product library must not link or load the oracle."""
+    import subprocess
+    import concrete_fft
+    out = subprocess.run(["ldd", concrete_fft.LIB_PATH], capture_output=True, text=True).stdout
+    assert "oracle" not in out
+    strings = open(concrete_fft.LIB_PATH, "rb").read()
+    assert b"liboracle" not in strings

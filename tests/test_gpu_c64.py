@@ -1,0 +1,160 @@
+"""GPU ordered/unordered c64 transforms vs the oracle: bit-identical results."""
+import os
+
+import numpy as np
+import pytest
+
+from conftest import bits
+
+pytestmark = pytest.mark.gpu
+GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+RNG = np.random.default_rng(7)
+
+
+def rand_c64(*shape):
+    return RNG.uniform(-1, 1, shape) + 1j * RNG.uniform(-1, 1, shape)
+
+
+def on_gpu(torch, x):
+    return torch.from_numpy(np.ascontiguousarray(x)).cuda()
+
+
+@pytest.mark.parametrize("algo", range(8))
+def test_ordered_all_sizes_bit_exact(cuda, oracle, algo):
+    import concrete_fft as cf
+    torch = cuda
+    for e in range(0, 11):
+        n = 1 << e
+        plan = cf.ordered.Plan(n, cf.ordered.Method.UserProvided(algo))
+        assert plan.fft_size() == n and plan.algo() == algo and plan.fft_scratch() == 0
+        batch = 3 if n > 64 else 37  # ragged: not a multiple of transforms per CTA
+        x = rand_c64(batch, n)
+        d = on_gpu(torch, x)
+        plan.fwd(d)
+        want = oracle.ordered_fwd(algo, x) if n > 1 else x
+        assert np.array_equal(bits(d.cpu().numpy()), bits(want)), (algo, n)
+        plan.inv(d)
+        want_inv = oracle.ordered_inv(algo, want) if n > 1 else x
+        assert np.array_equal(bits(d.cpu().numpy()), bits(want_inv)), (algo, n)
+
+
+def test_ordered_batch_256_n1024(cuda, oracle):
+    """The N = 1024, batch 256 fwd-then-inv workload."""
+    import concrete_fft as cf
+    torch = cuda
+    x = rand_c64(256, 1024)
+    for algo in (6, 7, 2):
+        plan = cf.ordered.Plan(1024, cf.ordered.Method.UserProvided(algo))
+        d = on_gpu(torch, x)
+        plan.fwd(d)
+        plan.inv(d)
+        want = oracle.ordered_inv(algo, oracle.ordered_fwd(algo, x))
+        assert np.array_equal(bits(d.cpu().numpy()), bits(want))
+        rel = np.linalg.norm(d.cpu().numpy() / 1024 - x) / np.linalg.norm(x)
+        assert rel < 1e-13
+
+
+def test_unordered_golden_vector_on_gpu(cuda):
+    """The reference's exact golden vector (src/unordered.rs:1176-9395) reproduced by the GPU."""
+    import concrete_fft as cf
+    torch = cuda
+    inp = np.load(os.path.join(GOLDEN, "unordered_fwd_n2048_dif4_base32_input.npy"))
+    exp = np.load(os.path.join(GOLDEN, "unordered_fwd_n2048_dif4_base32_expected.npy"))
+    plan = cf.unordered.Plan(2048, cf.unordered.Method.UserProvided(cf.FftAlgo.Dif4, 32))
+    d = on_gpu(torch, inp.copy())
+    plan.fwd(d)
+    assert np.array_equal(bits(d.cpu().numpy()), bits(exp))
+    h = inp.copy()
+    plan.fwd(h)  # host entry point
+    assert np.array_equal(bits(h), bits(exp))
+
+
+CASES = [(32, 32), (64, 32), (256, 32), (1024, 32), (1024, 512), (1024, 1024), (2048, 1024), (4096, 64),
+         (8192, 1024), (16384, 512), (65536, 1024), (65536, 32), (1 << 20, 1024)]
+
+
+@pytest.mark.parametrize("n,base", CASES)
+def test_unordered_bit_exact(cuda, oracle, n, base):
+    import concrete_fft as cf
+    torch = cuda
+    batch = max(1, min(5, (1 << 18) // n))
+    algos = (6, 3) if n < (1 << 18) else (6,)
+    for algo in algos:
+        plan = cf.unordered.Plan(n, cf.unordered.Method.UserProvided(algo, base))
+        x = rand_c64(batch, n)
+        d = on_gpu(torch, x)
+        plan.fwd(d)
+        want = oracle.unordered_fwd(algo, base, x, nthreads=0)
+        assert np.array_equal(bits(d.cpu().numpy()), bits(want)), (n, base, algo)
+        plan.inv(d)
+        want = oracle.unordered_inv(algo, base, want, nthreads=0)
+        assert np.array_equal(bits(d.cpu().numpy()), bits(want)), (n, base, algo)
+        assert np.abs(d.cpu().numpy() / n - x).max() < 1e-12
+
+
+@pytest.mark.parametrize("n", [256, 1024, 4096])
+def test_monomial_and_serde_order(cuda, oracle, n):
+    import concrete_fft as cf
+    torch = cuda
+    for base in {32, n // 4, min(n, 1024)}:
+        plan = cf.unordered.Plan(n, cf.unordered.Method.UserProvided(2, base))
+        for d in RNG.integers(0, n, 3):
+            buf = torch.zeros(n, dtype=torch.complex128, device="cuda")
+            plan.fwd_monomial(int(d), buf)
+            assert np.array_equal(bits(buf.cpu().numpy()), bits(oracle.fwd_monomial(n, base, int(d))))
+        x = rand_c64(2, n)
+        d = on_gpu(torch, x)
+        std = torch.empty_like(d)
+        plan.to_standard(d, std)
+        assert np.array_equal(bits(std.cpu().numpy()), bits(oracle.to_standard(n, base, x)))
+        back = torch.empty_like(d)
+        plan.from_standard(std, back)
+        assert np.array_equal(bits(back.cpu().numpy()), bits(x))
+
+
+def test_serde_roundtrip_across_bases(cuda, oracle):
+    """src/unordered.rs:9399-9466 on the GPU: base-32 forward, standard order, base-64 inverse."""
+    import concrete_fft as cf
+    torch = cuda
+    for n in (64, 128, 256, 512, 1024):
+        p1 = cf.unordered.Plan(n, cf.unordered.Method.UserProvided(2, 32))
+        p2 = cf.unordered.Plan(n, cf.unordered.Method.UserProvided(2, 64))
+        x = rand_c64(n)
+        d = on_gpu(torch, x)
+        p1.fwd(d)
+        std = p1.serialize_fourier_buffer(d)
+        back = torch.empty_like(d)
+        p2.deserialize_fourier_buffer(std, back)
+        p2.inv(back)
+        assert np.abs(back.cpu().numpy() / n - x).max() < 1e-12
+    with pytest.raises(cf.CfftError):
+        p2.deserialize_fourier_buffer(torch.zeros(n - 1, dtype=torch.complex128, device="cuda"), back)
+
+
+def test_measure_plans(cuda, oracle):
+    import concrete_fft as cf
+    torch = cuda
+    p = cf.ordered.Plan(1024, cf.ordered.Method.Measure(0.002))
+    x = rand_c64(4, 1024)
+    d = on_gpu(torch, x)
+    p.fwd(d)
+    assert np.array_equal(bits(d.cpu().numpy()), bits(oracle.ordered_fwd(int(p.algo()), x)))
+    u = cf.unordered.Plan(4096, cf.unordered.Method.Measure(0.002))
+    algo, base = u.algo()
+    assert base in (512, 1024)
+    d = on_gpu(torch, x.reshape(1, 4096))
+    u.fwd(d)
+    assert np.array_equal(bits(d.cpu().numpy()), bits(oracle.unordered_fwd(int(algo), base, x.reshape(1, 4096))))
+
+
+def test_invalid_calls_raise(cuda):
+    import concrete_fft as cf
+    torch = cuda
+    p = cf.ordered.Plan(64, cf.ordered.Method.UserProvided(0))
+    with pytest.raises(ValueError):
+        p.fwd(torch.zeros(65, dtype=torch.complex128, device="cuda"))
+    with pytest.raises(cf.CfftError):
+        cf.ordered.Plan(2048, cf.ordered.Method.UserProvided(0))
+    u = cf.unordered.Plan(64, cf.unordered.Method.UserProvided(0, 64))
+    with pytest.raises(cf.CfftError):
+        u.fwd_monomial(64, torch.zeros(64, dtype=torch.complex128, device="cuda"))

@@ -1,0 +1,100 @@
+"""Fused negacyclic products on the GPU: bit-identical to the oracle's CPU
+pipeline, and torus error against the exact wrapping-integer schoolbook."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+RNG = np.random.default_rng(3)
+
+
+def torus_err_bits(got, exact):
+    d = (got - exact).view(np.int64).astype(np.float64)
+    m = np.abs(d).max()
+    return 0.0 if m == 0 else float(np.log2(m))
+
+
+@pytest.mark.parametrize("N,base_algo,base_n", [(2048, 6, 1024), (2048, 2, 512), (2048, 7, 32), (64, 0, 32),
+                                                (1024, 5, 512), (4096, 6, 1024), (8192, 4, 1024)])
+def test_u64_product_bit_exact(cuda, oracle, N, base_algo, base_n):
+    import concrete_fft as cf
+    torch = cuda
+    count = 9
+    plan = cf.product.U64ProductPlan(N, base_algo, base_n)
+    assert plan.algo() == (base_algo, base_n)
+    a = RNG.integers(0, 2 ** 64, (count, N), dtype=np.uint64)
+    b = RNG.integers(-2 ** 7, 2 ** 7, (count, N))
+    db = torch.from_numpy(b).cuda()
+    bhat = torch.empty((count, N // 2), dtype=torch.complex128, device="cuda")
+    plan.prepare_operand(db, bhat)
+    want_bhat = oracle.u64_prepare(N, base_algo, base_n, b)
+    assert np.array_equal(bhat.cpu().numpy().view(np.uint64), want_bhat.view(np.uint64))
+    da = torch.from_numpy(a.view(np.int64)).cuda()
+    out = torch.empty_like(da)
+    plan.product(da, bhat, out)
+    got = out.cpu().numpy().view(np.uint64)
+    want = oracle.u64_product(N, base_algo, base_n, a, want_bhat, nthreads=0)
+    assert np.array_equal(got, want)
+    exact = oracle.u64_schoolbook(a[:2], b[:2])
+    assert torus_err_bits(got[:2], exact) <= torus_err_bits(want[:2], exact)
+
+
+def test_u64_product_exact_when_small(cuda, oracle):
+    """Bit-exact against the schoolbook wherever the exact sums fit in 53 bits."""
+    import concrete_fft as cf
+    torch = cuda
+    N = 2048
+    plan = cf.product.U64ProductPlan(N, 6, 1024)
+    a = RNG.integers(-2 ** 30, 2 ** 30, (4, N)).astype(np.int64)
+    b = RNG.integers(-2 ** 7, 2 ** 7, (4, N))
+    bhat = torch.empty((4, N // 2), dtype=torch.complex128, device="cuda")
+    plan.prepare_operand(torch.from_numpy(b).cuda(), bhat)
+    out = torch.empty((4, N), dtype=torch.int64, device="cuda")
+    plan.product(torch.from_numpy(a).cuda(), bhat, out)
+    assert np.array_equal(out.cpu().numpy().view(np.uint64), oracle.u64_schoolbook(a.view(np.uint64), b))
+
+
+def test_u64_product_shared_operand_and_host(cuda, oracle):
+    import concrete_fft as cf
+    torch = cuda
+    N = 2048
+    plan = cf.product.U64ProductPlan(N, 6, 1024)
+    a = RNG.integers(0, 2 ** 64, (6, N), dtype=np.uint64)
+    b = RNG.integers(-2 ** 7, 2 ** 7, (1, N))
+    bhat = torch.empty((1, N // 2), dtype=torch.complex128, device="cuda")
+    plan.prepare_operand(torch.from_numpy(b).cuda(), bhat)
+    out = np.zeros_like(a)
+    plan.product(a, bhat, out, shared_operand=True)  # host entry point
+    want = oracle.u64_product(N, 6, 1024, a, oracle.u64_prepare(N, 6, 1024, b))
+    assert np.array_equal(out, want)
+
+
+def test_u64_measure_plan(cuda, oracle):
+    import concrete_fft as cf
+    plan = cf.product.U64ProductPlan(2048, measure_seconds=0.001)
+    algo, base = plan.algo()
+    assert base in (512, 1024) and 0 <= int(algo) <= 7
+
+
+@pytest.mark.parametrize("N", [64, 1024, 4096])
+def test_u128_product_bit_exact(cuda, oracle, N):
+    import concrete_fft as cf
+    torch = cuda
+    count = 3
+    plan = cf.product.U128ProductPlan(N)
+    a = RNG.integers(0, 2 ** 64, (count, N, 2), dtype=np.uint64)
+    b = RNG.integers(-2 ** 15, 2 ** 15, (count, N))
+    bhat = torch.empty((count, 4, N // 2), dtype=torch.float64, device="cuda")
+    plan.prepare_operand(torch.from_numpy(b).cuda(), bhat)
+    want_bhat = oracle.u128_prepare(N, b)
+    assert np.array_equal(bhat.cpu().numpy().view(np.uint64), want_bhat.view(np.uint64))
+    da = torch.from_numpy(a.view(np.int64)).cuda()
+    out = torch.empty_like(da)
+    plan.product(da, bhat, out)
+    got = out.cpu().numpy().view(np.uint64)
+    assert np.array_equal(got, oracle.u128_product(N, a, want_bhat, nthreads=0))
+    small = RNG.integers(-2 ** 40, 2 ** 40, (1, N)).astype(np.int64)
+    a2 = np.stack([small.view(np.uint64), np.where(small < 0, np.uint64(2 ** 64 - 1), np.uint64(0))], -1)
+    da2 = torch.from_numpy(a2.view(np.int64)).cuda()
+    out2 = torch.empty_like(da2)
+    plan.product(da2, bhat[:1], out2)
+    assert np.array_equal(out2.cpu().numpy().view(np.uint64), oracle.u128_schoolbook(a2, b[:1]))

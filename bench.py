@@ -58,7 +58,7 @@ def fp64_ops_per_product(N, base_n, algo):
 
 class ClockSampler:
     """nvidia-smi sampling during the timed region (SM clock, throttle reasons)."""
-    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+    Q = ("timestamp,index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
          "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
          "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
 
@@ -66,6 +66,7 @@ class ClockSampler:
         self.index = index
         self.proc = None
         self.lines = []
+        self.window = None
 
     def __enter__(self):
         try:
@@ -80,7 +81,10 @@ class ClockSampler:
 
     def _read(self):
         for line in self.proc.stdout:
-            self.lines.append(line.strip())
+            self.lines.append((time.time(), line.strip()))
+
+    def mark(self, t0, t1):
+        self.window = (t0, t1)
 
     def __exit__(self, *exc):
         if self.proc:
@@ -93,16 +97,18 @@ class ClockSampler:
     def summary(self):
         sm, mx, reasons = [], None, set()
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        for ln in self.lines:
+        for ts, ln in self.lines:
+            if self.window and not (self.window[0] - 0.25 <= ts <= self.window[1] + 0.25):
+                continue
             f = [x.strip() for x in ln.split(",")]
-            if len(f) < 9:
+            if len(f) < 10:
                 continue
             try:
-                sm.append(float(f[1]))
-                mx = float(f[2])
+                sm.append(float(f[2]))
+                mx = float(f[3])
             except ValueError:
                 continue
-            for name, v in zip(names, f[5:9]):
+            for name, v in zip(names, f[6:10]):
                 if v.lower().startswith("active"):
                     reasons.add(name)
         if not sm:
@@ -207,12 +213,16 @@ def run_gb300(args):
     lib = cf.load()
     cf.check(lib.cfft_device_check())
 
-    plan = cf.product.U64ProductPlan(N_POLY, measure_seconds=0.002)
+    count = args.count
+    if args.base_algo is not None:
+        plan = cf.product.U64ProductPlan(N_POLY, cf.FftAlgo[args.base_algo], args.base_n)
+    else:
+        plan = cf.product.U64ProductPlan(N_POLY, measure_seconds=0.002)
     algo, base_n = plan.algo()
-    a_np, b_np = make_inputs(COUNT, BASE_SEED + rank)
+    a_np, b_np = make_inputs(count, BASE_SEED + rank)
     a = torch.from_numpy(a_np.view(np.int64)).cuda()
     b = torch.from_numpy(b_np).cuda()
-    bhat = torch.empty((COUNT, N_POLY // 2), dtype=torch.complex128, device="cuda")
+    bhat = torch.empty((count, N_POLY // 2), dtype=torch.complex128, device="cuda")
     plan.prepare_operand(b, bhat)
     out = torch.empty_like(a)
     stream = torch.cuda.current_stream()
@@ -223,24 +233,34 @@ def run_gb300(args):
             torch.distributed.barrier()
             torch.cuda.synchronize()
 
-    for _ in range(args.warmup):
+    if args.profile_case:  # one warm-up and one measured launch for ncu, nothing else
         plan.product(a, bhat, out)
-    barrier()
+        plan.product(a, bhat, out)
+        torch.cuda.synchronize()
+        print(json.dumps({"profile_case": "u64 product N=2048", "products": count, "base_algo": algo.name,
+                          "base_n": base_n}))
+        return
     e0 = torch.cuda.Event(enable_timing=True)
     e1 = torch.cuda.Event(enable_timing=True)
     with ClockSampler(local) as clk:
+        time.sleep(0.5)  # let the sampler start before the timed region
+        for _ in range(args.warmup):
+            plan.product(a, bhat, out)
+        barrier()
+        t_start = time.time()
         e0.record(stream)
         for _ in range(args.steps):
             plan.product(a, bhat, out)
         e1.record(stream)
         barrier()
+        clk.mark(t_start, time.time())
     ms = e0.elapsed_time(e1)
     if world > 1:
         t = torch.tensor([ms], device="cuda")
         torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
         ms = float(t.item())
     per_launch_s = ms * 1e-3 / args.steps
-    value = world * COUNT * args.steps / (ms * 1e-3)
+    value = world * count * args.steps / (ms * 1e-3)
 
     # end to end: pinned host A in, pinned host result out, through the C ABI host entry point
     ha = torch.from_numpy(a_np.view(np.int64)).pin_memory()
@@ -249,25 +269,26 @@ def run_gb300(args):
         plan.product(ha, bhat, hout)
     barrier()
     t0 = time.perf_counter()
-    for _ in range(args.steps):
+    e2e_steps = max(3, args.steps // 10)
+    for _ in range(e2e_steps):
         plan.product(ha, bhat, hout)
     e2e_s = time.perf_counter() - t0
     if world > 1:
         t = torch.tensor([e2e_s], device="cuda")
         torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
         e2e_s = float(t.item())
-    e2e = world * COUNT * args.steps / e2e_s
+    e2e = world * count * e2e_steps / e2e_s
     ok = bool(np.array_equal(hout.numpy(), out.cpu().numpy()))
 
     peaks, peak_kind = measured_peaks()
-    achieved_gbs = BYTES_PER_PRODUCT * COUNT / per_launch_s / 1e9
+    achieved_gbs = BYTES_PER_PRODUCT * count / per_launch_s / 1e9
     traffic = profiled_traffic("u64_product_n2048")
     import ctypes
     r = ctypes.c_double()
     cf.check(lib.cfft_diag_fp64_peak(ctypes.byref(r)))
     fp64_peak = r.value
     fp64_ops = fp64_ops_per_product(N_POLY, base_n, int(algo))
-    fp64_achieved = fp64_ops * COUNT / per_launch_s
+    fp64_achieved = fp64_ops * count / per_launch_s
 
     if rank != 0:
         return
@@ -283,18 +304,18 @@ def run_gb300(args):
         "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded numpy PCG64)",
         "config": {"workload": "u64 negacyclic product N=2048 (1024-point unordered c64 FFT), 8192 products "
                                "per launch, distinct resident Bhat per product",
-                   "base_algo": algo.name, "base_n": base_n, "products_per_step": COUNT,
+                   "base_algo": algo.name, "base_n": base_n, "products_per_step": count,
                    "l2": "inputs 384 MiB > L2 (no flush needed)", "parallelism": "replicas" if world > 1 else "1 GPU"},
         "roofline": {"bound": "hbm", "achieved": achieved_gbs, "peak": peaks.get("hbm_gbs"), "unit": "GB/s",
                      "frac": achieved_gbs / peaks.get("hbm_gbs"), "peak_kind": peak_kind,
                      "traffic": traffic.get("dram_bytes_per_launch") if traffic else None,
-                     "algorithmic_bytes_per_launch": BYTES_PER_PRODUCT * COUNT,
+                     "algorithmic_bytes_per_launch": BYTES_PER_PRODUCT * count,
                      "fp64": {"achieved_ops_per_s": fp64_achieved, "peak_ops_per_s": fp64_peak,
                               "frac": fp64_achieved / fp64_peak, "ops_per_product": fp64_ops,
                               "note": "binding roof: FP64 pipe (DFMA/DADD/DMUL issue rate, measured live)"}},
         "cpu_baseline": cpu,
-        "e2e": {"value": e2e, "unit": "products/s", "h2d_bytes_per_step": COUNT * N_POLY * 8,
-                "d2h_bytes_per_step": COUNT * N_POLY * 8, "matches_device_result": ok},
+        "e2e": {"value": e2e, "unit": "products/s", "h2d_bytes_per_step": count * N_POLY * 8,
+                "d2h_bytes_per_step": count * N_POLY * 8, "steps": e2e_steps, "matches_device_result": ok},
         "clocks": clk.summary(),
         "gpu_launches": args.steps,
     }
@@ -304,11 +325,16 @@ def run_gb300(args):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--steps", type=int, default=400)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
     ap.add_argument("--cpu-seconds", type=float, default=5.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--count", type=int, default=COUNT, help="products per launch")
+    ap.add_argument("--base-algo", default=None, help="fix the base algorithm (e.g. Dif4) instead of measuring")
+    ap.add_argument("--base-n", type=int, default=1024)
+    ap.add_argument("--profile-case", action="store_true",
+                    help="small fixed case for ncu: 1 warm-up + 1 launch, no timing")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

@@ -218,7 +218,10 @@ def run_gb300(args):
         plan = cf.product.U64ProductPlan(N_POLY, cf.FftAlgo[args.base_algo], args.base_n)
     else:
         plan = cf.product.U64ProductPlan(N_POLY, measure_seconds=0.002)
+    if args.int_adds is not None:
+        plan.set_int_adds(args.int_adds)
     algo, base_n = plan.algo()
+    int_adds = plan.int_adds()
     a_np, b_np = make_inputs(count, BASE_SEED + rank)
     a = torch.from_numpy(a_np.view(np.int64)).cuda()
     b = torch.from_numpy(b_np).cuda()
@@ -304,7 +307,8 @@ def run_gb300(args):
         "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded numpy PCG64)",
         "config": {"workload": "u64 negacyclic product N=2048 (1024-point unordered c64 FFT), 8192 products "
                                "per launch, distinct resident Bhat per product",
-                   "base_algo": algo.name, "base_n": base_n, "products_per_step": count,
+                   "base_algo": algo.name, "base_n": base_n, "int_adds_eighths": int_adds,
+                   "products_per_step": count,
                    "l2": "inputs 384 MiB > L2 (no flush needed)", "parallelism": "replicas" if world > 1 else "1 GPU"},
         "roofline": {"bound": "hbm", "achieved": achieved_gbs, "peak": peaks.get("hbm_gbs"), "unit": "GB/s",
                      "frac": achieved_gbs / peaks.get("hbm_gbs"), "peak_kind": peak_kind,
@@ -333,6 +337,8 @@ def main():
     ap.add_argument("--count", type=int, default=COUNT, help="products per launch")
     ap.add_argument("--base-algo", default=None, help="fix the base algorithm (e.g. Dif4) instead of measuring")
     ap.add_argument("--base-n", type=int, default=1024)
+    ap.add_argument("--int-adds", type=int, default=None,
+                    help="eighths of butterfly additions on the integer pipe (default: the plan's tuned value)")
     ap.add_argument("--profile-case", action="store_true",
                     help="small fixed case for ncu: 1 warm-up + 1 launch, no timing")
     args = ap.parse_args()

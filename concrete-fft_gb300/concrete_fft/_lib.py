@@ -36,6 +36,9 @@ _SIGS = [
     ("cfft_version", ctypes.c_char_p, []),
     ("cfft_device_check", c_int, []),
     ("cfft_diag_fp64_peak", c_int, [ctypes.POINTER(c_dbl)]),
+    ("cfft_diag_dadd_check", c_int, [ctypes.c_uint64, ctypes.c_uint64, ctypes.POINTER(ctypes.c_uint64),
+                                     ctypes.POINTER(ctypes.c_uint64)]),
+    ("cfft_diag_dadd_int_rate", c_int, [ctypes.POINTER(c_dbl)]),
     ("cfft_ordered_plan_create", c_int, [c_size, c_int, pp]),
     ("cfft_ordered_plan_create_measure", c_int, [c_size, c_dbl, pp]),
     ("cfft_ordered_plan_destroy", None, [vp]),
@@ -46,6 +49,10 @@ _SIGS = [
     ("cfft_ordered_inv", c_int, [vp, vp, c_size, vp]),
     ("cfft_ordered_fwd_host", c_int, [vp, vp, c_size]),
     ("cfft_ordered_inv_host", c_int, [vp, vp, c_size]),
+    ("cfft_ordered_set_int_adds", c_int, [vp, c_int]),
+    ("cfft_ordered_int_adds", c_int, [vp]),
+    ("cfft_unordered_set_int_adds", c_int, [vp, c_int]),
+    ("cfft_unordered_int_adds", c_int, [vp]),
     ("cfft_unordered_plan_create", c_int, [c_size, c_int, c_size, pp]),
     ("cfft_unordered_plan_create_measure", c_int, [c_size, c_dbl, pp]),
     ("cfft_unordered_plan_destroy", None, [vp]),
@@ -74,6 +81,8 @@ _SIGS = [
     ("cfft_u64_product_plan_destroy", None, [vp]),
     ("cfft_u64_product_poly_size", c_size, [vp]),
     ("cfft_u64_product_algo", None, [vp, ctypes.POINTER(c_int), ctypes.POINTER(c_size)]),
+    ("cfft_u64_product_set_int_adds", c_int, [vp, c_int]),
+    ("cfft_u64_product_int_adds", c_int, [vp]),
     ("cfft_u64_prepare_operand", c_int, [vp, vp, vp, c_size, vp]),
     ("cfft_u64_product", c_int, [vp, vp, vp, c_size, vp, c_size, vp]),
     ("cfft_u64_product_host", c_int, [vp, vp, vp, c_size, vp, c_size]),

@@ -61,6 +61,13 @@ class Plan:
     def algo(self):
         return FftAlgo(self._lib.cfft_ordered_algo(self._h))
 
+    def set_int_adds(self, eighths):
+        """Share (in eighths) of butterfly additions issued on the integer pipe; results are unchanged."""
+        check(self._lib.cfft_ordered_set_int_adds(self._h, int(eighths)))
+
+    def int_adds(self):
+        return self._lib.cfft_ordered_int_adds(self._h)
+
     def fft_scratch(self):
         """Bytes of caller scratch per call (0: the GPU path needs none)."""
         return self._lib.cfft_ordered_scratch_bytes(self._h)

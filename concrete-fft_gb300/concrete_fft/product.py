@@ -27,6 +27,13 @@ class U64ProductPlan:
             self._lib.cfft_u64_product_plan_destroy(self._h)
             self._h = None
 
+    def set_int_adds(self, eighths):
+        """Share (in eighths) of butterfly additions issued on the integer pipe; results are unchanged."""
+        check(self._lib.cfft_u64_product_set_int_adds(self._h, int(eighths)))
+
+    def int_adds(self):
+        return self._lib.cfft_u64_product_int_adds(self._h)
+
     def algo(self):
         a, b = ctypes.c_int(), ctypes.c_size_t()
         self._lib.cfft_u64_product_algo(self._h, ctypes.byref(a), ctypes.byref(b))

@@ -48,6 +48,13 @@ class Plan:
         self._lib.cfft_unordered_algo(self._h, ctypes.byref(a), ctypes.byref(b))
         return FftAlgo(a.value), b.value
 
+    def set_int_adds(self, eighths):
+        """Share (in eighths) of butterfly additions issued on the integer pipe; results are unchanged."""
+        check(self._lib.cfft_unordered_set_int_adds(self._h, int(eighths)))
+
+    def int_adds(self):
+        return self._lib.cfft_unordered_int_adds(self._h)
+
     def fft_scratch(self):
         return self._lib.cfft_unordered_scratch_bytes(self._h)
 

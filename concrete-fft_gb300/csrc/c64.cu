@@ -13,45 +13,11 @@
 
 #include "cfft_internal.h"
 #include "runtime.h"
-#include "stockham.cuh"
+#include "c64_kernels.cuh"
 
 using namespace cfft;
 
 namespace cfft {
-
-__global__ void __launch_bounds__(256) c64_smem_fwd_kernel(double2* data, int count, int tpc, DevLevels L, int d0,
-                                                           int base_algo, const double2* __restrict__ w) {
-  extern __shared__ double2 smem[];
-  const int log2sub = L.log2n[d0];
-  const long first = (long)blockIdx.x * tpc;
-  const int nch = (int)min((long)tpc, (long)count - first);
-  double2* x = smem;
-  double2* y = smem + ((long)tpc << log2sub);
-  double2* g = data + (first << log2sub);
-  const int npts = nch << log2sub;
-  const int tid = threadIdx.x, nth = blockDim.x;
-  for (int i = tid; i < npts; i += nth) x[i] = g[i];
-  __syncthreads();
-  const double2* r = unordered_smem<true>(L, d0, base_algo, nch, x, y, w, tid, nth);
-  for (int i = tid; i < npts; i += nth) g[i] = r[i];
-}
-
-__global__ void __launch_bounds__(256) c64_smem_inv_kernel(double2* data, int count, int tpc, DevLevels L, int d0,
-                                                           int base_algo, const double2* __restrict__ w) {
-  extern __shared__ double2 smem[];
-  const int log2sub = L.log2n[d0];
-  const long first = (long)blockIdx.x * tpc;
-  const int nch = (int)min((long)tpc, (long)count - first);
-  double2* x = smem;
-  double2* y = smem + ((long)tpc << log2sub);
-  double2* g = data + (first << log2sub);
-  const int npts = nch << log2sub;
-  const int tid = threadIdx.x, nth = blockDim.x;
-  for (int i = tid; i < npts; i += nth) x[i] = g[i];
-  __syncthreads();
-  const double2* r = unordered_smem<false>(L, d0, base_algo, nch, x, y, w, tid, nth);
-  for (int i = tid; i < npts; i += nth) g[i] = r[i];
-}
 
 // One unordered level in place in global memory, over every chunk of 2^log2nl points.
 template <bool FWD>
@@ -61,9 +27,9 @@ __global__ void __launch_bounds__(256) c64_level_kernel(double2* data, long tota
   for (long g = (long)blockIdx.x * blockDim.x + threadIdx.x; g < total; g += (long)gridDim.x * blockDim.x) {
     double2* zc = data + ((g >> lm) << log2nl);
     const int i = (int)(g & ((1L << lm) - 1));
-    if (log2r == 1) outer_group<2, FWD>(zc, lm, i, wl);
-    else if (log2r == 2) outer_group<4, FWD>(zc, lm, i, wl);
-    else outer_group<8, FWD>(zc, lm, i, wl);
+    if (log2r == 1) outer_group<2, FWD, 0>(zc, lm, i, wl);
+    else if (log2r == 2) outer_group<4, FWD, 0>(zc, lm, i, wl);
+    else outer_group<8, FWD, 0>(zc, lm, i, wl);
   }
 }
 
@@ -126,6 +92,7 @@ struct C64Plan {
   int d0 = 0;        // first level handled in shared memory
   int threads = 128;  // CTA size of the shared-memory kernel
   int tpc = 1;       // sub-transforms per CTA
+  int emu = 6;       // eighths of the butterfly additions issued on the integer pipe
 };
 
 struct cfft_ordered_plan {
@@ -169,14 +136,14 @@ void free_plan(C64Plan& p) {
   p.d_w = p.d_winv = p.d_mono = nullptr;
 }
 
-bool g_attr_done = false;
-cfft_status ensure_attrs() {
-  if (g_attr_done) return CFFT_OK;
-  const int max_smem = 2 * (1 << kSmemLog2Max) * (int)sizeof(double2);
-  CFFT_CUDA_TRY(cudaFuncSetAttribute(c64_smem_fwd_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, max_smem));
-  CFFT_CUDA_TRY(cudaFuncSetAttribute(c64_smem_inv_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, max_smem));
-  g_attr_done = true;
-  return CFFT_OK;
+int emu_level(const C64Plan& p) { return emu_level_for(p.base_algo, p.emu); }
+
+cfft_status launch_smem(const C64Plan& p, bool fwd, int blocks, size_t smem, cudaStream_t stream, double2* data,
+                        int nsub, const double2* w) {
+  DevLevels L = p.dlv;
+  int tpc = p.tpc, d0 = p.d0;
+  void* args[] = {&data, &nsub, &tpc, &L, &d0, (void*)&w};
+  return launch_kernel(c64_kernel(p.base_algo, p.emu, fwd), blocks, p.threads, args, smem, stream);
 }
 
 cfft_status build_plan(C64Plan& p, size_t n, size_t base_n, int algo, bool unordered) {
@@ -185,8 +152,7 @@ cfft_status build_plan(C64Plan& p, size_t n, size_t base_n, int algo, bool unord
   p.base_algo = algo;
   p.unordered = unordered;
   CFFT_CUDA_TRY(cudaGetDevice(&p.device));
-  cfft_status st = ensure_attrs();
-  if (st != CFFT_OK) return st;
+  cfft_status st = CFFT_OK;
   p.lv = make_levels(n, base_n);
   p.dlv = to_dev(p.lv);
   // first level whose sub-transforms fit in shared memory
@@ -226,12 +192,11 @@ cfft_status run_plan(const C64Plan& p, double* buf, size_t batch, bool fwd, cuda
       c64_level_kernel<true><<<grid, 256, 0, stream>>>(data, total, p.lv.log2r[l], p.lv.log2n[l], p.d_w + p.lv.w_off[l]);
       CFFT_CHECK_LAUNCH();
     }
-    c64_smem_fwd_kernel<<<blocks, p.threads, smem, stream>>>(data, (int)nsub, p.tpc, p.dlv, p.d0, p.base_algo, p.d_w);
-    CFFT_CHECK_LAUNCH();
+    cfft_status st = launch_smem(p, true, blocks, smem, stream, data, (int)nsub, p.d_w);
+    if (st != CFFT_OK) return st;
   } else {
-    c64_smem_inv_kernel<<<blocks, p.threads, smem, stream>>>(data, (int)nsub, p.tpc, p.dlv, p.d0, p.base_algo,
-                                                              p.d_winv);
-    CFFT_CHECK_LAUNCH();
+    cfft_status st = launch_smem(p, false, blocks, smem, stream, data, (int)nsub, p.d_winv);
+    if (st != CFFT_OK) return st;
     for (int l = p.d0 - 1; l >= 0; --l) {
       const long total = ((long)batch << log2n) >> p.lv.log2r[l];
       const int grid = (int)std::min<long>((total + 255) / 256, (long)nsm * 16);
@@ -340,6 +305,18 @@ void tune_launch(C64Plan& p, double2* scratch, size_t batch, double seconds) {
   }
   p.threads = bt;
   p.tpc = bp;
+  int be = p.emu;
+  for (int e : kEmuLevels) {
+    if (emu_level_for(p.base_algo, e) != e) continue;
+    C64Plan q = p;
+    q.emu = e;
+    const double t = time_forward(q, scratch, batch, seconds);
+    if (t < best) {
+      best = t;
+      be = e;
+    }
+  }
+  p.emu = be;
 }
 
 bool valid_algo(int a) { return a >= 0 && a <= 7; }
@@ -407,6 +384,20 @@ cfft_status cfft_ordered_inv_host(const cfft_ordered_plan* plan, double* buf, si
   if (!plan) return fail(CFFT_ERR_INVALID_ARGUMENT, "null plan");
   return run_host(plan->p, buf, batch, false);
 }
+
+cfft_status cfft_ordered_set_int_adds(cfft_ordered_plan* plan, int eighths) {
+  if (!plan || eighths < 0 || eighths > 8) return fail(CFFT_ERR_INVALID_ARGUMENT, "eighths must be in 0..8");
+  plan->p.emu = eighths;
+  return CFFT_OK;
+}
+int cfft_ordered_int_adds(const cfft_ordered_plan* plan) { return plan ? emu_level(plan->p) : -1; }
+
+cfft_status cfft_unordered_set_int_adds(cfft_unordered_plan* plan, int eighths) {
+  if (!plan || eighths < 0 || eighths > 8) return fail(CFFT_ERR_INVALID_ARGUMENT, "eighths must be in 0..8");
+  plan->p.emu = eighths;
+  return CFFT_OK;
+}
+int cfft_unordered_int_adds(const cfft_unordered_plan* plan) { return plan ? emu_level(plan->p) : -1; }
 
 cfft_status cfft_unordered_plan_create(size_t n, cfft_algo base_algo, size_t base_n, cfft_unordered_plan** out) {
   if (!out) return fail(CFFT_ERR_INVALID_ARGUMENT, "null output pointer");

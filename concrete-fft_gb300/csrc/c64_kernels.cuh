@@ -1,0 +1,116 @@
+// c64_kernels.cuh -- kernel templates of the c64 transforms and the u64 product.
+//
+// Each kernel is instantiated per (ordered base algorithm, integer-add level)
+// so that it carries exactly one algorithm's code; the instantiations live in
+// the kinst_*.cu translation units (compiled in parallel) and are reached
+// through the pointer tables declared at the end of this file.
+#pragma once
+#include "stockham.cuh"
+
+namespace cfft {
+
+// Sub-transforms of 2^log2n_{d0} points, `tpc` per CTA: load to shared memory,
+// run the unordered transform from level d0 (ordered plans have no levels),
+// store back.
+template <int ALGO, int E, bool FWD>
+__global__ void __launch_bounds__(256) c64_smem_kernel(double2* data, int count, int tpc, DevLevels L, int d0,
+                                                       const double2* __restrict__ w) {
+  extern __shared__ double2 smem[];
+  const int log2sub = L.log2n[d0];
+  const long first = (long)blockIdx.x * tpc;
+  const int nch = (int)min((long)tpc, (long)count - first);
+  double2* x = smem;
+  double2* y = smem + ((long)tpc << log2sub);
+  double2* g = data + (first << log2sub);
+  const int npts = nch << log2sub;
+  const int tid = threadIdx.x, nth = blockDim.x;
+  for (int i = tid; i < npts; i += nth) x[i] = g[i];
+  __syncthreads();
+  const double2* r = unordered_smem<FWD, E, ALGO>(L, d0, nch, x, y, w, tid, nth);
+  for (int i = tid; i < npts; i += nth) g[i] = r[i];
+}
+
+// Fused negacyclic u64 product (see product_u64.cu for the pipeline): one
+// product per CTA at a time, grid-stride over the batch.
+template <int ALGO, int E, int THREADS>
+__global__ void __launch_bounds__(THREADS) u64_product_kernel(const uint64_t* __restrict__ a,
+                                                             const double2* __restrict__ bhat, long bhat_stride,
+                                                             uint64_t* __restrict__ out, long count, DevLevels L,
+                                                             const double2* __restrict__ w,
+                                                             const double2* __restrict__ winv,
+                                                             const double2* __restrict__ tw,
+                                                             const double2* __restrict__ itw) {
+  extern __shared__ double2 smem[];
+  const int log2n = L.log2n[0];
+  const int n = 1 << log2n;
+  double2* x = smem;
+  double2* y = smem + n;
+  const int tid = threadIdx.x;
+  for (long prod = blockIdx.x; prod < count; prod += gridDim.x) {
+    const uint64_t* ap = a + (prod << (log2n + 1));
+    for (int j = tid; j < n; j += THREADS) {
+      const c64 v{i64_to_f64_rne((int64_t)__ldcs(ap + j)), i64_to_f64_rne((int64_t)__ldcs(ap + j + n))};
+      st(x + j, cmul(ldg(tw + j), v));
+    }
+    __syncthreads();
+    double2* r = unordered_smem<true, E, ALGO>(L, 0, 1, x, y, w, tid, THREADS);
+    const double2* bp = bhat + prod * bhat_stride;
+    for (int k = tid; k < n; k += THREADS) st(r + k, cmul(ldg(bp + k), ld(r + k)));
+    __syncthreads();
+    double2* o = (r == x) ? y : x;
+    double2* s = unordered_smem<false, E, ALGO>(L, 0, 1, r, o, winv, tid, THREADS);
+    uint64_t* op = out + (prod << (log2n + 1));
+    for (int j = tid; j < n; j += THREADS) {
+      const c64 t = cmul(ldg(itw + j), ld(s + j));
+      __stcs(op + j, round_half_up_mod64(t.re));
+      __stcs(op + j + n, round_half_up_mod64(t.im));
+    }
+    __syncthreads();
+  }
+}
+
+// Bhat = fwd(tau^j * (b_j + i b_{j+N/2})) for small signed digits b.
+template <int ALGO, int THREADS>
+__global__ void __launch_bounds__(THREADS) u64_prepare_kernel(const int64_t* __restrict__ b,
+                                                             double2* __restrict__ bhat, long count, DevLevels L,
+                                                             const double2* __restrict__ w,
+                                                             const double2* __restrict__ tw) {
+  extern __shared__ double2 smem[];
+  const int log2n = L.log2n[0];
+  const int n = 1 << log2n;
+  double2* x = smem;
+  double2* y = smem + n;
+  const int tid = threadIdx.x;
+  for (long prod = blockIdx.x; prod < count; prod += gridDim.x) {
+    const int64_t* bp = b + (prod << (log2n + 1));
+    for (int j = tid; j < n; j += THREADS) {
+      const c64 v{i64_to_f64_rne(bp[j]), i64_to_f64_rne(bp[j + n])};
+      st(x + j, cmul(ldg(tw + j), v));
+    }
+    __syncthreads();
+    const double2* r = unordered_smem<true, 0, ALGO>(L, 0, 1, x, y, w, tid, THREADS);
+    double2* op = bhat + (prod << log2n);
+    for (int k = tid; k < n; k += THREADS) op[k] = r[k];
+    __syncthreads();
+  }
+}
+
+constexpr int kProdThreads = 128;
+
+// Kernel-pointer tables (nullptr when the combination is not instantiated).
+const void* c64_kernel_e0(int algo, bool fwd);
+const void* c64_kernel_emu(int algo, int e, bool fwd);
+const void* u64_product_kernel_e0(int algo);
+const void* u64_product_kernel_emu(int algo, int e);
+const void* u64_prepare_kernel_ptr(int algo);
+
+inline const void* c64_kernel(int algo, int e, bool fwd) {
+  const int lvl = emu_level_for(algo, e);
+  return lvl == 0 ? c64_kernel_e0(algo, fwd) : c64_kernel_emu(algo, lvl, fwd);
+}
+inline const void* u64_product_kernel_ptr(int algo, int e) {
+  const int lvl = emu_level_for(algo, e);
+  return lvl == 0 ? u64_product_kernel_e0(algo) : u64_product_kernel_emu(algo, lvl);
+}
+
+}  // namespace cfft

@@ -1,0 +1,31 @@
+// Instantiations: fused u64 product and operand preparation, every algorithm, FP64-pipe additions only.
+#include "c64_kernels.cuh"
+
+namespace cfft {
+const void* u64_product_kernel_e0(int algo) {
+  switch (algo) {
+    case 0: return (const void*)u64_product_kernel<0, 0, kProdThreads>;
+    case 1: return (const void*)u64_product_kernel<1, 0, kProdThreads>;
+    case 2: return (const void*)u64_product_kernel<2, 0, kProdThreads>;
+    case 3: return (const void*)u64_product_kernel<3, 0, kProdThreads>;
+    case 4: return (const void*)u64_product_kernel<4, 0, kProdThreads>;
+    case 5: return (const void*)u64_product_kernel<5, 0, kProdThreads>;
+    case 6: return (const void*)u64_product_kernel<6, 0, kProdThreads>;
+    case 7: return (const void*)u64_product_kernel<7, 0, kProdThreads>;
+    default: return nullptr;
+  }
+}
+const void* u64_prepare_kernel_ptr(int algo) {
+  switch (algo) {
+    case 0: return (const void*)u64_prepare_kernel<0, kProdThreads>;
+    case 1: return (const void*)u64_prepare_kernel<1, kProdThreads>;
+    case 2: return (const void*)u64_prepare_kernel<2, kProdThreads>;
+    case 3: return (const void*)u64_prepare_kernel<3, kProdThreads>;
+    case 4: return (const void*)u64_prepare_kernel<4, kProdThreads>;
+    case 5: return (const void*)u64_prepare_kernel<5, kProdThreads>;
+    case 6: return (const void*)u64_prepare_kernel<6, kProdThreads>;
+    case 7: return (const void*)u64_prepare_kernel<7, kProdThreads>;
+    default: return nullptr;
+  }
+}
+}  // namespace cfft

@@ -24,76 +24,9 @@
 
 #include "cfft_internal.h"
 #include "runtime.h"
-#include "stockham.cuh"
+#include "c64_kernels.cuh"
 
 using namespace cfft;
-
-namespace cfft {
-
-template <int THREADS>
-__global__ void __launch_bounds__(THREADS) u64_product_kernel(const uint64_t* __restrict__ a,
-                                                             const double2* __restrict__ bhat, long bhat_stride,
-                                                             uint64_t* __restrict__ out, long count, DevLevels L,
-                                                             int base_algo, const double2* __restrict__ w,
-                                                             const double2* __restrict__ winv,
-                                                             const double2* __restrict__ tw,
-                                                             const double2* __restrict__ itw) {
-  extern __shared__ double2 smem[];
-  const int log2n = L.log2n[0];
-  const int n = 1 << log2n;
-  double2* x = smem;
-  double2* y = smem + n;
-  const int tid = threadIdx.x;
-  for (long prod = blockIdx.x; prod < count; prod += gridDim.x) {
-    const uint64_t* ap = a + (prod << (log2n + 1));
-    for (int j = tid; j < n; j += THREADS) {
-      const c64 v{i64_to_f64_rne((int64_t)__ldcs(ap + j)), i64_to_f64_rne((int64_t)__ldcs(ap + j + n))};
-      st(x + j, cmul(ldg(tw + j), v));
-    }
-    __syncthreads();
-    double2* r = unordered_smem<true>(L, 0, base_algo, 1, x, y, w, tid, THREADS);
-    const double2* bp = bhat + prod * bhat_stride;
-    for (int k = tid; k < n; k += THREADS) st(r + k, cmul(ldg(bp + k), ld(r + k)));
-    __syncthreads();
-    double2* o = (r == x) ? y : x;
-    double2* s = unordered_smem<false>(L, 0, base_algo, 1, r, o, winv, tid, THREADS);
-    uint64_t* op = out + (prod << (log2n + 1));
-    for (int j = tid; j < n; j += THREADS) {
-      const c64 t = cmul(ldg(itw + j), ld(s + j));
-      __stcs(op + j, round_half_up_mod64(t.re));
-      __stcs(op + j + n, round_half_up_mod64(t.im));
-    }
-    __syncthreads();
-  }
-}
-
-// Bhat = fwd(tau^j * (b_j + i b_{j+N/2})) for small signed digits b.
-template <int THREADS>
-__global__ void __launch_bounds__(THREADS) u64_prepare_kernel(const int64_t* __restrict__ b,
-                                                             double2* __restrict__ bhat, long count, DevLevels L,
-                                                             int base_algo, const double2* __restrict__ w,
-                                                             const double2* __restrict__ tw) {
-  extern __shared__ double2 smem[];
-  const int log2n = L.log2n[0];
-  const int n = 1 << log2n;
-  double2* x = smem;
-  double2* y = smem + n;
-  const int tid = threadIdx.x;
-  for (long prod = blockIdx.x; prod < count; prod += gridDim.x) {
-    const int64_t* bp = b + (prod << (log2n + 1));
-    for (int j = tid; j < n; j += THREADS) {
-      const c64 v{i64_to_f64_rne(bp[j]), i64_to_f64_rne(bp[j + n])};
-      st(x + j, cmul(ldg(tw + j), v));
-    }
-    __syncthreads();
-    const double2* r = unordered_smem<true>(L, 0, base_algo, 1, x, y, w, tid, THREADS);
-    double2* op = bhat + (prod << log2n);
-    for (int k = tid; k < n; k += THREADS) op[k] = r[k];
-    __syncthreads();
-  }
-}
-
-}  // namespace cfft
 
 struct cfft_u64_product_plan {
   size_t N = 0, n = 0, base_n = 0;
@@ -101,13 +34,10 @@ struct cfft_u64_product_plan {
   LevelDesc lv{};
   DevLevels dlv{};
   double2 *d_w = nullptr, *d_winv = nullptr, *d_tw = nullptr, *d_itw = nullptr;
-  int threads = 128;
-  int blocks_per_sm = 0;  // 0: enough CTAs for every product (capped at SM count x occupancy)
+  int emu = 7;  // eighths of the butterfly additions issued on the integer pipe
 };
 
 namespace {
-
-constexpr int kProdThreads = 128;
 
 void free_u64(cfft_u64_product_plan* p) {
   if (p->d_w) cudaFree(p->d_w);
@@ -131,29 +61,36 @@ DevLevels dev_levels(const LevelDesc& l) {
   return d;
 }
 
-bool g_u64_attr = false;
-cfft_status u64_attrs() {
-  if (g_u64_attr) return CFFT_OK;
-  const int max_smem = 2 * (1 << kSmemLog2Max) * (int)sizeof(double2);
-  CFFT_CUDA_TRY(cudaFuncSetAttribute(u64_product_kernel<kProdThreads>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                     max_smem));
-  CFFT_CUDA_TRY(cudaFuncSetAttribute(u64_prepare_kernel<kProdThreads>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                     max_smem));
-  g_u64_attr = true;
-  return CFFT_OK;
+int grid_for(const void* kernel, int threads, size_t smem, long count) {
+  const long cap = (long)sm_count() * max_blocks_per_sm(kernel, threads, smem);
+  return (int)std::max<long>(1, std::min<long>(count, cap));
 }
 
-int grid_for(const void* kernel, int threads, size_t smem, long count) {
-  int per_sm = 0;
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, threads, smem);
-  per_sm = std::max(per_sm, 1);
-  const long cap = (long)sm_count() * per_sm;
-  return (int)std::max<long>(1, std::min<long>(count, cap));
+cfft_status launch_product(const cfft_u64_product_plan* plan, const uint64_t* a, const double* bhat,
+                           size_t bhat_stride, uint64_t* out, size_t count, cudaStream_t stream) {
+  const void* fn = u64_product_kernel_ptr(plan->base_algo, plan->emu);
+  const size_t smem = 2 * plan->n * sizeof(double2);
+  const int grid = grid_for(fn, kProdThreads, smem, (long)count);
+  DevLevels L = plan->dlv;
+  long stride = (long)bhat_stride, cnt = (long)count;
+  const double2* bh = (const double2*)bhat;
+  void* args[] = {(void*)&a, (void*)&bh, &stride, (void*)&out, &cnt, &L, (void*)&plan->d_w, (void*)&plan->d_winv,
+                  (void*)&plan->d_tw, (void*)&plan->d_itw};
+  return launch_kernel(fn, grid, kProdThreads, args, smem, stream);
 }
 
 }  // namespace
 
 extern "C" {
+
+cfft_status cfft_u64_product_set_int_adds(cfft_u64_product_plan* plan, int eighths) {
+  if (!plan || eighths < 0 || eighths > 8) return fail(CFFT_ERR_INVALID_ARGUMENT, "eighths must be in 0..8");
+  plan->emu = eighths;
+  return CFFT_OK;
+}
+int cfft_u64_product_int_adds(const cfft_u64_product_plan* plan) {
+  return plan ? emu_level_for(plan->base_algo, plan->emu) : -1;
+}
 
 cfft_status cfft_u64_product_plan_create(size_t N, cfft_algo base_algo, size_t base_n, cfft_u64_product_plan** out) {
   if (!out) return fail(CFFT_ERR_INVALID_ARGUMENT, "null output pointer");
@@ -164,8 +101,7 @@ cfft_status cfft_u64_product_plan_create(size_t N, cfft_algo base_algo, size_t b
   if (!is_pow2(base_n) || base_n > n || (base_n != n && base_n < 32) || ilog2(base_n) > 10)
     return fail(CFFT_ERR_INVALID_ARGUMENT, "u64 product: invalid base_n");
   if (base_algo < 0 || base_algo > 7) return fail(CFFT_ERR_INVALID_ARGUMENT, "unknown FftAlgo");
-  cfft_status st = u64_attrs();
-  if (st != CFFT_OK) return st;
+  cfft_status st = CFFT_OK;
   auto* p = new cfft_u64_product_plan();
   p->N = N;
   p->n = n;
@@ -213,11 +149,13 @@ cfft_status cfft_u64_prepare_operand(const cfft_u64_product_plan* plan, const in
   if (!plan || !b || !bhat) return fail(CFFT_ERR_INVALID_ARGUMENT, "null argument");
   if (count == 0) return CFFT_OK;
   const size_t smem = 2 * plan->n * sizeof(double2);
-  const int grid = grid_for((const void*)u64_prepare_kernel<kProdThreads>, kProdThreads, smem, (long)count);
-  u64_prepare_kernel<kProdThreads><<<grid, kProdThreads, smem, (cudaStream_t)stream>>>(
-      b, (double2*)bhat, (long)count, plan->dlv, plan->base_algo, plan->d_w, plan->d_tw);
-  CFFT_CHECK_LAUNCH();
-  return CFFT_OK;
+  const void* fn = u64_prepare_kernel_ptr(plan->base_algo);
+  const int grid = grid_for(fn, kProdThreads, smem, (long)count);
+  DevLevels L = plan->dlv;
+  long cnt = (long)count;
+  double2* bh = (double2*)bhat;
+  void* args[] = {(void*)&b, &bh, &cnt, &L, (void*)&plan->d_w, (void*)&plan->d_tw};
+  return launch_kernel(fn, grid, kProdThreads, args, smem, (cudaStream_t)stream);
 }
 
 cfft_status cfft_u64_product(const cfft_u64_product_plan* plan, const uint64_t* a, const double* bhat,
@@ -226,13 +164,8 @@ cfft_status cfft_u64_product(const cfft_u64_product_plan* plan, const uint64_t* 
   if (bhat_stride != 0 && bhat_stride != plan->n)
     return fail(CFFT_ERR_INVALID_ARGUMENT, "bhat_stride must be 0 or N/2");
   if (count == 0) return CFFT_OK;
-  const size_t smem = 2 * plan->n * sizeof(double2);
-  const int grid = grid_for((const void*)u64_product_kernel<kProdThreads>, kProdThreads, smem, (long)count);
-  u64_product_kernel<kProdThreads><<<grid, kProdThreads, smem, (cudaStream_t)stream>>>(
-      a, (const double2*)bhat, (long)bhat_stride, out, (long)count, plan->dlv, plan->base_algo, plan->d_w,
-      plan->d_winv, plan->d_tw, plan->d_itw);
-  CFFT_CHECK_LAUNCH();
-  return CFFT_OK;
+  return launch_product(plan, a, bhat, bhat_stride, out, count, (cudaStream_t)stream);
+
 }
 
 // Method::Measure for the product: every (base_algo, base_n) the reference's
@@ -301,7 +234,43 @@ cfft_status cfft_u64_product_plan_create_measure(size_t N, double seconds, cfft_
   cudaFree(dout);
   cudaFree(dbhat);
   if (st != CFFT_OK) return st;
-  return cfft_u64_product_plan_create(N, (cfft_algo)best_algo, best_base, out);
+  st = cfft_u64_product_plan_create(N, (cfft_algo)best_algo, best_base, out);
+  if (st != CFFT_OK) return st;
+  // integer-pipe share of the additions for the winning algorithm
+  CFFT_CUDA_TRY(cudaMalloc(&da, count * N * sizeof(uint64_t)));
+  CFFT_CUDA_TRY(cudaMalloc(&dout, count * N * sizeof(uint64_t)));
+  CFFT_CUDA_TRY(cudaMalloc(&dbhat, count * n * sizeof(double2)));
+  CFFT_CUDA_TRY(cudaMemset(da, 0, count * N * sizeof(uint64_t)));
+  CFFT_CUDA_TRY(cudaMemset(dbhat, 0, count * n * sizeof(double2)));
+  CFFT_CUDA_TRY(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  double best_e = 1e30;
+  int be = (*out)->emu;
+  for (int e : kEmuLevels) {
+    if (emu_level_for(best_algo, e) != e) continue;
+    (*out)->emu = e;
+    cfft_u64_product(*out, da, dbhat, n, dout, count, s);
+    cudaEventRecord(e0, s);
+    const int reps = 8;
+    for (int r = 0; r < reps; ++r) cfft_u64_product(*out, da, dbhat, n, dout, count, s);
+    cudaEventRecord(e1, s);
+    cudaEventSynchronize(e1);
+    float ms = 0;
+    cudaEventElapsedTime(&ms, e0, e1);
+    if (ms < best_e) {
+      best_e = ms;
+      be = e;
+    }
+  }
+  (*out)->emu = be;
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  cudaStreamDestroy(s);
+  cudaFree(da);
+  cudaFree(dout);
+  cudaFree(dbhat);
+  return CFFT_OK;
 }
 
 cfft_status cfft_u64_product_host(const cfft_u64_product_plan* plan, const uint64_t* a, const double* bhat,

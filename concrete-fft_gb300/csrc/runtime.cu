@@ -3,6 +3,7 @@
 
 #include <mutex>
 #include <string>
+#include <vector>
 
 #include "cfft_internal.h"
 #include "runtime.h"
@@ -64,6 +65,42 @@ cfft_status host_staging(size_t bytes, void** dev_ptr, cudaStream_t* stream) {
   *dev_ptr = s.ptr;
   *stream = s.stream;
   return CFFT_OK;
+}
+
+namespace {
+std::mutex g_attr_mu;
+struct AttrEntry {
+  const void* fn;
+  int dev;
+  size_t smem;
+};
+std::vector<AttrEntry> g_attrs;
+cfft_status ensure_smem_attr(const void* fn, size_t smem) {
+  if (smem <= 48 * 1024) return CFFT_OK;
+  int dev = 0;
+  CFFT_CUDA_TRY(cudaGetDevice(&dev));
+  std::lock_guard<std::mutex> lk(g_attr_mu);
+  for (const auto& e : g_attrs)
+    if (e.fn == fn && e.dev == dev && e.smem >= smem) return CFFT_OK;
+  CFFT_CUDA_TRY(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  g_attrs.push_back({fn, dev, smem});
+  return CFFT_OK;
+}
+}  // namespace
+
+cfft_status launch_kernel(const void* fn, int grid, int block, void** args, size_t smem, cudaStream_t stream) {
+  if (!fn) return fail(CFFT_ERR_INVALID_ARGUMENT, "no kernel instantiated for this configuration");
+  cfft_status st = ensure_smem_attr(fn, smem);
+  if (st != CFFT_OK) return st;
+  CFFT_CUDA_TRY(cudaLaunchKernel(fn, dim3(grid), dim3(block), args, smem, stream));
+  return CFFT_OK;
+}
+
+int max_blocks_per_sm(const void* fn, int block, size_t smem) {
+  if (ensure_smem_attr(fn, smem) != CFFT_OK) return 1;
+  int per_sm = 0;
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, block, smem);
+  return per_sm > 0 ? per_sm : 1;
 }
 
 }  // namespace cfft
@@ -137,5 +174,117 @@ extern "C" cfft_status cfft_diag_fp64_peak(double* ops_per_second) {
   cudaFree(d);
   CFFT_CHECK_LAUNCH();
   *ops_per_second = (double)reps * blocks * threads * kPeakIters * 8 / (ms * 1e-3);
+  return CFFT_OK;
+}
+
+#include "int_fp64.cuh"
+
+namespace {
+__device__ __forceinline__ uint64_t mix64(uint64_t z) {  // splitmix64 finaliser
+  z += 0x9e3779b97f4a7c15ull;
+  z = (z ^ (z >> 30)) * 0xbf58476d1ce4e5b9ull;
+  z = (z ^ (z >> 27)) * 0x94d049bb133111ebull;
+  return z ^ (z >> 31);
+}
+
+__device__ void make_pair(uint64_t i, uint64_t seed, double& x, double& y) {
+  const uint64_t r0 = mix64(seed ^ (i * 4 + 0)), r1 = mix64(seed ^ (i * 4 + 1)), r2 = mix64(seed ^ (i * 4 + 2));
+  const int mode = (int)(i & 3);
+  uint64_t bx, by;
+  if (mode == 0) {  // raw bit patterns: every exponent, zeros, subnormals, inf, nan
+    bx = r0;
+    by = r1;
+  } else if (mode == 1) {  // normal operands with exponent gaps 0..70
+    const uint64_t ex = 200 + (r2 & 1023);
+    const uint64_t gap = (r2 >> 10) % 71;
+    bx = (r0 & 0x800fffffffffffffull) | (ex << 52);
+    by = (r1 & 0x800fffffffffffffull) | ((ex - gap) << 52);
+  } else if (mode == 2) {  // near cancellation: y ~ -x with low bits perturbed
+    const uint64_t ex = 100 + (r2 & 1023);
+    bx = (r0 & 0x000fffffffffffffull) | (ex << 52);
+    const int k = (int)((r2 >> 12) % 54);
+    by = (bx ^ (r1 & ((1ull << k) - 1))) | 0x8000000000000000ull;
+    if ((r2 >> 20) & 1) by += ((r2 >> 21) & 3) << 52;  // also exponent off by 0..3
+    if ((r2 >> 23) & 1) bx ^= 0x8000000000000000ull, by ^= 0x8000000000000000ull;
+  } else {  // rounding ties and near ties: y's bits straddle x's last place
+    const uint64_t ex = 300 + (r2 & 511);
+    const uint64_t gap = 52 + ((r2 >> 9) % 4);
+    bx = (r0 & 0x800fffffffffffffull) | (ex << 52);
+    uint64_t my = (r2 >> 16) & 0x7;  // few significant bits: exact halves are common
+    by = (r1 & 0x8000000000000000ull) | ((ex - gap) << 52) | (my << 49);
+  }
+  x = __longlong_as_double((long long)bx);
+  y = __longlong_as_double((long long)by);
+}
+
+__global__ void dadd_check_kernel(uint64_t count, uint64_t seed, unsigned long long* bad, unsigned long long* first) {
+  for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < count; i += (uint64_t)gridDim.x * blockDim.x) {
+    double x, y;
+    make_pair(i, seed, x, y);
+    const double a = cfft::dadd_int(x, y);
+    const double b = __dadd_rn(x, y);
+    const bool nan_both = (a != a) && (b != b);
+    if (!nan_both && __double_as_longlong(a) != __double_as_longlong(b)) {
+      if (atomicAdd(bad, 1ull) == 0) {
+        first[0] = (unsigned long long)__double_as_longlong(x);
+        first[1] = (unsigned long long)__double_as_longlong(y);
+      }
+    }
+  }
+}
+
+constexpr int kIntIters = 512;
+__global__ void dadd_int_rate_kernel(double* out, double seed) {
+  double a[4];
+#pragma unroll
+  for (int i = 0; i < 4; ++i) a[i] = seed + threadIdx.x * 1e-3 + i;
+  const double c = 1.0000000001e-3;
+  for (int it = 0; it < kIntIters; ++it) {
+#pragma unroll
+    for (int i = 0; i < 4; ++i) a[i] = cfft::dadd_int(a[i], c);
+  }
+  out[(size_t)blockIdx.x * blockDim.x + threadIdx.x] = a[0] + a[1] + a[2] + a[3];
+}
+}  // namespace
+
+extern "C" cfft_status cfft_diag_dadd_check(uint64_t count, uint64_t seed, uint64_t* mismatches, uint64_t* bad_pair) {
+  if (!mismatches) return cfft::fail(CFFT_ERR_INVALID_ARGUMENT, "null output pointer");
+  unsigned long long* d = nullptr;
+  CFFT_CUDA_TRY(cudaMalloc(&d, 3 * sizeof(unsigned long long)));
+  CFFT_CUDA_TRY(cudaMemset(d, 0, 3 * sizeof(unsigned long long)));
+  dadd_check_kernel<<<cfft::sm_count() * 8, 256>>>(count, seed, d, d + 1);
+  CFFT_CHECK_LAUNCH();
+  unsigned long long h[3];
+  CFFT_CUDA_TRY(cudaMemcpy(h, d, sizeof(h), cudaMemcpyDeviceToHost));
+  cudaFree(d);
+  *mismatches = h[0];
+  if (bad_pair) {
+    bad_pair[0] = h[1];
+    bad_pair[1] = h[2];
+  }
+  return CFFT_OK;
+}
+
+extern "C" cfft_status cfft_diag_dadd_int_rate(double* adds_per_second) {
+  if (!adds_per_second) return cfft::fail(CFFT_ERR_INVALID_ARGUMENT, "null output pointer");
+  const int blocks = cfft::sm_count() * 4, threads = 256;
+  double* d = nullptr;
+  CFFT_CUDA_TRY(cudaMalloc(&d, (size_t)blocks * threads * sizeof(double)));
+  cudaEvent_t e0, e1;
+  CFFT_CUDA_TRY(cudaEventCreate(&e0));
+  CFFT_CUDA_TRY(cudaEventCreate(&e1));
+  dadd_int_rate_kernel<<<blocks, threads>>>(d, 1.0);
+  CFFT_CUDA_TRY(cudaEventRecord(e0));
+  const int reps = 5;
+  for (int r = 0; r < reps; ++r) dadd_int_rate_kernel<<<blocks, threads>>>(d, 1.0);
+  CFFT_CUDA_TRY(cudaEventRecord(e1));
+  CFFT_CUDA_TRY(cudaEventSynchronize(e1));
+  float ms = 0;
+  cudaEventElapsedTime(&ms, e0, e1);
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  cudaFree(d);
+  CFFT_CHECK_LAUNCH();
+  *adds_per_second = (double)reps * blocks * threads * kIntIters * 4 / (ms * 1e-3);
   return CFFT_OK;
 }

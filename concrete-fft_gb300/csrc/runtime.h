@@ -44,6 +44,11 @@ cfft_status upload(const T* host, size_t count, T** dev) {
 
 int sm_count();
 
+// Launch a kernel through its pointer, raising its dynamic shared-memory limit
+// the first time it is used with more than 48 KiB.
+cfft_status launch_kernel(const void* fn, int grid, int block, void** args, size_t smem, cudaStream_t stream);
+int max_blocks_per_sm(const void* fn, int block, size_t smem);
+
 // Persistent scratch for the *_host convenience entry points (one per thread).
 cfft_status host_staging(size_t bytes, void** dev_ptr, cudaStream_t* stream);
 

@@ -36,7 +36,7 @@ struct Log2<16> {
 // DIF: in[k] = src[k*n/R + p*s + q], dst[R*s*p + k*s + q] = w_k * core(in)_k.
 // DIT: in[k] = w_k * src[R*s*p + k*s + q], dst[k*n/R + p*s + q] = core(in)_k.
 // w is the second half of the init_wt table: w_k = w[R*s*p + k].
-template <int R, bool FWD, bool DIT>
+template <int R, bool FWD, bool DIT, int E>
 __device__ __forceinline__ void stockham_pass(int log2n, int log2s, int nchunks, const double2* src, double2* dst,
                                               const double2* __restrict__ w, int tid, int nth) {
   constexpr int LR = Log2<R>::v;
@@ -55,7 +55,7 @@ __device__ __forceinline__ void stockham_pass(int log2n, int log2s, int nchunks,
     if (!DIT) {
 #pragma unroll
       for (int k = 0; k < R; ++k) v[k] = ld(sc + (k << lper) + (p << log2s) + q);
-      Core<R, FWD>::run(v);
+      Core<R, FWD, E>::run(v);
       double2* o = dc + (p << (log2s + LR)) + q;
       st(o, v[0]);
 #pragma unroll
@@ -65,7 +65,7 @@ __device__ __forceinline__ void stockham_pass(int log2n, int log2s, int nchunks,
       v[0] = ld(i0);
 #pragma unroll
       for (int k = 1; k < R; ++k) v[k] = cmul(ldg(tw + k), ld(i0 + (k << log2s)));
-      Core<R, FWD>::run(v);
+      Core<R, FWD, E>::run(v);
 #pragma unroll
       for (int k = 0; k < R; ++k) st(dc + (k << lper) + (p << log2s) + q, v[k]);
     }
@@ -73,7 +73,7 @@ __device__ __forceinline__ void stockham_pass(int log2n, int log2s, int nchunks,
 }
 
 // End butterfly of size M at stride n/M, in place (src/dif4.rs:195-244 and twins).
-template <int M, bool FWD>
+template <int M, bool FWD, int E>
 __device__ __forceinline__ void end_pass(int log2n, int nchunks, double2* x, int tid, int nth) {
   constexpr int LM = Log2<M>::v;
   const int log2s = log2n - LM;
@@ -84,23 +84,23 @@ __device__ __forceinline__ void end_pass(int log2n, int nchunks, double2* x, int
     c64 v[M];
 #pragma unroll
     for (int k = 0; k < M; ++k) v[k] = ld(xc + (k << log2s));
-    Core<M, FWD>::run(v);
+    Core<M, FWD, E>::run(v);
 #pragma unroll
     for (int k = 0; k < M; ++k) st(xc + (k << log2s), v[k]);
   }
 }
 
-template <int R, bool FWD>
+template <int R, bool FWD, int E>
 __device__ __forceinline__ void end_dispatch(int lm, int log2n, int nchunks, double2* x, int tid, int nth) {
-  if (lm == 1) end_pass<2, FWD>(log2n, nchunks, x, tid, nth);
+  if (lm == 1) end_pass<2, FWD, E>(log2n, nchunks, x, tid, nth);
   if constexpr (R >= 4) {
-    if (lm == 2) end_pass<4, FWD>(log2n, nchunks, x, tid, nth);
+    if (lm == 2) end_pass<4, FWD, E>(log2n, nchunks, x, tid, nth);
   }
   if constexpr (R >= 8) {
-    if (lm == 3) end_pass<8, FWD>(log2n, nchunks, x, tid, nth);
+    if (lm == 3) end_pass<8, FWD, E>(log2n, nchunks, x, tid, nth);
   }
   if constexpr (R >= 16) {
-    if (lm == 4) end_pass<16, FWD>(log2n, nchunks, x, tid, nth);
+    if (lm == 4) end_pass<16, FWD, E>(log2n, nchunks, x, tid, nth);
   }
 }
 
@@ -109,7 +109,7 @@ __device__ __forceinline__ void end_dispatch(int lm, int log2n, int nchunks, dou
 // remaining size exceeds R, then the end butterfly of the remaining size; DIT
 // runs the end butterfly first at the largest stride, then the passes in
 // reverse.  Returns the buffer (x or y) that holds the result.
-template <int R, bool FWD, bool DIT>
+template <int R, bool FWD, bool DIT, int E>
 __device__ double2* stockham_smem(int log2n, int nchunks, double2* x, double2* y, const double2* __restrict__ w,
                                   int tid, int nth) {
   constexpr int LR = Log2<R>::v;
@@ -123,19 +123,19 @@ __device__ double2* stockham_smem(int log2n, int nchunks, double2* x, double2* y
   double2* oth = y;
   if (!DIT) {
     for (int i = 0; i < npass; ++i) {
-      stockham_pass<R, FWD, false>(log2n, i * LR, nchunks, cur, oth, w, tid, nth);
+      stockham_pass<R, FWD, false, E>(log2n, i * LR, nchunks, cur, oth, w, tid, nth);
       __syncthreads();
       double2* t = cur;
       cur = oth;
       oth = t;
     }
-    end_dispatch<R, FWD>(lm, log2n, nchunks, cur, tid, nth);
+    end_dispatch<R, FWD, E>(lm, log2n, nchunks, cur, tid, nth);
     __syncthreads();
   } else {
-    end_dispatch<R, FWD>(lm, log2n, nchunks, cur, tid, nth);
+    end_dispatch<R, FWD, E>(lm, log2n, nchunks, cur, tid, nth);
     __syncthreads();
     for (int i = npass - 1; i >= 0; --i) {
-      stockham_pass<R, FWD, true>(log2n, i * LR, nchunks, cur, oth, w, tid, nth);
+      stockham_pass<R, FWD, true, E>(log2n, i * LR, nchunks, cur, oth, w, tid, nth);
       __syncthreads();
       double2* t = cur;
       cur = oth;
@@ -143,21 +143,6 @@ __device__ double2* stockham_smem(int log2n, int nchunks, double2* x, double2* y
     }
   }
   return cur;
-}
-
-template <bool FWD>
-__device__ double2* ordered_dispatch(int algo, int log2n, int nchunks, double2* x, double2* y,
-                                     const double2* __restrict__ w, int tid, int nth) {
-  switch (algo) {
-    case 0: return stockham_smem<2, FWD, false>(log2n, nchunks, x, y, w, tid, nth);
-    case 1: return stockham_smem<2, FWD, true>(log2n, nchunks, x, y, w, tid, nth);
-    case 2: return stockham_smem<4, FWD, false>(log2n, nchunks, x, y, w, tid, nth);
-    case 3: return stockham_smem<4, FWD, true>(log2n, nchunks, x, y, w, tid, nth);
-    case 4: return stockham_smem<8, FWD, false>(log2n, nchunks, x, y, w, tid, nth);
-    case 5: return stockham_smem<8, FWD, true>(log2n, nchunks, x, y, w, tid, nth);
-    case 6: return stockham_smem<16, FWD, false>(log2n, nchunks, x, y, w, tid, nth);
-    default: return stockham_smem<16, FWD, true>(log2n, nchunks, x, y, w, tid, nth);
-  }
 }
 
 // ---------------------------------------------------------------------------
@@ -173,14 +158,14 @@ __device__ __forceinline__ int slot(int k) {
   return ((k & 1) << 2) | (k & 2) | (k >> 2);
 }
 
-template <int R, bool FWD>
+template <int R, bool FWD, int E>
 __device__ __forceinline__ void outer_group(double2* zc, int lm, int i, const double2* __restrict__ wl) {
   c64 v[R];
   const double2* tw = wl + (R - 1) * i - 1;  // tw[k] = w_k, k >= 1
   if (FWD) {
 #pragma unroll
     for (int k = 0; k < R; ++k) v[k] = ld(zc + (k << lm) + i);
-    Core<R, true>::run(v);
+    Core<R, true, E>::run(v);
 #pragma unroll
     for (int k = 1; k < R; ++k) v[k] = cmul(ldg(tw + k), v[k]);
 #pragma unroll
@@ -189,14 +174,14 @@ __device__ __forceinline__ void outer_group(double2* zc, int lm, int i, const do
     v[0] = ld(zc + i);
 #pragma unroll
     for (int k = 1; k < R; ++k) v[k] = cmul(ldg(tw + k), ld(zc + (slot<R>(k) << lm) + i));
-    Core<R, false>::run(v);
+    Core<R, false, E>::run(v);
 #pragma unroll
     for (int k = 0; k < R; ++k) st(zc + (k << lm) + i, v[k]);
   }
 }
 
 // One level over `nchunks` chunks of 2^log2nl points stored back to back.
-template <bool FWD>
+template <bool FWD, int E>
 __device__ __forceinline__ void outer_level(int log2r, int log2nl, int nchunks, double2* z,
                                             const double2* __restrict__ wl, int tid, int nth) {
   const int lm = log2nl - log2r;
@@ -204,9 +189,9 @@ __device__ __forceinline__ void outer_level(int log2r, int log2nl, int nchunks, 
   for (int g = tid; g < total; g += nth) {
     double2* zc = z + ((g >> lm) << log2nl);
     const int i = g & ((1 << lm) - 1);
-    if (log2r == 1) outer_group<2, FWD>(zc, lm, i, wl);
-    else if (log2r == 2) outer_group<4, FWD>(zc, lm, i, wl);
-    else outer_group<8, FWD>(zc, lm, i, wl);
+    if (log2r == 1) outer_group<2, FWD, E>(zc, lm, i, wl);
+    else if (log2r == 2) outer_group<4, FWD, E>(zc, lm, i, wl);
+    else outer_group<8, FWD, E>(zc, lm, i, wl);
   }
 }
 
@@ -219,30 +204,53 @@ struct DevLevels {
   int winv_off[8];
 };
 
+template <int ALGO>
+struct AlgoInfo {
+  static constexpr int R = 2 << (ALGO / 2);
+  static constexpr bool DIT = (ALGO & 1) != 0;
+};
+
 // Unordered transform of `nchunks` (sub)transforms of size n_{d0} held in x:
-// fwd_depth (src/unordered.rs:392-439) or inv_depth (:442-489) from level d0.
-// w: the plan's forward table (forward) or inverse table (inverse).
-template <bool FWD>
-__device__ double2* unordered_smem(const DevLevels& L, int d0, int base_algo, int nchunks, double2* x, double2* y,
+// fwd_depth (src/unordered.rs:392-439) or inv_depth (:442-489) from level d0,
+// with the ordered base algorithm ALGO.  w: the plan's forward table
+// (forward) or inverse table (inverse).
+template <bool FWD, int E, int ALGO>
+__device__ double2* unordered_smem(const DevLevels& L, int d0, int nchunks, double2* x, double2* y,
                                    const double2* __restrict__ w, int tid, int nth) {
+  constexpr int R = AlgoInfo<ALGO>::R;
+  constexpr bool DIT = AlgoInfo<ALGO>::DIT;
   const int log2base = L.log2n[L.nlevels];
   const int log2sub = L.log2n[d0];
   const int nbase = nchunks << (log2sub - log2base);
   if (FWD) {
     for (int l = d0; l < L.nlevels; ++l) {
-      outer_level<true>(L.log2r[l], L.log2n[l], nchunks << (log2sub - L.log2n[l]), x, w + L.w_off[l], tid, nth);
+      outer_level<true, E>(L.log2r[l], L.log2n[l], nchunks << (log2sub - L.log2n[l]), x, w + L.w_off[l], tid, nth);
       __syncthreads();
     }
-    return ordered_dispatch<true>(base_algo, log2base, nbase, x, y, w + L.w_off[L.nlevels] + (1 << log2base), tid,
-                                  nth);
+    return stockham_smem<R, true, DIT, E>(log2base, nbase, x, y, w + L.w_off[L.nlevels] + (1 << log2base), tid,
+                                          nth);
   } else {
-    double2* r = ordered_dispatch<false>(base_algo, log2base, nbase, x, y, w + (1 << log2base), tid, nth);
+    double2* r = stockham_smem<R, false, DIT, E>(log2base, nbase, x, y, w + (1 << log2base), tid, nth);
     for (int l = L.nlevels - 1; l >= d0; --l) {
-      outer_level<false>(L.log2r[l], L.log2n[l], nchunks << (log2sub - L.log2n[l]), r, w + L.winv_off[l], tid, nth);
+      outer_level<false, E>(L.log2r[l], L.log2n[l], nchunks << (log2sub - L.log2n[l]), r, w + L.winv_off[l], tid,
+                            nth);
       __syncthreads();
     }
     return r;
   }
+}
+
+// Integer-add levels (eighths of the butterfly additions on the integer pipe)
+// that have kernel instantiations.  E = 0 exists for every algorithm; E > 0
+// only for the radix-4 algorithms (Dif4, Dit4), whose butterflies keep the
+// register footprint of the emulated additions small.
+constexpr int kEmuLevels[] = {0, 4, 6, 7, 8};
+inline int emu_level_for(int algo, int e) {
+  if (algo != 2 && algo != 3) return 0;
+  int best = 0;
+  for (int v : kEmuLevels)
+    if (v <= e) best = v;
+  return best;
 }
 
 }  // namespace cfft

@@ -85,6 +85,14 @@ cfft_status cfft_ordered_inv(const cfft_ordered_plan* plan, double* buf, size_t 
 cfft_status cfft_ordered_fwd_host(const cfft_ordered_plan* plan, double* buf, size_t batch);
 cfft_status cfft_ordered_inv_host(const cfft_ordered_plan* plan, double* buf, size_t batch);
 
+/* Integer-pipe share of the butterfly additions (no counterpart in the
+ * reference).  GB300 issues FP64 at 1/64 of its integer rate; `eighths` (0..8)
+ * of every butterfly's additions run as an exact integer-pipe IEEE add
+ * instead, alongside the FP64 pipe.  Results are bit-identical for every
+ * value; only the speed changes.  Measure-created plans tune it themselves. */
+cfft_status cfft_ordered_set_int_adds(cfft_ordered_plan* plan, int eighths);
+int cfft_ordered_int_adds(const cfft_ordered_plan* plan);
+
 /* ===================================================== unordered::Plan ====
  * Replaces src/unordered.rs:496-1036.  Any power-of-two n up to 2^20 with a
  * base (internal ordered) size base_n <= 1024, base_n >= 32 unless base_n == n
@@ -124,6 +132,10 @@ cfft_status cfft_unordered_to_standard_host(const cfft_unordered_plan* plan, con
 cfft_status cfft_unordered_from_standard_host(const cfft_unordered_plan* plan, const double* standard,
                                               double* permuted, size_t batch);
 
+/* Integer-pipe share of the butterfly additions, as cfft_ordered_set_int_adds. */
+cfft_status cfft_unordered_set_int_adds(cfft_unordered_plan* plan, int eighths);
+int cfft_unordered_int_adds(const cfft_unordered_plan* plan);
+
 /* ======================================================== fft128::Plan ====
  * Replaces src/fft128/mod.rs:1832-1960.  n a power of two, 32 <= n <= 8192.
  * Split double-double storage: four f64 arrays (re0, re1, im0, im1), each
@@ -160,6 +172,9 @@ cfft_status cfft_u64_product_plan_create_measure(size_t N, double seconds_per_al
 void cfft_u64_product_plan_destroy(cfft_u64_product_plan* plan);
 size_t cfft_u64_product_poly_size(const cfft_u64_product_plan* plan);
 void cfft_u64_product_algo(const cfft_u64_product_plan* plan, cfft_algo* base_algo, size_t* base_n);
+/* Integer-pipe share of the butterfly additions, as cfft_ordered_set_int_adds. */
+cfft_status cfft_u64_product_set_int_adds(cfft_u64_product_plan* plan, int eighths);
+int cfft_u64_product_int_adds(const cfft_u64_product_plan* plan);
 /* b: `count` polynomials of N signed digits -> bhat: count * N/2 c64. */
 cfft_status cfft_u64_prepare_operand(const cfft_u64_product_plan* plan, const int64_t* b, double* bhat, size_t count,
                                      void* stream);

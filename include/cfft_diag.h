@@ -15,6 +15,17 @@ extern "C" {
  * by this rate on GB300, where FP64 runs at 1/64 of the FP32 rate. */
 cfft_status cfft_diag_fp64_peak(double* ops_per_second);
 
+/* Self-check of the integer-pipe double addition used by the FFT kernels:
+ * `count` operand pairs from four generators (random bit patterns, random
+ * exponent gaps, near-cancellation, constructed rounding ties), each summed by
+ * the integer routine and by the native FP64 add.  *mismatches receives the
+ * number of pairs whose results differ in any bit (NaN payloads excepted);
+ * bad_pair (may be NULL) receives the first differing pair's bit patterns. */
+cfft_status cfft_diag_dadd_check(uint64_t count, uint64_t seed, uint64_t* mismatches, uint64_t* bad_pair);
+
+/* Issue rate of the integer-pipe double addition alone (additions per second). */
+cfft_status cfft_diag_dadd_int_rate(double* adds_per_second);
+
 #ifdef __cplusplus
 }
 #endif

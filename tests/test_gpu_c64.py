@@ -54,6 +54,34 @@ def test_ordered_batch_256_n1024(cuda, oracle):
         assert rel < 1e-13
 
 
+@pytest.mark.parametrize("algo", [2, 3])
+def test_int_adds_levels_bit_exact(cuda, oracle, algo):
+    """Ordered and unordered transforms at every integer-pipe addition level."""
+    import concrete_fft as cf
+    torch = cuda
+    for n in (16, 256, 1024):
+        plan = cf.ordered.Plan(n, cf.ordered.Method.UserProvided(algo))
+        x = rand_c64(7, n)
+        want_f = oracle.ordered_fwd(algo, x)
+        want_i = oracle.ordered_inv(algo, want_f)
+        for e in (0, 4, 6, 7, 8):
+            plan.set_int_adds(e)
+            d = on_gpu(torch, x)
+            plan.fwd(d)
+            assert np.array_equal(bits(d.cpu().numpy()), bits(want_f)), (n, e)
+            plan.inv(d)
+            assert np.array_equal(bits(d.cpu().numpy()), bits(want_i)), (n, e)
+    for n, base in ((2048, 512), (8192, 1024), (65536, 64)):
+        plan = cf.unordered.Plan(n, cf.unordered.Method.UserProvided(algo, base))
+        x = rand_c64(2, n)
+        want = oracle.unordered_fwd(algo, base, x, nthreads=0)
+        for e in (0, 6, 8):
+            plan.set_int_adds(e)
+            d = on_gpu(torch, x)
+            plan.fwd(d)
+            assert np.array_equal(bits(d.cpu().numpy()), bits(want)), (n, base, e)
+
+
 def test_unordered_golden_vector_on_gpu(cuda):
     """The reference's exact golden vector (src/unordered.rs:1176-9395) reproduced by the GPU."""
     import concrete_fft as cf

@@ -38,6 +38,27 @@ def test_u64_product_bit_exact(cuda, oracle, N, base_algo, base_n):
     assert torus_err_bits(got[:2], exact) <= torus_err_bits(want[:2], exact)
 
 
+@pytest.mark.parametrize("algo", [2, 3])
+def test_u64_product_int_adds_bit_exact(cuda, oracle, algo):
+    """Every integer-pipe addition level gives the same bits as the oracle."""
+    import concrete_fft as cf
+    torch = cuda
+    N, count = 2048, 5
+    a = RNG.integers(0, 2 ** 64, (count, N), dtype=np.uint64)
+    b = RNG.integers(-2 ** 7, 2 ** 7, (count, N))
+    for base in (1024, 512):
+        plan = cf.product.U64ProductPlan(N, algo, base)
+        bhat = torch.empty((count, N // 2), dtype=torch.complex128, device="cuda")
+        plan.prepare_operand(torch.from_numpy(b).cuda(), bhat)
+        want = oracle.u64_product(N, algo, base, a, oracle.u64_prepare(N, algo, base, b), nthreads=0)
+        for e in (0, 4, 6, 7, 8):
+            plan.set_int_adds(e)
+            assert plan.int_adds() == e
+            out = torch.empty((count, N), dtype=torch.int64, device="cuda")
+            plan.product(torch.from_numpy(a.view(np.int64)).cuda(), bhat, out)
+            assert np.array_equal(out.cpu().numpy().view(np.uint64), want), (algo, base, e)
+
+
 def test_u64_product_exact_when_small(cuda, oracle):
     """Bit-exact against the schoolbook wherever the exact sums fit in 53 bits."""
     import concrete_fft as cf

@@ -86,6 +86,12 @@ _SIGS = [
     ("cfft_u64_prepare_operand", c_int, [vp, vp, vp, c_size, vp]),
     ("cfft_u64_product", c_int, [vp, vp, vp, c_size, vp, c_size, vp]),
     ("cfft_u64_product_host", c_int, [vp, vp, vp, c_size, vp, c_size]),
+    ("cfft_batch_create", c_int, [vp, c_size, c_dbl, pp]),
+    ("cfft_batch_destroy", None, [vp]),
+    ("cfft_batch_units", c_size, [vp]),
+    ("cfft_batch_schedule", c_int, [vp, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_uint32, ctypes.POINTER(c_int),
+                                    ctypes.POINTER(c_size), ctypes.POINTER(ctypes.c_uint32)]),
+    ("cfft_batch_run", c_int, [vp, vp, vp]),
     ("cfft_u128_product_plan_create", c_int, [c_size, pp]),
     ("cfft_u128_product_plan_destroy", None, [vp]),
     ("cfft_u128_product_poly_size", c_size, [vp]),

@@ -92,7 +92,7 @@ struct C64Plan {
   int d0 = 0;        // first level handled in shared memory
   int threads = 128;  // CTA size of the shared-memory kernel
   int tpc = 1;       // sub-transforms per CTA
-  int emu = 6;       // eighths of the butterfly additions issued on the integer pipe
+  int emu = 0;       // eighths of the butterfly additions issued on the integer pipe
 };
 
 struct cfft_ordered_plan {

@@ -10,9 +10,6 @@ template <int A>
 static const void* pick_e(int e, bool fwd) {
   switch (e) {
     case 4: return pick<A, 4>(fwd);
-    case 6: return pick<A, 6>(fwd);
-    case 7: return pick<A, 7>(fwd);
-    case 8: return pick<A, 8>(fwd);
     default: return nullptr;
   }
 }

@@ -6,9 +6,6 @@ template <int A>
 static const void* pick(int e) {
   switch (e) {
     case 4: return (const void*)u64_product_kernel<A, 4, kProdThreads>;
-    case 6: return (const void*)u64_product_kernel<A, 6, kProdThreads>;
-    case 7: return (const void*)u64_product_kernel<A, 7, kProdThreads>;
-    case 8: return (const void*)u64_product_kernel<A, 8, kProdThreads>;
     default: return nullptr;
   }
 }

@@ -34,7 +34,7 @@ struct cfft_u64_product_plan {
   LevelDesc lv{};
   DevLevels dlv{};
   double2 *d_w = nullptr, *d_winv = nullptr, *d_tw = nullptr, *d_itw = nullptr;
-  int emu = 7;  // eighths of the butterfly additions issued on the integer pipe
+  int emu = 0;  // eighths of the butterfly additions issued on the integer pipe
 };
 
 namespace {
@@ -273,22 +273,37 @@ cfft_status cfft_u64_product_plan_create_measure(size_t N, double seconds, cfft_
   return CFFT_OK;
 }
 
+// Host-buffer products: the batch is cut into chunks that flow through three
+// streams, so the host-to-device copy of one chunk, the kernel of the previous
+// one and the device-to-host copy of the one before overlap (copy engines and
+// SMs work at once).  Returns when every result is in host memory.
 cfft_status cfft_u64_product_host(const cfft_u64_product_plan* plan, const uint64_t* a, const double* bhat,
                                   size_t bhat_stride, uint64_t* out, size_t count) {
   if (!plan || !a || !bhat || !out) return fail(CFFT_ERR_INVALID_ARGUMENT, "null argument");
+  if (bhat_stride != 0 && bhat_stride != plan->n)
+    return fail(CFFT_ERR_INVALID_ARGUMENT, "bhat_stride must be 0 or N/2");
   if (count == 0) return CFFT_OK;
-  const size_t bytes = count * plan->N * sizeof(uint64_t);
-  void* d;
-  cudaStream_t s;
-  cfft_status st = host_staging(2 * bytes, &d, &s);
+  constexpr int kSlots = 3;
+  const size_t poly_bytes = plan->N * sizeof(uint64_t);
+  // about 8 chunks per call, each at least one full wave of CTAs
+  const size_t min_chunk = (size_t)sm_count() * 4;
+  const size_t chunk = std::min(count, std::max(min_chunk, (count + 7) / 8));
+  PipeSlot slot[kSlots];
+  cfft_status st = host_pipeline(kSlots, 2 * chunk * poly_bytes, slot);
   if (st != CFFT_OK) return st;
-  uint64_t* da = (uint64_t*)d;
-  uint64_t* dout = (uint64_t*)((char*)d + bytes);
-  CFFT_CUDA_TRY(cudaMemcpyAsync(da, a, bytes, cudaMemcpyHostToDevice, s));
-  st = cfft_u64_product(plan, da, bhat, bhat_stride, dout, count, s);
-  if (st != CFFT_OK) return st;
-  CFFT_CUDA_TRY(cudaMemcpyAsync(out, dout, bytes, cudaMemcpyDeviceToHost, s));
-  CFFT_CUDA_TRY(cudaStreamSynchronize(s));
+  size_t i = 0;
+  for (size_t first = 0; first < count; first += chunk, ++i) {
+    const size_t c = std::min(chunk, count - first);
+    const PipeSlot& sl = slot[i % kSlots];
+    uint64_t* da = (uint64_t*)sl.dev;
+    uint64_t* dout = da + chunk * plan->N;
+    CFFT_CUDA_TRY(cudaMemcpyAsync(da, a + first * plan->N, c * poly_bytes, cudaMemcpyHostToDevice, sl.stream));
+    const double* bh = bhat + (bhat_stride ? first * bhat_stride * 2 : 0);
+    st = cfft_u64_product(plan, da, bh, bhat_stride, dout, c, sl.stream);
+    if (st != CFFT_OK) return st;
+    CFFT_CUDA_TRY(cudaMemcpyAsync(out + first * plan->N, dout, c * poly_bytes, cudaMemcpyDeviceToHost, sl.stream));
+  }
+  for (int k = 0; k < kSlots; ++k) CFFT_CUDA_TRY(cudaStreamSynchronize(slot[k].stream));
   return CFFT_OK;
 }
 

@@ -103,6 +103,42 @@ int max_blocks_per_sm(const void* fn, int block, size_t smem) {
   return per_sm > 0 ? per_sm : 1;
 }
 
+namespace {
+constexpr int kMaxSlots = 4;
+struct Pipeline {
+  void* ptr[kMaxSlots] = {nullptr, nullptr, nullptr, nullptr};
+  size_t cap = 0;
+  cudaStream_t stream[kMaxSlots] = {nullptr, nullptr, nullptr, nullptr};
+  int device = -1;
+};
+thread_local Pipeline t_pipe;
+}  // namespace
+
+cfft_status host_pipeline(int nslots, size_t bytes, PipeSlot* slots) {
+  if (nslots < 1 || nslots > kMaxSlots) return fail(CFFT_ERR_INVALID_ARGUMENT, "bad pipeline depth");
+  int dev = 0;
+  CFFT_CUDA_TRY(cudaGetDevice(&dev));
+  Pipeline& p = t_pipe;
+  if (p.device != dev) {
+    p = Pipeline();
+    p.device = dev;
+  }
+  for (int i = 0; i < kMaxSlots; ++i)
+    if (!p.stream[i]) CFFT_CUDA_TRY(cudaStreamCreateWithFlags(&p.stream[i], cudaStreamNonBlocking));
+  if (bytes > p.cap) {
+    for (int i = 0; i < kMaxSlots; ++i) {
+      CFFT_CUDA_TRY(cudaStreamSynchronize(p.stream[i]));
+      if (p.ptr[i]) CFFT_CUDA_TRY(cudaFree(p.ptr[i]));
+      p.ptr[i] = nullptr;
+    }
+    p.cap = 0;
+    for (int i = 0; i < kMaxSlots; ++i) CFFT_CUDA_TRY(cudaMalloc(&p.ptr[i], bytes));
+    p.cap = bytes;
+  }
+  for (int i = 0; i < nslots; ++i) slots[i] = PipeSlot{p.ptr[i], p.stream[i]};
+  return CFFT_OK;
+}
+
 }  // namespace cfft
 
 extern "C" {

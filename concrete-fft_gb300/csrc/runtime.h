@@ -52,4 +52,12 @@ int max_blocks_per_sm(const void* fn, int block, size_t smem);
 // Persistent scratch for the *_host convenience entry points (one per thread).
 cfft_status host_staging(size_t bytes, void** dev_ptr, cudaStream_t* stream);
 
+// Copy/compute pipeline of the *_host product entry points: `nslots` device
+// buffers of `bytes` each, one stream per slot (per thread, grown on demand).
+struct PipeSlot {
+  void* dev;
+  cudaStream_t stream;
+};
+cfft_status host_pipeline(int nslots, size_t bytes, PipeSlot* slots);
+
 }  // namespace cfft

@@ -241,10 +241,11 @@ __device__ double2* unordered_smem(const DevLevels& L, int d0, int nchunks, doub
 }
 
 // Integer-add levels (eighths of the butterfly additions on the integer pipe)
-// that have kernel instantiations.  E = 0 exists for every algorithm; E > 0
-// only for the radix-4 algorithms (Dif4, Dit4), whose butterflies keep the
-// register footprint of the emulated additions small.
-constexpr int kEmuLevels[] = {0, 4, 6, 7, 8};
+// that have kernel instantiations.  E = 0 exists for every algorithm; E = 4
+// only for the radix-4 algorithms (Dif4, Dit4).  Measured on GB300 the
+// integer-pipe add issues at half the FP64 add rate and raises register
+// pressure, so E = 0 is the default and the tuner's usual choice.
+constexpr int kEmuLevels[] = {0, 4};
 inline int emu_level_for(int algo, int e) {
   if (algo != 2 && algo != 3) return 0;
   int best = 0;

@@ -198,6 +198,35 @@ cfft_status cfft_u128_prepare_operand(const cfft_u128_product_plan* plan, const 
 cfft_status cfft_u128_product(const cfft_u128_product_plan* plan, const uint64_t* a, const double* bhat4,
                               size_t bhat_stride, uint64_t* out, size_t count, void* stream);
 
+/* ============================================ mixed-size batch (persistent) ====
+ * Many c64 transforms of different sizes and kinds in one persistent kernel
+ * launch (no counterpart in the reference, whose plans transform one buffer of
+ * one size per call).  Items live anywhere in one device buffer; each is the
+ * transform the matching ordered::Plan / unordered::Plan would compute, with
+ * the schedule below, and its result is bit-identical to that plan's. */
+typedef struct cfft_batch_item {
+  uint64_t offset;     /* first point of the item in the buffer (c64 units) */
+  uint32_t log2n;      /* size 2^log2n: ordered 1..10, unordered 1..16 */
+  uint32_t kind;       /* 0: ordered::Plan, 1: unordered::Plan */
+  uint32_t direction;  /* 1: fwd, 2: inv, 3: fwd then inv (one shared-memory residency) */
+  uint32_t reserved;   /* must be 0 */
+} cfft_batch_item;
+typedef struct cfft_batch cfft_batch;
+/* Groups the items into same-size work units ordered longest first and picks
+ * each size class's schedule (base algorithm, base size, transforms per unit).
+ * tune_seconds > 0 times the candidates on the device for about that long per
+ * candidate (the analogue of Method::Measure); 0 keeps the default schedule. */
+cfft_status cfft_batch_create(const cfft_batch_item* items, size_t count, double tune_seconds, cfft_batch** out);
+void cfft_batch_destroy(cfft_batch* batch);
+size_t cfft_batch_units(const cfft_batch* batch);
+/* The schedule chosen for one size class. */
+cfft_status cfft_batch_schedule(const cfft_batch* batch, uint32_t kind, uint32_t log2n, uint32_t direction,
+                                cfft_algo* base_algo, size_t* base_n, uint32_t* per_unit);
+/* One persistent launch over every item, in place on `data`.  On a non-NULL
+ * stream the launch is captured into a CUDA graph on first use (per stream and
+ * buffer) and replayed afterwards.  Runs of one batch must not overlap. */
+cfft_status cfft_batch_run(cfft_batch* batch, double* data, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

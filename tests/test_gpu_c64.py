@@ -64,7 +64,7 @@ def test_int_adds_levels_bit_exact(cuda, oracle, algo):
         x = rand_c64(7, n)
         want_f = oracle.ordered_fwd(algo, x)
         want_i = oracle.ordered_inv(algo, want_f)
-        for e in (0, 4, 6, 7, 8):
+        for e in (0, 4):
             plan.set_int_adds(e)
             d = on_gpu(torch, x)
             plan.fwd(d)
@@ -75,7 +75,7 @@ def test_int_adds_levels_bit_exact(cuda, oracle, algo):
         plan = cf.unordered.Plan(n, cf.unordered.Method.UserProvided(algo, base))
         x = rand_c64(2, n)
         want = oracle.unordered_fwd(algo, base, x, nthreads=0)
-        for e in (0, 6, 8):
+        for e in (0, 4):
             plan.set_int_adds(e)
             d = on_gpu(torch, x)
             plan.fwd(d)

@@ -51,7 +51,7 @@ def test_u64_product_int_adds_bit_exact(cuda, oracle, algo):
         bhat = torch.empty((count, N // 2), dtype=torch.complex128, device="cuda")
         plan.prepare_operand(torch.from_numpy(b).cuda(), bhat)
         want = oracle.u64_product(N, algo, base, a, oracle.u64_prepare(N, algo, base, b), nthreads=0)
-        for e in (0, 4, 6, 7, 8):
+        for e in (0, 4):
             plan.set_int_adds(e)
             assert plan.int_adds() == e
             out = torch.empty((count, N), dtype=torch.int64, device="cuda")

@@ -326,6 +326,210 @@ def run_gb300(args):
     print(json.dumps(line))
 
 
+# ---------------------------------------------------------------- other workloads
+def fp64_ops_ordered(n, algo):
+    return fp64_ops_per_transform(n, n, algo)
+
+
+def gpu_setup():
+    import torch
+    rank, world, local = dist_env()
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    sys.path.insert(0, PKG)
+    import concrete_fft as cf
+    cf.check(cf.load().cfft_device_check())
+    return torch, cf, rank, world, local
+
+
+def timed(torch, fn, steps, warmup, local, world):
+    """CUDA-event time of `steps` calls of fn (after warm-up), max over ranks, with clocks."""
+    stream = torch.cuda.current_stream()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    with ClockSampler(local) as clk:
+        time.sleep(0.5)
+        for _ in range(warmup):
+            fn()
+        torch.cuda.synchronize()
+        if world > 1:
+            torch.distributed.barrier()
+        t0 = time.time()
+        e0.record(stream)
+        for _ in range(steps):
+            fn()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        if world > 1:
+            torch.distributed.barrier()
+        clk.mark(t0, time.time())
+    ms = e0.elapsed_time(e1)
+    if world > 1:
+        t = torch.tensor([ms], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms = float(t.item())
+    return ms, clk.summary()
+
+
+def fp64_peak(cf):
+    import ctypes
+    r = ctypes.c_double()
+    cf.check(cf.load().cfft_diag_fp64_peak(ctypes.byref(r)))
+    return r.value
+
+
+def run_mixed(args):
+    """100,000 c64 transforms, sizes 2^k with k uniform in 8..16, half ordered and half unordered,
+    forward then inverse, one persistent launch per step (CUDA graph replay)."""
+    import numpy as np
+    torch, cf, rank, world, local = gpu_setup()
+    count = args.mixed_items
+    rng = np.random.default_rng(3 + rank)
+    log2n = rng.integers(8, 17, count)
+    kind = rng.integers(0, 2, count)
+    kind = np.where(log2n > 10, 1, kind)  # the reference has no ordered plan above 1024 points
+    sizes = (1 << log2n).astype(np.int64)
+    offs = np.concatenate([[0], np.cumsum(sizes)[:-1]]).astype(np.uint64)
+    items = np.zeros(count, dtype=cf.batch.ITEM_DTYPE)
+    items["offset"], items["log2n"], items["kind"], items["direction"] = offs, log2n, kind, 3
+    total = int(sizes.sum())
+    t0 = time.perf_counter()
+    b = cf.batch.Batch(items, tune_seconds=args.tune_seconds)
+    tune_s = time.perf_counter() - t0
+    g = torch.Generator(device="cuda")
+    g.manual_seed(3 + rank)
+    data = (torch.rand((total, 2), dtype=torch.float64, device="cuda", generator=g) * 2 - 1)
+    stream = torch.cuda.Stream()
+    with torch.cuda.stream(stream):
+        ms, clocks = timed(torch, lambda: b.run(data), args.steps, args.warmup, local, world)
+    transforms = 2 * count  # forward and inverse of every item
+    value = world * transforms * args.steps / (ms * 1e-3)
+    per_launch = ms * 1e-3 / args.steps
+    ops = 0
+    sched = {}
+    for k in range(8, 17):
+        for kd in (0, 1):
+            sel = (log2n == k) & (kind == kd)
+            if not sel.any():
+                continue
+            algo, base, tpc = b.schedule(kd, k, 3)
+            sched["%s%d" % ("o" if kd == 0 else "u", k)] = [algo.name, base, tpc]
+            ops += int(sel.sum()) * 2 * fp64_ops_per_transform(1 << k, base, int(algo))
+    peak = fp64_peak(cf)
+    bytes_alg = total * 32
+    peaks, kindp = measured_peaks()
+    # end to end: host data in, host data out through the same launch
+    host = data.cpu().pin_memory()
+    back = torch.empty_like(host).pin_memory()
+    torch.cuda.synchronize()
+    t1 = time.perf_counter()
+    e2e_steps = 2
+    with torch.cuda.stream(stream):
+        for _ in range(e2e_steps):
+            data.copy_(host, non_blocking=True)
+            b.run(data)
+            back.copy_(data, non_blocking=True)
+        torch.cuda.current_stream().synchronize()
+    e2e_s = time.perf_counter() - t1
+    if rank != 0:
+        return
+    print(json.dumps({
+        "metric": "mixed-size c64 transforms/s (100k items, n=2^8..2^16, fwd then inv)", "value": value,
+        "unit": "transforms/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f64", "data": "synthetic (seeded)",
+        "config": {"workload": "mixed batch, %d items, %d points, one persistent launch per step (graph)" % (count, total),
+                   "schedule": sched, "units": b.units(), "tune_seconds_total": tune_s,
+                   "ordered_items": int((kind == 0).sum())},
+        "roofline": {"bound": "hbm", "achieved": bytes_alg / per_launch / 1e9, "peak": peaks["hbm_gbs"],
+                     "unit": "GB/s", "frac": bytes_alg / per_launch / 1e9 / peaks["hbm_gbs"], "traffic": None,
+                     "fp64": {"achieved_ops_per_s": ops / per_launch, "peak_ops_per_s": peak,
+                              "frac": ops / per_launch / peak}},
+        "e2e": {"value": world * transforms * e2e_steps / e2e_s, "unit": "transforms/s",
+                "h2d_bytes_per_step": total * 16, "d2h_bytes_per_step": total * 16},
+        "clocks": clocks, "gpu_launches": args.steps,
+    }))
+
+
+def run_ordered(args):
+    """ordered::Plan n = 1024, fwd then inv, batch 256 (throughput) and batch 1 (latency)."""
+    import numpy as np
+    torch, cf, rank, world, local = gpu_setup()
+    plan = cf.ordered.Plan(1024, cf.ordered.Method.Measure(0.002))
+    rng = np.random.default_rng(1)
+    x = rng.uniform(-1, 1, (256, 1024)) + 1j * rng.uniform(-1, 1, (256, 1024))
+    d = torch.from_numpy(x).cuda()
+    one = d[:1].clone()
+
+    def step256():
+        plan.fwd(d)
+        plan.inv(d)
+
+    def step1():
+        plan.fwd(one)
+        plan.inv(one)
+
+    ms256, clocks = timed(torch, step256, args.steps, args.warmup, local, world)
+    ms1, _ = timed(torch, step1, args.steps, args.warmup, local, world)
+    per = ms256 * 1e-3 / args.steps
+    ops = 256 * 2 * fp64_ops_ordered(1024, int(plan.algo()))
+    peak = fp64_peak(cf)
+    h = x.copy()
+    t0 = time.perf_counter()
+    for _ in range(max(3, args.steps // 10)):
+        plan.fwd(h)
+        plan.inv(h)
+    e2e = world * 512 * max(3, args.steps // 10) / (time.perf_counter() - t0)
+    if rank != 0:
+        return
+    print(json.dumps({
+        "metric": "ordered c64 n=1024 transforms/s (batch 256, fwd then inv)",
+        "value": world * 512 * args.steps / (ms256 * 1e-3), "unit": "transforms/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms256 / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded numpy PCG64)",
+        "config": {"workload": "ordered::Plan n=1024 batch 256", "algo": plan.algo().name,
+                   "batch1_us_per_fwd_inv": ms1 * 1e3 / args.steps},
+        "roofline": {"bound": "hbm", "achieved": 256 * 65536 / per / 1e9, "peak": measured_peaks()[0]["hbm_gbs"],
+                     "unit": "GB/s", "frac": 256 * 65536 / per / 1e9 / measured_peaks()[0]["hbm_gbs"],
+                     "traffic": None, "fp64": {"achieved_ops_per_s": ops / per, "peak_ops_per_s": peak,
+                                               "frac": ops / per / peak}},
+        "e2e": {"value": e2e, "unit": "transforms/s", "h2d_bytes_per_step": 256 * 1024 * 16,
+                "d2h_bytes_per_step": 256 * 1024 * 16},
+        "clocks": clocks, "gpu_launches": 2 * args.steps,
+    }))
+
+
+def run_u128(args):
+    """u128 negacyclic products N = 1024 and 4096, 2048 per launch, B digits in [-2^15, 2^15)."""
+    import numpy as np
+    torch, cf, rank, world, local = gpu_setup()
+    res = {}
+    clocks = None
+    for N in (1024, 4096):
+        plan = cf.product.U128ProductPlan(N)
+        rng = np.random.default_rng(4)
+        count = 2048
+        a = torch.from_numpy(rng.integers(0, 2 ** 64, (count, N, 2), dtype=np.uint64).view(np.int64)).cuda()
+        b = torch.from_numpy(rng.integers(-2 ** 15, 2 ** 15, (count, N))).cuda()
+        bhat = torch.empty((count, 4, N // 2), dtype=torch.float64, device="cuda")
+        plan.prepare_operand(b, bhat)
+        out = torch.empty_like(a)
+        ms, clocks = timed(torch, lambda: plan.product(a, bhat, out), args.steps, args.warmup, local, world)
+        res[N] = world * count * args.steps / (ms * 1e-3)
+    if rank != 0:
+        return
+    print(json.dumps({
+        "metric": "u128 negacyclic polymul/s (double-double)", "value": res[1024], "unit": "products/s",
+        "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64x2 (double-double)", "data": "synthetic (seeded numpy PCG64)",
+        "config": {"workload": "u128 product, 2048 per launch", "N1024_products_per_s": res[1024],
+                   "N4096_products_per_s": res[4096]},
+        "clocks": clocks, "gpu_launches": 2 * args.steps,
+    }))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -341,11 +545,21 @@ def main():
                     help="eighths of butterfly additions on the integer pipe (default: the plan's tuned value)")
     ap.add_argument("--profile-case", action="store_true",
                     help="small fixed case for ncu: 1 warm-up + 1 launch, no timing")
+    ap.add_argument("--workload", choices=["u64_product", "mixed", "ordered", "u128_product"], default="u64_product",
+                    help="u64_product (default headline) or one of the other benchmark configurations")
+    ap.add_argument("--mixed-items", type=int, default=100000)
+    ap.add_argument("--tune-seconds", type=float, default=0.0005)
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
     if args.impl == "reference":
         run_reference(args)
+    elif args.workload == "mixed":
+        run_mixed(args)
+    elif args.workload == "ordered":
+        run_ordered(args)
+    elif args.workload == "u128_product":
+        run_u128(args)
     else:
         run_gb300(args)
 

@@ -81,6 +81,10 @@ _SIGS = [
     ("cfft_u64_product_plan_destroy", None, [vp]),
     ("cfft_u64_product_poly_size", c_size, [vp]),
     ("cfft_u64_product_algo", None, [vp, ctypes.POINTER(c_int), ctypes.POINTER(c_size)]),
+    ("cfft_u64_fold_twist", c_int, [vp, vp, vp, c_size, vp]),
+    ("cfft_c64_pointwise", c_int, [vp, c_size, vp, c_size, c_size, vp]),
+    ("cfft_u64_untwist_round", c_int, [vp, vp, vp, c_size, vp]),
+    ("cfft_u64_product_fft", vp, [vp]),
     ("cfft_u64_product_set_int_adds", c_int, [vp, c_int]),
     ("cfft_u64_product_int_adds", c_int, [vp]),
     ("cfft_u64_prepare_operand", c_int, [vp, vp, vp, c_size, vp]),
@@ -92,6 +96,21 @@ _SIGS = [
     ("cfft_batch_schedule", c_int, [vp, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_uint32, ctypes.POINTER(c_int),
                                     ctypes.POINTER(c_size), ctypes.POINTER(ctypes.c_uint32)]),
     ("cfft_batch_run", c_int, [vp, vp, vp]),
+    ("cfft_product_engine_create", c_int, [vp, c_size, pp]),
+    ("cfft_product_engine_destroy", None, [vp]),
+    ("cfft_product_engine_workspace_bytes", c_size, [vp]),
+    ("cfft_product_engine_plan", vp, [vp, ctypes.c_uint32]),
+    ("cfft_product_engine_run", c_int, [vp, vp, c_size, vp, vp, vp]),
+    ("cfft_server_create", c_int, [vp, vp, c_size, ctypes.c_uint64, ctypes.c_uint64, ctypes.c_uint64, pp]),
+    ("cfft_server_destroy", None, [vp]),
+    ("cfft_server_run", c_int, [vp, vp, vp]),
+    ("cfft_server_recorded", c_size, [vp]),
+    ("cfft_server_recorded_ids", c_int, [vp, vp, c_size]),
+    ("cfft_server_recorded_output", c_int, [vp, ctypes.c_uint64, vp, c_size]),
+    ("cfft_server_request_shape", c_int, [vp, vp, ctypes.c_uint64, ctypes.POINTER(ctypes.c_uint32),
+                                          ctypes.POINTER(ctypes.c_uint32)]),
+    ("cfft_server_request_inputs", c_int, [vp, vp, ctypes.c_uint64, vp, vp]),
+    ("cfft_server_run_alone", c_int, [vp, vp, ctypes.c_uint64, vp, c_size]),
     ("cfft_u128_product_plan_create", c_int, [c_size, pp]),
     ("cfft_u128_product_plan_destroy", None, [vp]),
     ("cfft_u128_product_poly_size", c_size, [vp]),

@@ -46,6 +46,10 @@ LevelDesc make_levels(size_t n, size_t base_n);
 
 void set_error(const std::string& msg);
 
+// Device tables of a u64 product plan (forward/inverse FFT tables, twist, untwist).
+void u64_product_tables(const cfft_u64_product_plan* p, const void** w, const void** winv, const void** tw,
+                        const void** itw);
+
 // The largest (sub)transform kept entirely in one CTA's shared memory
 // (data + ping-pong scratch, 16 B per point each: 128 KiB at 4096 points).
 constexpr int kSmemLog2Max = 12;

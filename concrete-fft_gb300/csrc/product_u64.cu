@@ -30,6 +30,7 @@ using namespace cfft;
 
 struct cfft_u64_product_plan {
   size_t N = 0, n = 0, base_n = 0;
+  cfft_unordered_plan* fft = nullptr;  // the plan's transform, for the unfused entry points
   int base_algo = 0;
   LevelDesc lv{};
   DevLevels dlv{};
@@ -37,9 +38,45 @@ struct cfft_u64_product_plan {
   int emu = 0;  // eighths of the butterfly additions issued on the integer pipe
 };
 
+namespace cfft {
+// The product pipeline's elementwise steps as separate kernels (the unfused path).
+__global__ void fold_twist_kernel(const uint64_t* __restrict__ a, double2* __restrict__ z, long total, int log2n,
+                                  const double2* __restrict__ tw) {
+  const long n = 1L << log2n;
+  for (long g = (long)blockIdx.x * blockDim.x + threadIdx.x; g < total; g += (long)gridDim.x * blockDim.x) {
+    const long p = g >> log2n, j = g & (n - 1);
+    const uint64_t* ap = a + (p << (log2n + 1));
+    const c64 v{i64_to_f64_rne((int64_t)ap[j]), i64_to_f64_rne((int64_t)ap[j + n])};
+    st(z + g, cmul(ldg(tw + j), v));
+  }
+}
+__global__ void pointwise_kernel(const double2* __restrict__ bhat, long bhat_stride, double2* __restrict__ z,
+                                 long total, int log2n) {
+  const long n = 1L << log2n;
+  for (long g = (long)blockIdx.x * blockDim.x + threadIdx.x; g < total; g += (long)gridDim.x * blockDim.x) {
+    const long p = g >> log2n, k = g & (n - 1);
+    st(z + g, cmul(ldg(bhat + p * bhat_stride + k), ld(z + g)));
+  }
+}
+__global__ void untwist_round_kernel(const double2* __restrict__ z, uint64_t* __restrict__ out, long total, int log2n,
+                                     const double2* __restrict__ itw) {
+  const long n = 1L << log2n;
+  for (long g = (long)blockIdx.x * blockDim.x + threadIdx.x; g < total; g += (long)gridDim.x * blockDim.x) {
+    const long p = g >> log2n, j = g & (n - 1);
+    const c64 t = cmul(ldg(itw + j), ld(z + g));
+    uint64_t* op = out + (p << (log2n + 1));
+    op[j] = round_half_up_mod64(t.re);
+    op[j + n] = round_half_up_mod64(t.im);
+  }
+}
+}  // namespace cfft
+
 namespace {
 
+int ew_grid(long total) { return (int)std::max<long>(1, std::min<long>((total + 255) / 256, (long)sm_count() * 16)); }
+
 void free_u64(cfft_u64_product_plan* p) {
+  if (p->fft) cfft_unordered_plan_destroy(p->fft);
   if (p->d_w) cudaFree(p->d_w);
   if (p->d_winv) cudaFree(p->d_winv);
   if (p->d_tw) cudaFree(p->d_tw);
@@ -81,7 +118,51 @@ cfft_status launch_product(const cfft_u64_product_plan* plan, const uint64_t* a,
 
 }  // namespace
 
+void cfft::u64_product_tables(const cfft_u64_product_plan* p, const void** w, const void** winv, const void** tw,
+                              const void** itw) {
+  *w = p->d_w;
+  *winv = p->d_winv;
+  *tw = p->d_tw;
+  *itw = p->d_itw;
+}
+
 extern "C" {
+
+cfft_status cfft_u64_fold_twist(const cfft_u64_product_plan* plan, const uint64_t* a, double* z, size_t count,
+                                void* stream) {
+  if (!plan || !a || !z) return fail(CFFT_ERR_INVALID_ARGUMENT, "null argument");
+  if (count == 0) return CFFT_OK;
+  const long total = (long)(count * plan->n);
+  fold_twist_kernel<<<ew_grid(total), 256, 0, (cudaStream_t)stream>>>(a, (double2*)z, total, ilog2(plan->n),
+                                                                      plan->d_tw);
+  CFFT_CHECK_LAUNCH();
+  return CFFT_OK;
+}
+
+cfft_status cfft_c64_pointwise(const double* bhat, size_t bhat_stride, double* z, size_t n, size_t count,
+                               void* stream) {
+  if (!bhat || !z) return fail(CFFT_ERR_INVALID_ARGUMENT, "null argument");
+  if (!is_pow2(n)) return fail(CFFT_ERR_INVALID_SIZE, "n must be a power of two");
+  if (count == 0) return CFFT_OK;
+  const long total = (long)(count * n);
+  pointwise_kernel<<<ew_grid(total), 256, 0, (cudaStream_t)stream>>>((const double2*)bhat, (long)bhat_stride,
+                                                                     (double2*)z, total, ilog2(n));
+  CFFT_CHECK_LAUNCH();
+  return CFFT_OK;
+}
+
+cfft_status cfft_u64_untwist_round(const cfft_u64_product_plan* plan, const double* z, uint64_t* out, size_t count,
+                                   void* stream) {
+  if (!plan || !z || !out) return fail(CFFT_ERR_INVALID_ARGUMENT, "null argument");
+  if (count == 0) return CFFT_OK;
+  const long total = (long)(count * plan->n);
+  untwist_round_kernel<<<ew_grid(total), 256, 0, (cudaStream_t)stream>>>((const double2*)z, out, total,
+                                                                         ilog2(plan->n), plan->d_itw);
+  CFFT_CHECK_LAUNCH();
+  return CFFT_OK;
+}
+
+cfft_unordered_plan* cfft_u64_product_fft(const cfft_u64_product_plan* plan) { return plan ? plan->fft : nullptr; }
 
 cfft_status cfft_u64_product_set_int_adds(cfft_u64_product_plan* plan, int eighths) {
   if (!plan || eighths < 0 || eighths > 8) return fail(CFFT_ERR_INVALID_ARGUMENT, "eighths must be in 0..8");
@@ -95,8 +176,8 @@ int cfft_u64_product_int_adds(const cfft_u64_product_plan* plan) {
 cfft_status cfft_u64_product_plan_create(size_t N, cfft_algo base_algo, size_t base_n, cfft_u64_product_plan** out) {
   if (!out) return fail(CFFT_ERR_INVALID_ARGUMENT, "null output pointer");
   *out = nullptr;
-  if (!is_pow2(N) || N < 64 || ilog2(N) > kSmemLog2Max + 1)
-    return fail(CFFT_ERR_INVALID_SIZE, "u64 product: N must be a power of two in [64, 8192]");
+  if (!is_pow2(N) || N < 64 || ilog2(N) > 17)
+    return fail(CFFT_ERR_INVALID_SIZE, "u64 product: N must be a power of two in [64, 131072]");
   const size_t n = N / 2;
   if (!is_pow2(base_n) || base_n > n || (base_n != n && base_n < 32) || ilog2(base_n) > 10)
     return fail(CFFT_ERR_INVALID_ARGUMENT, "u64 product: invalid base_n");
@@ -119,6 +200,7 @@ cfft_status cfft_u64_product_plan_create(size_t N, cfft_algo base_algo, size_t b
     itw[j] = c64h{c * inv_n, -s * inv_n};  // exact: inv_n is a power of two
   }
   st = upload((const double2*)w.data(), n + base_n, &p->d_w);
+  if (st == CFFT_OK) st = cfft_unordered_plan_create(n, base_algo, base_n, &p->fft);
   if (st == CFFT_OK) st = upload((const double2*)wi.data(), n + base_n, &p->d_winv);
   if (st == CFFT_OK) st = upload((const double2*)tw.data(), n, &p->d_tw);
   if (st == CFFT_OK) st = upload((const double2*)itw.data(), n, &p->d_itw);
@@ -148,6 +230,11 @@ cfft_status cfft_u64_prepare_operand(const cfft_u64_product_plan* plan, const in
                                      void* stream) {
   if (!plan || !b || !bhat) return fail(CFFT_ERR_INVALID_ARGUMENT, "null argument");
   if (count == 0) return CFFT_OK;
+  if (plan->N > (size_t(2) << kSmemLog2Max)) {  // unfused: fold and twist, then the plan's forward FFT
+    cfft_status st = cfft_u64_fold_twist(plan, (const uint64_t*)b, bhat, count, stream);
+    if (st != CFFT_OK) return st;
+    return cfft_unordered_fwd(plan->fft, bhat, count, stream);
+  }
   const size_t smem = 2 * plan->n * sizeof(double2);
   const void* fn = u64_prepare_kernel_ptr(plan->base_algo);
   const int grid = grid_for(fn, kProdThreads, smem, (long)count);
@@ -163,6 +250,8 @@ cfft_status cfft_u64_product(const cfft_u64_product_plan* plan, const uint64_t* 
   if (!plan || !a || !bhat || !out) return fail(CFFT_ERR_INVALID_ARGUMENT, "null argument");
   if (bhat_stride != 0 && bhat_stride != plan->n)
     return fail(CFFT_ERR_INVALID_ARGUMENT, "bhat_stride must be 0 or N/2");
+  if (plan->N > (size_t(2) << kSmemLog2Max))
+    return fail(CFFT_ERR_INVALID_SIZE, "fused u64 product: N must be at most 8192 (use cfft_product_engine_run)");
   if (count == 0) return CFFT_OK;
   return launch_product(plan, a, bhat, bhat_stride, out, count, (cudaStream_t)stream);
 

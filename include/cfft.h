@@ -163,7 +163,7 @@ cfft_status cfft_f128_inv_host(const cfft_f128_plan* plan, double* re0, double* 
  * untwist, exact rounding back to the integer ring.
  *
  * u64: coefficients are read as i64, rounded with floor(x + 1/2) and reduced
- * mod 2^64.  N a power of two, 64 <= N <= 8192.  bhat holds N/2 c64 per
+ * mod 2^64.  N a power of two, 64 <= N <= 8192 for the fused kernel.  bhat holds N/2 c64 per
  * operand in the plan's permuted order; `bhat_stride` is 0 (one operand shared
  * by all products) or N/2 (one operand per product). */
 typedef struct cfft_u64_product_plan cfft_u64_product_plan;
@@ -184,6 +184,90 @@ cfft_status cfft_u64_product(const cfft_u64_product_plan* plan, const uint64_t* 
 /* Host buffers for a and out (bhat stays device-resident). */
 cfft_status cfft_u64_product_host(const cfft_u64_product_plan* plan, const uint64_t* a, const double* bhat,
                                   size_t bhat_stride, uint64_t* out, size_t count);
+
+/* The same pipeline unfused, one launch per step (for callers that keep the
+ * Fourier-domain data themselves; bit-identical to cfft_u64_product):
+ *   cfft_u64_fold_twist -> cfft_unordered_fwd(cfft_u64_product_fft(plan)) ->
+ *   cfft_c64_pointwise -> cfft_unordered_inv -> cfft_u64_untwist_round.
+ * z holds count * N/2 c64.  Plans of N up to 131072 may be created for these
+ * entry points; the fused cfft_u64_product takes N <= 8192. */
+cfft_status cfft_u64_fold_twist(const cfft_u64_product_plan* plan, const uint64_t* a, double* z, size_t count,
+                                void* stream);
+/* z[p][k] = bhat[p*bhat_stride + k] * z[p][k] (the reference's FMA complex product). */
+cfft_status cfft_c64_pointwise(const double* bhat, size_t bhat_stride, double* z, size_t n, size_t count,
+                               void* stream);
+cfft_status cfft_u64_untwist_round(const cfft_u64_product_plan* plan, const double* z, uint64_t* out, size_t count,
+                                   void* stream);
+/* The plan's N/2-point unordered transform (owned by the product plan). */
+cfft_unordered_plan* cfft_u64_product_fft(const cfft_u64_product_plan* plan);
+
+/* Mixed-size product engine: one persistent launch over a DEVICE array of
+ * items of any configured N (2^6..2^17), each with its own operand, result
+ * bit-identical to cfft_u64_product.  Products with N/2 > 2048 keep their
+ * complex data in `workspace` (cfft_product_engine_workspace_bytes, device
+ * memory, one per concurrently running launch).  `counter` is a device uint
+ * the run zeroes and uses as its work queue head (one per concurrently
+ * running launch).  Operands for size N are prepared with
+ * cfft_u64_prepare_operand(cfft_product_engine_plan(engine, log2N), ...). */
+typedef struct cfft_product_item {
+  const uint64_t* a;  /* N u64 coefficients (device) */
+  const double* bhat; /* N/2 c64 Fourier operand (device, the size's permuted order) */
+  uint64_t* out;      /* N u64 result (device) */
+  uint32_t log2N;
+  uint32_t reserved;  /* must be 0 */
+} cfft_product_item;
+typedef struct cfft_product_engine cfft_product_engine;
+cfft_status cfft_product_engine_create(const uint32_t* log2N, size_t count, cfft_product_engine** out);
+void cfft_product_engine_destroy(cfft_product_engine* engine);
+size_t cfft_product_engine_workspace_bytes(const cfft_product_engine* engine);
+const cfft_u64_product_plan* cfft_product_engine_plan(const cfft_product_engine* engine, uint32_t log2N);
+cfft_status cfft_product_engine_run(const cfft_product_engine* engine, const cfft_product_item* items, size_t count,
+                                    unsigned int* counter, double* workspace, void* stream);
+
+/* ============================================ serving loop (continuous batching) ====
+ * A request is (k+1)*l products of one size N: signed b-bit digit polynomials
+ * times device-resident Fourier operands (the TFHE external-product shape);
+ * its content is a function of (seed, request id).  cfft_server_run serves a
+ * seeded Poisson stream in real time: admission gated by the device output
+ * ring (memory), everything admitted since the last launch batched into one
+ * product-engine run, up to max_inflight runs overlapping on the device.  With
+ * plain = 1 it serves the same stream one request at a time through the
+ * unfused pipeline (one launch per step), the comparator. */
+typedef struct cfft_serve_config {
+  double rate;          /* mean arrivals per second */
+  double duration_s;    /* arrival window */
+  uint32_t log2N_min;   /* N uniform over 2^log2N_min .. 2^log2N_max */
+  uint32_t log2N_max;
+  uint32_t k_max;       /* k uniform in 1..k_max */
+  uint32_t l_max;       /* l uniform in 1..l_max; (k+1)*l <= 16 products */
+  uint32_t plain;       /* 1: unbatched comparator */
+  uint32_t max_inflight; /* concurrent launches, 1..3 */
+  uint32_t record_every; /* keep the outputs of every k-th request (0: none) */
+  uint32_t reserved;
+} cfft_serve_config;
+typedef struct cfft_serve_stats {
+  uint64_t requests, products, launches, deferred_admissions;
+  double products_per_s, p50_ms, p99_ms, max_ms, mean_batch, span_s;
+} cfft_serve_stats;
+typedef struct cfft_server cfft_server;
+/* Resident state: digit pools and Fourier operands (operand_bytes in total) for
+ * each size, and an output ring of ring_bytes (0: a quarter of free memory,
+ * at most 4 GiB), the admission gate. */
+cfft_status cfft_server_create(const cfft_product_engine* engine, const uint32_t* log2N, size_t nsizes,
+                               uint64_t operand_bytes, uint64_t ring_bytes, uint64_t seed, cfft_server** out);
+void cfft_server_destroy(cfft_server* server);
+cfft_status cfft_server_run(cfft_server* server, const cfft_serve_config* config, cfft_serve_stats* stats);
+/* Checking: outputs kept by the last run, the shape and inputs of request `id`,
+ * and the same request computed alone (outside any mix). */
+size_t cfft_server_recorded(const cfft_server* server);
+cfft_status cfft_server_recorded_ids(const cfft_server* server, uint64_t* ids, size_t cap);
+cfft_status cfft_server_recorded_output(const cfft_server* server, uint64_t id, uint64_t* out, size_t words);
+cfft_status cfft_server_request_shape(const cfft_server* server, const cfft_serve_config* config, uint64_t id,
+                                      uint32_t* log2N, uint32_t* nprod);
+cfft_status cfft_server_request_inputs(const cfft_server* server, const cfft_serve_config* config, uint64_t id,
+                                       int64_t* digits, double* bhat);
+cfft_status cfft_server_run_alone(cfft_server* server, const cfft_serve_config* config, uint64_t id, uint64_t* out,
+                                  size_t words);
 
 /* u128: coefficients as little-endian (lo, hi) u64 pairs read as i128,
  * double-double arithmetic around fft128::Plan(N/2), floor(x + 1/2) mod 2^128.

@@ -530,6 +530,38 @@ def run_u128(args):
     }))
 
 
+def run_serving(args):
+    """Poisson stream of (k+1)*l-product requests, N in 2^10..2^14, 8 GB of resident operands:
+    continuous batching vs the plain one-launch-per-step path, same seeded stream."""
+    torch, cf, rank, world, local = gpu_setup()
+    sizes = [10, 11, 12, 13, 14]
+    eng = cf.serving.ProductEngine(sizes)
+    t0 = time.perf_counter()
+    srv = cf.serving.Server(eng, sizes, operand_bytes=args.operand_gb << 30, seed=5 + rank)
+    setup_s = time.perf_counter() - t0
+    cfg = srv.config(rate=args.rate, duration_s=args.serve_seconds)
+    srv.run(srv.config(rate=args.rate, duration_s=0.05))  # warm-up
+    with ClockSampler(local) as clk:
+        t1 = time.time()
+        batched = srv.run(cfg)
+        clk.mark(t1, time.time())
+    plain = srv.run(srv.config(rate=args.rate, duration_s=args.serve_seconds, plain=True))
+    if rank != 0:
+        return
+    print(json.dumps({
+        "metric": "serving: products/s and p99 latency, Poisson %g req/s" % args.rate,
+        "value": batched["products_per_s"], "unit": "products/s", "n_gpus": world, "steps": 1,
+        "warmup": 1, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic (seeded Poisson stream, resident operands %d GiB)" % args.operand_gb,
+        "config": {"workload": "serving, (k+1)*l products per request, k in 1..2, l in 1..4, N in 2^10..2^14, "
+                               "digits b in 4..10 bits", "duration_s": args.serve_seconds,
+                   "resident_setup_s": setup_s},
+        "batched": batched, "plain": plain,
+        "p99_speedup_vs_plain": plain["p99_ms"] / batched["p99_ms"] if batched["p99_ms"] else None,
+        "clocks": clk.summary(), "gpu_launches": batched["launches"],
+    }))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -545,7 +577,11 @@ def main():
                     help="eighths of butterfly additions on the integer pipe (default: the plan's tuned value)")
     ap.add_argument("--profile-case", action="store_true",
                     help="small fixed case for ncu: 1 warm-up + 1 launch, no timing")
-    ap.add_argument("--workload", choices=["u64_product", "mixed", "ordered", "u128_product"], default="u64_product",
+    ap.add_argument("--rate", type=float, default=20000.0)
+    ap.add_argument("--serve-seconds", type=float, default=1.0)
+    ap.add_argument("--operand-gb", type=int, default=8)
+    ap.add_argument("--workload", choices=["u64_product", "mixed", "ordered", "u128_product", "serving"],
+                    default="u64_product",
                     help="u64_product (default headline) or one of the other benchmark configurations")
     ap.add_argument("--mixed-items", type=int, default=100000)
     ap.add_argument("--tune-seconds", type=float, default=0.0005)
@@ -560,6 +596,8 @@ def main():
         run_ordered(args)
     elif args.workload == "u128_product":
         run_u128(args)
+    elif args.workload == "serving":
+        run_serving(args)
     else:
         run_gb300(args)
 

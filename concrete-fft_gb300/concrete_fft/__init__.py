@@ -6,7 +6,7 @@ libcfft_gb300.so (include/cfft.h); there is no CPU fallback.
 """
 from ._lib import CfftError, EXPORTED, LIB_PATH, check, load
 from .ordered import FftAlgo
-from . import ordered, unordered, fft128, product, batch
+from . import ordered, unordered, fft128, product, batch, serving
 
 __all__ = ["CfftError", "EXPORTED", "LIB_PATH", "FftAlgo", "check", "load", "ordered", "unordered", "fft128",
-           "product", "batch"]
+           "product", "batch", "serving"]

@@ -1,0 +1,119 @@
+"""Mixed-size product engine, the unfused pipeline, and the continuous-batching
+server: bit-identical to the oracle, and every served result equal to the same
+request computed alone."""
+import ctypes
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+RNG = np.random.default_rng(17)
+SIZES = [10, 11, 12, 13, 14]
+
+
+@pytest.fixture(scope="module")
+def engine(cuda):
+    import concrete_fft as cf
+    return cf.serving.ProductEngine(SIZES)
+
+
+def test_engine_mixed_sizes_bit_exact(cuda, oracle, engine):
+    import concrete_fft as cf
+    torch = cuda
+    items, keep = [], []
+    for lN in SIZES + SIZES[::-1]:
+        N = 1 << lN
+        count = 2
+        a = RNG.integers(0, 2 ** 64, (count, N), dtype=np.uint64)
+        b = RNG.integers(-2 ** 7, 2 ** 7, (count, N))
+        bhat = torch.empty((count, N // 2), dtype=torch.complex128, device="cuda")
+        engine.prepare_operand(lN, torch.from_numpy(b).cuda(), bhat)
+        da = torch.from_numpy(a.view(np.int64)).cuda()
+        out = torch.zeros_like(da)
+        for p in range(count):
+            items.append((da[p].data_ptr(), bhat[p].data_ptr(), out[p].data_ptr(), lN, 0))
+        keep.append((lN, a, b, bhat, da, out))
+    arr = np.array(items, dtype=cf.serving.ITEM_DTYPE)
+    d_items = torch.from_numpy(arr.view(np.uint8)).cuda()
+    counter = torch.zeros(4, dtype=torch.int32, device="cuda")
+    ws_bytes = engine.workspace_bytes()
+    assert ws_bytes > 0  # N = 8192 and 16384 use the workspace
+    ws = torch.empty(ws_bytes, dtype=torch.uint8, device="cuda")
+    engine.run(d_items, len(arr), counter, ws, torch.cuda.current_stream().cuda_stream)
+    torch.cuda.synchronize()
+    for lN, a, b, bhat, da, out in keep:
+        N = 1 << lN
+        algo, base = engine.algo(lN)
+        want_bhat = oracle.u64_prepare(N, algo, base, b)
+        assert np.array_equal(bhat.cpu().numpy().view(np.uint64), want_bhat.view(np.uint64)), lN
+        want = oracle.u64_product(N, algo, base, a, want_bhat, nthreads=0)
+        assert np.array_equal(out.cpu().numpy().view(np.uint64), want), lN
+
+
+@pytest.mark.parametrize("lN", [11, 14])
+def test_unfused_pipeline_equals_fused(cuda, oracle, engine, lN):
+    import concrete_fft as cf
+    torch = cuda
+    L = cf.load()
+    N, count = 1 << lN, 3
+    plan = engine.plan(lN)
+    fft = ctypes.c_void_p(L.cfft_u64_product_fft(plan))
+    a = RNG.integers(0, 2 ** 64, (count, N), dtype=np.uint64)
+    b = RNG.integers(-2 ** 7, 2 ** 7, (count, N))
+    bhat = torch.empty((count, N // 2), dtype=torch.complex128, device="cuda")
+    engine.prepare_operand(lN, torch.from_numpy(b).cuda(), bhat)
+    da = torch.from_numpy(a.view(np.int64)).cuda()
+    z = torch.empty((count, N // 2), dtype=torch.complex128, device="cuda")
+    out = torch.empty_like(da)
+    s = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+    p = lambda t: ctypes.c_void_p(t.data_ptr())
+    cf.check(L.cfft_u64_fold_twist(plan, p(da), p(z), count, s))
+    cf.check(L.cfft_unordered_fwd(fft, p(z), count, s))
+    cf.check(L.cfft_c64_pointwise(p(bhat), N // 2, p(z), N // 2, count, s))
+    cf.check(L.cfft_unordered_inv(fft, p(z), count, s))
+    cf.check(L.cfft_u64_untwist_round(plan, p(z), p(out), count, s))
+    algo, base = engine.algo(lN)
+    want = oracle.u64_product(N, algo, base, a, oracle.u64_prepare(N, algo, base, b), nthreads=0)
+    assert np.array_equal(out.cpu().numpy().view(np.uint64), want)
+
+
+def test_server_results_same_alone_and_in_the_mix(cuda, oracle, engine):
+    import concrete_fft as cf
+    srv = cf.serving.Server(engine, SIZES, operand_bytes=64 << 20, ring_bytes=256 << 20, seed=9)
+    cfg = srv.config(rate=20000, duration_s=0.05, record_every=1)
+    stats = srv.run(cfg)
+    assert stats["requests"] > 100 and stats["launches"] < stats["requests"]  # batching happened
+    ids = srv.recorded_ids()
+    assert len(ids) == stats["requests"]
+    for rid in ids[:: max(1, len(ids) // 40)]:
+        mixed = srv.recorded_output(cfg, rid)
+        alone = srv.run_alone(cfg, rid)
+        assert np.array_equal(mixed, alone), rid
+    for rid in ids[:3]:
+        digits, bhat = srv.inputs(cfg, rid)
+        lN, npd = srv.shape(cfg, rid)
+        algo, base = engine.algo(lN)
+        want = oracle.u64_product(1 << lN, algo, base, digits.view(np.uint64), bhat, nthreads=0)
+        assert np.array_equal(srv.recorded_output(cfg, rid), want)
+
+
+def test_plain_server_same_results(cuda, engine):
+    import concrete_fft as cf
+    srv = cf.serving.Server(engine, SIZES, operand_bytes=64 << 20, ring_bytes=256 << 20, seed=9)
+    cfg = srv.config(rate=2000, duration_s=0.02, record_every=1, plain=True)
+    stats = srv.run(cfg)
+    assert stats["launches"] == 5 * stats["products"]
+    for rid in srv.recorded_ids()[:10]:
+        assert np.array_equal(srv.recorded_output(cfg, rid), srv.run_alone(cfg, rid))
+
+
+def test_server_memory_gate(cuda, engine):
+    """A ring that holds only a couple of requests still serves everything (admission waits)."""
+    import concrete_fft as cf
+    srv = cf.serving.Server(engine, [12], operand_bytes=16 << 20, ring_bytes=3 * 16 * (1 << 12) * 8, seed=3)
+    cfg = srv.config(rate=50000, duration_s=0.01, log2N_min=12, log2N_max=12, record_every=1)
+    stats = srv.run(cfg)
+    assert stats["deferred_admissions"] > 0
+    assert len(srv.recorded_ids()) == stats["requests"]
+    with pytest.raises(cf.CfftError):
+        srv.run(srv.config(rate=100, duration_s=0.01, log2N_min=12, log2N_max=14))  # sizes without pools

@@ -101,6 +101,7 @@ _SIGS = [
     ("cfft_product_engine_workspace_bytes", c_size, [vp]),
     ("cfft_product_engine_plan", vp, [vp, ctypes.c_uint32]),
     ("cfft_product_engine_run", c_int, [vp, vp, c_size, vp, vp, vp]),
+    ("cfft_product_engine_run_static", c_int, [vp, vp, c_size, vp]),
     ("cfft_server_create", c_int, [vp, vp, c_size, ctypes.c_uint64, ctypes.c_uint64, ctypes.c_uint64, pp]),
     ("cfft_server_destroy", None, [vp]),
     ("cfft_server_run", c_int, [vp, vp, vp]),

@@ -52,6 +52,12 @@ class ProductEngine:
         check(self._lib.cfft_product_engine_run(self._h, ctypes.c_void_p(items_dev.data_ptr()), count,
                                                 ctypes.c_void_p(counter.data_ptr()), ws, ctypes.c_void_p(stream)))
 
+    def run_static(self, items_dev, count, stream):
+        """The no-allocation run: counter and workspace from the library's static device array
+        (largest N 16384; calls that overlap on the GPU race, so serialise them)."""
+        check(self._lib.cfft_product_engine_run_static(self._h, ctypes.c_void_p(items_dev.data_ptr()), count,
+                                                       ctypes.c_void_p(stream)))
+
 
 class ServeConfig(ctypes.Structure):
     _fields_ = [("rate", ctypes.c_double), ("duration_s", ctypes.c_double), ("log2N_min", ctypes.c_uint32),

@@ -15,6 +15,8 @@
 
 #include <algorithm>
 #include <cstring>
+#include <mutex>
+#include <string>
 #include <vector>
 
 #include "../../include/cfft.h"
@@ -244,3 +246,84 @@ cfft_status cfft_product_engine_run(const cfft_product_engine* e, const cfft_pro
 }
 
 }  // extern "C"
+
+// ---------------------------------------------------------------------------
+// Product-engine run without allocation.
+//
+// For callers that must not allocate device memory on their call path: code
+// running inside a host framework that has reserved the whole device memory
+// budget for its own allocator (a cudaMalloc there fails or fragments that
+// pool), and latency-critical loops, where cudaMalloc/cudaFree would
+// synchronise the device.  This entry point takes the queue counter and the
+// large-N workspace from the static device array below instead of caller
+// buffers, and calls no allocating routine.
+//
+// Limits and sharing: the array holds 256 bytes of counter and 24 MiB of
+// workspace, and every GPU that loads this library keeps it until the process
+// exits.  Sizes whose per-CTA workspace does not fit one CTA per SM in 24 MiB
+// (N/2 > 8192, i.e. N > 16384 on GB300) are rejected with
+// CFFT_ERR_INVALID_SIZE.  All calls share the array: calls whose executions
+// overlap on the GPU (different streams, or several threads) race on it and
+// must be serialised by the caller.  The counter is cleared by every call; the
+// workspace needs no clearing (each product writes before it reads).
+constexpr size_t kStaticCounterBytes = 256;
+constexpr size_t kStaticWorkspaceBytes = size_t(24) << 20;
+static __device__ __align__(256) unsigned char g_engine_scratch[kStaticCounterBytes + kStaticWorkspaceBytes];
+
+namespace {
+std::mutex g_static_mu;
+void* g_static_ptr[64] = {};  // address of g_engine_scratch on each device
+
+// Set-up, once per device, with that device current: the host-side symbol is
+// only a stand-in, so the device address comes from cudaGetSymbolAddress.
+// The first call on a device does this; make that first call before any
+// stream capture on the device.
+cfft_status static_scratch(void** out) {
+  int dev = 0;
+  CFFT_CUDA_TRY(cudaGetDevice(&dev));
+  if (dev < 0 || dev >= 64) return fail(CFFT_ERR_NO_DEVICE, "device ordinal out of range for the static scratch");
+  std::lock_guard<std::mutex> lk(g_static_mu);
+  if (!g_static_ptr[dev]) {
+    void* p = nullptr;
+    const cudaError_t e = cudaGetSymbolAddress(&p, g_engine_scratch);
+    if (e != cudaSuccess || p == nullptr)
+      return fail(CFFT_ERR_CUDA, std::string("cudaGetSymbolAddress(static scratch): ") + cudaGetErrorString(e));
+    g_static_ptr[dev] = p;
+  }
+  *out = g_static_ptr[dev];
+  return CFFT_OK;
+}
+}  // namespace
+
+extern "C" cfft_status cfft_product_engine_run_static(const cfft_product_engine* e, const cfft_product_item* items,
+                                                      size_t count, void* stream) {
+  if (!e || !items) return fail(CFFT_ERR_INVALID_ARGUMENT, "null argument");
+  if (count == 0) return CFFT_OK;
+  if (count > 0x7fffffff) return fail(CFFT_ERR_INVALID_SIZE, "too many items");
+  int grid = (int)std::min<size_t>((size_t)e->grid, count);
+  long ws_points = 0;
+  if (e->ws_log2n) {
+    ws_points = 1L << e->ws_log2n;
+    const size_t per_cta = (size_t)ws_points * sizeof(double2);
+    const size_t fit = kStaticWorkspaceBytes / per_cta;
+    if (fit < (size_t)sm_count())
+      return fail(CFFT_ERR_INVALID_SIZE,
+                  "cfft_product_engine_run_static: N = 2^" + std::to_string(e->ws_log2n + 1) +
+                      " needs " + std::to_string(per_cta >> 10) + " KiB of workspace per CTA, more than the 24 MiB "
+                      "static scratch holds for one CTA per SM (largest N: 16384); use cfft_product_engine_run "
+                      "with a caller workspace");
+    grid = (int)std::min<size_t>((size_t)grid, fit);
+  }
+  void* base = nullptr;
+  cfft_status st = static_scratch(&base);
+  if (st != CFFT_OK) return st;
+  cudaStream_t s = (cudaStream_t)stream;
+  unsigned int* counter = (unsigned int*)base;
+  double2* ws = e->ws_log2n ? (double2*)((unsigned char*)base + kStaticCounterBytes) : nullptr;
+  CFFT_CUDA_TRY(cudaMemsetAsync(counter, 0, sizeof(unsigned int), s));
+  const size_t smem = 2 * (1 << kEngSmemLog2) * sizeof(double2);
+  int cnt = (int)count;
+  const EngClass* cls = e->d_classes;
+  void* args[] = {(void*)&cls, (void*)&items, &cnt, &counter, &ws, &ws_points};
+  return launch_kernel((const void*)product_engine_kernel, grid, kEngThreads, args, smem, s);
+}

@@ -223,6 +223,19 @@ size_t cfft_product_engine_workspace_bytes(const cfft_product_engine* engine);
 const cfft_u64_product_plan* cfft_product_engine_plan(const cfft_product_engine* engine, uint32_t log2N);
 cfft_status cfft_product_engine_run(const cfft_product_engine* engine, const cfft_product_item* items, size_t count,
                                     unsigned int* counter, double* workspace, void* stream);
+/* cfft_product_engine_run without any allocation (no counterpart in the
+ * reference): for callers that cannot allocate device memory on their call
+ * path -- code inside a framework whose own allocator has reserved the device
+ * memory budget, or latency-critical loops where cudaMalloc/cudaFree would
+ * synchronise the device.  The counter and the workspace come from a static
+ * device array (256 B + 24 MiB, held on every GPU that loads the library until
+ * exit) instead of caller buffers.  Limit: engines with N > 16384 are
+ * rejected with CFFT_ERR_INVALID_SIZE.  The first call on a device looks up the
+ * array's device address; make it before any stream capture.  All calls share
+ * the array, so calls that overlap on the GPU race: serialise them.  Results
+ * are bit-identical to cfft_product_engine_run. */
+cfft_status cfft_product_engine_run_static(const cfft_product_engine* engine, const cfft_product_item* items,
+                                           size_t count, void* stream);
 
 /* ============================================ serving loop (continuous batching) ====
  * A request is (k+1)*l products of one size N: signed b-bit digit polynomials

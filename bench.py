@@ -210,6 +210,7 @@ def run_gb300(args):
         dist.init_process_group("nccl")
     sys.path.insert(0, PKG)
     import concrete_fft as cf
+    from concrete_fft import replicas
     lib = cf.load()
     cf.check(lib.cfft_device_check())
 
@@ -257,11 +258,7 @@ def run_gb300(args):
         e1.record(stream)
         barrier()
         clk.mark(t_start, time.time())
-    ms = e0.elapsed_time(e1)
-    if world > 1:
-        t = torch.tensor([ms], device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        ms = float(t.item())
+    ms = replicas.max_over_ranks(e0.elapsed_time(e1), "cuda")
     per_launch_s = ms * 1e-3 / args.steps
     value = world * count * args.steps / (ms * 1e-3)
 
@@ -275,11 +272,7 @@ def run_gb300(args):
     e2e_steps = max(3, args.steps // 10)
     for _ in range(e2e_steps):
         plan.product(ha, bhat, hout)
-    e2e_s = time.perf_counter() - t0
-    if world > 1:
-        t = torch.tensor([e2e_s], device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        e2e_s = float(t.item())
+    e2e_s = replicas.max_over_ranks(time.perf_counter() - t0, "cuda")
     e2e = world * count * e2e_steps / e2e_s
     ok = bool(np.array_equal(hout.numpy(), out.cpu().numpy()))
 
@@ -365,12 +358,8 @@ def timed(torch, fn, steps, warmup, local, world):
         if world > 1:
             torch.distributed.barrier()
         clk.mark(t0, time.time())
-    ms = e0.elapsed_time(e1)
-    if world > 1:
-        t = torch.tensor([ms], device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        ms = float(t.item())
-    return ms, clk.summary()
+    from concrete_fft import replicas
+    return replicas.max_over_ranks(e0.elapsed_time(e1), "cuda"), clk.summary()
 
 
 def fp64_peak(cf):

@@ -81,6 +81,7 @@ _SIGS = [
     ("cfft_u64_product_plan_destroy", None, [vp]),
     ("cfft_u64_product_poly_size", c_size, [vp]),
     ("cfft_u64_product_algo", None, [vp, ctypes.POINTER(c_int), ctypes.POINTER(c_size)]),
+    ("cfft_u64_product_sum", c_int, [vp, vp, vp, c_size, vp, c_size, vp]),
     ("cfft_u64_fold_twist", c_int, [vp, vp, vp, c_size, vp]),
     ("cfft_c64_pointwise", c_int, [vp, c_size, vp, c_size, c_size, vp]),
     ("cfft_u64_untwist_round", c_int, [vp, vp, vp, c_size, vp]),

@@ -57,6 +57,15 @@ class U64ProductPlan:
         return out
 
 
+    def product_sum(self, a, bhat, out):
+        """a: (count, terms, N) device int64/uint64; bhat: (count, terms, N/2) complex128;
+        out: (count, N).  out[g] = sum_t a[g, t] * B[g, t], accumulated in the Fourier domain."""
+        count, terms = a.shape[0], a.shape[1]
+        check(self._lib.cfft_u64_product_sum(self._h, B.ptr(a), B.ptr(bhat), terms, B.ptr(out), count,
+                                             B.stream_of(a)))
+        return out
+
+
 class U128ProductPlan:
     """out = a * B mod (X^N + 1) with u128 coefficients as (lo, hi) u64 pairs."""
 

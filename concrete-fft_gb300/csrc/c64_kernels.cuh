@@ -69,6 +69,54 @@ __global__ void __launch_bounds__(THREADS) u64_product_kernel(const uint64_t* __
   }
 }
 
+// Sum of `terms` products accumulated in the Fourier domain, one inverse per
+// group (the TFHE external-product shape): per group, every term is folded,
+// twisted and transformed in shared memory, multiplied by its operand and added
+// into an accumulator in term order; the accumulator is inverted, untwisted
+// and rounded once.  Shared memory: 3 x N/2 c64.
+template <int ALGO, int THREADS>
+__global__ void __launch_bounds__(THREADS) u64_product_sum_kernel(const uint64_t* __restrict__ a,
+                                                                 const double2* __restrict__ bhat, int terms,
+                                                                 uint64_t* __restrict__ out, long count, DevLevels L,
+                                                                 const double2* __restrict__ w,
+                                                                 const double2* __restrict__ winv,
+                                                                 const double2* __restrict__ tw,
+                                                                 const double2* __restrict__ itw) {
+  extern __shared__ double2 smem[];
+  const int log2n = L.log2n[0];
+  const int n = 1 << log2n;
+  double2* x = smem;
+  double2* y = smem + n;
+  double2* acc = smem + 2 * n;
+  const int tid = threadIdx.x;
+  for (long g = blockIdx.x; g < count; g += gridDim.x) {
+    for (int t = 0; t < terms; ++t) {
+      const long term = g * terms + t;
+      const uint64_t* ap = a + (term << (log2n + 1));
+      for (int j = tid; j < n; j += THREADS) {
+        const c64 v{i64_to_f64_rne((int64_t)__ldcs(ap + j)), i64_to_f64_rne((int64_t)__ldcs(ap + j + n))};
+        st(x + j, cmul(ldg(tw + j), v));
+      }
+      __syncthreads();
+      const double2* r = unordered_smem<true, 0, ALGO>(L, 0, 1, x, y, w, tid, THREADS);
+      const double2* bp = bhat + (term << log2n);
+      for (int k = tid; k < n; k += THREADS) {
+        const c64 p = cmul(ldg(bp + k), ld(r + k));
+        st(acc + k, t == 0 ? p : cadd(ld(acc + k), p));
+      }
+      __syncthreads();
+    }
+    const double2* s = unordered_smem<false, 0, ALGO>(L, 0, 1, acc, x, winv, tid, THREADS);
+    uint64_t* op = out + (g << (log2n + 1));
+    for (int j = tid; j < n; j += THREADS) {
+      const c64 v = cmul(ldg(itw + j), ld(s + j));
+      __stcs(op + j, round_half_up_mod64(v.re));
+      __stcs(op + j + n, round_half_up_mod64(v.im));
+    }
+    __syncthreads();
+  }
+}
+
 // Bhat = fwd(tau^j * (b_j + i b_{j+N/2})) for small signed digits b.
 template <int ALGO, int THREADS>
 __global__ void __launch_bounds__(THREADS) u64_prepare_kernel(const int64_t* __restrict__ b,
@@ -103,6 +151,7 @@ const void* c64_kernel_emu(int algo, int e, bool fwd);
 const void* u64_product_kernel_e0(int algo);
 const void* u64_product_kernel_emu(int algo, int e);
 const void* u64_prepare_kernel_ptr(int algo);
+const void* u64_product_sum_kernel_ptr(int algo);
 
 inline const void* c64_kernel(int algo, int e, bool fwd) {
   const int lvl = emu_level_for(algo, e);

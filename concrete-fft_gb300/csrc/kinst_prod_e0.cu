@@ -28,4 +28,17 @@ const void* u64_prepare_kernel_ptr(int algo) {
     default: return nullptr;
   }
 }
+const void* u64_product_sum_kernel_ptr(int algo) {
+  switch (algo) {
+    case 0: return (const void*)u64_product_sum_kernel<0, kProdThreads>;
+    case 1: return (const void*)u64_product_sum_kernel<1, kProdThreads>;
+    case 2: return (const void*)u64_product_sum_kernel<2, kProdThreads>;
+    case 3: return (const void*)u64_product_sum_kernel<3, kProdThreads>;
+    case 4: return (const void*)u64_product_sum_kernel<4, kProdThreads>;
+    case 5: return (const void*)u64_product_sum_kernel<5, kProdThreads>;
+    case 6: return (const void*)u64_product_sum_kernel<6, kProdThreads>;
+    case 7: return (const void*)u64_product_sum_kernel<7, kProdThreads>;
+    default: return nullptr;
+  }
+}
 }  // namespace cfft

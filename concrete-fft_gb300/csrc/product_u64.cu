@@ -162,6 +162,25 @@ cfft_status cfft_u64_untwist_round(const cfft_u64_product_plan* plan, const doub
   return CFFT_OK;
 }
 
+cfft_status cfft_u64_product_sum(const cfft_u64_product_plan* plan, const uint64_t* a, const double* bhat,
+                                 size_t terms, uint64_t* out, size_t count, void* stream) {
+  if (!plan || !a || !bhat || !out) return fail(CFFT_ERR_INVALID_ARGUMENT, "null argument");
+  if (terms == 0 || terms > 0x7fffffff) return fail(CFFT_ERR_INVALID_ARGUMENT, "terms must be at least 1");
+  if (plan->N > (size_t(2) << kSmemLog2Max))
+    return fail(CFFT_ERR_INVALID_SIZE, "product sum: N must be at most 8192");
+  if (count == 0) return CFFT_OK;
+  const void* fn = u64_product_sum_kernel_ptr(plan->base_algo);
+  const size_t smem = 3 * plan->n * sizeof(double2);
+  const int grid = grid_for(fn, kProdThreads, smem, (long)count);
+  DevLevels L = plan->dlv;
+  long cnt = (long)count;
+  int tr = (int)terms;
+  const double2* bh = (const double2*)bhat;
+  void* args[] = {(void*)&a, (void*)&bh, &tr, (void*)&out, &cnt, &L, (void*)&plan->d_w, (void*)&plan->d_winv,
+                  (void*)&plan->d_tw, (void*)&plan->d_itw};
+  return launch_kernel(fn, grid, kProdThreads, args, smem, (cudaStream_t)stream);
+}
+
 cfft_unordered_plan* cfft_u64_product_fft(const cfft_u64_product_plan* plan) { return plan ? plan->fft : nullptr; }
 
 cfft_status cfft_u64_product_set_int_adds(cfft_u64_product_plan* plan, int eighths) {

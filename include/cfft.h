@@ -185,6 +185,15 @@ cfft_status cfft_u64_product(const cfft_u64_product_plan* plan, const uint64_t* 
 cfft_status cfft_u64_product_host(const cfft_u64_product_plan* plan, const uint64_t* a, const double* bhat,
                                   size_t bhat_stride, uint64_t* out, size_t count);
 
+/* Products summed in the Fourier domain (the external-product shape; no
+ * counterpart in the reference): out[g] = sum_{t < terms} a[g][t] * B[g][t]
+ * mod (X^N + 1), every term transformed forward, multiplied and accumulated
+ * in term order, then one inverse per group instead of one per term.
+ * a: count * terms * N u64; bhat: count * terms * N/2 c64; out: count * N u64.
+ * N <= 8192. */
+cfft_status cfft_u64_product_sum(const cfft_u64_product_plan* plan, const uint64_t* a, const double* bhat,
+                                 size_t terms, uint64_t* out, size_t count, void* stream);
+
 /* The same pipeline unfused, one launch per step (for callers that keep the
  * Fourier-domain data themselves; bit-identical to cfft_u64_product):
  *   cfft_u64_fold_twist -> cfft_unordered_fwd(cfft_u64_product_fft(plan)) ->

@@ -1178,6 +1178,40 @@ int oracle_u64_product_batch(size_t N, int base_algo, size_t base_n, size_t coun
   return 0;
 }
 
+// Sum of `terms` products accumulated in the Fourier domain (the external
+// product shape): acc = sum_t Bhat_t * fwd(twist(a_t)) in term order, then one
+// inverse, untwist and rounding.  Groups are independent.
+int oracle_u64_product_sum(size_t N, int base_algo, size_t base_n, size_t terms, size_t count, const uint64_t* a,
+                           const double* bhat, uint64_t* out, int nthreads) {
+  if (!is_pow2(N) || N < 4 || !unordered_args_ok(N / 2, base_n) || base_algo < 0 || base_algo > 7 || terms == 0)
+    return -1;
+  const U64Pipeline P(N, base_algo, base_n);
+  const size_t n = N / 2;
+  parallel_for(count, nthreads, [&](size_t b, size_t e) {
+    std::vector<c64> z(n), acc(n), scratch(base_n);
+    for (size_t g = b; g < e; ++g) {
+      for (size_t t = 0; t < terms; ++t) {
+        const uint64_t* at = a + (g * terms + t) * N;
+        const c64* bt = ((const c64*)bhat) + (g * terms + t) * n;
+        for (size_t j = 0; j < n; ++j) z[j] = mul(P.tw[j], c64{(double)(int64_t)at[j], (double)(int64_t)at[j + n]});
+        P.forward(z.data(), scratch.data());
+        for (size_t k = 0; k < n; ++k) {
+          const c64 p = mul(bt[k], z[k]);
+          acc[k] = t == 0 ? p : add(acc[k], p);
+        }
+      }
+      P.inverse(acc.data(), scratch.data());
+      uint64_t* og = out + g * N;
+      for (size_t j = 0; j < n; ++j) {
+        const c64 t = mul(P.itw[j], acc[j]);
+        og[j] = round_half_up_mod64(t.re);
+        og[j + n] = round_half_up_mod64(t.im);
+      }
+    }
+  });
+  return 0;
+}
+
 int oracle_u128_prepare_b(size_t N, const int64_t* b, double* bhat4) {
   if (!is_pow2(N) || N < 64) return -1;
   const U128Pipeline P(N);

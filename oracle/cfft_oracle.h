@@ -73,7 +73,11 @@ int oracle_u64_product(size_t N, int base_algo, size_t base_n, const uint64_t* a
 /* batched + threaded version for the CPU baseline (nthreads <= 0: all cores) */
 int oracle_u64_product_batch(size_t N, int base_algo, size_t base_n, size_t count,
                              const uint64_t* a, const double* bhat, uint64_t* out, int nthreads);
-/* f64 -> integer mod 2^64, round half away from zero, exact for any finite input */
+/* Fourier-domain accumulation: out[g] = sum_t a[g][t] * B[g][t] mod (X^N + 1),
+ * the products summed in the Fourier domain in term order, one inverse. */
+int oracle_u64_product_sum(size_t N, int base_algo, size_t base_n, size_t terms, size_t count, const uint64_t* a,
+                           const double* bhat, uint64_t* out, int nthreads);
+/* f64 -> integer mod 2^64, floor(x + 1/2), exact for any finite input */
 uint64_t oracle_round_mod64(double x);
 
 /* The double-double product pipeline around the reference's fft128 plan.

@@ -201,6 +201,17 @@ def u64_product(N, base_algo, base_n, a, bhat, nthreads=1):
     return out
 
 
+def u64_product_sum(N, base_algo, base_n, a, bhat, nthreads=1):
+    """a: (count, terms, N) uint64; bhat: (count, terms, N/2) complex128 -> (count, N) uint64."""
+    a = np.ascontiguousarray(a, dtype=np.uint64)
+    bhat = np.ascontiguousarray(bhat, dtype=np.complex128)
+    count, terms = a.shape[0], a.shape[1]
+    out = np.zeros((count, N), np.uint64)
+    _ok(lib().oracle_u64_product_sum(S(N), int(base_algo), S(base_n), S(terms), S(count), P(a), P(bhat), P(out),
+                                     nthreads))
+    return out
+
+
 def u128_schoolbook(a, b):
     """a: (..., N, 2) uint64 (lo, hi); b: (..., N) int64."""
     a = np.ascontiguousarray(a, dtype=np.uint64)

@@ -119,3 +119,24 @@ def test_u128_product_bit_exact(cuda, oracle, N):
     out2 = torch.empty_like(da2)
     plan.product(da2, bhat[:1], out2)
     assert np.array_equal(out2.cpu().numpy().view(np.uint64), oracle.u128_schoolbook(a2, b[:1]))
+
+
+@pytest.mark.parametrize("N,algo,base,terms", [(2048, 2, 1024, 8), (1024, 4, 512, 3), (4096, 6, 1024, 1),
+                                               (8192, 3, 1024, 2)])
+def test_u64_product_sum_bit_exact(cuda, oracle, N, algo, base, terms):
+    """Fourier-domain accumulation of `terms` products, one inverse per group."""
+    import concrete_fft as cf
+    torch = cuda
+    count = 4
+    plan = cf.product.U64ProductPlan(N, algo, base)
+    a = RNG.integers(0, 2 ** 64, (count, terms, N), dtype=np.uint64)
+    b = RNG.integers(-2 ** 7, 2 ** 7, (count * terms, N))
+    bhat = torch.empty((count, terms, N // 2), dtype=torch.complex128, device="cuda")
+    plan.prepare_operand(torch.from_numpy(b).cuda(), bhat)
+    out = torch.empty((count, N), dtype=torch.int64, device="cuda")
+    plan.product_sum(torch.from_numpy(a.view(np.int64)).cuda(), bhat, out)
+    want_bhat = oracle.u64_prepare(N, algo, base, b).reshape(count, terms, N // 2)
+    want = oracle.u64_product_sum(N, algo, base, a, want_bhat, nthreads=0)
+    assert np.array_equal(out.cpu().numpy().view(np.uint64), want)
+    exact = sum(oracle.u64_schoolbook(a[0, t], b[t]) for t in range(terms))
+    assert torus_err_bits(want[0], exact.astype(np.uint64)) < 30

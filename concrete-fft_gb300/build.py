@@ -22,7 +22,7 @@ BUILD = os.path.join(PKG, "_build")
 LIB = os.path.join(PKG, "lib", "libcfft_gb300.so")
 
 CUDA_SOURCES = ["c64.cu", "product_u64.cu", "f128.cu", "runtime.cu", "batch.cu", "product_engine.cu", "server.cu", "kinst_c64_e0.cu", "kinst_c64_emu.cu", "kinst_prod_e0.cu", "kinst_prod_emu.cu"]
-CXX_SOURCES = ["twiddles.cpp"]
+CXX_SOURCES = ["twiddles.cpp", "tune_cache.cpp"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 

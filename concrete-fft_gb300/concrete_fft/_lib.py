@@ -36,6 +36,10 @@ _SIGS = [
     ("cfft_version", ctypes.c_char_p, []),
     ("cfft_device_check", c_int, []),
     ("cfft_diag_fp64_peak", c_int, [ctypes.POINTER(c_dbl)]),
+    ("cfft_tune_save", c_int, [ctypes.c_char_p]),
+    ("cfft_tune_load", c_int, [ctypes.c_char_p]),
+    ("cfft_tune_clear", None, []),
+    ("cfft_tune_entries", c_size, []),
     ("cfft_diag_dadd_check", c_int, [ctypes.c_uint64, ctypes.c_uint64, ctypes.POINTER(ctypes.c_uint64),
                                      ctypes.POINTER(ctypes.c_uint64)]),
     ("cfft_diag_dadd_int_rate", c_int, [ctypes.POINTER(c_dbl)]),

@@ -14,6 +14,7 @@
 #include "cfft_internal.h"
 #include "runtime.h"
 #include "c64_kernels.cuh"
+#include "tune_cache.h"
 
 using namespace cfft;
 
@@ -347,6 +348,16 @@ cfft_status cfft_ordered_plan_create_measure(size_t n, double seconds, cfft_orde
   *out = nullptr;
   if (!is_pow2(n) || ilog2(n) >= 11) return fail(CFFT_ERR_INVALID_SIZE, "ordered plan: n must be 2^k, k <= 10");
   if (n == 1) return cfft_ordered_plan_create(n, CFFT_DIF2, out);
+  TuneVal tv;
+  if (tune_lookup(0, n, &tv)) {  // measured before on this GPU model
+    cfft_status st = cfft_ordered_plan_create(n, (cfft_algo)tv.algo, out);
+    if (st == CFFT_OK) {
+      (*out)->p.threads = tv.threads;
+      (*out)->p.tpc = tv.tpc;
+      (*out)->p.emu = tv.emu;
+    }
+    return st;
+  }
   double2* scratch = nullptr;
   size_t batch = 0;
   cfft_status st = alloc_measure_scratch(n, &scratch, &batch);
@@ -354,7 +365,11 @@ cfft_status cfft_ordered_plan_create_measure(size_t n, double seconds, cfft_orde
   double t = 0;
   if (st == CFFT_OK) st = measure_ordered(n, seconds, scratch, batch, &algo, &th, &tpc, &t);
   if (st == CFFT_OK) st = cfft_ordered_plan_create(n, (cfft_algo)algo, out);
-  if (st == CFFT_OK) tune_launch((*out)->p, scratch, batch, seconds);
+  if (st == CFFT_OK) {
+    tune_launch((*out)->p, scratch, batch, seconds);
+    const C64Plan& p = (*out)->p;
+    tune_store(0, n, TuneVal{p.base_algo, p.base_n, p.threads, p.tpc, p.emu});
+  }
   if (scratch) cudaFree(scratch);
   return st;
 }
@@ -426,6 +441,16 @@ cfft_status cfft_unordered_plan_create_measure(size_t n, double seconds, cfft_un
   if (!out) return fail(CFFT_ERR_INVALID_ARGUMENT, "null output pointer");
   *out = nullptr;
   if (!is_pow2(n) || ilog2(n) > 20) return fail(CFFT_ERR_INVALID_SIZE, "unordered plan: n must be 2^k, k <= 20");
+  TuneVal tv;
+  if (tune_lookup(1, n, &tv)) {  // measured before on this GPU model
+    cfft_status st = cfft_unordered_plan_create(n, (cfft_algo)tv.algo, tv.base_n, out);
+    if (st == CFFT_OK) {
+      (*out)->p.threads = tv.threads;
+      (*out)->p.tpc = tv.tpc;
+      (*out)->p.emu = tv.emu;
+    }
+    return st;
+  }
   double2* scratch = nullptr;
   size_t batch = 0;
   cfft_status st = alloc_measure_scratch(n, &scratch, &batch);
@@ -462,7 +487,11 @@ cfft_status cfft_unordered_plan_create_measure(size_t n, double seconds, cfft_un
     }
   }
   if (st == CFFT_OK) st = cfft_unordered_plan_create(n, (cfft_algo)best_algo, best_base, out);
-  if (st == CFFT_OK) tune_launch((*out)->p, scratch, batch, seconds);
+  if (st == CFFT_OK) {
+    tune_launch((*out)->p, scratch, batch, seconds);
+    const C64Plan& p = (*out)->p;
+    tune_store(1, n, TuneVal{p.base_algo, p.base_n, p.threads, p.tpc, p.emu});
+  }
   cudaFree(scratch);
   return st;
 }

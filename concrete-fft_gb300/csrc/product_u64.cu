@@ -25,6 +25,7 @@
 #include "cfft_internal.h"
 #include "runtime.h"
 #include "c64_kernels.cuh"
+#include "tune_cache.h"
 
 using namespace cfft;
 
@@ -286,6 +287,12 @@ cfft_status cfft_u64_product_plan_create_measure(size_t N, double seconds, cfft_
   if (!is_pow2(N) || N < 64 || ilog2(N) > kSmemLog2Max + 1)
     return fail(CFFT_ERR_INVALID_SIZE, "u64 product: N must be a power of two in [64, 8192]");
   const size_t n = N / 2;
+  TuneVal tv;
+  if (tune_lookup(2, N, &tv)) {  // measured before on this GPU model
+    cfft_status st = cfft_u64_product_plan_create(N, (cfft_algo)tv.algo, tv.base_n, out);
+    if (st == CFFT_OK) (*out)->emu = tv.emu;
+    return st;
+  }
   std::vector<size_t> bases;
   if (n <= 256) bases.push_back(n);
   else
@@ -372,6 +379,7 @@ cfft_status cfft_u64_product_plan_create_measure(size_t N, double seconds, cfft_
     }
   }
   (*out)->emu = be;
+  tune_store(2, N, TuneVal{best_algo, best_base, kProdThreads, 1, be});
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
   cudaStreamDestroy(s);

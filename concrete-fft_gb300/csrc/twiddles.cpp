@@ -10,6 +10,7 @@
 #include <string>
 
 #include "cfft_internal.h"
+#include "tune_cache.h"
 
 namespace cfft {
 
@@ -265,6 +266,10 @@ static std::string g_err;
 void set_error(const std::string& msg) {
   std::lock_guard<std::mutex> lk(g_err_mu);
   g_err = msg;
+}
+cfft_status fail_status(cfft_status s, const std::string& msg) {
+  set_error(msg);
+  return s;
 }
 std::string get_error() {
   std::lock_guard<std::mutex> lk(g_err_mu);

@@ -61,6 +61,16 @@ const char* cfft_version(void);
 /* 0 when a device of compute capability 10.3 is usable, else a cfft_status. */
 cfft_status cfft_device_check(void);
 
+/* Persisted Method::Measure results (no counterpart in the reference, whose
+ * Measure re-times on every Plan::new).  Every *_create_measure call first
+ * looks up (GPU model, plan kind, size) in a process-wide table and times the
+ * candidates only on a miss, storing its choice.  save/load write and read
+ * the table as text (one tab-separated entry per line). */
+cfft_status cfft_tune_save(const char* path);
+cfft_status cfft_tune_load(const char* path);
+void cfft_tune_clear(void);
+size_t cfft_tune_entries(void);
+
 /* ======================================================= ordered::Plan ====
  * Replaces src/ordered.rs:187-373.  Sizes: powers of two, 1 <= n <= 1024
  * (the reference asserts n.trailing_zeros() < 11, src/ordered.rs:244). */

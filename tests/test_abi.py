@@ -60,3 +60,22 @@ def test_library_has_no_oracle_dependency():
     assert "oracle" not in out
     strings = open(concrete_fft.LIB_PATH, "rb").read()
     assert b"liboracle" not in strings
+
+
+def test_tune_cache_file_round_trip(cfft_lib, tmp_path):
+    """Persisted Measure results: load, count, save, reload; malformed lines are rejected."""
+    L = cfft_lib
+    L.cfft_tune_clear()
+    src = tmp_path / "tune.txt"
+    src.write_text("NVIDIA GB300\t2\t2048\t2\t1024\t128\t1\t0\nNVIDIA GB300\t0\t1024\t3\t1024\t256\t1\t0\n")
+    assert L.cfft_tune_load(str(src).encode()) == 0
+    assert L.cfft_tune_entries() == 2
+    out = tmp_path / "saved.txt"
+    assert L.cfft_tune_save(str(out).encode()) == 0
+    assert sorted(out.read_text().splitlines()) == sorted(src.read_text().splitlines())
+    bad = tmp_path / "bad.txt"
+    bad.write_text("NVIDIA GB300\t2\t2048\t9\t1024\t128\t1\t0\n")  # algo 9 does not exist
+    assert L.cfft_tune_load(str(bad).encode()) == -2
+    assert b"out of range" in L.cfft_last_error()
+    L.cfft_tune_clear()
+    assert L.cfft_tune_entries() == 0

@@ -175,6 +175,29 @@ def test_measure_plans(cuda, oracle):
     assert np.array_equal(bits(d.cpu().numpy()), bits(oracle.unordered_fwd(int(algo), base, x.reshape(1, 4096))))
 
 
+def test_measure_results_are_persisted(cuda, oracle, tmp_path):
+    """A second Measure plan of the same size reuses the stored choice (no re-timing);
+    after save / clear / load it is reused again."""
+    import time
+    import concrete_fft as cf
+    L = cf.load()
+    L.cfft_tune_clear()
+    t0 = time.perf_counter()
+    p1 = cf.unordered.Plan(2048, cf.unordered.Method.Measure(0.002))
+    t_measure = time.perf_counter() - t0
+    assert L.cfft_tune_entries() == 1
+    path = str(tmp_path / "tune.txt").encode()
+    cf.check(L.cfft_tune_save(path))
+    L.cfft_tune_clear()
+    cf.check(L.cfft_tune_load(path))
+    t0 = time.perf_counter()
+    p2 = cf.unordered.Plan(2048, cf.unordered.Method.Measure(0.002))
+    t_cached = time.perf_counter() - t0
+    assert p2.algo() == p1.algo() and p2.int_adds() == p1.int_adds()
+    assert t_cached < t_measure / 5
+    L.cfft_tune_clear()
+
+
 def test_invalid_calls_raise(cuda):
     import concrete_fft as cf
     torch = cuda

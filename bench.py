@@ -462,6 +462,21 @@ def run_ordered(args):
 
     ms256, clocks = timed(torch, step256, args.steps, args.warmup, local, world)
     ms1, _ = timed(torch, step1, args.steps, args.warmup, local, world)
+    # CTAs per transform (1 = one CTA, 2/4/8 = thread-block cluster) at a few batch sizes, fwd then inv
+    sweep = {}
+    for batch in (1, 16, 64, 256):
+        sub = d[:batch].clone()
+
+        def step_b():
+            plan.fwd(sub)
+            plan.inv(sub)
+        row = {}
+        for ctas in (1, 2, 4, 8):
+            plan.set_cluster_size(ctas)
+            ms_b, _ = timed(torch, step_b, max(10, args.steps // 4), args.warmup, local, world)
+            row[ctas] = round(ms_b * 1e3 / max(10, args.steps // 4), 2)
+        sweep[batch] = row
+    plan.set_cluster_size(0)
     per = ms256 * 1e-3 / args.steps
     ops = 256 * 2 * fp64_ops_ordered(1024, int(plan.algo()))
     peak = fp64_peak(cf)
@@ -479,7 +494,8 @@ def run_ordered(args):
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms256 / args.steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded numpy PCG64)",
         "config": {"workload": "ordered::Plan n=1024 batch 256", "algo": plan.algo().name,
-                   "batch1_us_per_fwd_inv": ms1 * 1e3 / args.steps},
+                   "batch1_us_per_fwd_inv": ms1 * 1e3 / args.steps,
+                   "us_per_fwd_inv_by_batch_and_ctas_per_transform": sweep},
         "roofline": {"bound": "hbm", "achieved": 256 * 65536 / per / 1e9, "peak": measured_peaks()[0]["hbm_gbs"],
                      "unit": "GB/s", "frac": 256 * 65536 / per / 1e9 / measured_peaks()[0]["hbm_gbs"],
                      "traffic": None, "fp64": {"achieved_ops_per_s": ops / per, "peak_ops_per_s": peak,

@@ -54,6 +54,8 @@ _SIGS = [
     ("cfft_ordered_fwd_host", c_int, [vp, vp, c_size]),
     ("cfft_ordered_inv_host", c_int, [vp, vp, c_size]),
     ("cfft_ordered_set_int_adds", c_int, [vp, c_int]),
+    ("cfft_ordered_set_cluster_size", c_int, [vp, c_int]),
+    ("cfft_unordered_set_cluster_size", c_int, [vp, c_int]),
     ("cfft_ordered_int_adds", c_int, [vp]),
     ("cfft_unordered_set_int_adds", c_int, [vp, c_int]),
     ("cfft_unordered_int_adds", c_int, [vp]),

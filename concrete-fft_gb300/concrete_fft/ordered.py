@@ -65,6 +65,10 @@ class Plan:
         """Share (in eighths) of butterfly additions issued on the integer pipe; results are unchanged."""
         check(self._lib.cfft_ordered_set_int_adds(self._h, int(eighths)))
 
+    def set_cluster_size(self, ctas):
+        """CTAs per transform: 0 automatic, 1 one CTA, 2/4/8 a thread-block cluster; results unchanged."""
+        check(self._lib.cfft_ordered_set_cluster_size(self._h, int(ctas)))
+
     def int_adds(self):
         return self._lib.cfft_ordered_int_adds(self._h)
 

@@ -94,6 +94,7 @@ struct C64Plan {
   int threads = 128;  // CTA size of the shared-memory kernel
   int tpc = 1;       // sub-transforms per CTA
   int emu = 0;       // eighths of the butterfly additions issued on the integer pipe
+  int cluster = 0;   // CTAs per transform: 0 automatic, 1 one CTA, 2/4/8 a cluster of that size
 };
 
 struct cfft_ordered_plan {
@@ -174,6 +175,45 @@ cfft_status build_plan(C64Plan& p, size_t n, size_t base_n, int algo, bool unord
   return st;
 }
 
+// CTAs per transform for a call, as a log2 (0: one CTA).  A transform is
+// split over S = 2^ls CTAs (split.cuh) when the batch is too small to give
+// every SM work, or as the plan forces.  Only plans whose transform fits one
+// CTA whole (d0 == 0).  S is bounded by the radix of the step that is split
+// (the base radix without outer levels, level 0's radix with them) and by 8.
+int split_log2(const C64Plan& p, long nsub, int* mode) {
+  if (p.d0 != 0 || p.cluster == 1) return 0;
+  const int log2n = p.lv.log2n[0];
+  int max_ls;
+  if (p.lv.nlevels == 0) {
+    *mode = 0;
+    const int lr = ilog2((size_t)algo_radix(p.base_algo));
+    max_ls = std::min(3, std::min(lr, log2n - lr - 1));
+  } else {
+    *mode = 1;
+    max_ls = std::min(3, p.lv.log2r[0]);
+  }
+  if (log2n < 6 || max_ls < 1) return 0;
+  if (p.cluster >= 2) return std::min(max_ls, ilog2((size_t)p.cluster));
+  const long target = 4L * sm_count();
+  int ls = 0;
+  while (ls < max_ls && (nsub << ls) < target) ++ls;
+  return ls;
+}
+
+cfft_status launch_split(const C64Plan& p, bool fwd, int ls, int mode, long nsub, cudaStream_t stream,
+                         double2* data) {
+  const void* fn = c64_split_kernel_ptr(p.base_algo, fwd, ls, mode);
+  const size_t part = p.n >> ls;
+  const size_t smem = 2 * part * sizeof(double2);
+  const int threads = (int)std::min<size_t>(256, std::max<size_t>(32, part / 2));
+  DevLevels L = p.dlv;
+  const double2* w = fwd ? p.d_w : p.d_winv;
+  void* args[] = {&data, &L, (void*)&w};
+  if ((nsub << ls) > 0x7fffffffL) return fail(CFFT_ERR_INVALID_SIZE, "batch too large");
+  const int grid = (int)(nsub << ls);
+  return launch_kernel_cluster(fn, grid, threads, 1 << ls, args, smem, stream);
+}
+
 cfft_status run_plan(const C64Plan& p, double* buf, size_t batch, bool fwd, cudaStream_t stream) {
   if (batch == 0) return CFFT_OK;
   if (buf == nullptr) return fail(CFFT_ERR_INVALID_ARGUMENT, "null buffer");
@@ -183,6 +223,9 @@ cfft_status run_plan(const C64Plan& p, double* buf, size_t batch, bool fwd, cuda
   const int log2sub = p.lv.log2n[p.d0];
   const long nsub = (long)batch << (log2n - log2sub);
   if (nsub > 0x7fffffffL * (long)p.tpc) return fail(CFFT_ERR_INVALID_SIZE, "batch too large");
+  int mode = 0;
+  const int ls = split_log2(p, nsub, &mode);
+  if (ls > 0) return launch_split(p, fwd, ls, mode, nsub, stream, data);
   const int blocks = (int)((nsub + p.tpc - 1) / p.tpc);
   const size_t smem = smem_bytes(p);
   const int nsm = sm_count();
@@ -406,6 +449,20 @@ cfft_status cfft_ordered_set_int_adds(cfft_ordered_plan* plan, int eighths) {
   return CFFT_OK;
 }
 int cfft_ordered_int_adds(const cfft_ordered_plan* plan) { return plan ? emu_level(plan->p) : -1; }
+
+cfft_status cfft_ordered_set_cluster_size(cfft_ordered_plan* plan, int ctas) {
+  if (!plan || !(ctas == 0 || ctas == 1 || ctas == 2 || ctas == 4 || ctas == 8))
+    return fail(CFFT_ERR_INVALID_ARGUMENT, "cluster size must be 0 (automatic), 1, 2, 4 or 8");
+  plan->p.cluster = ctas;
+  return CFFT_OK;
+}
+
+cfft_status cfft_unordered_set_cluster_size(cfft_unordered_plan* plan, int ctas) {
+  if (!plan || !(ctas == 0 || ctas == 1 || ctas == 2 || ctas == 4 || ctas == 8))
+    return fail(CFFT_ERR_INVALID_ARGUMENT, "cluster size must be 0 (automatic), 1, 2, 4 or 8");
+  plan->p.cluster = ctas;
+  return CFFT_OK;
+}
 
 cfft_status cfft_unordered_set_int_adds(cfft_unordered_plan* plan, int eighths) {
   if (!plan || eighths < 0 || eighths > 8) return fail(CFFT_ERR_INVALID_ARGUMENT, "eighths must be in 0..8");

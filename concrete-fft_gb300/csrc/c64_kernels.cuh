@@ -73,8 +73,12 @@ __global__ void __launch_bounds__(THREADS) u64_product_kernel(const uint64_t* __
 // group (the TFHE external-product shape): per group, every term is folded,
 // twisted and transformed in shared memory, multiplied by its operand and added
 // into an accumulator in term order; the accumulator is inverted, untwisted
-// and rounded once.  Shared memory: 3 x N/2 c64.
-template <int ALGO, int THREADS>
+// and rounded once.  ACC = 0: the accumulator is a third shared buffer (3 x N/2
+// c64).  ACC > 0 (N/2 <= ACC x THREADS): each thread keeps the accumulator
+// entries k = tid + j x THREADS it multiplies in registers, so shared memory
+// is the 2 x N/2 ping-pong pair and more CTAs fit on an SM; the additions and
+// their order are the same.
+template <int ALGO, int THREADS, int ACC>
 __global__ void __launch_bounds__(THREADS) u64_product_sum_kernel(const uint64_t* __restrict__ a,
                                                                  const double2* __restrict__ bhat, int terms,
                                                                  uint64_t* __restrict__ out, long count, DevLevels L,
@@ -87,7 +91,8 @@ __global__ void __launch_bounds__(THREADS) u64_product_sum_kernel(const uint64_t
   const int n = 1 << log2n;
   double2* x = smem;
   double2* y = smem + n;
-  double2* acc = smem + 2 * n;
+  double2* acc = smem + 2 * n;  // ACC == 0 only
+  c64 racc[ACC > 0 ? ACC : 1];
   const int tid = threadIdx.x;
   for (long g = blockIdx.x; g < count; g += gridDim.x) {
     for (int t = 0; t < terms; ++t) {
@@ -100,13 +105,34 @@ __global__ void __launch_bounds__(THREADS) u64_product_sum_kernel(const uint64_t
       __syncthreads();
       const double2* r = unordered_smem<true, 0, ALGO>(L, 0, 1, x, y, w, tid, THREADS);
       const double2* bp = bhat + (term << log2n);
-      for (int k = tid; k < n; k += THREADS) {
-        const c64 p = cmul(ldg(bp + k), ld(r + k));
-        st(acc + k, t == 0 ? p : cadd(ld(acc + k), p));
+      if (ACC > 0) {
+#pragma unroll
+        for (int j = 0; j < (ACC > 0 ? ACC : 1); ++j) {
+          const int k = tid + j * THREADS;
+          if (k < n) {
+            const c64 p = cmul(ldg(bp + k), ld(r + k));
+            racc[j] = t == 0 ? p : cadd(racc[j], p);
+          }
+        }
+      } else {
+        for (int k = tid; k < n; k += THREADS) {
+          const c64 p = cmul(ldg(bp + k), ld(r + k));
+          st(acc + k, t == 0 ? p : cadd(ld(acc + k), p));
+        }
       }
       __syncthreads();
     }
-    const double2* s = unordered_smem<false, 0, ALGO>(L, 0, 1, acc, x, winv, tid, THREADS);
+    double2* src = acc;
+    if (ACC > 0) {
+#pragma unroll
+      for (int j = 0; j < (ACC > 0 ? ACC : 1); ++j) {
+        const int k = tid + j * THREADS;
+        if (k < n) st(y + k, racc[j]);
+      }
+      __syncthreads();
+      src = y;
+    }
+    const double2* s = unordered_smem<false, 0, ALGO>(L, 0, 1, src, x, winv, tid, THREADS);
     uint64_t* op = out + (g << (log2n + 1));
     for (int j = tid; j < n; j += THREADS) {
       const c64 v = cmul(ldg(itw + j), ld(s + j));
@@ -116,6 +142,10 @@ __global__ void __launch_bounds__(THREADS) u64_product_sum_kernel(const uint64_t
     __syncthreads();
   }
 }
+
+// Accumulator entries per thread in the register variant of the sum kernel:
+// covers N/2 <= 8 x 128 = 1024 (N <= 2048).
+constexpr int kSumRegAcc = 8;
 
 // Bhat = fwd(tau^j * (b_j + i b_{j+N/2})) for small signed digits b.
 template <int ALGO, int THREADS>
@@ -147,11 +177,13 @@ constexpr int kProdThreads = 128;
 
 // Kernel-pointer tables (nullptr when the combination is not instantiated).
 const void* c64_kernel_e0(int algo, bool fwd);
+// one transform over 2^ls CTAs (split.cuh); mode 0 no outer levels, 1 with levels
+const void* c64_split_kernel_ptr(int algo, bool fwd, int ls, int mode);
 const void* c64_kernel_emu(int algo, int e, bool fwd);
 const void* u64_product_kernel_e0(int algo);
 const void* u64_product_kernel_emu(int algo, int e);
 const void* u64_prepare_kernel_ptr(int algo);
-const void* u64_product_sum_kernel_ptr(int algo);
+const void* u64_product_sum_kernel_ptr(int algo, bool reg_acc);
 
 inline const void* c64_kernel(int algo, int e, bool fwd) {
   const int lvl = emu_level_for(algo, e);

@@ -19,4 +19,17 @@ const void* c64_kernel_e0(int algo, bool fwd) {
     default: return nullptr;
   }
 }
+const void* c64_split_ptr_01(int algo, bool fwd, int ls, int mode);
+const void* c64_split_ptr_23(int algo, bool fwd, int ls, int mode);
+const void* c64_split_ptr_45(int algo, bool fwd, int ls, int mode);
+const void* c64_split_ptr_67(int algo, bool fwd, int ls, int mode);
+const void* c64_split_kernel_ptr(int algo, bool fwd, int ls, int mode) {
+  switch (algo >> 1) {
+    case 0: return c64_split_ptr_01(algo, fwd, ls, mode);
+    case 1: return c64_split_ptr_23(algo, fwd, ls, mode);
+    case 2: return c64_split_ptr_45(algo, fwd, ls, mode);
+    case 3: return c64_split_ptr_67(algo, fwd, ls, mode);
+    default: return nullptr;
+  }
+}
 }  // namespace cfft

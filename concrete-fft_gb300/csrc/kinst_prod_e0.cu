@@ -28,16 +28,21 @@ const void* u64_prepare_kernel_ptr(int algo) {
     default: return nullptr;
   }
 }
-const void* u64_product_sum_kernel_ptr(int algo) {
+template <int A>
+static const void* pick_sum(bool reg_acc) {
+  return reg_acc ? (const void*)u64_product_sum_kernel<A, kProdThreads, kSumRegAcc>
+                 : (const void*)u64_product_sum_kernel<A, kProdThreads, 0>;
+}
+const void* u64_product_sum_kernel_ptr(int algo, bool reg_acc) {
   switch (algo) {
-    case 0: return (const void*)u64_product_sum_kernel<0, kProdThreads>;
-    case 1: return (const void*)u64_product_sum_kernel<1, kProdThreads>;
-    case 2: return (const void*)u64_product_sum_kernel<2, kProdThreads>;
-    case 3: return (const void*)u64_product_sum_kernel<3, kProdThreads>;
-    case 4: return (const void*)u64_product_sum_kernel<4, kProdThreads>;
-    case 5: return (const void*)u64_product_sum_kernel<5, kProdThreads>;
-    case 6: return (const void*)u64_product_sum_kernel<6, kProdThreads>;
-    case 7: return (const void*)u64_product_sum_kernel<7, kProdThreads>;
+    case 0: return pick_sum<0>(reg_acc);
+    case 1: return pick_sum<1>(reg_acc);
+    case 2: return pick_sum<2>(reg_acc);
+    case 3: return pick_sum<3>(reg_acc);
+    case 4: return pick_sum<4>(reg_acc);
+    case 5: return pick_sum<5>(reg_acc);
+    case 6: return pick_sum<6>(reg_acc);
+    case 7: return pick_sum<7>(reg_acc);
     default: return nullptr;
   }
 }

@@ -99,9 +99,12 @@ DevLevels dev_levels(const LevelDesc& l) {
   return d;
 }
 
+// One CTA per product (the block scheduler hands the next product to the
+// first SM with room, which balances the SMs to within one product) up to a
+// large count; beyond it a grid of the resident CTAs strides over the batch.
 int grid_for(const void* kernel, int threads, size_t smem, long count) {
-  const long cap = (long)sm_count() * max_blocks_per_sm(kernel, threads, smem);
-  return (int)std::max<long>(1, std::min<long>(count, cap));
+  if (count <= (1L << 20)) return (int)std::max<long>(1, count);
+  return (int)((long)sm_count() * max_blocks_per_sm(kernel, threads, smem));
 }
 
 cfft_status launch_product(const cfft_u64_product_plan* plan, const uint64_t* a, const double* bhat,
@@ -170,8 +173,9 @@ cfft_status cfft_u64_product_sum(const cfft_u64_product_plan* plan, const uint64
   if (plan->N > (size_t(2) << kSmemLog2Max))
     return fail(CFFT_ERR_INVALID_SIZE, "product sum: N must be at most 8192");
   if (count == 0) return CFFT_OK;
-  const void* fn = u64_product_sum_kernel_ptr(plan->base_algo);
-  const size_t smem = 3 * plan->n * sizeof(double2);
+  const bool reg_acc = plan->n <= (size_t)(kSumRegAcc * kProdThreads);
+  const void* fn = u64_product_sum_kernel_ptr(plan->base_algo, reg_acc);
+  const size_t smem = (reg_acc ? 2 : 3) * plan->n * sizeof(double2);
   const int grid = grid_for(fn, kProdThreads, smem, (long)count);
   DevLevels L = plan->dlv;
   long cnt = (long)count;
@@ -399,11 +403,13 @@ cfft_status cfft_u64_product_host(const cfft_u64_product_plan* plan, const uint6
   if (bhat_stride != 0 && bhat_stride != plan->n)
     return fail(CFFT_ERR_INVALID_ARGUMENT, "bhat_stride must be 0 or N/2");
   if (count == 0) return CFFT_OK;
-  constexpr int kSlots = 3;
+  // About 24 chunks per call on 6 streams: the first copy in and the last
+  // copy out, which nothing overlaps, are then 1/24 of the data each, and 6
+  // chunks in flight keep kernels of several chunks resident at once.
+  constexpr int kSlots = 6;
   const size_t poly_bytes = plan->N * sizeof(uint64_t);
-  // about 8 chunks per call, each at least one full wave of CTAs
-  const size_t min_chunk = (size_t)sm_count() * 4;
-  const size_t chunk = std::min(count, std::max(min_chunk, (count + 7) / 8));
+  const size_t min_chunk = (size_t)sm_count() * 2;
+  const size_t chunk = std::min(count, std::max(min_chunk, (count + 23) / 24));
   PipeSlot slot[kSlots];
   cfft_status st = host_pipeline(kSlots, 2 * chunk * poly_bytes, slot);
   if (st != CFFT_OK) return st;

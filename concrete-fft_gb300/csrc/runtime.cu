@@ -96,6 +96,28 @@ cfft_status launch_kernel(const void* fn, int grid, int block, void** args, size
   return CFFT_OK;
 }
 
+cfft_status launch_kernel_cluster(const void* fn, int grid, int block, int cluster, void** args, size_t smem,
+                                  cudaStream_t stream) {
+  if (!fn) return fail(CFFT_ERR_INVALID_ARGUMENT, "no kernel instantiated for this configuration");
+  if (cluster < 1 || cluster > 8 || grid % cluster != 0) return fail(CFFT_ERR_INVALID_ARGUMENT, "bad cluster shape");
+  cfft_status st = ensure_smem_attr(fn, smem);
+  if (st != CFFT_OK) return st;
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3((unsigned)grid);
+  cfg.blockDim = dim3((unsigned)block);
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = stream;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeClusterDimension;
+  attr[0].val.clusterDim.x = (unsigned)cluster;
+  attr[0].val.clusterDim.y = 1;
+  attr[0].val.clusterDim.z = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  CFFT_CUDA_TRY(cudaLaunchKernelExC(&cfg, fn, args));
+  return CFFT_OK;
+}
+
 int max_blocks_per_sm(const void* fn, int block, size_t smem) {
   if (ensure_smem_attr(fn, smem) != CFFT_OK) return 1;
   int per_sm = 0;
@@ -104,11 +126,11 @@ int max_blocks_per_sm(const void* fn, int block, size_t smem) {
 }
 
 namespace {
-constexpr int kMaxSlots = 4;
+constexpr int kMaxSlots = 8;
 struct Pipeline {
-  void* ptr[kMaxSlots] = {nullptr, nullptr, nullptr, nullptr};
+  void* ptr[kMaxSlots] = {};
   size_t cap = 0;
-  cudaStream_t stream[kMaxSlots] = {nullptr, nullptr, nullptr, nullptr};
+  cudaStream_t stream[kMaxSlots] = {};
   int device = -1;
 };
 thread_local Pipeline t_pipe;

@@ -47,6 +47,9 @@ int sm_count();
 // Launch a kernel through its pointer, raising its dynamic shared-memory limit
 // the first time it is used with more than 48 KiB.
 cfft_status launch_kernel(const void* fn, int grid, int block, void** args, size_t smem, cudaStream_t stream);
+// The same with a thread-block cluster of `cluster` CTAs (grid a multiple of it).
+cfft_status launch_kernel_cluster(const void* fn, int grid, int block, int cluster, void** args, size_t smem,
+                                  cudaStream_t stream);
 int max_blocks_per_sm(const void* fn, int block, size_t smem);
 
 // Persistent scratch for the *_host convenience entry points (one per thread).

@@ -1,0 +1,293 @@
+// split.cuh -- one c64 transform spread over S = 2^LS CTAs, with at most one
+// exchange between them.
+//
+// A Stockham pass at stride s >= S only combines elements whose indices agree
+// mod S: its inputs k*n/R + p*s + q and outputs R*s*p + k*s + q are all
+// congruent to q.  So after the first DIF pass (s = 1) the residue classes mod
+// S are independent problems of n/S points, which keep the full transform's
+// twiddles (at stride s); before the last DIT pass the same holds in reverse.
+// Likewise the unordered outer level 0 of radix r splits a transform into r
+// contiguous slices that the later levels and the base treat independently.
+//
+// The S CTAs of a transform form a thread-block cluster.
+//
+// "First" kernels: every CTA reads the whole transform from global memory,
+// computes the outputs of the first step that fall in its own part --
+// selected at compile time, so the arithmetic of the other outputs is dropped
+// -- then finishes its part alone and stores it.  The transform is updated in
+// place, so a CTA stores only after every CTA of its cluster has read (a
+// cluster barrier split into an arrive after the reads and a wait before the
+// stores).  Used for DIF-structured transforms (ordered DIF algorithms, the
+// unordered base with no outer levels) and for the forward unordered
+// transform with levels.
+//
+// "Last" kernels: each CTA loads its part and runs everything but the last
+// step alone; the last step reads the other parts through distributed shared
+// memory.  Used for DIT-structured transforms and for the inverse unordered
+// transform with levels.
+//
+// Each butterfly does the same operations on the same values as in the
+// one-CTA kernels, so results are bit-identical.
+#pragma once
+#include <cooperative_groups.h>
+
+#include "stockham.cuh"
+
+namespace cfft {
+
+template <int V>
+struct IntC {
+  static constexpr int value = V;
+};
+
+// Cluster barrier in two halves: arrive (releasing this thread's prior memory
+// operations) and wait (acquiring the other threads').
+__device__ __forceinline__ void cluster_arrive() { asm volatile("barrier.cluster.arrive.release.aligned;\n" ::: "memory"); }
+__device__ __forceinline__ void cluster_wait() { asm volatile("barrier.cluster.wait.acquire.aligned;\n" ::: "memory"); }
+
+// Calls f(IntC<c>{}) for the runtime rank c < 2^LS.
+template <int LS, int C = 0, class F>
+__device__ __forceinline__ void with_rank(int c, F&& f) {
+  if constexpr (C < (1 << LS)) {
+    if (c == C) f(IntC<C>{});
+    else with_rank<LS, C + 1>(c, f);
+  }
+}
+
+// Passes 1 .. npass-1 and the end butterfly of a DIF transform of 2^log2n
+// points, run on one residue class mod 2^LS compacted to 2^(log2n - LS) points.
+template <int R, bool FWD>
+__device__ __forceinline__ FlatBuf dif_after_first(int log2n, int ls, FlatBuf x, FlatBuf y,
+                                                   const double2* __restrict__ wb, int tid, int nth) {
+  constexpr int LR = Log2<R>::v;
+  int lm = log2n, npass = 0;
+  while (lm > LR) {
+    lm -= LR;
+    ++npass;
+  }
+  const int log2c = log2n - ls;
+  FlatBuf cur = x, oth = y;
+  for (int i = 1; i < npass; ++i) {
+    stockham_pass<R, FWD, false, 0>(log2c, i * LR - ls, 1, cur, oth, wb, tid, nth, ls);
+    __syncthreads();
+    const FlatBuf t = cur;
+    cur = oth;
+    oth = t;
+  }
+  end_dispatch<R, FWD, 0>(lm, log2c, 1, cur, tid, nth);
+  __syncthreads();
+  return cur;
+}
+
+// The end butterfly and passes npass-1 .. 1 of a DIT transform, on one
+// residue class mod 2^LS (compacted), i.e. everything but the s = 1 pass.
+template <int R, bool FWD>
+__device__ __forceinline__ FlatBuf dit_before_last(int log2n, int ls, FlatBuf x, FlatBuf y,
+                                                   const double2* __restrict__ wb, int tid, int nth) {
+  constexpr int LR = Log2<R>::v;
+  int lm = log2n, npass = 0;
+  while (lm > LR) {
+    lm -= LR;
+    ++npass;
+  }
+  const int log2c = log2n - ls;
+  FlatBuf cur = x, oth = y;
+  end_dispatch<R, FWD, 0>(lm, log2c, 1, cur, tid, nth);
+  __syncthreads();
+  for (int i = npass - 1; i >= 1; --i) {
+    stockham_pass<R, FWD, true, 0>(log2c, i * LR - ls, 1, cur, oth, wb, tid, nth, ls);
+    __syncthreads();
+    const FlatBuf t = cur;
+    cur = oth;
+    oth = t;
+  }
+  return cur;
+}
+
+// Forward unordered level 0 of radix R0, outputs of part C only (slots
+// [C*R0/S, (C+1)*R0/S)), read from global g, written compacted to x.
+template <int R0, int LS, int C>
+__device__ __forceinline__ void level0_first(const double2* g, int lm, double2* x, const double2* __restrict__ wl,
+                                             int tid, int nth) {
+  constexpr int LR0 = Log2<R0>::v;
+  for (int i = tid; i < (1 << lm); i += nth) {
+    c64 v[R0];
+#pragma unroll
+    for (int k = 0; k < R0; ++k) v[k] = ld(g + (k << lm) + i);
+    Core<R0, true, 0>::run(v);
+    const double2* tw = wl + (R0 - 1) * i - 1;
+#pragma unroll
+    for (int k = 0; k < R0; ++k) {
+      if ((slot<R0>(k) >> (LR0 - LS)) == C) {
+        const c64 o = k == 0 ? v[0] : cmul(ldg(tw + k), v[k]);
+        st(x + ((slot<R0>(k) & ((R0 >> LS) - 1)) << lm) + i, o);
+      }
+    }
+  }
+}
+
+// Inverse unordered level 0 of radix R0 for butterflies [i0, i1): inputs from
+// the cluster's parts (part j holds slots [j*R0/S, (j+1)*R0/S) at `peer[j]`),
+// outputs to global g.
+template <int R0, int LS>
+__device__ __forceinline__ void level0_last(double2* g, int lm, double2* const* peer, int i0, int i1,
+                                            const double2* __restrict__ wl, int tid, int nth) {
+  constexpr int LR0 = Log2<R0>::v;
+  for (int i = i0 + tid; i < i1; i += nth) {
+    c64 v[R0];
+    const double2* tw = wl + (R0 - 1) * i - 1;
+    v[0] = ld(peer[0] + i);
+#pragma unroll
+    for (int k = 1; k < R0; ++k) {
+      const int sl = slot<R0>(k);
+      v[k] = cmul(ldg(tw + k), ld(peer[sl >> (LR0 - LS)] + ((sl & ((R0 >> LS) - 1)) << lm) + i));
+    }
+    Core<R0, false, 0>::run(v);
+#pragma unroll
+    for (int k = 0; k < R0; ++k) st(g + (k << lm) + i, v[k]);
+  }
+}
+
+// MODE 0: the plan has no outer levels (ordered plan, or unordered with
+// n = base_n); the base algorithm's structure decides (DIF: first, DIT: last).
+// MODE 1: unordered with outer levels (forward: first, inverse: last).
+// One transform per S consecutive CTAs; w is the plan's forward table
+// (forward) or inverse table (inverse).
+template <int ALGO, bool FWD, int LS, int MODE>
+__global__ void __launch_bounds__(256) c64_split_kernel(double2* data, DevLevels L, const double2* __restrict__ w) {
+  constexpr int R = AlgoInfo<ALGO>::R;
+  constexpr int LR = Log2<R>::v;
+  constexpr int S = 1 << LS;
+  constexpr bool LAST = MODE == 0 ? AlgoInfo<ALGO>::DIT : !FWD;
+  extern __shared__ double2 smem[];
+  const int log2n = L.log2n[0];
+  const int log2c = log2n - LS;
+  const int c = (int)(blockIdx.x & (S - 1));
+  const long t = blockIdx.x >> LS;
+  double2* g = data + (t << log2n);
+  double2* xs = smem;
+  double2* ys = smem + (1 << log2c);
+  const int tid = threadIdx.x, nth = blockDim.x;
+  const int log2base = L.log2n[L.nlevels];
+  const double2* wb = FWD ? w + L.w_off[L.nlevels] + (1 << log2base) : w + (1 << log2base);
+
+  if constexpr (MODE == 0 && !LAST) {
+    // DIF: pass 0 (s = 1) from global, own residue class only.
+    const int lper = log2n - LR;
+    with_rank<LS>(c, [&](auto C) {
+      for (int p = tid; p < (1 << lper); p += nth) {
+        c64 v[R];
+#pragma unroll
+        for (int k = 0; k < R; ++k) v[k] = ld(g + (k << lper) + p);
+        Core<R, FWD, 0>::run(v);
+        const double2* tw = wb + (p << LR);
+#pragma unroll
+        for (int k = 0; k < R; ++k) {
+          if ((k & (S - 1)) == decltype(C)::value) {
+            const c64 o = k == 0 ? v[0] : cmul(ldg(tw + k), v[k]);
+            st(xs + (((p << LR) + k) >> LS), o);
+          }
+        }
+      }
+    });
+    __syncthreads();
+    cluster_arrive();
+    const FlatBuf r = dif_after_first<R, FWD>(log2n, LS, FlatBuf{xs}, FlatBuf{ys}, wb, tid, nth);
+    cluster_wait();
+    for (int j = tid; j < (1 << log2c); j += nth) g[(j << LS) + c] = r.p[j];
+  } else if constexpr (MODE == 0 && LAST) {
+    // DIT: own residue class through every pass but the last, then the s = 1
+    // pass over the cluster.
+    namespace cg = cooperative_groups;
+    cg::cluster_group cl = cg::this_cluster();
+    for (int j = tid; j < (1 << log2c); j += nth) xs[j] = g[(j << LS) + c];
+    __syncthreads();
+    const FlatBuf r = dit_before_last<R, FWD>(log2n, LS, FlatBuf{xs}, FlatBuf{ys}, wb, tid, nth);
+    double2* peer[S];
+#pragma unroll
+    for (int j = 0; j < S; ++j) peer[j] = cl.map_shared_rank(r.p, (unsigned)j);
+    cl.sync();
+    const int lper = log2n - LR;
+    const int per = (1 << lper) >> LS;
+    for (int p = c * per + tid; p < (c + 1) * per; p += nth) {
+      c64 v[R];
+      const double2* tw = wb + (p << LR);
+      const int lo = p << (LR - LS);
+      v[0] = ld(peer[0] + lo);
+#pragma unroll
+      for (int k = 1; k < R; ++k) v[k] = cmul(ldg(tw + k), ld(peer[k & (S - 1)] + lo + (k >> LS)));
+      Core<R, FWD, 0>::run(v);
+#pragma unroll
+      for (int k = 0; k < R; ++k) st(g + (k << lper) + p, v[k]);
+    }
+    cl.sync();
+  } else if constexpr (MODE == 1 && !LAST) {
+    // forward unordered: level 0 from global, own slots only; then levels
+    // 1.. and the base on the R0/S slices of this part.
+    const int lr0 = L.log2r[0];
+    const int lm = log2n - lr0;
+    const double2* wl = w + L.w_off[0];
+    if (lr0 == 1) {
+      if constexpr (LS <= 1) with_rank<LS>(c, [&](auto C) { level0_first<2, LS, decltype(C)::value>(g, lm, xs, wl, tid, nth); });
+    } else if (lr0 == 2) {
+      if constexpr (LS <= 2) with_rank<LS>(c, [&](auto C) { level0_first<4, LS, decltype(C)::value>(g, lm, xs, wl, tid, nth); });
+    } else {
+      with_rank<LS>(c, [&](auto C) { level0_first<8, LS, decltype(C)::value>(g, lm, xs, wl, tid, nth); });
+    }
+    __syncthreads();
+    cluster_arrive();
+    const FlatBuf r = unordered_t<true, 0, ALGO>(L, 1, 1 << (lr0 - LS), FlatBuf{xs}, FlatBuf{ys}, w, tid, nth);
+    cluster_wait();
+    double2* gp = g + ((long)c << log2c);
+    for (int j = tid; j < (1 << log2c); j += nth) gp[j] = r.p[j];
+  } else {
+    // inverse unordered: this part's slices through the base and levels
+    // nlevels-1 .. 1, then level 0 over the cluster.
+    namespace cg = cooperative_groups;
+    cg::cluster_group cl = cg::this_cluster();
+    const double2* gp = g + ((long)c << log2c);
+    for (int j = tid; j < (1 << log2c); j += nth) xs[j] = gp[j];
+    __syncthreads();
+    const int lr0 = L.log2r[0];
+    const int lm = log2n - lr0;
+    const FlatBuf r = unordered_t<false, 0, ALGO>(L, 1, 1 << (lr0 - LS), FlatBuf{xs}, FlatBuf{ys}, w, tid, nth);
+    double2* peer[S];
+#pragma unroll
+    for (int j = 0; j < S; ++j) peer[j] = cl.map_shared_rank(r.p, (unsigned)j);
+    cl.sync();
+    const double2* wl = w + L.winv_off[0];
+    const int per = (1 << lm) >> LS;
+    if (lr0 == 1) {
+      if constexpr (LS <= 1) level0_last<2, LS>(g, lm, peer, c * per, (c + 1) * per, wl, tid, nth);
+    } else if (lr0 == 2) {
+      if constexpr (LS <= 2) level0_last<4, LS>(g, lm, peer, c * per, (c + 1) * per, wl, tid, nth);
+    } else {
+      level0_last<8, LS>(g, lm, peer, c * per, (c + 1) * per, wl, tid, nth);
+    }
+    cl.sync();
+  }
+}
+
+// Kernel pointer for (ALGO, direction, LS, MODE); nullptr where S = 2^LS
+// exceeds the radix that is split.
+template <int A, int LS>
+const void* split_ptr_ls(bool fwd, int mode) {
+  if (mode == 0) {
+    if constexpr (LS <= Log2<AlgoInfo<A>::R>::v)
+      return fwd ? (const void*)c64_split_kernel<A, true, LS, 0> : (const void*)c64_split_kernel<A, false, LS, 0>;
+    else
+      return nullptr;
+  }
+  return fwd ? (const void*)c64_split_kernel<A, true, LS, 1> : (const void*)c64_split_kernel<A, false, LS, 1>;
+}
+template <int A>
+const void* split_ptr(bool fwd, int ls, int mode) {
+  switch (ls) {
+    case 1: return split_ptr_ls<A, 1>(fwd, mode);
+    case 2: return split_ptr_ls<A, 2>(fwd, mode);
+    case 3: return split_ptr_ls<A, 3>(fwd, mode);
+    default: return nullptr;
+  }
+}
+
+}  // namespace cfft

@@ -120,6 +120,39 @@ def test_unordered_bit_exact(cuda, oracle, n, base):
         assert np.abs(d.cpu().numpy() / n - x).max() < 1e-12
 
 
+@pytest.mark.parametrize("ctas", [1, 2, 4, 8, 0])
+def test_cluster_sizes_bit_exact(cuda, oracle, ctas):
+    """One transform spread over a thread-block cluster (distributed shared memory)
+    gives the same bits as one CTA per transform, for every algorithm and size."""
+    import concrete_fft as cf
+    torch = cuda
+    for algo in range(8):
+        for e in (6, 7, 9, 10):
+            n = 1 << e
+            plan = cf.ordered.Plan(n, cf.ordered.Method.UserProvided(algo))
+            plan.set_cluster_size(ctas)
+            x = rand_c64(3, n)
+            d = on_gpu(torch, x)
+            plan.fwd(d)
+            want = oracle.ordered_fwd(algo, x)
+            assert np.array_equal(bits(d.cpu().numpy()), bits(want)), (algo, n, ctas)
+            plan.inv(d)
+            want = oracle.ordered_inv(algo, want)
+            assert np.array_equal(bits(d.cpu().numpy()), bits(want)), (algo, n, ctas)
+    for n, base in [(256, 32), (1024, 64), (2048, 1024), (4096, 512)]:
+        for algo in (2, 7):
+            plan = cf.unordered.Plan(n, cf.unordered.Method.UserProvided(algo, base))
+            plan.set_cluster_size(ctas)
+            x = rand_c64(2, n)
+            d = on_gpu(torch, x)
+            plan.fwd(d)
+            want = oracle.unordered_fwd(algo, base, x)
+            assert np.array_equal(bits(d.cpu().numpy()), bits(want)), (n, base, algo, ctas)
+            plan.inv(d)
+            want = oracle.unordered_inv(algo, base, want)
+            assert np.array_equal(bits(d.cpu().numpy()), bits(want)), (n, base, algo, ctas)
+
+
 @pytest.mark.parametrize("n", [256, 1024, 4096])
 def test_monomial_and_serde_order(cuda, oracle, n):
     import concrete_fft as cf

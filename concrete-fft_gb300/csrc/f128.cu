@@ -182,6 +182,17 @@ cfft_status build_f128(cfft_f128_plan* p, size_t n) {
   return upload(tw.data(), 4 * n, &p->d_tw);
 }
 
+// One CTA per unit (a product, or a shared-memory block of a transform) up
+// to 2^20: the block scheduler then balances the SMs to within one unit.
+// Beyond that, the resident CTAs stride over the batch.
+static int product_grid(const void* kernel, int threads, size_t smem, long count) {
+  if (count <= (1L << 20)) return (int)std::max<long>(1, count);
+  int per_sm = 1;
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, threads, smem);
+  return (int)((long)sm_count() * std::max(per_sm, 1));
+}
+
+
 int f128_threads(int log2c) { return std::min(256, std::max(64, (1 << log2c) / 8)); }
 
 cfft_status run_f128(const cfft_f128_plan* p, double* re0, double* re1, double* im0, double* im1, size_t batch,
@@ -195,11 +206,8 @@ cfft_status run_f128(const cfft_f128_plan* p, double* re0, double* re1, double* 
   const long nblocks = (long)batch << (log2n - log2c);
   const int threads = f128_threads(log2c);
   const size_t smem = (size_t)4 * (size_t(1) << log2c) * sizeof(double);
-  int per_sm = 1;
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fwd ? (const void*)f128_smem_kernel<true>
-                                                              : (const void*)f128_smem_kernel<false>,
-                                                threads, smem);
-  const int grid = (int)std::max<long>(1, std::min<long>(nblocks, (long)sm_count() * std::max(per_sm, 1)));
+  const int grid = product_grid(fwd ? (const void*)f128_smem_kernel<true> : (const void*)f128_smem_kernel<false>,
+                                threads, smem, nblocks);
   const long total = (long)batch << (log2n - 1);
   const int sgrid = (int)std::min<long>((total + 255) / 256, (long)sm_count() * 16);
   if (fwd) {
@@ -316,9 +324,7 @@ cfft_status cfft_u128_prepare_operand(const cfft_u128_product_plan* p, const int
   const int log2n = ilog2(p->f.n);
   const int threads = f128_threads(log2n);
   const size_t smem = 4 * p->f.n * sizeof(double);
-  int per_sm = 1;
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, u128_prepare_kernel, threads, smem);
-  const int grid = (int)std::max<long>(1, std::min<long>((long)count, (long)sm_count() * std::max(per_sm, 1)));
+  const int grid = product_grid((const void*)u128_prepare_kernel, threads, smem, (long)count);
   u128_prepare_kernel<<<grid, threads, smem, (cudaStream_t)stream>>>(b, bhat4, (long)count, log2n, p->f.tw());
   CFFT_CHECK_LAUNCH();
   return CFFT_OK;
@@ -333,9 +339,7 @@ cfft_status cfft_u128_product(const cfft_u128_product_plan* p, const uint64_t* a
   const int log2n = ilog2(p->f.n);
   const int threads = f128_threads(log2n);
   const size_t smem = 4 * p->f.n * sizeof(double);
-  int per_sm = 1;
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, u128_product_kernel, threads, smem);
-  const int grid = (int)std::max<long>(1, std::min<long>((long)count, (long)sm_count() * std::max(per_sm, 1)));
+  const int grid = product_grid((const void*)u128_product_kernel, threads, smem, (long)count);
   u128_product_kernel<<<grid, threads, smem, (cudaStream_t)stream>>>(
       a, bhat4, (long)bhat_stride, out, (long)count, log2n, p->f.tw(), 2.0 / (double)p->N);
   CFFT_CHECK_LAUNCH();

@@ -214,7 +214,7 @@ def run_gb300(args):
     lib = cf.load()
     cf.check(lib.cfft_device_check())
 
-    count = args.count
+    count = args.count or COUNT
     if args.base_algo is not None:
         plan = cf.product.U64ProductPlan(N_POLY, cf.FftAlgo[args.base_algo], args.base_n)
     else:
@@ -275,14 +275,22 @@ def run_gb300(args):
     e2e_s = replicas.max_over_ranks(time.perf_counter() - t0, "cuda")
     e2e = world * count * e2e_steps / e2e_s
     ok = bool(np.array_equal(hout.numpy(), out.cpu().numpy()))
+    # the copies alone (pinned host <-> device, one direction at a time): the e2e ceiling
+    copy_gbs = {}
+    for name, (dst_t, src_t) in {"h2d": (a, ha), "d2h": (hout, out)}.items():
+        dst_t.copy_(src_t, non_blocking=True)
+        torch.cuda.synchronize()
+        c0 = time.perf_counter()
+        for _ in range(3):
+            dst_t.copy_(src_t, non_blocking=True)
+        torch.cuda.synchronize()
+        copy_gbs[name] = 3 * src_t.numel() * 8 / (time.perf_counter() - c0) / 1e9
 
     peaks, peak_kind = measured_peaks()
     achieved_gbs = BYTES_PER_PRODUCT * count / per_launch_s / 1e9
     traffic = profiled_traffic("u64_product_n2048")
-    import ctypes
-    r = ctypes.c_double()
-    cf.check(lib.cfft_diag_fp64_peak(ctypes.byref(r)))
-    fp64_peak = r.value
+    rates = fp64_rates(cf)
+    fp64_peak = max(rates.values())
     fp64_ops = fp64_ops_per_product(N_POLY, base_n, int(algo))
     fp64_achieved = fp64_ops * count / per_launch_s
 
@@ -309,10 +317,12 @@ def run_gb300(args):
                      "algorithmic_bytes_per_launch": BYTES_PER_PRODUCT * count,
                      "fp64": {"achieved_ops_per_s": fp64_achieved, "peak_ops_per_s": fp64_peak,
                               "frac": fp64_achieved / fp64_peak, "ops_per_product": fp64_ops,
-                              "note": "binding roof: FP64 pipe (DFMA/DADD/DMUL issue rate, measured live)"}},
+                              "microbenchmark_rates": rates,
+                              "note": "binding roof: FP64 pipe (best DFMA/DADD/DMUL/mix issue rate, measured live)"}},
         "cpu_baseline": cpu,
         "e2e": {"value": e2e, "unit": "products/s", "h2d_bytes_per_step": count * N_POLY * 8,
-                "d2h_bytes_per_step": count * N_POLY * 8, "steps": e2e_steps, "matches_device_result": ok},
+                "d2h_bytes_per_step": count * N_POLY * 8, "steps": e2e_steps, "matches_device_result": ok,
+                "copy_only_gbs": copy_gbs},
         "clocks": clk.summary(),
         "gpu_launches": args.steps,
     }
@@ -362,11 +372,17 @@ def timed(torch, fn, steps, warmup, local, world):
     return replicas.max_over_ranks(e0.elapsed_time(e1), "cuda"), clk.summary()
 
 
-def fp64_peak(cf):
+def fp64_rates(cf):
+    """FP64 thread-instruction rates of the DFMA, DADD, DMUL and mixed microbenchmarks."""
     import ctypes
-    r = ctypes.c_double()
-    cf.check(cf.load().cfft_diag_fp64_peak(ctypes.byref(r)))
-    return r.value
+    r = (ctypes.c_double * 4)()
+    cf.check(cf.load().cfft_diag_fp64_rates(r))
+    return dict(zip(("dfma", "dadd", "dmul", "mix_2add_1fma_1mul"), list(r)))
+
+
+def fp64_peak(cf):
+    """The FP64 roof: the best of the microbenchmark rates."""
+    return max(fp64_rates(cf).values())
 
 
 def run_mixed(args):
@@ -409,17 +425,15 @@ def run_mixed(args):
     peak = fp64_peak(cf)
     bytes_alg = total * 32
     peaks, kindp = measured_peaks()
-    # end to end: host data in, host data out through the same launch
+    # end to end: pinned host data in and out, chunks of items pipelined (cfft_batch_run_host)
     host = data.cpu().pin_memory()
-    back = torch.empty_like(host).pin_memory()
-    torch.cuda.synchronize()
-    t1 = time.perf_counter()
-    e2e_steps = 2
     with torch.cuda.stream(stream):
+        b.run_host(host, data)  # builds the chunk tables
+        torch.cuda.current_stream().synchronize()
+        t1 = time.perf_counter()
+        e2e_steps = 3
         for _ in range(e2e_steps):
-            data.copy_(host, non_blocking=True)
-            b.run(data)
-            back.copy_(data, non_blocking=True)
+            b.run_host(host, data)
         torch.cuda.current_stream().synchronize()
     e2e_s = time.perf_counter() - t1
     if rank != 0:
@@ -599,6 +613,42 @@ def run_serving(args):
     }))
 
 
+def run_serde(args):
+    """Permuted <-> standard order conversion (serialize/deserialize_fourier_buffer's element
+    order) of 65536 unordered transforms of n = 1024 (base 32): 1 GiB in, 1 GiB out per call.
+    HBM-bound: 32 bytes moved per point."""
+    torch, cf, rank, world, local = gpu_setup()
+    n, base = 1024, 32
+    batch = args.count or 65536
+    plan = cf.unordered.Plan(n, cf.unordered.Method.UserProvided(2, base))
+    src = torch.randn(batch, n, dtype=torch.complex128, device="cuda")
+    dst = torch.empty_like(src)
+    ms_to, clocks = timed(torch, lambda: plan.to_standard(src, dst), args.steps, args.warmup, local, world)
+    ms_from, _ = timed(torch, lambda: plan.from_standard(dst, src), args.steps, args.warmup, local, world)
+    nbytes = 2 * batch * n * 16
+    gbs_to = nbytes * args.steps / (ms_to * 1e-3) / 1e9
+    gbs_from = nbytes * args.steps / (ms_from * 1e-3) / 1e9
+    peaks, peak_kind = measured_peaks()
+    prof = profiled_traffic("permute_tile_n1024")
+    traffic = prof["dram_bytes_per_point"] * batch * n if prof else None
+    if rank != 0:
+        return
+    print(json.dumps({
+        "metric": "unordered permuted->standard order conversion, n=1024 (GB/s moved)", "value": world * gbs_to,
+        "unit": "GB/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": ms_to / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "c64 copy", "data": "synthetic (torch.randn)",
+        "config": {"workload": "to_standard / from_standard, %d x 1024 points, base 32, %.2f GiB per call"
+                               % (batch, nbytes / 2 ** 30),
+                   "from_standard_gbs": world * gbs_from, "l2": "inputs larger than L2"},
+        "roofline": {"bound": "hbm", "achieved": gbs_to, "peak": peaks["hbm_gbs"], "unit": "GB/s",
+                     "frac": gbs_to / peaks["hbm_gbs"], "traffic": traffic, "peak_kind": peak_kind,
+                     "algorithmic_bytes_per_launch": nbytes,
+                     "from_standard_frac": gbs_from / peaks["hbm_gbs"]},
+        "clocks": clocks, "gpu_launches": 2 * args.steps,
+    }))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -607,7 +657,8 @@ def main():
     ap.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
     ap.add_argument("--cpu-seconds", type=float, default=5.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--count", type=int, default=COUNT, help="products per launch")
+    ap.add_argument("--count", type=int, default=None,
+                    help="products per launch (u64_product, default %d) or transforms per call (serde, default 65536)" % COUNT)
     ap.add_argument("--base-algo", default=None, help="fix the base algorithm (e.g. Dif4) instead of measuring")
     ap.add_argument("--base-n", type=int, default=1024)
     ap.add_argument("--int-adds", type=int, default=None,
@@ -617,7 +668,7 @@ def main():
     ap.add_argument("--rate", type=float, default=20000.0)
     ap.add_argument("--serve-seconds", type=float, default=1.0)
     ap.add_argument("--operand-gb", type=int, default=8)
-    ap.add_argument("--workload", choices=["u64_product", "mixed", "ordered", "u128_product", "serving", "product_sum"],
+    ap.add_argument("--workload", choices=["u64_product", "mixed", "ordered", "u128_product", "serving", "product_sum", "serde"],
                     default="u64_product",
                     help="u64_product (default headline) or one of the other benchmark configurations")
     ap.add_argument("--mixed-items", type=int, default=100000)
@@ -633,6 +684,8 @@ def main():
         run_ordered(args)
     elif args.workload == "u128_product":
         run_u128(args)
+    elif args.workload == "serde":
+        run_serde(args)
     elif args.workload == "serving":
         run_serving(args)
     elif args.workload == "product_sum":

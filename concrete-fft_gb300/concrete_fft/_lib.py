@@ -36,6 +36,7 @@ _SIGS = [
     ("cfft_version", ctypes.c_char_p, []),
     ("cfft_device_check", c_int, []),
     ("cfft_diag_fp64_peak", c_int, [ctypes.POINTER(c_dbl)]),
+    ("cfft_diag_fp64_rates", c_int, [ctypes.POINTER(c_dbl)]),
     ("cfft_tune_save", c_int, [ctypes.c_char_p]),
     ("cfft_tune_load", c_int, [ctypes.c_char_p]),
     ("cfft_tune_clear", None, []),
@@ -103,6 +104,7 @@ _SIGS = [
     ("cfft_batch_schedule", c_int, [vp, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_uint32, ctypes.POINTER(c_int),
                                     ctypes.POINTER(c_size), ctypes.POINTER(ctypes.c_uint32)]),
     ("cfft_batch_run", c_int, [vp, vp, vp]),
+    ("cfft_batch_run_host", c_int, [vp, vp, vp, vp]),
     ("cfft_product_engine_create", c_int, [vp, c_size, pp]),
     ("cfft_product_engine_destroy", None, [vp]),
     ("cfft_product_engine_workspace_bytes", c_size, [vp]),

@@ -49,3 +49,18 @@ class Batch:
         s = B.stream_of(data) if stream is None else ctypes.c_void_p(stream)
         check(self._lib.cfft_batch_run(self._h, B.ptr(data), s))
         return data
+
+    def run_host(self, host, dev, stream=None):
+        """The batch from host memory and back through the device buffer `dev` (same
+        layout), copies and transforms pipelined over chunks of items.  `host` is a
+        C-contiguous complex128/float64 array or CPU tensor, best pinned; it is
+        updated in place (only the items' point ranges)."""
+        if not B.is_device(dev):
+            raise TypeError("dev must be a CUDA tensor")
+        if B.is_device(host):
+            raise TypeError("host must be host memory")
+        if B.points(host, 16) != B.points(dev, 16):
+            raise ValueError("host and device buffers differ in size")
+        s = B.stream_of(dev) if stream is None else ctypes.c_void_p(stream)
+        check(self._lib.cfft_batch_run_host(self._h, B.ptr(host), B.ptr(dev), s))
+        return host

@@ -209,6 +209,19 @@ struct cfft_batch {
   cudaStream_t g_stream = nullptr;
   double* g_data = nullptr;
   cudaGraphExec_t g_exec = nullptr;
+  // pipelined host runs: the items split into data-contiguous chunks, each
+  // with its own units and work counter (built on first use)
+  struct Chunk {
+    uint64_t lo = 0, hi = 0;  // point range [lo, hi) covered by the chunk's items
+    uint64_t* d_offs = nullptr;
+    Unit* d_units = nullptr;
+    int nunits = 0;
+  };
+  std::vector<cfft_batch_item> items;
+  std::vector<Chunk> chunks;
+  unsigned int* d_heads = nullptr;
+  cudaStream_t pstream[3] = {};
+  cudaEvent_t pevent[4] = {};
 };
 
 namespace {
@@ -336,10 +349,73 @@ cfft_status tune_class(cfft_batch* b, size_t ci, double seconds) {
 void destroy_batch(cfft_batch* b) {
   if (!b) return;
   if (b->g_exec) cudaGraphExecDestroy(b->g_exec);
+  for (auto& c : b->chunks) {
+    if (c.d_offs) cudaFree(c.d_offs);
+    if (c.d_units) cudaFree(c.d_units);
+  }
+  if (b->d_heads) cudaFree(b->d_heads);
+  for (cudaStream_t st : b->pstream)
+    if (st) cudaStreamDestroy(st);
+  for (cudaEvent_t ev : b->pevent)
+    if (ev) cudaEventDestroy(ev);
   for (auto& c : b->classes) free_tables(c);
   free_batch_device(b);
   if (b->d_head) cudaFree(b->d_head);
   delete b;
+}
+
+// Splits the items, in offset order, into about kChunks groups of equal
+// points; each group gets the units of its items (same classes and
+// schedules as the whole batch, longest first) and its own work counter.
+constexpr int kChunks = 16;
+cfft_status build_chunks(cfft_batch* b) {
+  std::map<ClassKey, int> cls;
+  for (size_t ci = 0; ci < b->classes.size(); ++ci) cls[b->classes[ci].key] = (int)ci;
+  std::vector<size_t> order(b->items.size());
+  for (size_t i = 0; i < order.size(); ++i) order[i] = i;
+  std::stable_sort(order.begin(), order.end(),
+                   [&](size_t x, size_t y) { return b->items[x].offset < b->items[y].offset; });
+  const size_t target = std::max<size_t>(1, b->total_points / kChunks);
+  size_t i = 0;
+  while (i < order.size()) {
+    size_t j = i, pts = 0;
+    while (j < order.size() && (pts < target || j == i)) pts += size_t(1) << b->items[order[j++]].log2n;
+    cfft_batch::Chunk ch;
+    ch.lo = b->items[order[i]].offset;
+    ch.hi = b->items[order[j - 1]].offset + (uint64_t(1) << b->items[order[j - 1]].log2n);
+    // per class, this chunk's items in offset order
+    std::vector<std::vector<uint64_t>> per(b->classes.size());
+    for (size_t k = i; k < j; ++k) {
+      const cfft_batch_item& it = b->items[order[k]];
+      per[cls[ClassKey{(int)it.kind, (int)it.log2n, (int)it.direction}]].push_back(it.offset);
+    }
+    std::vector<uint64_t> offs;
+    std::vector<std::pair<double, Unit>> u;
+    for (size_t ci = 0; ci < per.size(); ++ci) {
+      if (per[ci].empty()) continue;
+      const ClassHost& c = b->classes[ci];
+      const int first = (int)offs.size();
+      offs.insert(offs.end(), per[ci].begin(), per[ci].end());
+      const int tpc = device_class(c).d0 == 0 ? c.tpc : 1;
+      for (size_t k = 0; k < per[ci].size(); k += (size_t)tpc) {
+        Unit un{(int)ci, first + (int)k, (int)std::min<size_t>(tpc, per[ci].size() - k), c.key.dir};
+        u.push_back({unit_cost(c.key.log2n, un.count, un.dir), un});
+      }
+    }
+    std::stable_sort(u.begin(), u.end(), [](const auto& x, const auto& y) { return x.first > y.first; });
+    std::vector<Unit> units;
+    for (auto& pu : u) units.push_back(pu.second);
+    ch.nunits = (int)units.size();
+    b->chunks.push_back(ch);
+    cfft_status st = upload(offs.data(), offs.size(), &b->chunks.back().d_offs);
+    if (st == CFFT_OK) st = upload(units.data(), units.size(), &b->chunks.back().d_units);
+    if (st != CFFT_OK) return st;
+    i = j;
+  }
+  CFFT_CUDA_TRY(cudaMalloc(&b->d_heads, b->chunks.size() * sizeof(unsigned int)));
+  for (cudaStream_t& st : b->pstream) CFFT_CUDA_TRY(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
+  for (cudaEvent_t& ev : b->pevent) CFFT_CUDA_TRY(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
+  return CFFT_OK;
 }
 
 }  // namespace
@@ -365,6 +441,7 @@ cfft_status cfft_batch_create(const cfft_batch_item* items, size_t count, double
   if (st != CFFT_OK) return st;
   auto* b = new cfft_batch();
   b->total_points = total;
+  b->items.assign(items, items + count);
   int per_sm = 0;
   cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, batch_kernel, kBatchThreads,
                                                 2 * (1 << kBatchSmemLog2) * sizeof(double2));
@@ -435,6 +512,38 @@ cfft_status cfft_batch_run(cfft_batch* b, double* data, void* stream) {
     b->g_data = data;
   }
   CFFT_CUDA_TRY(cudaGraphLaunch(b->g_exec, s));
+  return CFFT_OK;
+}
+
+cfft_status cfft_batch_run_host(cfft_batch* b, double* host, double* dev, void* stream) {
+  if (!b || !host || !dev) return fail(CFFT_ERR_INVALID_ARGUMENT, "null argument");
+  if (b->units.empty()) return CFFT_OK;
+  std::lock_guard<std::mutex> lk(b->mu);
+  if (b->chunks.empty()) {
+    cfft_status st = build_chunks(b);
+    if (st != CFFT_OK) return st;
+  }
+  cudaStream_t s = (cudaStream_t)stream;
+  CFFT_CUDA_TRY(cudaEventRecord(b->pevent[3], s));
+  for (cudaStream_t ps : b->pstream) CFFT_CUDA_TRY(cudaStreamWaitEvent(ps, b->pevent[3], 0));
+  const size_t smem = 2 * (1 << kBatchSmemLog2) * sizeof(double2);
+  for (size_t k = 0; k < b->chunks.size(); ++k) {
+    const cfft_batch::Chunk& c = b->chunks[k];
+    cudaStream_t ps = b->pstream[k % 3];
+    const size_t bytes = (size_t)(c.hi - c.lo) * sizeof(double2);
+    double* hp = host + 2 * c.lo;
+    double* dp = dev + 2 * c.lo;
+    CFFT_CUDA_TRY(cudaMemcpyAsync(dp, hp, bytes, cudaMemcpyHostToDevice, ps));
+    CFFT_CUDA_TRY(cudaMemsetAsync(b->d_heads + k, 0, sizeof(unsigned int), ps));
+    batch_kernel<<<b->grid, kBatchThreads, smem, ps>>>((double2*)dev, b->d_classes, c.d_offs, c.d_units, c.nunits,
+                                                        b->d_heads + k);
+    CFFT_CHECK_LAUNCH();
+    CFFT_CUDA_TRY(cudaMemcpyAsync(hp, dp, bytes, cudaMemcpyDeviceToHost, ps));
+  }
+  for (int i = 0; i < 3; ++i) {
+    CFFT_CUDA_TRY(cudaEventRecord(b->pevent[i], b->pstream[i]));
+    CFFT_CUDA_TRY(cudaStreamWaitEvent(s, b->pevent[i], 0));
+  }
   return CFFT_OK;
 }
 

@@ -62,6 +62,47 @@ __global__ void c64_permute_kernel(const double2* __restrict__ src, double2* __r
   }
 }
 
+// The same conversion through shared memory, for n <= 4096: a CTA reads a
+// tile of whole transforms with coalesced loads, then writes the tile's
+// destination in order, gathering from shared memory.  Shared-memory slot of
+// element e: e with its low 3 bits XORed with its higher 3-bit groups, so the
+// 8 lanes of a 128-bit access phase hit distinct bank groups both for the
+// linear writes and for the permuted reads (whose varying bits are 3
+// adjacent bit positions of e).  TO_STD gathers with bit_rev_twice (standard
+// from permuted), otherwise with its inverse (permuted from standard).
+__device__ __forceinline__ int perm_slot(int e) { return e ^ (((e >> 3) ^ (e >> 6) ^ (e >> 9)) & 7); }
+
+template <bool TO_STD>
+__global__ void __launch_bounds__(256) c64_permute_tile_kernel(const double2* __restrict__ src,
+                                                               double2* __restrict__ dst, int nbits, int base_nbits,
+                                                               int log2tile) {
+  extern __shared__ double2 tile[];
+  const int npts = 1 << log2tile;
+  const long off = (long)blockIdx.x << log2tile;
+  // eight loads in flight per thread before any shared-memory store
+  constexpr int kU = 8;
+  for (int b = 0; b < npts; b += kU * 256) {
+    double2 v[kU];
+#pragma unroll
+    for (int u = 0; u < kU; ++u) {
+      const int i = b + u * 256 + (int)threadIdx.x;
+      if (i < npts) v[u] = __ldcs(src + off + i);
+    }
+#pragma unroll
+    for (int u = 0; u < kU; ++u) {
+      const int i = b + u * 256 + (int)threadIdx.x;
+      if (i < npts) tile[perm_slot(i)] = v[u];
+    }
+  }
+  __syncthreads();
+  const int mask = (1 << nbits) - 1;
+  for (int k = threadIdx.x; k < npts; k += blockDim.x) {
+    const unsigned kk = (unsigned)(k & mask);
+    const unsigned e = TO_STD ? bit_rev_twice_dev(nbits, base_nbits, kk) : bit_rev_twice_inv_dev(nbits, base_nbits, kk);
+    __stcs(dst + off + k, tile[perm_slot((k & ~mask) | (int)e)]);
+  }
+}
+
 // src/unordered.rs:844-900
 __global__ void c64_monomial_kernel(double2* __restrict__ buf, const double2* __restrict__ tw, int nbits,
                                     int base_nbits, unsigned long long degree) {
@@ -615,6 +656,19 @@ static cfft_status permute(const cfft_unordered_plan* plan, const double* src, d
   if (batch == 0) return CFFT_OK;
   const long total = (long)(batch * plan->p.n);
   const int nbits = ilog2(plan->p.n), bb = ilog2(plan->p.base_n);
+  if (nbits >= 6 && nbits <= 12) {
+    // tiles of 2048 points (whole transforms; 4096 for n = 4096), one CTA each
+    const int log2tile = std::max(nbits, std::min(11, nbits + ilog2(batch & (~batch + 1))));
+    const long tiles = total >> log2tile;
+    if (tiles > 0x7fffffffL) return fail(CFFT_ERR_INVALID_SIZE, "batch too large");
+    const size_t smem = sizeof(double2) << log2tile;
+    const void* fn = to_std ? (const void*)c64_permute_tile_kernel<true> : (const void*)c64_permute_tile_kernel<false>;
+    const double2* s2 = (const double2*)src;
+    double2* d2 = (double2*)dst;
+    int nb = nbits, bbits = bb, lt = log2tile;
+    void* args[] = {(void*)&s2, (void*)&d2, &nb, &bbits, &lt};
+    return launch_kernel(fn, (int)tiles, 256, args, smem, stream);
+  }
   const int grid = (int)std::min<long>((total + 255) / 256, (long)sm_count() * 16);
   if (to_std)
     c64_permute_kernel<true><<<grid, 256, 0, stream>>>((const double2*)src, (double2*)dst, total, nbits, bb);

@@ -182,14 +182,13 @@ cfft_status build_f128(cfft_f128_plan* p, size_t n) {
   return upload(tw.data(), 4 * n, &p->d_tw);
 }
 
-// One CTA per unit (a product, or a shared-memory block of a transform) up
-// to 2^20: the block scheduler then balances the SMs to within one unit.
-// Beyond that, the resident CTAs stride over the batch.
+// The resident CTAs (13 per SM for N = 1024) stride over the batch.  For
+// these small CTAs this measured 5% faster than one CTA per product (0.94 M
+// vs 0.89 M products/s at N = 1024, 2048 per launch).
 static int product_grid(const void* kernel, int threads, size_t smem, long count) {
-  if (count <= (1L << 20)) return (int)std::max<long>(1, count);
   int per_sm = 1;
   cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, threads, smem);
-  return (int)((long)sm_count() * std::max(per_sm, 1));
+  return (int)std::max<long>(1, std::min<long>(count, (long)sm_count() * std::max(per_sm, 1)));
 }
 
 

@@ -196,33 +196,45 @@ cfft_status cfft_device_check(void) {
 
 namespace {
 constexpr int kPeakIters = 2048;
+// OP 0: DFMA chains, 1: DADD, 2: DMUL, 3: the product kernel's mix.  Eight
+// independent chains per thread, 64 warps per SM; every chain stays near 1.
+template <int OP>
 __global__ void fp64_peak_kernel(double* out, double seed) {
   double a[8];
 #pragma unroll
-  for (int i = 0; i < 8; ++i) a[i] = seed + threadIdx.x + i;
+  for (int i = 0; i < 8; ++i) a[i] = seed + 1e-3 * (threadIdx.x & 7) + 1e-4 * i;
   for (int it = 0; it < kPeakIters; ++it) {
 #pragma unroll
-    for (int i = 0; i < 8; ++i) a[i] = __fma_rn(a[i], 0.999999, 1e-9);
+    for (int i = 0; i < 8; ++i) {
+      if (OP == 0) a[i] = __fma_rn(a[i], 0.999999, 1e-6);
+      if (OP == 1) a[i] = __dadd_rn(a[i], (it & 1) ? 1e-9 : -1e-9);
+      if (OP == 2) a[i] = __dmul_rn(a[i], (it & 1) ? 1.000001 : 0.999999);
+      if (OP == 3) {  // 2 DADD : 1 DFMA : 1 DMUL, the product kernel's 40960 : 18432 : 18432
+        if (i < 4) a[i] = __dadd_rn(a[i], (it & 1) ? 1e-9 : -1e-9);
+        else if (i < 6) a[i] = __fma_rn(a[i], 0.999999, 1e-6);
+        else a[i] = __dmul_rn(a[i], (it & 1) ? 1.000001 : 0.999999);
+      }
+    }
   }
   double s = 0;
 #pragma unroll
   for (int i = 0; i < 8; ++i) s += a[i];
   out[(size_t)blockIdx.x * blockDim.x + threadIdx.x] = s;
 }
-}  // namespace
 
-extern "C" cfft_status cfft_diag_fp64_peak(double* ops_per_second) {
-  if (!ops_per_second) return cfft::fail(CFFT_ERR_INVALID_ARGUMENT, "null output pointer");
-  const int blocks = cfft::sm_count() * 4, threads = 256;
+cfft_status time_fp64(const void* fn, double* ops_per_second) {
+  const int blocks = cfft::sm_count() * 8, threads = 256;  // 64 warps per SM
   double* d = nullptr;
   CFFT_CUDA_TRY(cudaMalloc(&d, (size_t)blocks * threads * sizeof(double)));
   cudaEvent_t e0, e1;
   CFFT_CUDA_TRY(cudaEventCreate(&e0));
   CFFT_CUDA_TRY(cudaEventCreate(&e1));
-  fp64_peak_kernel<<<blocks, threads>>>(d, 1.0);
+  double seed = 1.0;
+  void* args[] = {&d, &seed};
+  CFFT_CUDA_TRY(cudaLaunchKernel(fn, dim3(blocks), dim3(threads), args, 0, 0));
   CFFT_CUDA_TRY(cudaEventRecord(e0));
   const int reps = 5;
-  for (int r = 0; r < reps; ++r) fp64_peak_kernel<<<blocks, threads>>>(d, 1.0);
+  for (int r = 0; r < reps; ++r) CFFT_CUDA_TRY(cudaLaunchKernel(fn, dim3(blocks), dim3(threads), args, 0, 0));
   CFFT_CUDA_TRY(cudaEventRecord(e1));
   CFFT_CUDA_TRY(cudaEventSynchronize(e1));
   float ms = 0;
@@ -232,6 +244,27 @@ extern "C" cfft_status cfft_diag_fp64_peak(double* ops_per_second) {
   cudaFree(d);
   CFFT_CHECK_LAUNCH();
   *ops_per_second = (double)reps * blocks * threads * kPeakIters * 8 / (ms * 1e-3);
+  return CFFT_OK;
+}
+}  // namespace
+
+extern "C" cfft_status cfft_diag_fp64_rates(double* rates4) {
+  if (!rates4) return cfft::fail(CFFT_ERR_INVALID_ARGUMENT, "null output pointer");
+  const void* fns[4] = {(const void*)fp64_peak_kernel<0>, (const void*)fp64_peak_kernel<1>,
+                        (const void*)fp64_peak_kernel<2>, (const void*)fp64_peak_kernel<3>};
+  for (int k = 0; k < 4; ++k) {
+    cfft_status st = time_fp64(fns[k], rates4 + k);
+    if (st != CFFT_OK) return st;
+  }
+  return CFFT_OK;
+}
+
+extern "C" cfft_status cfft_diag_fp64_peak(double* ops_per_second) {
+  if (!ops_per_second) return cfft::fail(CFFT_ERR_INVALID_ARGUMENT, "null output pointer");
+  double r[4];
+  cfft_status st = cfft_diag_fp64_rates(r);
+  if (st != CFFT_OK) return st;
+  *ops_per_second = std::max(std::max(r[0], r[1]), std::max(r[2], r[3]));
   return CFFT_OK;
 }
 

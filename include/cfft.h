@@ -354,6 +354,16 @@ cfft_status cfft_batch_schedule(const cfft_batch* batch, uint32_t kind, uint32_t
  * stream the launch is captured into a CUDA graph on first use (per stream and
  * buffer) and replayed afterwards.  Runs of one batch must not overlap. */
 cfft_status cfft_batch_run(cfft_batch* batch, double* data, void* stream);
+/* The batch from host memory and back (no counterpart in the reference): the
+ * items, in offset order, are split into about 16 chunks of equal size; each
+ * chunk's points are copied host -> device into `dev` (same layout as `host`),
+ * transformed by a persistent launch over the chunk's items, and copied back,
+ * the chunks pipelined over three internal streams so that copies overlap
+ * transforms.  Ordered after prior work on `stream`; later work on `stream`
+ * waits for it.  Only the point ranges of items are copied.  `host` should be
+ * pinned (page-locked) memory for the copies to overlap.  Runs of one batch
+ * must not overlap on the GPU. */
+cfft_status cfft_batch_run_host(cfft_batch* batch, double* host, double* dev, void* stream);
 
 #ifdef __cplusplus
 }

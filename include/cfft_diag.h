@@ -9,10 +9,14 @@
 extern "C" {
 #endif
 
-/* Measures the device's FP64 issue rate: independent DFMA chains on every SM,
- * timed with CUDA events.  Writes FP64 instructions per second (one DFMA, DADD
- * or DMUL each) to *ops_per_second.  The FFT kernels of this library are bound
- * by this rate on GB300, where FP64 runs at 1/64 of the FP32 rate. */
+/* Measures the device's FP64 issue rate: eight independent chains per thread
+ * on every SM, timed with CUDA events, for DFMA, DADD, DMUL and the product
+ * kernel's mix (2 DADD : 1 DFMA : 1 DMUL).  rates4 receives FP64 thread
+ * instructions per second for each, in that order.  The FFT kernels of this
+ * library are bound by this rate on GB300, where FP64 runs at 1/64 of the
+ * FP32 rate. */
+cfft_status cfft_diag_fp64_rates(double* rates4);
+/* The largest of the four rates of cfft_diag_fp64_rates. */
 cfft_status cfft_diag_fp64_peak(double* ops_per_second);
 
 /* Self-check of the integer-pipe double addition used by the FFT kernels:

@@ -77,6 +77,31 @@ def test_graph_replay_and_default_stream(cuda, oracle):
     assert np.array_equal(bits(d.cpu().numpy()), bits(want))
 
 
+def test_host_pipelined_run_bit_exact(cuda, oracle):
+    """cfft_batch_run_host: items with gaps between them, in shuffled order, split into
+    chunks and pipelined; every item equals the oracle, gaps stay untouched on the host."""
+    import concrete_fft as cf
+    torch = cuda
+    rng = np.random.default_rng(5)
+    items, off = [], 0
+    for _ in range(90):
+        kind = int(rng.integers(0, 2))
+        log2n = int(rng.integers(4, (10 if kind == 0 else 14) + 1))
+        items.append((off, log2n, kind, int(rng.integers(1, 4))))
+        off += (1 << log2n) + int(rng.integers(0, 3)) * 8  # gaps of 0, 8 or 16 points
+    items = [items[i] for i in rng.permutation(len(items))]
+    data = rng.uniform(-1, 1, off) + 1j * rng.uniform(-1, 1, off)
+    b = cf.batch.Batch(items)
+    host = torch.from_numpy(data.copy()).pin_memory()
+    dev = torch.zeros(off, dtype=torch.complex128, device="cuda")
+    for _ in range(2):  # second call reuses the chunk tables
+        host.copy_(torch.from_numpy(data))
+        b.run_host(host, dev)
+        torch.cuda.synchronize()
+        got = host.numpy()
+        assert np.array_equal(bits(got), bits(expected(oracle, b, items, data)))
+
+
 def test_batch_rejects_bad_items(cuda):
     import concrete_fft as cf
     with pytest.raises(cf.CfftError):

@@ -173,6 +173,24 @@ def test_monomial_and_serde_order(cuda, oracle, n):
         assert np.array_equal(bits(back.cpu().numpy()), bits(x))
 
 
+@pytest.mark.parametrize("batch", [1, 3, 8, 24])
+def test_serde_tiles_and_batches(cuda, oracle, batch):
+    """Standard-order conversion at every size class (shared-memory tiles of one or
+    several transforms for n = 64..4096, global gather otherwise) and ragged batches."""
+    import concrete_fft as cf
+    torch = cuda
+    for n, base in [(32, 32), (64, 32), (128, 64), (1024, 32), (1024, 512), (2048, 1024), (4096, 64), (8192, 1024)]:
+        plan = cf.unordered.Plan(n, cf.unordered.Method.UserProvided(2, base))
+        x = rand_c64(batch, n)
+        d = on_gpu(torch, x)
+        std = torch.empty_like(d)
+        plan.to_standard(d, std)
+        assert np.array_equal(bits(std.cpu().numpy()), bits(oracle.to_standard(n, base, x))), (n, base, batch)
+        back = torch.empty_like(d)
+        plan.from_standard(std, back)
+        assert np.array_equal(bits(back.cpu().numpy()), bits(x)), (n, base, batch)
+
+
 def test_serde_roundtrip_across_bases(cuda, oracle):
     """src/unordered.rs:9399-9466 on the GPU: base-32 forward, standard order, base-64 inverse."""
     import concrete_fft as cf

@@ -21,3 +21,15 @@ def test_dadd_int_rate_is_reported(cuda, cfft_lib):
     r = ctypes.c_double()
     cf.check(cfft_lib.cfft_diag_dadd_int_rate(ctypes.byref(r)))
     assert r.value > 1e10
+
+
+def test_fp64_rates(cfft_lib):
+    """The FP64 roof microbenchmarks: four positive rates, the peak is their best."""
+    import concrete_fft as cf
+    r = (ctypes.c_double * 4)()
+    cf.check(cfft_lib.cfft_diag_fp64_rates(r))
+    rates = list(r)
+    assert all(x > 1e10 for x in rates), rates
+    p = ctypes.c_double()
+    cf.check(cfft_lib.cfft_diag_fp64_peak(ctypes.byref(p)))
+    assert p.value > 0.9 * max(rates)

@@ -89,6 +89,23 @@ def test_u64_product_shared_operand_and_host(cuda, oracle):
     assert np.array_equal(out, want)
 
 
+def test_u64_product_host_pipeline_chunks(cuda, oracle):
+    """Host entry point over many chunks: more chunks than copy/compute streams, a
+    ragged last chunk, one distinct operand per product."""
+    import concrete_fft as cf
+    torch = cuda
+    N, count = 2048, 2000
+    plan = cf.product.U64ProductPlan(N, 2, 1024)
+    a = RNG.integers(0, 2 ** 64, (count, N), dtype=np.uint64)
+    b = RNG.integers(-2 ** 7, 2 ** 7, (count, N))
+    bhat = torch.empty((count, N // 2), dtype=torch.complex128, device="cuda")
+    plan.prepare_operand(torch.from_numpy(b).cuda(), bhat)
+    out = np.zeros_like(a)
+    plan.product(a, bhat, out)  # host entry point
+    want = oracle.u64_product(N, 2, 1024, a, bhat.cpu().numpy(), nthreads=0)
+    assert np.array_equal(out, want)
+
+
 def test_u64_measure_plan(cuda, oracle):
     import concrete_fft as cf
     plan = cf.product.U64ProductPlan(2048, measure_seconds=0.001)

@@ -460,10 +460,19 @@ def run_ordered(args):
     """ordered::Plan n = 1024, fwd then inv, batch 256 (throughput) and batch 1 (latency)."""
     import numpy as np
     torch, cf, rank, world, local = gpu_setup()
-    plan = cf.ordered.Plan(1024, cf.ordered.Method.Measure(0.002))
     rng = np.random.default_rng(1)
     x = rng.uniform(-1, 1, (256, 1024)) + 1j * rng.uniform(-1, 1, (256, 1024))
     d = torch.from_numpy(x).cuda()
+    if args.profile_case:  # for ncu: 4 forward calls of batch 256 split over 4 CTAs per transform
+        algo = cf.FftAlgo[args.base_algo] if args.base_algo else cf.FftAlgo.Dit4
+        plan = cf.ordered.Plan(1024, cf.ordered.Method.UserProvided(algo))
+        plan.set_cluster_size(4)
+        for _ in range(4):
+            plan.fwd(d)
+        torch.cuda.synchronize()
+        print(json.dumps({"profile_case": "ordered n=1024 batch 256, 4 CTAs per transform", "algo": algo.name}))
+        return
+    plan = cf.ordered.Plan(1024, cf.ordered.Method.Measure(0.002))
     one = d[:1].clone()
 
     def step256():
@@ -476,21 +485,24 @@ def run_ordered(args):
 
     ms256, clocks = timed(torch, step256, args.steps, args.warmup, local, world)
     ms1, _ = timed(torch, step1, args.steps, args.warmup, local, world)
-    # CTAs per transform (1 = one CTA, 2/4/8 = thread-block cluster) at a few batch sizes, fwd then inv
+    # CTAs per transform (1 = one CTA, 2/4/8 = split over a cluster) at a few batch sizes, fwd then inv,
+    # for a DIT algorithm (one exchange through distributed shared memory) and a DIF one (none)
     sweep = {}
-    for batch in (1, 16, 64, 256):
-        sub = d[:batch].clone()
+    for aname in ("Dit4", "Dif4"):
+        sp = cf.ordered.Plan(1024, cf.ordered.Method.UserProvided(cf.FftAlgo[aname]))
+        sweep[aname] = {}
+        for batch in (1, 16, 64, 256):
+            sub = d[:batch].clone()
 
-        def step_b():
-            plan.fwd(sub)
-            plan.inv(sub)
-        row = {}
-        for ctas in (1, 2, 4, 8):
-            plan.set_cluster_size(ctas)
-            ms_b, _ = timed(torch, step_b, max(10, args.steps // 4), args.warmup, local, world)
-            row[ctas] = round(ms_b * 1e3 / max(10, args.steps // 4), 2)
-        sweep[batch] = row
-    plan.set_cluster_size(0)
+            def step_b():
+                sp.fwd(sub)
+                sp.inv(sub)
+            row = {}
+            for ctas in (1, 2, 4, 8):
+                sp.set_cluster_size(ctas)
+                ms_b, _ = timed(torch, step_b, max(10, args.steps // 4), args.warmup, local, world)
+                row[ctas] = round(ms_b * 1e3 / max(10, args.steps // 4), 2)
+            sweep[aname][batch] = row
     per = ms256 * 1e-3 / args.steps
     ops = 256 * 2 * fp64_ops_ordered(1024, int(plan.algo()))
     peak = fp64_peak(cf)

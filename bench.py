@@ -262,6 +262,23 @@ def run_gb300(args):
     per_launch_s = ms * 1e-3 / args.steps
     value = world * count * args.steps / (ms * 1e-3)
 
+    # the plain Plan path on the same products: five launches (fold+twist, forward FFT, pointwise,
+    # inverse FFT, untwist+round) per batch, and per product (one launch per transform)
+    z = torch.empty((count, N_POLY // 2), dtype=torch.complex128, device="cuda")
+    out_plain = torch.empty_like(out)
+    plain_steps = max(3, args.steps // 20)
+    ms_pb, _ = timed(torch, lambda: plan.product_unfused(a, bhat, out_plain, z), plain_steps, 2, local, world)
+    plain_ok = bool(torch.equal(out_plain, out))
+    sample = 256
+
+    def per_product():
+        for i in range(sample):
+            plan.product_unfused(a[i:i + 1], bhat[i:i + 1], out_plain[i:i + 1], z[i:i + 1])
+    ms_pp, _ = timed(torch, per_product, 2, 1, local, world)
+    plain = {"batched_5_launches_products_per_s": world * count * plain_steps / (ms_pb * 1e-3),
+             "per_product_5_launches_products_per_s": world * sample * 2 / (ms_pp * 1e-3),
+             "per_product_sample": sample, "matches_fused_result": plain_ok}
+
     # end to end: pinned host A in, pinned host result out, through the C ABI host entry point
     ha = torch.from_numpy(a_np.view(np.int64)).pin_memory()
     hout = torch.empty_like(ha).pin_memory()
@@ -319,6 +336,7 @@ def run_gb300(args):
                               "frac": fp64_achieved / fp64_peak, "ops_per_product": fp64_ops,
                               "microbenchmark_rates": rates,
                               "note": "binding roof: FP64 pipe (best DFMA/DADD/DMUL/mix issue rate, measured live)"}},
+        "plain_path": plain,
         "cpu_baseline": cpu,
         "e2e": {"value": e2e, "unit": "products/s", "h2d_bytes_per_step": count * N_POLY * 8,
                 "d2h_bytes_per_step": count * N_POLY * 8, "steps": e2e_steps, "matches_device_result": ok,
@@ -557,6 +575,11 @@ def run_u128(args):
         "vs_baseline": None, "dtype": "f64x2 (double-double)", "data": "synthetic (seeded numpy PCG64)",
         "config": {"workload": "u128 product, 2048 per launch", "N1024_products_per_s": res[1024],
                    "N4096_products_per_s": res[4096]},
+        "roofline": {"bound": "hbm", "achieved": res[1024] * 49152 / 1e9, "peak": measured_peaks()[0]["hbm_gbs"],
+                     "unit": "GB/s", "frac": res[1024] * 49152 / 1e9 / measured_peaks()[0]["hbm_gbs"],
+                     "traffic": (profiled_traffic("u128_product_n1024") or {}).get("dram_bytes_per_launch"),
+                     "note": "N=1024: 49,152 algorithmic bytes per product; bound by the FP64 pipe "
+                             "(double-double arithmetic), see profiles/u128_product_n1024.md"},
         "clocks": clocks, "gpu_launches": 2 * args.steps,
     }))
 
@@ -609,6 +632,11 @@ def run_serving(args):
         batched = srv.run(cfg)
         clk.mark(t1, time.time())
     plain = srv.run(srv.config(rate=args.rate, duration_s=args.serve_seconds, plain=True))
+    # capacity: the continuous-batching loop at higher arrival rates (same request mix)
+    sweep = {}
+    for rate in (50000.0, 100000.0, 200000.0):
+        st = srv.run(srv.config(rate=rate, duration_s=0.5))
+        sweep["%d" % rate] = {k: st[k] for k in ("products_per_s", "p50_ms", "p99_ms") if k in st}
     if rank != 0:
         return
     print(json.dumps({
@@ -619,7 +647,7 @@ def run_serving(args):
         "config": {"workload": "serving, (k+1)*l products per request, k in 1..2, l in 1..4, N in 2^10..2^14, "
                                "digits b in 4..10 bits", "duration_s": args.serve_seconds,
                    "resident_setup_s": setup_s},
-        "batched": batched, "plain": plain,
+        "batched": batched, "plain": plain, "capacity_sweep_req_per_s": sweep,
         "p99_speedup_vs_plain": plain["p99_ms"] / batched["p99_ms"] if batched["p99_ms"] else None,
         "clocks": clk.summary(), "gpu_launches": batched["launches"],
     }))

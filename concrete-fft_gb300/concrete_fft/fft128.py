@@ -44,3 +44,39 @@ class Plan:
     def inv(self, re0, re1, im0, im1):
         """Inverse negacyclic FFT, unnormalised (src/fft128/mod.rs:1938-1960)."""
         self._run(re0, re1, im0, im1, False)
+
+
+def init_negacyclic_twiddles(twid_re0, twid_re1, twid_im0, twid_im1):
+    """src/fft128/mod.rs:1805-1828: fills positions 1..n-1 of four host float64 arrays of
+    n = len(twid_re0) (position 0 is left as it is)."""
+    arrs = (twid_re0, twid_re1, twid_im0, twid_im1)
+    n = len(twid_re0)
+    for a in arrs:
+        B.check_dtype(a, ("float64",))
+        if B.is_device(a) or len(a) != n:
+            raise ValueError("twiddles: four host arrays of equal length")
+    check(load().cfft_f128_init_negacyclic_twiddles(n, *[B.ptr(a) for a in arrs]))
+
+
+def _raw(data, twid, fwd):
+    for a in (*data, *twid):
+        B.check_dtype(a, ("float64",))
+        if not B.is_device(a):
+            raise TypeError("negacyclic_fwd_fft/inv_fft take CUDA tensors")
+    n = twid[0].numel()
+    batch = B.batch_of(data[0], n, 8)
+    if any(B.batch_of(d, n, 8) != batch for d in data) or any(t.numel() != n for t in twid):
+        raise ValueError("data arrays must hold the same whole number of transforms of the twiddles' length")
+    lib = load()
+    fn = lib.cfft_f128_negacyclic_fwd if fwd else lib.cfft_f128_negacyclic_inv
+    check(fn(n, batch, *[B.ptr(d) for d in data], *[B.ptr(t) for t in twid], B.stream_of(data[0])))
+
+
+def negacyclic_fwd_fft(data_re0, data_re1, data_im0, data_im1, twid_re0, twid_re1, twid_im0, twid_im1):
+    """src/fft128/mod.rs:1041-1071 on device tensors (batched over whole multiples of n)."""
+    _raw((data_re0, data_re1, data_im0, data_im1), (twid_re0, twid_re1, twid_im0, twid_im1), True)
+
+
+def negacyclic_inv_fft(data_re0, data_re1, data_im0, data_im1, twid_re0, twid_re1, twid_im0, twid_im1):
+    """src/fft128/mod.rs:1073-1104 on device tensors (unnormalised)."""
+    _raw((data_re0, data_re1, data_im0, data_im1), (twid_re0, twid_re1, twid_im0, twid_im1), False)

@@ -57,6 +57,21 @@ class U64ProductPlan:
         return out
 
 
+    def product_unfused(self, a, bhat, out, z):
+        """The same product as five separate launches (fold+twist, the N/2-point unordered
+        forward transform, pointwise product, inverse transform, untwist+round): the plain
+        Plan path.  a, out: (count, N) device; z: (count, N/2) complex128 device scratch.
+        Bit-identical to product()."""
+        count = B.batch_of(a, self.N, 8)
+        s = B.stream_of(a)
+        fft = self._lib.cfft_u64_product_fft(self._h)
+        check(self._lib.cfft_u64_fold_twist(self._h, B.ptr(a), B.ptr(z), count, s))
+        check(self._lib.cfft_unordered_fwd(fft, B.ptr(z), count, s))
+        check(self._lib.cfft_c64_pointwise(B.ptr(bhat), self.N // 2, B.ptr(z), self.N // 2, count, s))
+        check(self._lib.cfft_unordered_inv(fft, B.ptr(z), count, s))
+        check(self._lib.cfft_u64_untwist_round(self._h, B.ptr(z), B.ptr(out), count, s))
+        return out
+
     def product_sum(self, a, bhat, out):
         """a: (count, terms, N) device int64/uint64; bhat: (count, terms, N/2) complex128;
         out: (count, N).  out[g] = sum_t a[g, t] * B[g, t], accumulated in the Fourier domain."""

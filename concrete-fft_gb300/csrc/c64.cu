@@ -246,7 +246,8 @@ cfft_status launch_split(const C64Plan& p, bool fwd, int ls, int mode, long nsub
   const void* fn = c64_split_kernel_ptr(p.base_algo, fwd, ls, mode);
   const size_t part = p.n >> ls;
   const size_t smem = 2 * part * sizeof(double2);
-  const int threads = (int)std::min<size_t>(256, std::max<size_t>(32, part / 2));
+  // one thread per butterfly of a pass over the part (more would idle at the barriers)
+  const int threads = (int)std::min<size_t>(256, std::max<size_t>(32, part / (size_t)algo_radix(p.base_algo)));
   DevLevels L = p.dlv;
   const double2* w = fwd ? p.d_w : p.d_winv;
   void* args[] = {&data, &L, (void*)&w};

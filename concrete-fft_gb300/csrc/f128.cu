@@ -194,14 +194,17 @@ static int product_grid(const void* kernel, int threads, size_t smem, long count
 
 int f128_threads(int log2c) { return std::min(256, std::max(64, (1 << log2c) / 8)); }
 
-cfft_status run_f128(const cfft_f128_plan* p, double* re0, double* re1, double* im0, double* im1, size_t batch,
-                     bool fwd, cudaStream_t stream) {
-  if (!p || !re0 || !re1 || !im0 || !im1) return fail(CFFT_ERR_INVALID_ARGUMENT, "null argument");
+// `batch` negacyclic transforms of n points stored back to back in each of
+// the four arrays, with the twiddle arrays tw (init_negacyclic_twiddles).
+cfft_status run_f128_tw(size_t n, const F128Tw& tw, double* re0, double* re1, double* im0, double* im1, size_t batch,
+                        bool fwd, cudaStream_t stream) {
+  if (!re0 || !re1 || !im0 || !im1) return fail(CFFT_ERR_INVALID_ARGUMENT, "null argument");
   if (batch == 0) return CFFT_OK;
-  const int log2n = ilog2(p->n);
+  cfft_status ast = f128_attrs();
+  if (ast != CFFT_OK) return ast;
+  const int log2n = ilog2(n);
   const int log2c = std::min(log2n, kF128SmemLog2);
   F128Arrays g{re0, re1, im0, im1};
-  const F128Tw tw = p->tw();
   const long nblocks = (long)batch << (log2n - log2c);
   const int threads = f128_threads(log2c);
   const size_t smem = (size_t)4 * (size_t(1) << log2c) * sizeof(double);
@@ -225,6 +228,12 @@ cfft_status run_f128(const cfft_f128_plan* p, double* re0, double* re1, double* 
     }
   }
   return CFFT_OK;
+}
+
+cfft_status run_f128(const cfft_f128_plan* p, double* re0, double* re1, double* im0, double* im1, size_t batch,
+                     bool fwd, cudaStream_t stream) {
+  if (!p) return fail(CFFT_ERR_INVALID_ARGUMENT, "null plan");
+  return run_f128_tw(p->n, p->tw(), re0, re1, im0, im1, batch, fwd, stream);
 }
 
 cfft_status run_f128_host(const cfft_f128_plan* p, double* re0, double* re1, double* im0, double* im1, size_t batch,
@@ -290,6 +299,37 @@ cfft_status cfft_f128_fwd_host(const cfft_f128_plan* p, double* re0, double* re1
 cfft_status cfft_f128_inv_host(const cfft_f128_plan* p, double* re0, double* re1, double* im0, double* im1,
                                size_t batch) {
   return run_f128_host(p, re0, re1, im0, im1, batch, false);
+}
+
+cfft_status cfft_f128_init_negacyclic_twiddles(size_t n, double* re0, double* re1, double* im0, double* im1) {
+  if (!re0 || !re1 || !im0 || !im1) return fail(CFFT_ERR_INVALID_ARGUMENT, "null argument");
+  if (!is_pow2(n) || ilog2(n) > 16) return fail(CFFT_ERR_INVALID_SIZE, "n must be a power of two <= 65536");
+  if (n < 2) return CFFT_OK;
+  std::vector<double> tw(4 * n);
+  f128_twiddles(n, tw.data(), tw.data() + n, tw.data() + 2 * n, tw.data() + 3 * n);
+  double* dst[4] = {re0, re1, im0, im1};
+  for (int k = 0; k < 4; ++k)  // positions 1..n-1, as the reference; position 0 is left as it is
+    std::copy(tw.begin() + (long)k * (long)n + 1, tw.begin() + (long)(k + 1) * (long)n, dst[k] + 1);
+  return CFFT_OK;
+}
+
+static cfft_status raw_f128(size_t n, size_t batch, double* re0, double* re1, double* im0, double* im1,
+                            const double* t0, const double* t1, const double* t2, const double* t3, bool fwd,
+                            void* stream) {
+  if (!t0 || !t1 || !t2 || !t3) return fail(CFFT_ERR_INVALID_ARGUMENT, "null twiddle array");
+  if (!is_pow2(n) || n < 2 || ilog2(n) > 16)
+    return fail(CFFT_ERR_INVALID_SIZE, "n must be a power of two in [2, 65536]");
+  return run_f128_tw(n, F128Tw{t0, t1, t2, t3}, re0, re1, im0, im1, batch, fwd, (cudaStream_t)stream);
+}
+cfft_status cfft_f128_negacyclic_fwd(size_t n, size_t batch, double* re0, double* re1, double* im0, double* im1,
+                                     const double* twid_re0, const double* twid_re1, const double* twid_im0,
+                                     const double* twid_im1, void* stream) {
+  return raw_f128(n, batch, re0, re1, im0, im1, twid_re0, twid_re1, twid_im0, twid_im1, true, stream);
+}
+cfft_status cfft_f128_negacyclic_inv(size_t n, size_t batch, double* re0, double* re1, double* im0, double* im1,
+                                     const double* twid_re0, const double* twid_re1, const double* twid_im0,
+                                     const double* twid_im1, void* stream) {
+  return raw_f128(n, batch, re0, re1, im0, im1, twid_re0, twid_re1, twid_im0, twid_im1, false, stream);
 }
 
 cfft_status cfft_u128_product_plan_create(size_t N, cfft_u128_product_plan** out) {

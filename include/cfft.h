@@ -176,6 +176,22 @@ cfft_status cfft_f128_fwd_host(const cfft_f128_plan* plan, double* re0, double* 
 cfft_status cfft_f128_inv_host(const cfft_f128_plan* plan, double* re0, double* re1, double* im0, double* im1,
                                size_t batch);
 
+/* The crate's #[doc(hidden)] free functions, used by its benchmarks:
+ * init_negacyclic_twiddles (src/fft128/mod.rs:1805-1828) fills positions
+ * 1..n-1 of four host arrays of n (position 0 is left as it is), and
+ * negacyclic_fwd_fft / negacyclic_inv_fft (src/fft128/mod.rs:1041-1104, one
+ * entry for the _scalar/_avxfma/_avx512 variants, whose results are equal)
+ * transform `batch` sets of n points with explicit twiddle arrays.  Data and
+ * twiddles are DEVICE arrays here; n is a power of two in [2, 65536]. */
+cfft_status cfft_f128_init_negacyclic_twiddles(size_t n, double* twid_re0, double* twid_re1, double* twid_im0,
+                                               double* twid_im1);
+cfft_status cfft_f128_negacyclic_fwd(size_t n, size_t batch, double* re0, double* re1, double* im0, double* im1,
+                                     const double* twid_re0, const double* twid_re1, const double* twid_im0,
+                                     const double* twid_im1, void* stream);
+cfft_status cfft_f128_negacyclic_inv(size_t n, size_t batch, double* re0, double* re1, double* im0, double* im1,
+                                     const double* twid_re0, const double* twid_re1, const double* twid_im0,
+                                     const double* twid_im1, void* stream);
+
 /* ================================================ negacyclic products ====
  * The reference's caller (TFHE-rs) builds polynomial products mod X^N + 1 on
  * unordered::Plan (u64 torus) and fft128::Plan (u128 torus); the crate itself

@@ -1094,21 +1094,24 @@ int oracle_f128_sincospi(double x0, double x1, double* s2, double* c2) {
   return 0;
 }
 
+// Plan::new requires n >= 32 (src/fft128/mod.rs:1865-1866); the free functions
+// init_negacyclic_twiddles and negacyclic_{fwd,inv}_fft_scalar (:1805, :352,
+// :1105) take any power of two, as these entry points do.
 int oracle_f128_twiddles(size_t n, double* re0, double* re1, double* im0, double* im1) {
-  if (!is_pow2(n) || n < 32) return -1;  // src/fft128/mod.rs:1865-1866
+  if (!is_pow2(n) || n < 2) return -1;
   f128_twiddles(n, re0, re1, im0, im1);
   return 0;
 }
 
 int oracle_f128_fwd(size_t n, double* re0, double* re1, double* im0, double* im1, const double* a, const double* b,
                     const double* c, const double* d) {
-  if (!is_pow2(n) || n < 32) return -1;
+  if (!is_pow2(n) || n < 2) return -1;
   f128_fwd(n, re0, re1, im0, im1, a, b, c, d);
   return 0;
 }
 int oracle_f128_inv(size_t n, double* re0, double* re1, double* im0, double* im1, const double* a, const double* b,
                     const double* c, const double* d) {
-  if (!is_pow2(n) || n < 32) return -1;
+  if (!is_pow2(n) || n < 2) return -1;
   f128_inv(n, re0, re1, im0, im1, a, b, c, d);
   return 0;
 }

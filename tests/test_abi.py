@@ -79,3 +79,18 @@ def test_tune_cache_file_round_trip(cfft_lib, tmp_path):
     assert b"out of range" in L.cfft_last_error()
     L.cfft_tune_clear()
     assert L.cfft_tune_entries() == 0
+
+
+def test_f128_init_negacyclic_twiddles_matches_oracle(cfft_lib, oracle):
+    """init_negacyclic_twiddles is host code: positions 1..n-1 equal the oracle's table
+    bit for bit, position 0 is left untouched (src/fft128/mod.rs:1805-1828)."""
+    import numpy as np
+    import concrete_fft as cf
+    for n in (2, 16, 512, 4096):
+        t = [np.full(n, 7.0) for _ in range(4)]
+        cf.fft128.init_negacyclic_twiddles(*t)
+        want = oracle.f128_twiddles(n)
+        for k in range(4):
+            assert t[k][0] == 7.0
+            assert np.array_equal(t[k][1:].view(np.uint64), want[k][1:].view(np.uint64)), (n, k)
+    assert cfft_lib.cfft_f128_init_negacyclic_twiddles(24, *[ctypes.c_void_p(t[0].ctypes.data)] * 4) == -1

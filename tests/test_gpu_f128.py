@@ -34,6 +34,29 @@ def test_f128_fwd_inv_bit_exact(cuda, oracle, n):
         assert np.array_equal(bits(h), bits(w))
 
 
+@pytest.mark.parametrize("n", [2, 4, 16, 64, 1024, 8192])
+def test_f128_raw_negacyclic_functions(cuda, oracle, n):
+    """negacyclic_fwd_fft / negacyclic_inv_fft with caller-owned twiddle arrays
+    (src/fft128/mod.rs:1041-1104), batched, against the oracle."""
+    import concrete_fft as cf
+    torch = cuda
+    tw = [np.zeros(n) for _ in range(4)]
+    cf.fft128.init_negacyclic_twiddles(*tw)
+    dtw = [torch.from_numpy(t).cuda() for t in tw]
+    rng = np.random.default_rng(n)
+    hi = [rng.uniform(-1, 1, (3, n)) for _ in range(2)]
+    data = [hi[0], hi[0] * 2.0 ** -60, hi[1], hi[1] * 2.0 ** -60]
+    d = [torch.from_numpy(np.ascontiguousarray(x)).cuda() for x in data]
+    cf.fft128.negacyclic_fwd_fft(*d, *dtw)
+    want = oracle.f128_fwd(*data)
+    for k in range(4):
+        assert np.array_equal(d[k].cpu().numpy().view(np.uint64), want[k].view(np.uint64)), (n, k)
+    cf.fft128.negacyclic_inv_fft(*d, *dtw)
+    want = oracle.f128_inv(*want)
+    for k in range(4):
+        assert np.array_equal(d[k].cpu().numpy().view(np.uint64), want[k].view(np.uint64)), (n, k)
+
+
 def test_f128_invalid_size(cuda):
     import concrete_fft as cf
     with pytest.raises(cf.CfftError):

@@ -627,6 +627,10 @@ def run_serving(args):
     setup_s = time.perf_counter() - t0
     cfg = srv.config(rate=args.rate, duration_s=args.serve_seconds)
     srv.run(srv.config(rate=args.rate, duration_s=0.05))  # warm-up
+    if args.profile_case:  # for ncu: a short batched run only
+        st = srv.run(srv.config(rate=args.rate, duration_s=0.1))
+        print(json.dumps({"profile_case": "serving 0.1 s", "launches": st.get("launches")}))
+        return
     with ClockSampler(local) as clk:
         t1 = time.time()
         batched = srv.run(cfg)

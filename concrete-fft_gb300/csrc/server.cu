@@ -47,6 +47,10 @@ inline double u01(uint64_t& s) { return (double)(splitmix(s) >> 11) * (1.0 / 900
 
 constexpr int kPoolRows = 64;   // digit polynomials per size
 constexpr int kSlots = 3;       // launch slots (concurrent runs)
+// Item records per launch slot, allocated at creation: growing them inside the
+// loop (cudaFree synchronises the device, cudaMallocHost is slow) showed up as
+// millisecond latency spikes the first time a larger batch formed.
+constexpr size_t kSlotItems = 65536;
 
 struct ReqDesc {
   uint64_t id;
@@ -268,7 +272,7 @@ cfft_status cfft_server_create(const cfft_product_engine* engine, const uint32_t
         st = fail(CFFT_ERR_OUT_OF_MEMORY, "server launch slots");
         break;
       }
-      st = ensure_items(sl, 1024);
+      st = ensure_items(sl, kSlotItems);
       if (st != CFFT_OK) break;
     }
   }

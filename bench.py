@@ -503,6 +503,11 @@ def run_ordered(args):
 
     ms256, clocks = timed(torch, step256, args.steps, args.warmup, local, world)
     ms1, _ = timed(torch, step1, args.steps, args.warmup, local, world)
+    # the same batch-1 fwd+inv captured by the caller into a CUDA graph and replayed
+    graph = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(graph):
+        step1()
+    ms1g, _ = timed(torch, graph.replay, args.steps, args.warmup, local, world)
     # CTAs per transform (1 = one CTA, 2/4/8 = split over a cluster) at a few batch sizes, fwd then inv,
     # for a DIT algorithm (one exchange through distributed shared memory) and a DIF one (none)
     sweep = {}
@@ -539,6 +544,7 @@ def run_ordered(args):
         "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded numpy PCG64)",
         "config": {"workload": "ordered::Plan n=1024 batch 256", "algo": plan.algo().name,
                    "batch1_us_per_fwd_inv": ms1 * 1e3 / args.steps,
+                   "batch1_us_per_fwd_inv_graph_replay": ms1g * 1e3 / args.steps,
                    "us_per_fwd_inv_by_batch_and_ctas_per_transform": sweep},
         "roofline": {"bound": "hbm", "achieved": 256 * 65536 / per / 1e9, "peak": measured_peaks()[0]["hbm_gbs"],
                      "unit": "GB/s", "frac": 256 * 65536 / per / 1e9 / measured_peaks()[0]["hbm_gbs"],
@@ -639,6 +645,7 @@ def run_serving(args):
     # capacity: the continuous-batching loop at higher arrival rates (same request mix)
     sweep = {}
     for rate in (50000.0, 100000.0, 200000.0):
+        srv.run(srv.config(rate=rate, duration_s=0.05))  # warm-up at this rate (clocks ramp up after the plain run)
         st = srv.run(srv.config(rate=rate, duration_s=0.5))
         sweep["%d" % rate] = {k: st[k] for k in ("products_per_s", "p50_ms", "p99_ms") if k in st}
     if rank != 0:

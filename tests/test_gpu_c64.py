@@ -153,6 +153,33 @@ def test_cluster_sizes_bit_exact(cuda, oracle, ctas):
             assert np.array_equal(bits(d.cpu().numpy()), bits(want)), (n, base, algo, ctas)
 
 
+@pytest.mark.parametrize("batch", [1, 256])
+def test_plan_calls_capture_into_a_cuda_graph(cuda, oracle, batch):
+    """fwd and inv enqueue only kernels on the caller's stream, so a caller can capture
+    them into a CUDA graph and replay it; replays give the oracle's bits."""
+    import concrete_fft as cf
+    torch = cuda
+    for algo in (2, 3):
+        plan = cf.ordered.Plan(1024, cf.ordered.Method.UserProvided(algo))
+        x = rand_c64(batch, 1024)
+        d = on_gpu(torch, x)
+        plan.fwd(d)  # first calls outside the capture (kernel attributes are set once)
+        plan.inv(d)
+        g = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(g):
+            plan.fwd(d)
+            plan.inv(d)
+        d.copy_(on_gpu(torch, x))
+        g.replay()
+        want = oracle.ordered_inv(algo, oracle.ordered_fwd(algo, x))
+        assert np.array_equal(bits(d.cpu().numpy()), bits(want)), (algo, batch)
+        d.copy_(on_gpu(torch, x))
+        g.replay()
+        g.replay()
+        want = oracle.ordered_inv(algo, oracle.ordered_fwd(algo, want))
+        assert np.array_equal(bits(d.cpu().numpy()), bits(want)), (algo, batch)
+
+
 @pytest.mark.parametrize("n", [256, 1024, 4096])
 def test_monomial_and_serde_order(cuda, oracle, n):
     import concrete_fft as cf

@@ -573,6 +573,15 @@ def run_u128(args):
         out = torch.empty_like(a)
         ms, clocks = timed(torch, lambda: plan.product(a, bhat, out), args.steps, args.warmup, local, world)
         res[N] = world * count * args.steps / (ms * 1e-3)
+        if N == 1024:  # end to end: pinned host A in and results out through the host entry point
+            ha = a.cpu().pin_memory()
+            hout = torch.empty_like(ha).pin_memory()
+            plan.product(ha, bhat, hout)
+            t0 = time.perf_counter()
+            for _ in range(max(3, args.steps // 10)):
+                plan.product(ha, bhat, hout)
+            e2e = world * count * max(3, args.steps // 10) / (time.perf_counter() - t0)
+            e2e_ok = bool(torch.equal(hout, out.cpu()))
     if rank != 0:
         return
     print(json.dumps({
@@ -581,6 +590,8 @@ def run_u128(args):
         "vs_baseline": None, "dtype": "f64x2 (double-double)", "data": "synthetic (seeded numpy PCG64)",
         "config": {"workload": "u128 product, 2048 per launch", "N1024_products_per_s": res[1024],
                    "N4096_products_per_s": res[4096]},
+        "e2e": {"value": e2e, "unit": "products/s", "h2d_bytes_per_step": count * 1024 * 16,
+                "d2h_bytes_per_step": count * 1024 * 16, "matches_device_result": e2e_ok, "N": 1024},
         "roofline": {"bound": "hbm", "achieved": res[1024] * 49152 / 1e9, "peak": measured_peaks()[0]["hbm_gbs"],
                      "unit": "GB/s", "frac": res[1024] * 49152 / 1e9 / measured_peaks()[0]["hbm_gbs"],
                      "traffic": (profiled_traffic("u128_product_n1024") or {}).get("dram_bytes_per_launch"),
@@ -641,13 +652,14 @@ def run_serving(args):
         t1 = time.time()
         batched = srv.run(cfg)
         clk.mark(t1, time.time())
-    plain = srv.run(srv.config(rate=args.rate, duration_s=args.serve_seconds, plain=True))
     # capacity: the continuous-batching loop at higher arrival rates (same request mix)
     sweep = {}
-    for rate in (50000.0, 100000.0, 200000.0):
-        srv.run(srv.config(rate=rate, duration_s=0.05))  # warm-up at this rate (clocks ramp up after the plain run)
+    for rate in (50000.0, 100000.0, 150000.0, 200000.0):
         st = srv.run(srv.config(rate=rate, duration_s=0.5))
-        sweep["%d" % rate] = {k: st[k] for k in ("products_per_s", "p50_ms", "p99_ms") if k in st}
+        sweep["%d" % rate] = {k: st[k] for k in ("products_per_s", "p50_ms", "p99_ms", "max_ms", "launches",
+                                                 "mean_batch", "deferred_admissions") if k in st}
+    # the comparator last: it saturates and queues for seconds
+    plain = srv.run(srv.config(rate=args.rate, duration_s=args.serve_seconds, plain=True))
     if rank != 0:
         return
     print(json.dumps({

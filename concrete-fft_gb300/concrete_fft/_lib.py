@@ -129,6 +129,7 @@ _SIGS = [
     ("cfft_u128_product_poly_size", c_size, [vp]),
     ("cfft_u128_prepare_operand", c_int, [vp, vp, vp, c_size, vp]),
     ("cfft_u128_product", c_int, [vp, vp, vp, c_size, vp, c_size, vp]),
+    ("cfft_u128_product_host", c_int, [vp, vp, vp, c_size, vp, c_size]),
 ]
 
 EXPORTED = [s[0] for s in _SIGS]

@@ -103,8 +103,12 @@ class U128ProductPlan:
         return bhat4
 
     def product(self, a, bhat4, out, shared_operand=False):
+        """a, out: (count, N, 2) u64 (lo, hi) words, device or host (bhat4 always on device)."""
         count = B.batch_of(a, 2 * self.N, 8)
         stride = 0 if shared_operand else 2 * self.N
-        check(self._lib.cfft_u128_product(self._h, B.ptr(a), B.ptr(bhat4), stride, B.ptr(out), count,
-                                          B.stream_of(a)))
+        if B.is_device(a):
+            check(self._lib.cfft_u128_product(self._h, B.ptr(a), B.ptr(bhat4), stride, B.ptr(out), count,
+                                              B.stream_of(a)))
+        else:
+            check(self._lib.cfft_u128_product_host(self._h, B.ptr(a), B.ptr(bhat4), stride, B.ptr(out), count))
         return out

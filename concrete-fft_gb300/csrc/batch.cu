@@ -184,13 +184,8 @@ double unit_cost(int log2n, int count, int dir) {
   return (double)count * (double)(1L << log2n) * log2n * ((dir == 3) ? 2 : 1);
 }
 
-bool g_batch_attr = false;
 cfft_status batch_attr() {
-  if (g_batch_attr) return CFFT_OK;
-  CFFT_CUDA_TRY(cudaFuncSetAttribute(batch_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                     2 * (1 << kBatchSmemLog2) * (int)sizeof(double2)));
-  g_batch_attr = true;
-  return CFFT_OK;
+  return ensure_smem((const void*)batch_kernel, 2 * (1 << kBatchSmemLog2) * sizeof(double2));
 }
 
 }  // namespace

@@ -8,6 +8,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <mutex>
 #include <vector>
 
 #include "cfft_internal.h"
@@ -161,15 +162,21 @@ struct cfft_u128_product_plan {
 
 namespace {
 
-bool g_f128_attr = false;
+// Raises the fft128 kernels' dynamic shared-memory limit once per device.
+std::mutex g_f128_attr_mu;
+std::vector<int> g_f128_attr_devices;
 cfft_status f128_attrs() {
-  if (g_f128_attr) return CFFT_OK;
+  int dev = 0;
+  CFFT_CUDA_TRY(cudaGetDevice(&dev));
+  std::lock_guard<std::mutex> lk(g_f128_attr_mu);
+  for (int d : g_f128_attr_devices)
+    if (d == dev) return CFFT_OK;
   const int max_smem = 4 * (1 << kF128SmemLog2) * (int)sizeof(double);
   CFFT_CUDA_TRY(cudaFuncSetAttribute(f128_smem_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, max_smem));
   CFFT_CUDA_TRY(cudaFuncSetAttribute(f128_smem_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, max_smem));
   CFFT_CUDA_TRY(cudaFuncSetAttribute(u128_product_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, max_smem));
   CFFT_CUDA_TRY(cudaFuncSetAttribute(u128_prepare_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, max_smem));
-  g_f128_attr = true;
+  g_f128_attr_devices.push_back(dev);
   return CFFT_OK;
 }
 
@@ -382,6 +389,35 @@ cfft_status cfft_u128_product(const cfft_u128_product_plan* p, const uint64_t* a
   u128_product_kernel<<<grid, threads, smem, (cudaStream_t)stream>>>(
       a, bhat4, (long)bhat_stride, out, (long)count, log2n, p->f.tw(), 2.0 / (double)p->N);
   CFFT_CHECK_LAUNCH();
+  return CFFT_OK;
+}
+
+cfft_status cfft_u128_product_host(const cfft_u128_product_plan* p, const uint64_t* a, const double* bhat4,
+                                   size_t bhat_stride, uint64_t* out, size_t count) {
+  if (!p || !a || !bhat4 || !out) return fail(CFFT_ERR_INVALID_ARGUMENT, "null argument");
+  if (bhat_stride != 0 && bhat_stride != 2 * p->N)
+    return fail(CFFT_ERR_INVALID_ARGUMENT, "bhat_stride must be 0 or 2N");
+  if (count == 0) return CFFT_OK;
+  // about 16 chunks on 4 streams, each at least two CTAs per SM
+  constexpr int kSlots = 4;
+  const size_t poly_bytes = p->N * 2 * sizeof(uint64_t);
+  const size_t chunk = std::min(count, std::max((size_t)sm_count() * 2, (count + 15) / 16));
+  PipeSlot slot[kSlots];
+  cfft_status st = host_pipeline(kSlots, 2 * chunk * poly_bytes, slot);
+  if (st != CFFT_OK) return st;
+  size_t i = 0;
+  for (size_t first = 0; first < count; first += chunk, ++i) {
+    const size_t c = std::min(chunk, count - first);
+    const PipeSlot& sl = slot[i % kSlots];
+    uint64_t* da = (uint64_t*)sl.dev;
+    uint64_t* dout = da + chunk * 2 * p->N;
+    CFFT_CUDA_TRY(cudaMemcpyAsync(da, a + first * 2 * p->N, c * poly_bytes, cudaMemcpyHostToDevice, sl.stream));
+    const double* bh = bhat4 + (bhat_stride ? first * bhat_stride : 0);
+    st = cfft_u128_product(p, da, bh, bhat_stride, dout, c, sl.stream);
+    if (st != CFFT_OK) return st;
+    CFFT_CUDA_TRY(cudaMemcpyAsync(out + first * 2 * p->N, dout, c * poly_bytes, cudaMemcpyDeviceToHost, sl.stream));
+  }
+  for (int k = 0; k < kSlots; ++k) CFFT_CUDA_TRY(cudaStreamSynchronize(slot[k].stream));
   return CFFT_OK;
 }
 

@@ -118,6 +118,8 @@ cfft_status launch_kernel_cluster(const void* fn, int grid, int block, int clust
   return CFFT_OK;
 }
 
+cfft_status ensure_smem(const void* fn, size_t smem) { return ensure_smem_attr(fn, smem); }
+
 int max_blocks_per_sm(const void* fn, int block, size_t smem) {
   if (ensure_smem_attr(fn, smem) != CFFT_OK) return 1;
   int per_sm = 0;

@@ -47,6 +47,9 @@ int sm_count();
 // Launch a kernel through its pointer, raising its dynamic shared-memory limit
 // the first time it is used with more than 48 KiB.
 cfft_status launch_kernel(const void* fn, int grid, int block, void** args, size_t smem, cudaStream_t stream);
+// Raises a kernel's dynamic shared-memory limit to `smem` on the current
+// device, once (thread-safe); a no-op up to 48 KiB.
+cfft_status ensure_smem(const void* fn, size_t smem);
 // The same with a thread-block cluster of `cluster` CTAs (grid a multiple of it).
 cfft_status launch_kernel_cluster(const void* fn, int grid, int block, int cluster, void** args, size_t smem,
                                   cudaStream_t stream);

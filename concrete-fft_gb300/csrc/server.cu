@@ -414,9 +414,27 @@ cfft_status cfft_server_run(cfft_server* s, const cfft_serve_config* cfg, cfft_s
                                         cudaMemcpyHostToDevice, sl.stream));
           st = cfft_product_engine_run(s->engine, sl.d_items, nitems, sl.counter, sl.ws, sl.stream);
           if (st != CFFT_OK) return st;
-          for (size_t ri : batch)
-            CFFT_CUDA_TRY(cudaMemcpyAsync(s->h_ring + reqs[ri].ring_off, s->d_ring + reqs[ri].ring_off,
-                                          reqs[ri].ring_bytes, cudaMemcpyDeviceToHost, sl.stream));
+          // results back to the pinned host ring: the batch's requests were allocated in
+          // admission order, so they are contiguous (256-byte aligned) except across the
+          // wrap; one copy per contiguous run
+          uint64_t run_off = 0, run_end = 0;
+          bool have_run = false;
+          for (size_t ri : batch) {
+            const uint64_t off = reqs[ri].ring_off, end = off + reqs[ri].ring_bytes;
+            if (have_run && off == ((run_end + 255) & ~uint64_t(255))) {
+              run_end = end;
+              continue;
+            }
+            if (have_run)
+              CFFT_CUDA_TRY(cudaMemcpyAsync(s->h_ring + run_off, s->d_ring + run_off, run_end - run_off,
+                                            cudaMemcpyDeviceToHost, sl.stream));
+            run_off = off;
+            run_end = end;
+            have_run = true;
+          }
+          if (have_run)
+            CFFT_CUDA_TRY(cudaMemcpyAsync(s->h_ring + run_off, s->d_ring + run_off, run_end - run_off,
+                                          cudaMemcpyDeviceToHost, sl.stream));
           CFFT_CUDA_TRY(cudaEventRecord(sl.done, sl.stream));
           sl.busy = true;
           sl.reqs = batch;

@@ -341,6 +341,11 @@ cfft_status cfft_u128_prepare_operand(const cfft_u128_product_plan* plan, const 
                                       size_t count, void* stream);
 cfft_status cfft_u128_product(const cfft_u128_product_plan* plan, const uint64_t* a, const double* bhat4,
                               size_t bhat_stride, uint64_t* out, size_t count, void* stream);
+/* Host buffers for a and out (bhat4 stays device-resident): the count is split
+ * into chunks whose copies in, products and copies out are pipelined over
+ * several streams.  Returns when the results are in `out`. */
+cfft_status cfft_u128_product_host(const cfft_u128_product_plan* plan, const uint64_t* a, const double* bhat4,
+                                   size_t bhat_stride, uint64_t* out, size_t count);
 
 /* ============================================ mixed-size batch (persistent) ====
  * Many c64 transforms of different sizes and kinds in one persistent kernel

@@ -43,6 +43,14 @@ def test_argument_errors_without_device(cfft_lib):
     assert L.cfft_u64_product_plan_create(100, 6, 32, ctypes.byref(h)) == -1
     assert L.cfft_u128_product_plan_create(16384, ctypes.byref(h)) == -1
     assert b"power of two" in L.cfft_last_error()
+    buf = (ctypes.c_double * 8)()
+    assert L.cfft_batch_run_host(None, buf, buf, None) == -2                 # null batch
+    assert L.cfft_u128_product_host(None, buf, buf, 0, buf, 1) == -2         # null plan
+    assert L.cfft_u64_product_host(None, buf, buf, 0, buf, 1) == -2
+    assert L.cfft_f128_negacyclic_fwd(24, 1, *[buf] * 8, None) == -1         # not a power of two
+    assert L.cfft_f128_negacyclic_inv(2048, 1, *[buf] * 4, None, buf, buf, buf, None) == -2  # null twiddles
+    assert L.cfft_ordered_set_cluster_size(None, 4) == -2
+    assert L.cfft_unordered_set_cluster_size(None, 3) == -2
 
 
 def test_no_device_is_reported(cfft_lib):

@@ -138,6 +138,28 @@ def test_u128_product_bit_exact(cuda, oracle, N):
     assert np.array_equal(out2.cpu().numpy().view(np.uint64), oracle.u128_schoolbook(a2, b[:1]))
 
 
+def test_u128_product_host_pipeline(cuda, oracle):
+    """Host entry point for u128 products over several pipelined chunks, one operand per
+    product, against the device entry point (itself checked against the oracle above)."""
+    import concrete_fft as cf
+    torch = cuda
+    N, count = 1024, 700
+    plan = cf.product.U128ProductPlan(N)
+    a = RNG.integers(0, 2 ** 64, (count, N, 2), dtype=np.uint64)
+    b = RNG.integers(-2 ** 15, 2 ** 15, (count, N))
+    bhat = torch.empty((count, 4, N // 2), dtype=torch.float64, device="cuda")
+    plan.prepare_operand(torch.from_numpy(b).cuda(), bhat)
+    host_out = np.zeros_like(a)
+    plan.product(a, bhat, host_out)
+    da = torch.from_numpy(a.view(np.int64)).cuda()
+    out = torch.empty_like(da)
+    plan.product(da, bhat, out)
+    assert np.array_equal(host_out, out.cpu().numpy().view(np.uint64))
+    sel = [0, 299, 699]
+    want = oracle.u128_product(N, a[sel], bhat[sel].cpu().numpy(), nthreads=0)
+    assert np.array_equal(host_out[sel], want)
+
+
 @pytest.mark.parametrize("N,algo,base,terms", [(2048, 2, 1024, 8), (1024, 4, 512, 3), (4096, 6, 1024, 1),
                                                (8192, 3, 1024, 2)])
 def test_u64_product_sum_bit_exact(cuda, oracle, N, algo, base, terms):

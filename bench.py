@@ -676,6 +676,46 @@ def run_serving(args):
     }))
 
 
+def run_u64_large(args):
+    """Fused u64 products above N = 8192 (one product per thread-block cluster) against the
+    plain five-launch path on the same products: N = 16384, 32768, 65536."""
+    import numpy as np
+    torch, cf, rank, world, local = gpu_setup()
+    peak = fp64_peak(cf)
+    rows = {}
+    clocks = None
+    for N in (16384, 32768, 65536):
+        count = 8192 * 2048 // N
+        plan = cf.product.U64ProductPlan(N, cf.FftAlgo.Dif4, 1024)
+        rng = np.random.default_rng(N)
+        a = torch.from_numpy(rng.integers(0, 2 ** 64, (count, N), dtype=np.uint64).view(np.int64)).cuda()
+        b = torch.from_numpy(rng.integers(-2 ** 7, 2 ** 7, (count, N))).cuda()
+        bhat = torch.empty((count, N // 2), dtype=torch.complex128, device="cuda")
+        plan.prepare_operand(b, bhat)
+        out = torch.empty_like(a)
+        ms, clocks = timed(torch, lambda: plan.product(a, bhat, out), args.steps, args.warmup, local, world)
+        z = torch.empty((count, N // 2), dtype=torch.complex128, device="cuda")
+        out2 = torch.empty_like(a)
+        ms_u, _ = timed(torch, lambda: plan.product_unfused(a, bhat, out2, z), max(3, args.steps // 4), 2, local,
+                        world)
+        per = ms * 1e-3 / args.steps
+        ops = fp64_ops_per_product(N, 1024, int(cf.FftAlgo.Dif4)) * count
+        rows[N] = {"products_per_s": world * count / per, "fp64_frac": ops / per / peak,
+                   "unfused_products_per_s": world * count * max(3, args.steps // 4) / (ms_u * 1e-3),
+                   "matches_unfused": bool(torch.equal(out, out2)), "count": count}
+    if rank != 0:
+        return
+    print(json.dumps({
+        "metric": "fused u64 products/s above N=8192 (one product per thread-block cluster)",
+        "value": rows[16384]["products_per_s"], "unit": "products/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic (seeded numpy PCG64)",
+        "config": {"workload": "u64 products N=16384/32768/65536, Dif4 base 1024, 16 MiB of A per launch",
+                   "by_N": rows},
+        "clocks": clocks, "gpu_launches": 3 * args.steps,
+    }))
+
+
 def run_serde(args):
     """Permuted <-> standard order conversion (serialize/deserialize_fourier_buffer's element
     order) of 65536 unordered transforms of n = 1024 (base 32): 1 GiB in, 1 GiB out per call.
@@ -731,7 +771,8 @@ def main():
     ap.add_argument("--rate", type=float, default=20000.0)
     ap.add_argument("--serve-seconds", type=float, default=1.0)
     ap.add_argument("--operand-gb", type=int, default=8)
-    ap.add_argument("--workload", choices=["u64_product", "mixed", "ordered", "u128_product", "serving", "product_sum", "serde"],
+    ap.add_argument("--workload", choices=["u64_product", "mixed", "ordered", "u128_product", "serving", "product_sum", "serde",
+                             "u64_large"],
                     default="u64_product",
                     help="u64_product (default headline) or one of the other benchmark configurations")
     ap.add_argument("--mixed-items", type=int, default=100000)
@@ -749,6 +790,8 @@ def main():
         run_u128(args)
     elif args.workload == "serde":
         run_serde(args)
+    elif args.workload == "u64_large":
+        run_u64_large(args)
     elif args.workload == "serving":
         run_serving(args)
     elif args.workload == "product_sum":

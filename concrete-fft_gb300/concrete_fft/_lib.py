@@ -97,6 +97,7 @@ _SIGS = [
     ("cfft_u64_untwist_round", c_int, [vp, vp, vp, c_size, vp]),
     ("cfft_u64_product_fft", vp, [vp]),
     ("cfft_u64_product_set_int_adds", c_int, [vp, c_int]),
+    ("cfft_u64_product_set_cluster_size", c_int, [vp, c_int]),
     ("cfft_u64_product_int_adds", c_int, [vp]),
     ("cfft_u64_prepare_operand", c_int, [vp, vp, vp, c_size, vp]),
     ("cfft_u64_product", c_int, [vp, vp, vp, c_size, vp, c_size, vp]),

@@ -57,6 +57,10 @@ class U64ProductPlan:
         return out
 
 
+    def set_cluster_size(self, ctas):
+        """CTAs per product: 0 automatic, 1 one CTA, 2/4/8 a thread-block cluster; results unchanged."""
+        check(self._lib.cfft_u64_product_set_cluster_size(self._h, int(ctas)))
+
     def product_unfused(self, a, bhat, out, z):
         """The same product as five separate launches (fold+twist, the N/2-point unordered
         forward transform, pointwise product, inverse transform, untwist+round): the plain

@@ -25,6 +25,7 @@
 #include "cfft_internal.h"
 #include "runtime.h"
 #include "c64_kernels.cuh"
+#include "split_product.cuh"
 #include "tune_cache.h"
 
 using namespace cfft;
@@ -37,6 +38,7 @@ struct cfft_u64_product_plan {
   DevLevels dlv{};
   double2 *d_w = nullptr, *d_winv = nullptr, *d_tw = nullptr, *d_itw = nullptr;
   int emu = 0;  // eighths of the butterfly additions issued on the integer pipe
+  int cluster = 0;  // CTAs per product: 0 automatic, 1 one CTA, 2/4/8 a cluster of that size
 };
 
 namespace cfft {
@@ -120,6 +122,43 @@ cfft_status launch_product(const cfft_u64_product_plan* plan, const uint64_t* a,
   return launch_kernel(fn, grid, kProdThreads, args, smem, stream);
 }
 
+// CTAs per product as a log2 (0: one CTA).  A product whose N/2-point
+// transform exceeds one CTA's shared memory (N > 8192) always runs on a
+// cluster, S = 2^ls with S <= level 0's radix, S <= 8 and n/S <= 4096 points
+// per CTA (so N <= 65536); its default S gives each CTA 1024 points (the base
+// size) where possible.  Smaller products use a cluster when the batch is too
+// small to give every SM a product, or as the plan forces.
+int product_split_log2(const cfft_u64_product_plan* p, size_t count, bool* ok) {
+  *ok = true;
+  const int log2n = ilog2(p->n);
+  const int max_ls = p->lv.nlevels >= 1 ? std::min(3, p->lv.log2r[0]) : 0;
+  const int min_ls = std::max(0, log2n - kSmemLog2Max);
+  if (min_ls > max_ls) {
+    *ok = false;
+    return 0;
+  }
+  if (p->cluster >= 2) return std::max(min_ls, std::min(max_ls, ilog2((size_t)p->cluster)));
+  if (min_ls > 0) return std::max(min_ls, std::min(max_ls, log2n - 10));
+  if (p->cluster == 1 || max_ls == 0) return 0;
+  int ls = 0;
+  while (ls < max_ls && (count << ls) < (size_t)sm_count()) ++ls;
+  return ls;
+}
+
+cfft_status launch_split_product(const cfft_u64_product_plan* plan, int ls, const uint64_t* a, const double* bhat,
+                                 size_t bhat_stride, uint64_t* out, size_t count, cudaStream_t stream) {
+  const void* fn = plan->base_algo < 4 ? u64_product_split_ptr_0123(plan->base_algo, ls)
+                                       : u64_product_split_ptr_4567(plan->base_algo, ls);
+  const size_t smem = 2 * (plan->n >> ls) * sizeof(double2);
+  if ((count << ls) > 0x7fffffffUL) return fail(CFFT_ERR_INVALID_SIZE, "batch too large");
+  DevLevels L = plan->dlv;
+  long stride = (long)bhat_stride;
+  const double2* bh = (const double2*)bhat;
+  void* args[] = {(void*)&a, (void*)&bh, &stride, (void*)&out, &L, (void*)&plan->d_w, (void*)&plan->d_winv,
+                  (void*)&plan->d_tw, (void*)&plan->d_itw};
+  return launch_kernel_cluster(fn, (int)(count << ls), kSplitProdThreads, 1 << ls, args, smem, stream);
+}
+
 }  // namespace
 
 void cfft::u64_product_tables(const cfft_u64_product_plan* p, const void** w, const void** winv, const void** tw,
@@ -187,6 +226,13 @@ cfft_status cfft_u64_product_sum(const cfft_u64_product_plan* plan, const uint64
 }
 
 cfft_unordered_plan* cfft_u64_product_fft(const cfft_u64_product_plan* plan) { return plan ? plan->fft : nullptr; }
+
+cfft_status cfft_u64_product_set_cluster_size(cfft_u64_product_plan* plan, int ctas) {
+  if (!plan || !(ctas == 0 || ctas == 1 || ctas == 2 || ctas == 4 || ctas == 8))
+    return fail(CFFT_ERR_INVALID_ARGUMENT, "cluster size must be 0 (automatic), 1, 2, 4 or 8");
+  plan->cluster = ctas;
+  return CFFT_OK;
+}
 
 cfft_status cfft_u64_product_set_int_adds(cfft_u64_product_plan* plan, int eighths) {
   if (!plan || eighths < 0 || eighths > 8) return fail(CFFT_ERR_INVALID_ARGUMENT, "eighths must be in 0..8");
@@ -274,9 +320,11 @@ cfft_status cfft_u64_product(const cfft_u64_product_plan* plan, const uint64_t* 
   if (!plan || !a || !bhat || !out) return fail(CFFT_ERR_INVALID_ARGUMENT, "null argument");
   if (bhat_stride != 0 && bhat_stride != plan->n)
     return fail(CFFT_ERR_INVALID_ARGUMENT, "bhat_stride must be 0 or N/2");
-  if (plan->N > (size_t(2) << kSmemLog2Max))
-    return fail(CFFT_ERR_INVALID_SIZE, "fused u64 product: N must be at most 8192 (use cfft_product_engine_run)");
+  bool ok = true;
+  const int ls = product_split_log2(plan, count, &ok);
+  if (!ok) return fail(CFFT_ERR_INVALID_SIZE, "fused u64 product: N must be at most 65536 (use cfft_product_engine_run)");
   if (count == 0) return CFFT_OK;
+  if (ls > 0) return launch_split_product(plan, ls, a, bhat, bhat_stride, out, count, (cudaStream_t)stream);
   return launch_product(plan, a, bhat, bhat_stride, out, count, (cudaStream_t)stream);
 
 }
@@ -288,8 +336,8 @@ cfft_status cfft_u64_product(const cfft_u64_product_plan* plan, const uint64_t* 
 cfft_status cfft_u64_product_plan_create_measure(size_t N, double seconds, cfft_u64_product_plan** out) {
   if (!out) return fail(CFFT_ERR_INVALID_ARGUMENT, "null output pointer");
   *out = nullptr;
-  if (!is_pow2(N) || N < 64 || ilog2(N) > kSmemLog2Max + 1)
-    return fail(CFFT_ERR_INVALID_SIZE, "u64 product: N must be a power of two in [64, 8192]");
+  if (!is_pow2(N) || N < 64 || ilog2(N) > 16)
+    return fail(CFFT_ERR_INVALID_SIZE, "u64 product: N must be a power of two in [64, 65536]");
   const size_t n = N / 2;
   TuneVal tv;
   if (tune_lookup(2, N, &tv)) {  // measured before on this GPU model
@@ -302,7 +350,8 @@ cfft_status cfft_u64_product_plan_create_measure(size_t N, double seconds, cfft_
   else
     for (size_t b : {size_t(512), size_t(1024)})
       if (b <= n) bases.push_back(b);
-  const size_t count = (size_t)sm_count() * 8;
+  // eight products per SM up to N = 8192, the same number of CTAs for larger N
+  const size_t count = (size_t)sm_count() * std::max<size_t>(1, 8 * 8192 / std::max<size_t>(N, 8192));
   uint64_t *da = nullptr, *dout = nullptr;
   double* dbhat = nullptr;
   CFFT_CUDA_TRY(cudaMalloc(&da, count * N * sizeof(uint64_t)));

@@ -1,0 +1,174 @@
+// split_product.cuh -- one negacyclic u64 product spread over a thread-block
+// cluster of S = 2^LS CTAs, for products whose N/2-point transform does not
+// fit one CTA's shared memory (N > 8192) and for small batches.
+//
+// The transform of n = N/2 points has at least one unordered outer level; its
+// level 0 of radix R0 >= S splits it into R0 contiguous slices of m = n/R0
+// points that the later levels and the base treat independently (split.cuh).
+// CTA c owns part c: points [c*n/S, (c+1)*n/S), i.e. R0/S slices.
+//   1. CTA c folds and twists its own part of the input into shared memory.
+//   2. Cluster barrier.  Level 0 forward: CTA c computes, for every butterfly,
+//      the outputs that land in its part, reading the inputs from the parts of
+//      all CTAs through distributed shared memory.
+//   3. Cluster barrier (the peers are done reading the twisted parts).  Levels
+//      1.. and the base forward on the CTA's slices, the pointwise product with
+//      the resident operand (its permuted order is part-contiguous), the base
+//      and levels .. 1 inverse.
+//   4. Cluster barrier.  Level 0 inverse: CTA c takes butterflies
+//      [c*m/S, (c+1)*m/S), reads their inputs from the parts of all CTAs,
+//      untwists and rounds the R0 outputs of each and stores them.
+//   5. Cluster barrier, so that no CTA exits while a peer reads its memory.
+// Every butterfly and elementwise step does the operations of the one-CTA
+// product kernel on the same values, so results are bit-identical to it.
+#pragma once
+#include <cooperative_groups.h>
+
+#include "split.cuh"
+
+namespace cfft {
+
+constexpr int kSplitProdThreads = 256;
+
+// Step 2 for radix R0: outputs of part C (slots [C*R0/S, (C+1)*R0/S)) of every
+// butterfly, inputs from the twisted parts `src[j]` of the cluster's CTAs.
+template <int R0, int LS, int C>
+__device__ __forceinline__ void level0_fwd_from_peers(double2* const* src, int lm, double2* x,
+                                                      const double2* __restrict__ wl, int tid, int nth) {
+  constexpr int LR0 = Log2<R0>::v;
+  constexpr int SL = R0 >> LS;  // slices per part
+  for (int i = tid; i < (1 << lm); i += nth) {
+    c64 v[R0];
+#pragma unroll
+    for (int k = 0; k < R0; ++k) v[k] = ld(src[k / SL] + ((k % SL) << lm) + i);
+    Core<R0, true, 0>::run(v);
+    const double2* tw = wl + (R0 - 1) * i - 1;
+#pragma unroll
+    for (int k = 0; k < R0; ++k) {
+      if ((slot<R0>(k) >> (LR0 - LS)) == C) {
+        const c64 o = k == 0 ? v[0] : cmul(ldg(tw + k), v[k]);
+        st(x + ((slot<R0>(k) & (SL - 1)) << lm) + i, o);
+      }
+    }
+  }
+}
+
+// Step 4 for radix R0: butterflies [i0, i1), inputs from the parts `src[j]`,
+// outputs k*m + i untwisted by itw and rounded into the product's N words.
+template <int R0, int LS>
+__device__ __forceinline__ void level0_inv_untwist(double2* const* src, int lm, int log2n, int i0, int i1,
+                                                   const double2* __restrict__ wl, const double2* __restrict__ itw,
+                                                   uint64_t* __restrict__ op, int tid, int nth) {
+  constexpr int LR0 = Log2<R0>::v;
+  constexpr int SL = R0 >> LS;
+  const int n = 1 << log2n;
+  for (int i = i0 + tid; i < i1; i += nth) {
+    c64 v[R0];
+    const double2* tw = wl + (R0 - 1) * i - 1;
+    v[0] = ld(src[0] + i);
+#pragma unroll
+    for (int k = 1; k < R0; ++k) {
+      const int sl = slot<R0>(k);
+      v[k] = cmul(ldg(tw + k), ld(src[sl >> (LR0 - LS)] + ((sl & (SL - 1)) << lm) + i));
+    }
+    Core<R0, false, 0>::run(v);
+#pragma unroll
+    for (int k = 0; k < R0; ++k) {
+      const int j = (k << lm) + i;
+      const c64 t = cmul(ldg(itw + j), v[k]);
+      __stcs(op + j, round_half_up_mod64(t.re));
+      __stcs(op + j + n, round_half_up_mod64(t.im));
+    }
+  }
+}
+
+// One product per cluster of S CTAs (blockIdx.x >> LS).  Shared memory: two
+// buffers of n/S points.  a, out: N u64 per product; bhat: n c64 per operand
+// at bhat_stride (0: one shared operand).  Requires L.nlevels >= 1 and
+// 2^L.log2r[0] >= S.
+template <int ALGO, int LS>
+__global__ void __launch_bounds__(kSplitProdThreads) u64_product_split_kernel(
+    const uint64_t* __restrict__ a, const double2* __restrict__ bhat, long bhat_stride, uint64_t* __restrict__ out,
+    DevLevels L, const double2* __restrict__ w, const double2* __restrict__ winv, const double2* __restrict__ tw,
+    const double2* __restrict__ itw) {
+  namespace cg = cooperative_groups;
+  cg::cluster_group cl = cg::this_cluster();
+  extern __shared__ double2 smem[];
+  const int log2n = L.log2n[0];
+  const int log2c = log2n - LS;  // points per part
+  const int c = (int)(blockIdx.x & ((1 << LS) - 1));
+  const long prod = (long)(blockIdx.x >> LS);
+  double2* x = smem;
+  double2* y = smem + (1 << log2c);
+  const int tid = threadIdx.x, nth = blockDim.x;
+  const int n = 1 << log2n;
+
+  // 1. fold and twist this CTA's part into y
+  const uint64_t* ap = a + (prod << (log2n + 1));
+  const int base = c << log2c;
+  for (int j = tid; j < (1 << log2c); j += nth) {
+    const int g = base + j;
+    const c64 v{i64_to_f64_rne((int64_t)__ldcs(ap + g)), i64_to_f64_rne((int64_t)__ldcs(ap + g + n))};
+    st(y + j, cmul(ldg(tw + g), v));
+  }
+  double2* peer_y[1 << LS];
+#pragma unroll
+  for (int j = 0; j < (1 << LS); ++j) peer_y[j] = cl.map_shared_rank(y, (unsigned)j);
+  cl.sync();
+
+  // 2. level 0 forward, this part's outputs, into x
+  const int lr0 = L.log2r[0];
+  const int lm = log2n - lr0;
+  const double2* wl = w + L.w_off[0];
+  if (lr0 == 1) {
+    if constexpr (LS <= 1)
+      with_rank<LS>(c, [&](auto C) { level0_fwd_from_peers<2, LS, decltype(C)::value>(peer_y, lm, x, wl, tid, nth); });
+  } else if (lr0 == 2) {
+    if constexpr (LS <= 2)
+      with_rank<LS>(c, [&](auto C) { level0_fwd_from_peers<4, LS, decltype(C)::value>(peer_y, lm, x, wl, tid, nth); });
+  } else {
+    with_rank<LS>(c, [&](auto C) { level0_fwd_from_peers<8, LS, decltype(C)::value>(peer_y, lm, x, wl, tid, nth); });
+  }
+  cl.sync();  // every peer has read this CTA's y: it becomes the ping-pong buffer
+
+  // 3. the slices: forward, pointwise product, inverse
+  const int nsl = 1 << (lr0 - LS);
+  const FlatBuf r = unordered_t<true, 0, ALGO>(L, 1, nsl, FlatBuf{x}, FlatBuf{y}, w, tid, nth);
+  const double2* bp = bhat + prod * bhat_stride + base;
+  for (int j = tid; j < (1 << log2c); j += nth) st(r.p + j, cmul(ldg(bp + j), ld(r.p + j)));
+  __syncthreads();
+  double2* o = (r.p == x) ? y : x;
+  const FlatBuf s = unordered_t<false, 0, ALGO>(L, 1, nsl, r, FlatBuf{o}, winv, tid, nth);
+  double2* peer_s[1 << LS];
+#pragma unroll
+  for (int j = 0; j < (1 << LS); ++j) peer_s[j] = cl.map_shared_rank(s.p, (unsigned)j);
+  cl.sync();
+
+  // 4. level 0 inverse, untwist and round
+  const double2* wli = winv + L.winv_off[0];
+  const int per = (1 << lm) >> LS;
+  uint64_t* op = out + (prod << (log2n + 1));
+  if (lr0 == 1) {
+    if constexpr (LS <= 1) level0_inv_untwist<2, LS>(peer_s, lm, log2n, c * per, (c + 1) * per, wli, itw, op, tid, nth);
+  } else if (lr0 == 2) {
+    if constexpr (LS <= 2) level0_inv_untwist<4, LS>(peer_s, lm, log2n, c * per, (c + 1) * per, wli, itw, op, tid, nth);
+  } else {
+    level0_inv_untwist<8, LS>(peer_s, lm, log2n, c * per, (c + 1) * per, wli, itw, op, tid, nth);
+  }
+  cl.sync();  // 5.
+}
+
+// kernel pointers by base algorithm (kinst_split_prod_*.cu)
+const void* u64_product_split_ptr_0123(int algo, int ls);
+const void* u64_product_split_ptr_4567(int algo, int ls);
+
+template <int A>
+const void* split_product_ptr(int ls) {
+  switch (ls) {
+    case 1: return (const void*)u64_product_split_kernel<A, 1>;
+    case 2: return (const void*)u64_product_split_kernel<A, 2>;
+    case 3: return (const void*)u64_product_split_kernel<A, 3>;
+    default: return nullptr;
+  }
+}
+
+}  // namespace cfft

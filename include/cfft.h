@@ -201,9 +201,11 @@ cfft_status cfft_f128_negacyclic_inv(size_t n, size_t batch, double* re0, double
  * untwist, exact rounding back to the integer ring.
  *
  * u64: coefficients are read as i64, rounded with floor(x + 1/2) and reduced
- * mod 2^64.  N a power of two, 64 <= N <= 8192 for the fused kernel.  bhat holds N/2 c64 per
- * operand in the plan's permuted order; `bhat_stride` is 0 (one operand shared
- * by all products) or N/2 (one operand per product). */
+ * mod 2^64.  N a power of two, 64 <= N <= 65536 for the fused product: one CTA
+ * per product up to N = 8192, a thread-block cluster of 2..8 CTAs per product
+ * above (and for small batches, see cfft_u64_product_set_cluster_size).  bhat
+ * holds N/2 c64 per operand in the plan's permuted order; `bhat_stride` is 0
+ * (one operand shared by all products) or N/2 (one operand per product). */
 typedef struct cfft_u64_product_plan cfft_u64_product_plan;
 cfft_status cfft_u64_product_plan_create(size_t N, cfft_algo base_algo, size_t base_n, cfft_u64_product_plan** out);
 cfft_status cfft_u64_product_plan_create_measure(size_t N, double seconds_per_algo, cfft_u64_product_plan** out);
@@ -213,6 +215,12 @@ void cfft_u64_product_algo(const cfft_u64_product_plan* plan, cfft_algo* base_al
 /* Integer-pipe share of the butterfly additions, as cfft_ordered_set_int_adds. */
 cfft_status cfft_u64_product_set_int_adds(cfft_u64_product_plan* plan, int eighths);
 int cfft_u64_product_int_adds(const cfft_u64_product_plan* plan);
+/* CTAs per product (no counterpart in the reference): 0 chooses per call (a
+ * cluster when N > 8192, which needs one, or when the batch is too small to
+ * give every SM a product), 1 one CTA (N <= 8192), 2/4/8 force a cluster of
+ * that size, capped at what the plan allows (level 0's radix; N > 8192 also
+ * needs N/2/S <= 4096).  Results are bit-identical for every value. */
+cfft_status cfft_u64_product_set_cluster_size(cfft_u64_product_plan* plan, int ctas);
 /* b: `count` polynomials of N signed digits -> bhat: count * N/2 c64. */
 cfft_status cfft_u64_prepare_operand(const cfft_u64_product_plan* plan, const int64_t* b, double* bhat, size_t count,
                                      void* stream);

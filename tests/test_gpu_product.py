@@ -138,6 +138,53 @@ def test_u128_product_bit_exact(cuda, oracle, N):
     assert np.array_equal(out2.cpu().numpy().view(np.uint64), oracle.u128_schoolbook(a2, b[:1]))
 
 
+@pytest.mark.parametrize("N,algo,base", [(16384, 2, 1024), (16384, 5, 512), (32768, 2, 1024), (65536, 6, 1024)])
+def test_u64_product_large_N_on_a_cluster(cuda, oracle, N, algo, base):
+    """N > 8192: the fused product on a thread-block cluster, bit-exact against the CPU
+    pipeline, exact against the schoolbook when the sums fit in 53 bits."""
+    import concrete_fft as cf
+    torch = cuda
+    plan = cf.product.U64ProductPlan(N, algo, base)
+    count = 3
+    a = RNG.integers(0, 2 ** 64, (count, N), dtype=np.uint64)
+    b = RNG.integers(-2 ** 7, 2 ** 7, (count, N))
+    bhat = torch.empty((count, N // 2), dtype=torch.complex128, device="cuda")
+    plan.prepare_operand(torch.from_numpy(b).cuda(), bhat)
+    da = torch.from_numpy(a.view(np.int64)).cuda()
+    out = torch.empty_like(da)
+    plan.product(da, bhat, out)
+    want = oracle.u64_product(N, algo, base, a, bhat.cpu().numpy(), nthreads=0)
+    assert np.array_equal(out.cpu().numpy().view(np.uint64), want)
+    if N == 16384:
+        small = RNG.integers(-2 ** 20, 2 ** 20, (1, N)).astype(np.int64)
+        out1 = torch.empty((1, N), dtype=torch.int64, device="cuda")
+        plan.product(torch.from_numpy(small).cuda(), bhat[:1], out1)
+        exact = oracle.u64_schoolbook(small.view(np.uint64), b[:1])
+        assert np.array_equal(out1.cpu().numpy().view(np.uint64), exact)
+
+
+@pytest.mark.parametrize("N,base", [(4096, 1024), (8192, 1024), (8192, 256), (2048, 64)])
+def test_u64_product_cluster_sizes_bit_identical(cuda, N, base):
+    """Small batches on clusters of 2/4/8 CTAs give the one-CTA kernel's bits."""
+    import concrete_fft as cf
+    torch = cuda
+    for algo in (2, 3, 4):
+        plan = cf.product.U64ProductPlan(N, algo, base)
+        count = 5
+        a = torch.from_numpy(RNG.integers(0, 2 ** 64, (count, N), dtype=np.uint64).view(np.int64)).cuda()
+        b = torch.from_numpy(RNG.integers(-2 ** 7, 2 ** 7, (count, N))).cuda()
+        bhat = torch.empty((count, N // 2), dtype=torch.complex128, device="cuda")
+        plan.prepare_operand(b, bhat)
+        ref = torch.empty_like(a)
+        plan.set_cluster_size(1)
+        plan.product(a, bhat, ref)
+        for ctas in (2, 4, 8, 0):
+            plan.set_cluster_size(ctas)
+            out = torch.zeros_like(a)
+            plan.product(a, bhat, out)
+            assert torch.equal(out, ref), (N, base, algo, ctas)
+
+
 def test_u128_product_host_pipeline(cuda, oracle):
     """Host entry point for u128 products over several pipelined chunks, one operand per
     product, against the device entry point (itself checked against the oracle above)."""

@@ -3,12 +3,12 @@
 #include "split_product.cuh"
 
 namespace cfft {
-const void* u64_product_split_ptr_4567(int algo, int ls) {
+const void* u64_product_split_ptr_4567(int algo, int ls, bool big) {
   switch (algo) {
-    case 4: return split_product_ptr<4>(ls);
-    case 5: return split_product_ptr<5>(ls);
-    case 6: return split_product_ptr<6>(ls);
-    case 7: return split_product_ptr<7>(ls);
+    case 4: return split_product_ptr<4>(ls, big);
+    case 5: return split_product_ptr<5>(ls, big);
+    case 6: return split_product_ptr<6>(ls, big);
+    case 7: return split_product_ptr<7>(ls, big);
     default: return nullptr;
   }
 }

@@ -147,8 +147,10 @@ int product_split_log2(const cfft_u64_product_plan* p, size_t count, bool* ok) {
 
 cfft_status launch_split_product(const cfft_u64_product_plan* plan, int ls, const uint64_t* a, const double* bhat,
                                  size_t bhat_stride, uint64_t* out, size_t count, cudaStream_t stream) {
-  const void* fn = plan->base_algo < 4 ? u64_product_split_ptr_0123(plan->base_algo, ls)
-                                       : u64_product_split_ptr_4567(plan->base_algo, ls);
+  const size_t part = plan->n >> ls;
+  const bool big = part > 2048;  // 4096 points per CTA: one CTA per SM, 512 threads
+  const void* fn = plan->base_algo < 4 ? u64_product_split_ptr_0123(plan->base_algo, ls, big)
+                                       : u64_product_split_ptr_4567(plan->base_algo, ls, big);
   const size_t smem = 2 * (plan->n >> ls) * sizeof(double2);
   if ((count << ls) > 0x7fffffffUL) return fail(CFFT_ERR_INVALID_SIZE, "batch too large");
   DevLevels L = plan->dlv;
@@ -156,7 +158,10 @@ cfft_status launch_split_product(const cfft_u64_product_plan* plan, int ls, cons
   const double2* bh = (const double2*)bhat;
   void* args[] = {(void*)&a, (void*)&bh, &stride, (void*)&out, &L, (void*)&plan->d_w, (void*)&plan->d_winv,
                   (void*)&plan->d_tw, (void*)&plan->d_itw};
-  return launch_kernel_cluster(fn, (int)(count << ls), kSplitProdThreads, 1 << ls, args, smem, stream);
+  // 128 threads (several CTAs per SM) for parts up to 1024 points, 256 for 2048
+  // (shared memory allows 3 CTAs per SM), 512 for 4096 (one CTA per SM)
+  const int threads = part <= 1024 ? 128 : (part <= 2048 ? kSplitProdThreads : kSplitProdThreadsBig);
+  return launch_kernel_cluster(fn, (int)(count << ls), threads, 1 << ls, args, smem, stream);
 }
 
 }  // namespace

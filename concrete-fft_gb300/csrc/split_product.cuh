@@ -7,9 +7,10 @@
 // points that the later levels and the base treat independently (split.cuh).
 // CTA c owns part c: points [c*n/S, (c+1)*n/S), i.e. R0/S slices.
 //   1. CTA c folds and twists its own part of the input into shared memory.
-//   2. Cluster barrier.  Level 0 forward: CTA c computes, for every butterfly,
-//      the outputs that land in its part, reading the inputs from the parts of
-//      all CTAs through distributed shared memory.
+//   2. Cluster barrier.  Level 0 forward: CTA c takes butterflies
+//      [c*m/S, (c+1)*m/S), reads their inputs from the parts of all CTAs and
+//      stores each output into the part that owns its slot, both through
+//      distributed shared memory.
 //   3. Cluster barrier (the peers are done reading the twisted parts).  Levels
 //      1.. and the base forward on the CTA's slices, the pointwise product with
 //      the resident operand (its permuted order is part-contiguous), the base
@@ -27,16 +28,21 @@
 
 namespace cfft {
 
+// CTA sizes of the split product kernel: up to 256 threads (registers for
+// several CTAs per SM), and a 512-thread variant for parts of 4096 points,
+// where shared memory allows one CTA per SM.
 constexpr int kSplitProdThreads = 256;
+constexpr int kSplitProdThreadsBig = 512;
 
-// Step 2 for radix R0: outputs of part C (slots [C*R0/S, (C+1)*R0/S)) of every
-// butterfly, inputs from the twisted parts `src[j]` of the cluster's CTAs.
-template <int R0, int LS, int C>
-__device__ __forceinline__ void level0_fwd_from_peers(double2* const* src, int lm, double2* x,
-                                                      const double2* __restrict__ wl, int tid, int nth) {
+// Step 2 for radix R0: butterflies [i0, i1), inputs from the twisted parts
+// `src[j]` of the cluster's CTAs, each output stored into the part that owns
+// its slot (`dst[j]`, distributed shared memory).
+template <int R0, int LS>
+__device__ __forceinline__ void level0_fwd_scatter(double2* const* src, double2* const* dst, int lm, int i0, int i1,
+                                                   const double2* __restrict__ wl, int tid, int nth) {
   constexpr int LR0 = Log2<R0>::v;
   constexpr int SL = R0 >> LS;  // slices per part
-  for (int i = tid; i < (1 << lm); i += nth) {
+  for (int i = i0 + tid; i < i1; i += nth) {
     c64 v[R0];
 #pragma unroll
     for (int k = 0; k < R0; ++k) v[k] = ld(src[k / SL] + ((k % SL) << lm) + i);
@@ -44,10 +50,9 @@ __device__ __forceinline__ void level0_fwd_from_peers(double2* const* src, int l
     const double2* tw = wl + (R0 - 1) * i - 1;
 #pragma unroll
     for (int k = 0; k < R0; ++k) {
-      if ((slot<R0>(k) >> (LR0 - LS)) == C) {
-        const c64 o = k == 0 ? v[0] : cmul(ldg(tw + k), v[k]);
-        st(x + ((slot<R0>(k) & (SL - 1)) << lm) + i, o);
-      }
+      const c64 o = k == 0 ? v[0] : cmul(ldg(tw + k), v[k]);
+      const int sl = slot<R0>(k);
+      st(dst[sl >> (LR0 - LS)] + ((sl & (SL - 1)) << lm) + i, o);
     }
   }
 }
@@ -85,8 +90,8 @@ __device__ __forceinline__ void level0_inv_untwist(double2* const* src, int lm, 
 // buffers of n/S points.  a, out: N u64 per product; bhat: n c64 per operand
 // at bhat_stride (0: one shared operand).  Requires L.nlevels >= 1 and
 // 2^L.log2r[0] >= S.
-template <int ALGO, int LS>
-__global__ void __launch_bounds__(kSplitProdThreads) u64_product_split_kernel(
+template <int ALGO, int LS, int MAXT>
+__global__ void __launch_bounds__(MAXT) u64_product_split_kernel(
     const uint64_t* __restrict__ a, const double2* __restrict__ bhat, long bhat_stride, uint64_t* __restrict__ out,
     DevLevels L, const double2* __restrict__ w, const double2* __restrict__ winv, const double2* __restrict__ tw,
     const double2* __restrict__ itw) {
@@ -111,24 +116,27 @@ __global__ void __launch_bounds__(kSplitProdThreads) u64_product_split_kernel(
     st(y + j, cmul(ldg(tw + g), v));
   }
   double2* peer_y[1 << LS];
+  double2* peer_x[1 << LS];
 #pragma unroll
-  for (int j = 0; j < (1 << LS); ++j) peer_y[j] = cl.map_shared_rank(y, (unsigned)j);
+  for (int j = 0; j < (1 << LS); ++j) {
+    peer_y[j] = cl.map_shared_rank(y, (unsigned)j);
+    peer_x[j] = cl.map_shared_rank(x, (unsigned)j);
+  }
   cl.sync();
 
-  // 2. level 0 forward, this part's outputs, into x
+  // 2. level 0 forward: 1/S of the butterflies, each output into its owner's x
   const int lr0 = L.log2r[0];
   const int lm = log2n - lr0;
   const double2* wl = w + L.w_off[0];
+  const int per = (1 << lm) >> LS;
   if (lr0 == 1) {
-    if constexpr (LS <= 1)
-      with_rank<LS>(c, [&](auto C) { level0_fwd_from_peers<2, LS, decltype(C)::value>(peer_y, lm, x, wl, tid, nth); });
+    if constexpr (LS <= 1) level0_fwd_scatter<2, LS>(peer_y, peer_x, lm, c * per, (c + 1) * per, wl, tid, nth);
   } else if (lr0 == 2) {
-    if constexpr (LS <= 2)
-      with_rank<LS>(c, [&](auto C) { level0_fwd_from_peers<4, LS, decltype(C)::value>(peer_y, lm, x, wl, tid, nth); });
+    if constexpr (LS <= 2) level0_fwd_scatter<4, LS>(peer_y, peer_x, lm, c * per, (c + 1) * per, wl, tid, nth);
   } else {
-    with_rank<LS>(c, [&](auto C) { level0_fwd_from_peers<8, LS, decltype(C)::value>(peer_y, lm, x, wl, tid, nth); });
+    level0_fwd_scatter<8, LS>(peer_y, peer_x, lm, c * per, (c + 1) * per, wl, tid, nth);
   }
-  cl.sync();  // every peer has read this CTA's y: it becomes the ping-pong buffer
+  cl.sync();  // every part's x is complete and every peer has read this CTA's y (now the ping-pong buffer)
 
   // 3. the slices: forward, pointwise product, inverse
   const int nsl = 1 << (lr0 - LS);
@@ -145,7 +153,6 @@ __global__ void __launch_bounds__(kSplitProdThreads) u64_product_split_kernel(
 
   // 4. level 0 inverse, untwist and round
   const double2* wli = winv + L.winv_off[0];
-  const int per = (1 << lm) >> LS;
   uint64_t* op = out + (prod << (log2n + 1));
   if (lr0 == 1) {
     if constexpr (LS <= 1) level0_inv_untwist<2, LS>(peer_s, lm, log2n, c * per, (c + 1) * per, wli, itw, op, tid, nth);
@@ -158,15 +165,17 @@ __global__ void __launch_bounds__(kSplitProdThreads) u64_product_split_kernel(
 }
 
 // kernel pointers by base algorithm (kinst_split_prod_*.cu)
-const void* u64_product_split_ptr_0123(int algo, int ls);
-const void* u64_product_split_ptr_4567(int algo, int ls);
+// (big: the 512-thread variant, S = 8 only)
+const void* u64_product_split_ptr_0123(int algo, int ls, bool big);
+const void* u64_product_split_ptr_4567(int algo, int ls, bool big);
 
 template <int A>
-const void* split_product_ptr(int ls) {
+const void* split_product_ptr(int ls, bool big) {
+  if (big) return ls == 3 ? (const void*)u64_product_split_kernel<A, 3, kSplitProdThreadsBig> : nullptr;
   switch (ls) {
-    case 1: return (const void*)u64_product_split_kernel<A, 1>;
-    case 2: return (const void*)u64_product_split_kernel<A, 2>;
-    case 3: return (const void*)u64_product_split_kernel<A, 3>;
+    case 1: return (const void*)u64_product_split_kernel<A, 1, kSplitProdThreads>;
+    case 2: return (const void*)u64_product_split_kernel<A, 2, kSplitProdThreads>;
+    case 3: return (const void*)u64_product_split_kernel<A, 3, kSplitProdThreads>;
     default: return nullptr;
   }
 }

@@ -146,7 +146,8 @@ int product_split_log2(const cfft_u64_product_plan* p, size_t count, bool* ok) {
 }
 
 cfft_status launch_split_product(const cfft_u64_product_plan* plan, int ls, const uint64_t* a, const double* bhat,
-                                 size_t bhat_stride, uint64_t* out, size_t count, cudaStream_t stream) {
+                                 size_t bhat_stride, uint64_t* out, size_t count, cudaStream_t stream,
+                                 const cfft_product_item* items = nullptr) {
   const size_t part = plan->n >> ls;
   const bool big = part > 2048;  // 4096 points per CTA: one CTA per SM, 512 threads
   const void* fn = plan->base_algo < 4 ? u64_product_split_ptr_0123(plan->base_algo, ls, big)
@@ -156,8 +157,8 @@ cfft_status launch_split_product(const cfft_u64_product_plan* plan, int ls, cons
   DevLevels L = plan->dlv;
   long stride = (long)bhat_stride;
   const double2* bh = (const double2*)bhat;
-  void* args[] = {(void*)&a, (void*)&bh, &stride, (void*)&out, &L, (void*)&plan->d_w, (void*)&plan->d_winv,
-                  (void*)&plan->d_tw, (void*)&plan->d_itw};
+  void* args[] = {(void*)&a, (void*)&bh, &stride, (void*)&out, (void*)&items, &L, (void*)&plan->d_w,
+                  (void*)&plan->d_winv, (void*)&plan->d_tw, (void*)&plan->d_itw};
   // 128 threads (several CTAs per SM) for parts up to 1024 points, 256 for 2048
   // (shared memory allows 3 CTAs per SM), 512 for 4096 (one CTA per SM)
   const int threads = part <= 1024 ? 128 : (part <= 2048 ? kSplitProdThreads : kSplitProdThreadsBig);
@@ -165,6 +166,22 @@ cfft_status launch_split_product(const cfft_u64_product_plan* plan, int ls, cons
 }
 
 }  // namespace
+
+// Products given as device items (all of the plan's N) on the largest cluster
+// the plan allows, for latency: the serving loop's large products.
+bool cfft::u64_product_splittable(const cfft_u64_product_plan* plan) {
+  const int max_ls = plan->lv.nlevels >= 1 ? std::min(3, plan->lv.log2r[0]) : 0;
+  const int min_ls = std::max(0, ilog2(plan->n) - kSmemLog2Max);
+  return max_ls >= 1 && min_ls <= max_ls;
+}
+
+cfft_status cfft::u64_product_split_items(const cfft_u64_product_plan* plan, const cfft_product_item* items,
+                                          size_t count, void* stream) {
+  if (!u64_product_splittable(plan)) return fail(CFFT_ERR_INVALID_SIZE, "product size cannot be split over a cluster");
+  if (count == 0) return CFFT_OK;
+  const int max_ls = std::min(3, plan->lv.log2r[0]);
+  return launch_split_product(plan, max_ls, nullptr, nullptr, 0, nullptr, count, (cudaStream_t)stream, items);
+}
 
 void cfft::u64_product_tables(const cfft_u64_product_plan* p, const void** w, const void** winv, const void** tw,
                               const void** itw) {

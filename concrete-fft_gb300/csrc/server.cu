@@ -11,7 +11,10 @@
 // while the device output ring has room (the memory gate), and as soon as one
 // of `max_inflight` launch slots is free, launches everything admitted since
 // the previous launch as one product-engine run on that slot's stream,
-// followed by the copy of the results into a pinned host ring.  Launch slots
+// followed by the copy of the results into a pinned host ring.  Products of
+// N >= 8192 (cluster_log2N) leave the engine launch: a second stream of the
+// slot runs them one per thread-block cluster (split_product.cuh), beside the
+// engine, so a large product takes 1/4-1/8 of its one-CTA time.  Launch slots
 // run concurrently, so requests that arrive while others are on the GPU are
 // admitted and overlap with them.  A request is done when its launch's event
 // has completed; its latency is measured on the host clock from its arrival.
@@ -68,7 +71,9 @@ struct SizePool {
 
 struct Slot {
   cudaStream_t stream = nullptr;
+  cudaStream_t stream2 = nullptr;  // cluster launches of the slot's large products
   cudaEvent_t done = nullptr;
+  cudaEvent_t items_ready = nullptr, big_done = nullptr;
   unsigned int* counter = nullptr;
   double* ws = nullptr;
   cfft_product_item* d_items = nullptr;
@@ -178,7 +183,10 @@ void free_server(cfft_server* s) {
   }
   for (auto& sl : s->slots) {
     if (sl.stream) cudaStreamDestroy(sl.stream);
+    if (sl.stream2) cudaStreamDestroy(sl.stream2);
     if (sl.done) cudaEventDestroy(sl.done);
+    if (sl.items_ready) cudaEventDestroy(sl.items_ready);
+    if (sl.big_done) cudaEventDestroy(sl.big_done);
     if (sl.counter) cudaFree(sl.counter);
     if (sl.ws) cudaFree(sl.ws);
     if (sl.d_items) cudaFree(sl.d_items);
@@ -267,7 +275,10 @@ cfft_status cfft_server_create(const cfft_product_engine* engine, const uint32_t
     const size_t ws = cfft_product_engine_workspace_bytes(engine);
     for (auto& sl : s->slots) {
       if (cudaStreamCreateWithFlags(&sl.stream, cudaStreamNonBlocking) != cudaSuccess ||
+          cudaStreamCreateWithFlags(&sl.stream2, cudaStreamNonBlocking) != cudaSuccess ||
           cudaEventCreateWithFlags(&sl.done, cudaEventDisableTiming) != cudaSuccess ||
+          cudaEventCreateWithFlags(&sl.items_ready, cudaEventDisableTiming) != cudaSuccess ||
+          cudaEventCreateWithFlags(&sl.big_done, cudaEventDisableTiming) != cudaSuccess ||
           cudaMalloc(&sl.counter, 64) != cudaSuccess || (ws && cudaMalloc(&sl.ws, ws) != cudaSuccess)) {
         st = fail(CFFT_ERR_OUT_OF_MEMORY, "server launch slots");
         break;
@@ -332,6 +343,14 @@ cfft_status cfft_server_run(cfft_server* s, const cfft_serve_config* cfg, cfft_s
   uint64_t deferred = 0, launches = 0;
   const auto t0 = std::chrono::steady_clock::now();
   const uint32_t nslots = std::max<uint32_t>(1, std::min<uint32_t>(c.max_inflight ? c.max_inflight : kSlots, kSlots));
+  // products of at least this size run one per thread-block cluster (only sizes whose
+  // plan has an unordered outer level can)
+  const uint32_t big_log2N = c.cluster_log2N ? c.cluster_log2N : 13;
+  bool on_cluster[18] = {};
+  for (uint32_t lN = big_log2N; lN <= 17; ++lN) {
+    const cfft_u64_product_plan* p = cfft_product_engine_plan(s->engine, lN);
+    on_cluster[lN] = p && u64_product_splittable(p);
+  }
   size_t done_count = 0;
 
   auto record = [&](size_t ri) {
@@ -405,15 +424,43 @@ cfft_status cfft_server_run(cfft_server* s, const cfft_serve_config* cfg, cfft_s
           for (size_t ri : batch) nitems += reqs[ri].d.nprod;
           cfft_status st = ensure_items(sl, nitems);
           if (st != CFFT_OK) return st;
+          // item records: the engine's products first, then the large ones grouped by N
           size_t at = 0;
-          for (size_t ri : batch) {
-            fill_items(s, reqs[ri].d, s->d_ring + reqs[ri].ring_off, sl.h_items + at);
-            at += reqs[ri].d.nprod;
+          for (size_t ri : batch)
+            if (!on_cluster[reqs[ri].d.log2N]) {
+              fill_items(s, reqs[ri].d, s->d_ring + reqs[ri].ring_off, sl.h_items + at);
+              at += reqs[ri].d.nprod;
+            }
+          const size_t nsmall = at;
+          size_t group_first[18] = {}, group_count[18] = {};
+          for (uint32_t lN = 0; lN <= 17; ++lN) {
+            if (!on_cluster[lN]) continue;
+            group_first[lN] = at;
+            for (size_t ri : batch)
+              if (reqs[ri].d.log2N == lN) {
+                fill_items(s, reqs[ri].d, s->d_ring + reqs[ri].ring_off, sl.h_items + at);
+                at += reqs[ri].d.nprod;
+              }
+            group_count[lN] = at - group_first[lN];
           }
           CFFT_CUDA_TRY(cudaMemcpyAsync(sl.d_items, sl.h_items, nitems * sizeof(cfft_product_item),
                                         cudaMemcpyHostToDevice, sl.stream));
-          st = cfft_product_engine_run(s->engine, sl.d_items, nitems, sl.counter, sl.ws, sl.stream);
-          if (st != CFFT_OK) return st;
+          if (nsmall < nitems) {
+            CFFT_CUDA_TRY(cudaEventRecord(sl.items_ready, sl.stream));
+            CFFT_CUDA_TRY(cudaStreamWaitEvent(sl.stream2, sl.items_ready, 0));
+            for (uint32_t lN = 0; lN <= 17; ++lN) {
+              if (!group_count[lN]) continue;
+              st = u64_product_split_items(cfft_product_engine_plan(s->engine, lN), sl.d_items + group_first[lN],
+                                           group_count[lN], sl.stream2);
+              if (st != CFFT_OK) return st;
+            }
+            CFFT_CUDA_TRY(cudaEventRecord(sl.big_done, sl.stream2));
+          }
+          if (nsmall) {
+            st = cfft_product_engine_run(s->engine, sl.d_items, nsmall, sl.counter, sl.ws, sl.stream);
+            if (st != CFFT_OK) return st;
+          }
+          if (nsmall < nitems) CFFT_CUDA_TRY(cudaStreamWaitEvent(sl.stream, sl.big_done, 0));
           // results back to the pinned host ring: the batch's requests were allocated in
           // admission order, so they are contiguous (256-byte aligned) except across the
           // wrap; one copy per contiguous run

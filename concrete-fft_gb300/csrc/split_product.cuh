@@ -24,6 +24,7 @@
 #pragma once
 #include <cooperative_groups.h>
 
+#include "../../include/cfft.h"
 #include "split.cuh"
 
 namespace cfft {
@@ -88,13 +89,14 @@ __device__ __forceinline__ void level0_inv_untwist(double2* const* src, int lm, 
 
 // One product per cluster of S CTAs (blockIdx.x >> LS).  Shared memory: two
 // buffers of n/S points.  a, out: N u64 per product; bhat: n c64 per operand
-// at bhat_stride (0: one shared operand).  Requires L.nlevels >= 1 and
-// 2^L.log2r[0] >= S.
+// at bhat_stride (0: one shared operand).  When `items` is not null, product p
+// takes its three pointers from items[p] instead (all of the plan's N).
+// Requires L.nlevels >= 1 and 2^L.log2r[0] >= S.
 template <int ALGO, int LS, int MAXT>
 __global__ void __launch_bounds__(MAXT) u64_product_split_kernel(
     const uint64_t* __restrict__ a, const double2* __restrict__ bhat, long bhat_stride, uint64_t* __restrict__ out,
-    DevLevels L, const double2* __restrict__ w, const double2* __restrict__ winv, const double2* __restrict__ tw,
-    const double2* __restrict__ itw) {
+    const cfft_product_item* __restrict__ items, DevLevels L, const double2* __restrict__ w,
+    const double2* __restrict__ winv, const double2* __restrict__ tw, const double2* __restrict__ itw) {
   namespace cg = cooperative_groups;
   cg::cluster_group cl = cg::this_cluster();
   extern __shared__ double2 smem[];
@@ -107,8 +109,20 @@ __global__ void __launch_bounds__(MAXT) u64_product_split_kernel(
   const int tid = threadIdx.x, nth = blockDim.x;
   const int n = 1 << log2n;
 
+  const uint64_t* ap;
+  const double2* bprod;
+  uint64_t* op;
+  if (items) {
+    ap = items[prod].a;
+    bprod = (const double2*)items[prod].bhat;
+    op = items[prod].out;
+  } else {
+    ap = a + (prod << (log2n + 1));
+    bprod = bhat + prod * bhat_stride;
+    op = out + (prod << (log2n + 1));
+  }
+
   // 1. fold and twist this CTA's part into y
-  const uint64_t* ap = a + (prod << (log2n + 1));
   const int base = c << log2c;
   for (int j = tid; j < (1 << log2c); j += nth) {
     const int g = base + j;
@@ -141,7 +155,7 @@ __global__ void __launch_bounds__(MAXT) u64_product_split_kernel(
   // 3. the slices: forward, pointwise product, inverse
   const int nsl = 1 << (lr0 - LS);
   const FlatBuf r = unordered_t<true, 0, ALGO>(L, 1, nsl, FlatBuf{x}, FlatBuf{y}, w, tid, nth);
-  const double2* bp = bhat + prod * bhat_stride + base;
+  const double2* bp = bprod + base;
   for (int j = tid; j < (1 << log2c); j += nth) st(r.p + j, cmul(ldg(bp + j), ld(r.p + j)));
   __syncthreads();
   double2* o = (r.p == x) ? y : x;
@@ -153,7 +167,6 @@ __global__ void __launch_bounds__(MAXT) u64_product_split_kernel(
 
   // 4. level 0 inverse, untwist and round
   const double2* wli = winv + L.winv_off[0];
-  uint64_t* op = out + (prod << (log2n + 1));
   if (lr0 == 1) {
     if constexpr (LS <= 1) level0_inv_untwist<2, LS>(peer_s, lm, log2n, c * per, (c + 1) * per, wli, itw, op, tid, nth);
   } else if (lr0 == 2) {

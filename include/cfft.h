@@ -311,7 +311,8 @@ typedef struct cfft_serve_config {
   uint32_t plain;       /* 1: unbatched comparator */
   uint32_t max_inflight; /* concurrent launches, 1..3 */
   uint32_t record_every; /* keep the outputs of every k-th request (0: none) */
-  uint32_t reserved;
+  uint32_t cluster_log2N; /* batched mode: products with N >= 2^cluster_log2N run one per
+                             thread-block cluster beside the engine launch (0: 13; > 17: never) */
 } cfft_serve_config;
 typedef struct cfft_serve_stats {
   uint64_t requests, products, launches, deferred_admissions;

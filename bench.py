@@ -503,6 +503,22 @@ def run_ordered(args):
 
     ms256, clocks = timed(torch, step256, args.steps, args.warmup, local, world)
     ms1, _ = timed(torch, step1, args.steps, args.warmup, local, world)
+    # one unordered transform of 4096..32768 points (base 1024), fwd then inv: split over a
+    # cluster (automatic) against one CTA / the global-level path
+    large = {}
+    for lgn in (12, 13, 14, 15):
+        up = cf.unordered.Plan(1 << lgn, cf.unordered.Method.UserProvided(cf.FftAlgo.Dif4, 1024))
+        u1 = torch.from_numpy(rng.uniform(-1, 1, (1, 1 << lgn)) + 0j).cuda()
+
+        def stepu():
+            up.fwd(u1)
+            up.inv(u1)
+        row = {}
+        for ctas, name in ((0, "split"), (1, "one_cta_or_levels")):
+            up.set_cluster_size(ctas)
+            msu, _ = timed(torch, stepu, max(10, args.steps // 4), args.warmup, local, world)
+            row[name] = round(msu * 1e3 / max(10, args.steps // 4), 2)
+        large[1 << lgn] = row
     # the same batch-1 fwd+inv captured by the caller into a CUDA graph and replayed
     graph = torch.cuda.CUDAGraph()
     with torch.cuda.graph(graph):
@@ -545,6 +561,7 @@ def run_ordered(args):
         "config": {"workload": "ordered::Plan n=1024 batch 256", "algo": plan.algo().name,
                    "batch1_us_per_fwd_inv": ms1 * 1e3 / args.steps,
                    "batch1_us_per_fwd_inv_graph_replay": ms1g * 1e3 / args.steps,
+                   "unordered_batch1_us_per_fwd_inv_by_n": large,
                    "us_per_fwd_inv_by_batch_and_ctas_per_transform": sweep},
         "roofline": {"bound": "hbm", "achieved": 256 * 65536 / per / 1e9, "peak": measured_peaks()[0]["hbm_gbs"],
                      "unit": "GB/s", "frac": 256 * 65536 / per / 1e9 / measured_peaks()[0]["hbm_gbs"],
@@ -687,7 +704,7 @@ def run_u64_large(args):
     peak = fp64_peak(cf)
     rows = {}
     clocks = None
-    for N in (16384, 32768, 65536):
+    for N in ((16384,) if args.profile_case else (16384, 32768, 65536)):
         count = 8192 * 2048 // N
         plan = cf.product.U64ProductPlan(N, cf.FftAlgo.Dif4, 1024)
         rng = np.random.default_rng(N)

@@ -18,8 +18,12 @@
 // place, so a CTA stores only after every CTA of its cluster has read (a
 // cluster barrier split into an arrive after the reads and a wait before the
 // stores).  Used for DIF-structured transforms (ordered DIF algorithms, the
-// unordered base with no outer levels) and for the forward unordered
-// transform with levels.
+// unordered base with no outer levels).
+//
+// The forward unordered transform with levels exchanges once instead: each
+// CTA loads its own part, and level 0 takes 1/S of the butterflies per CTA,
+// reading inputs from and storing outputs to the parts that hold them
+// (distributed shared memory), so no arithmetic is repeated.
 //
 // "Last" kernels: each CTA loads its part and runs everything but the last
 // step alone; the last step reads the other parts through distributed shared
@@ -104,24 +108,25 @@ __device__ __forceinline__ FlatBuf dit_before_last(int log2n, int ls, FlatBuf x,
   return cur;
 }
 
-// Forward unordered level 0 of radix R0, outputs of part C only (slots
-// [C*R0/S, (C+1)*R0/S)), read from global g, written compacted to x.
-template <int R0, int LS, int C>
-__device__ __forceinline__ void level0_first(const double2* g, int lm, double2* x, const double2* __restrict__ wl,
-                                             int tid, int nth) {
+// Forward unordered level 0 of radix R0 for butterflies [i0, i1): inputs from
+// the parts `src[j]` (part j holds slices [j*R0/S, (j+1)*R0/S)), each output
+// stored into the part that owns its slot (`dst[j]`).
+template <int R0, int LS>
+__device__ __forceinline__ void level0_scatter(double2* const* src, double2* const* dst, int lm, int i0, int i1,
+                                               const double2* __restrict__ wl, int tid, int nth) {
   constexpr int LR0 = Log2<R0>::v;
-  for (int i = tid; i < (1 << lm); i += nth) {
+  constexpr int SL = R0 >> LS;  // slices per part
+  for (int i = i0 + tid; i < i1; i += nth) {
     c64 v[R0];
 #pragma unroll
-    for (int k = 0; k < R0; ++k) v[k] = ld(g + (k << lm) + i);
+    for (int k = 0; k < R0; ++k) v[k] = ld(src[k / SL] + ((k % SL) << lm) + i);
     Core<R0, true, 0>::run(v);
     const double2* tw = wl + (R0 - 1) * i - 1;
 #pragma unroll
     for (int k = 0; k < R0; ++k) {
-      if ((slot<R0>(k) >> (LR0 - LS)) == C) {
-        const c64 o = k == 0 ? v[0] : cmul(ldg(tw + k), v[k]);
-        st(x + ((slot<R0>(k) & ((R0 >> LS) - 1)) << lm) + i, o);
-      }
+      const c64 o = k == 0 ? v[0] : cmul(ldg(tw + k), v[k]);
+      const int sl = slot<R0>(k);
+      st(dst[sl >> (LR0 - LS)] + ((sl & (SL - 1)) << lm) + i, o);
     }
   }
 }
@@ -222,24 +227,37 @@ __global__ void __launch_bounds__(256) c64_split_kernel(double2* data, DevLevels
     }
     cl.sync();
   } else if constexpr (MODE == 1 && !LAST) {
-    // forward unordered: level 0 from global, own slots only; then levels
-    // 1.. and the base on the R0/S slices of this part.
+    // forward unordered: each CTA loads its part; level 0 takes 1/S of the
+    // butterflies per CTA, inputs from every part and each output stored into
+    // the part that owns its slot (distributed shared memory); then levels 1..
+    // and the base on the R0/S slices of this part.
+    namespace cg = cooperative_groups;
+    cg::cluster_group cl = cg::this_cluster();
+    const double2* gp = g + ((long)c << log2c);
+    for (int j = tid; j < (1 << log2c); j += nth) ys[j] = gp[j];
+    double2* peer_y[S];
+    double2* peer_x[S];
+#pragma unroll
+    for (int j = 0; j < S; ++j) {
+      peer_y[j] = cl.map_shared_rank(ys, (unsigned)j);
+      peer_x[j] = cl.map_shared_rank(xs, (unsigned)j);
+    }
+    cl.sync();
     const int lr0 = L.log2r[0];
     const int lm = log2n - lr0;
     const double2* wl = w + L.w_off[0];
+    const int per = (1 << lm) >> LS;
     if (lr0 == 1) {
-      if constexpr (LS <= 1) with_rank<LS>(c, [&](auto C) { level0_first<2, LS, decltype(C)::value>(g, lm, xs, wl, tid, nth); });
+      if constexpr (LS <= 1) level0_scatter<2, LS>(peer_y, peer_x, lm, c * per, (c + 1) * per, wl, tid, nth);
     } else if (lr0 == 2) {
-      if constexpr (LS <= 2) with_rank<LS>(c, [&](auto C) { level0_first<4, LS, decltype(C)::value>(g, lm, xs, wl, tid, nth); });
+      if constexpr (LS <= 2) level0_scatter<4, LS>(peer_y, peer_x, lm, c * per, (c + 1) * per, wl, tid, nth);
     } else {
-      with_rank<LS>(c, [&](auto C) { level0_first<8, LS, decltype(C)::value>(g, lm, xs, wl, tid, nth); });
+      level0_scatter<8, LS>(peer_y, peer_x, lm, c * per, (c + 1) * per, wl, tid, nth);
     }
-    __syncthreads();
-    cluster_arrive();
+    cl.sync();  // every part's xs is complete, and every peer is done reading this CTA's ys
     const FlatBuf r = unordered_t<true, 0, ALGO>(L, 1, 1 << (lr0 - LS), FlatBuf{xs}, FlatBuf{ys}, w, tid, nth);
-    cluster_wait();
-    double2* gp = g + ((long)c << log2c);
-    for (int j = tid; j < (1 << log2c); j += nth) gp[j] = r.p[j];
+    double2* gw = g + ((long)c << log2c);
+    for (int j = tid; j < (1 << log2c); j += nth) gw[j] = r.p[j];
   } else {
     // inverse unordered: this part's slices through the base and levels
     // nlevels-1 .. 1, then level 0 over the cluster.

@@ -35,29 +35,6 @@ namespace cfft {
 constexpr int kSplitProdThreads = 256;
 constexpr int kSplitProdThreadsBig = 512;
 
-// Step 2 for radix R0: butterflies [i0, i1), inputs from the twisted parts
-// `src[j]` of the cluster's CTAs, each output stored into the part that owns
-// its slot (`dst[j]`, distributed shared memory).
-template <int R0, int LS>
-__device__ __forceinline__ void level0_fwd_scatter(double2* const* src, double2* const* dst, int lm, int i0, int i1,
-                                                   const double2* __restrict__ wl, int tid, int nth) {
-  constexpr int LR0 = Log2<R0>::v;
-  constexpr int SL = R0 >> LS;  // slices per part
-  for (int i = i0 + tid; i < i1; i += nth) {
-    c64 v[R0];
-#pragma unroll
-    for (int k = 0; k < R0; ++k) v[k] = ld(src[k / SL] + ((k % SL) << lm) + i);
-    Core<R0, true, 0>::run(v);
-    const double2* tw = wl + (R0 - 1) * i - 1;
-#pragma unroll
-    for (int k = 0; k < R0; ++k) {
-      const c64 o = k == 0 ? v[0] : cmul(ldg(tw + k), v[k]);
-      const int sl = slot<R0>(k);
-      st(dst[sl >> (LR0 - LS)] + ((sl & (SL - 1)) << lm) + i, o);
-    }
-  }
-}
-
 // Step 4 for radix R0: butterflies [i0, i1), inputs from the parts `src[j]`,
 // outputs k*m + i untwisted by itw and rounded into the product's N words.
 template <int R0, int LS>
@@ -144,11 +121,11 @@ __global__ void __launch_bounds__(MAXT) u64_product_split_kernel(
   const double2* wl = w + L.w_off[0];
   const int per = (1 << lm) >> LS;
   if (lr0 == 1) {
-    if constexpr (LS <= 1) level0_fwd_scatter<2, LS>(peer_y, peer_x, lm, c * per, (c + 1) * per, wl, tid, nth);
+    if constexpr (LS <= 1) level0_scatter<2, LS>(peer_y, peer_x, lm, c * per, (c + 1) * per, wl, tid, nth);
   } else if (lr0 == 2) {
-    if constexpr (LS <= 2) level0_fwd_scatter<4, LS>(peer_y, peer_x, lm, c * per, (c + 1) * per, wl, tid, nth);
+    if constexpr (LS <= 2) level0_scatter<4, LS>(peer_y, peer_x, lm, c * per, (c + 1) * per, wl, tid, nth);
   } else {
-    level0_fwd_scatter<8, LS>(peer_y, peer_x, lm, c * per, (c + 1) * per, wl, tid, nth);
+    level0_scatter<8, LS>(peer_y, peer_x, lm, c * per, (c + 1) * per, wl, tid, nth);
   }
   cl.sync();  // every part's x is complete and every peer has read this CTA's y (now the ping-pong buffer)
 

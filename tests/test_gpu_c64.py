@@ -139,7 +139,7 @@ def test_cluster_sizes_bit_exact(cuda, oracle, ctas):
             plan.inv(d)
             want = oracle.ordered_inv(algo, want)
             assert np.array_equal(bits(d.cpu().numpy()), bits(want)), (algo, n, ctas)
-    for n, base in [(256, 32), (1024, 64), (2048, 1024), (4096, 512)]:
+    for n, base in [(256, 32), (1024, 64), (2048, 1024), (4096, 512), (8192, 1024), (16384, 512), (32768, 1024)]:
         for algo in (2, 7):
             plan = cf.unordered.Plan(n, cf.unordered.Method.UserProvided(algo, base))
             plan.set_cluster_size(ctas)

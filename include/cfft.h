@@ -104,13 +104,13 @@ cfft_status cfft_ordered_set_int_adds(cfft_ordered_plan* plan, int eighths);
 int cfft_ordered_int_adds(const cfft_ordered_plan* plan);
 
 /* CTAs per transform (no counterpart in the reference): 0 chooses per call
- * (each transform split over 2..8 CTAs when the batch is too small to give
- * every SM work), 1 keeps one CTA per transform, 2/4/8 force that split.  A
- * forced value is capped at what the plan allows (the radix of the step that
- * is split, and 8); plans whose transform does not fit one CTA's shared memory
- * are not split.  The DIT algorithms and the unordered inverse exchange data
- * once through a thread-block cluster.  Results are bit-identical for every
- * value. */
+ * (each transform split over 2..8 CTAs of a thread-block cluster when the
+ * batch is too small to give every SM work; unordered transforms above 4096
+ * points only up to 8192), 1 keeps the one-CTA / global-level path, 2/4/8
+ * force that split.  A forced value is capped at what the plan allows (the
+ * radix of the step that is split, and 8) and raised to the smallest split
+ * whose parts fit shared memory (4096 points, so unordered n <= 32768).  Results
+ * are bit-identical for every value. */
 cfft_status cfft_ordered_set_cluster_size(cfft_ordered_plan* plan, int ctas);
 
 /* ===================================================== unordered::Plan ====
@@ -154,7 +154,7 @@ cfft_status cfft_unordered_from_standard_host(const cfft_unordered_plan* plan, c
 
 /* Integer-pipe share of the butterfly additions, as cfft_ordered_set_int_adds. */
 cfft_status cfft_unordered_set_int_adds(cfft_unordered_plan* plan, int eighths);
-/* CTAs per transform, as cfft_ordered_set_cluster_size (plans of up to 4096 points). */
+/* CTAs per transform, as cfft_ordered_set_cluster_size. */
 cfft_status cfft_unordered_set_cluster_size(cfft_unordered_plan* plan, int ctas);
 int cfft_unordered_int_adds(const cfft_unordered_plan* plan);
 

@@ -147,7 +147,7 @@ int product_split_log2(const cfft_u64_product_plan* p, size_t count, bool* ok) {
 
 cfft_status launch_split_product(const cfft_u64_product_plan* plan, int ls, const uint64_t* a, const double* bhat,
                                  size_t bhat_stride, uint64_t* out, size_t count, cudaStream_t stream,
-                                 const cfft_product_item* items = nullptr) {
+                                 const cfft_product_item* items = nullptr, int terms = 1) {
   const size_t part = plan->n >> ls;
   const bool big = part > 2048;  // 4096 points per CTA: one CTA per SM, 512 threads
   const void* fn = plan->base_algo < 4 ? u64_product_split_ptr_0123(plan->base_algo, ls, big)
@@ -157,7 +157,7 @@ cfft_status launch_split_product(const cfft_u64_product_plan* plan, int ls, cons
   DevLevels L = plan->dlv;
   long stride = (long)bhat_stride;
   const double2* bh = (const double2*)bhat;
-  void* args[] = {(void*)&a, (void*)&bh, &stride, (void*)&out, (void*)&items, &L, (void*)&plan->d_w,
+  void* args[] = {(void*)&a, (void*)&bh, &stride, (void*)&out, &terms, (void*)&items, &L, (void*)&plan->d_w,
                   (void*)&plan->d_winv, (void*)&plan->d_tw, (void*)&plan->d_itw};
   // 128 threads (several CTAs per SM) for parts up to 1024 points, 256 for 2048
   // (shared memory allows 3 CTAs per SM), 512 for 4096 (one CTA per SM)
@@ -231,8 +231,13 @@ cfft_status cfft_u64_product_sum(const cfft_u64_product_plan* plan, const uint64
                                  size_t terms, uint64_t* out, size_t count, void* stream) {
   if (!plan || !a || !bhat || !out) return fail(CFFT_ERR_INVALID_ARGUMENT, "null argument");
   if (terms == 0 || terms > 0x7fffffff) return fail(CFFT_ERR_INVALID_ARGUMENT, "terms must be at least 1");
-  if (plan->N > (size_t(2) << kSmemLog2Max))
-    return fail(CFFT_ERR_INVALID_SIZE, "product sum: N must be at most 8192");
+  if (plan->N > (size_t(2) << kSmemLog2Max)) {  // one output per thread-block cluster
+    bool ok = true;
+    const int ls = product_split_log2(plan, count, &ok);
+    if (!ok) return fail(CFFT_ERR_INVALID_SIZE, "product sum: N must be at most 65536");
+    if (count == 0) return CFFT_OK;
+    return launch_split_product(plan, ls, a, bhat, plan->n, out, count, (cudaStream_t)stream, nullptr, (int)terms);
+  }
   if (count == 0) return CFFT_OK;
   const bool reg_acc = plan->n <= (size_t)(kSumRegAcc * kProdThreads);
   const void* fn = u64_product_sum_kernel_ptr(plan->base_algo, reg_acc);

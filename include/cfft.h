@@ -236,7 +236,7 @@ cfft_status cfft_u64_product_host(const cfft_u64_product_plan* plan, const uint6
  * mod (X^N + 1), every term transformed forward, multiplied and accumulated
  * in term order, then one inverse per group instead of one per term.
  * a: count * terms * N u64; bhat: count * terms * N/2 c64; out: count * N u64.
- * N <= 8192. */
+ * N <= 65536 (one output per thread-block cluster above 8192). */
 cfft_status cfft_u64_product_sum(const cfft_u64_product_plan* plan, const uint64_t* a, const double* bhat,
                                  size_t terms, uint64_t* out, size_t count, void* stream);
 

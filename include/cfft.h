@@ -19,7 +19,10 @@
  * operation sequence in IEEE FP64, with the reference's twiddle tables).
  *
  * Plans are immutable after creation and may be shared across threads, like
- * the reference's `Plan: Clone + Send + Sync`.
+ * the reference's `Plan: Clone + Send + Sync`.  The speed knobs without a
+ * reference counterpart (cfft_*_set_int_adds, cfft_*_set_cluster_size) change
+ * a plan: call them before sharing it, not while another thread uses it.
+ * Results never depend on them.
  */
 #ifndef CFFT_H
 #define CFFT_H

@@ -335,6 +335,17 @@ def run_gb300(args):
             dst_t.copy_(src_t, non_blocking=True)
         torch.cuda.synchronize()
         copy_gbs[name] = 3 * src_t.numel() * 8 / (time.perf_counter() - c0) / 1e9
+    # both directions at once on two streams (what the pipelined e2e path does)
+    s_in, s_out = torch.cuda.Stream(), torch.cuda.Stream()
+    torch.cuda.synchronize()
+    c0 = time.perf_counter()
+    for _ in range(3):
+        with torch.cuda.stream(s_in):
+            a.copy_(ha, non_blocking=True)
+        with torch.cuda.stream(s_out):
+            hout.copy_(out, non_blocking=True)
+    torch.cuda.synchronize()
+    copy_gbs["both_directions_total"] = 3 * 2 * ha.numel() * 8 / (time.perf_counter() - c0) / 1e9
 
     peaks, peak_kind = measured_peaks()
     achieved_gbs = BYTES_PER_PRODUCT * count / per_launch_s / 1e9

@@ -645,6 +645,17 @@ def run_u128(args):
                 plan.product(ha, bhat, hout)
             e2e = world * count * max(3, args.steps // 10) / (time.perf_counter() - t0)
             e2e_ok = bool(torch.equal(hout, out.cpu()))
+    # fft128::Plan itself: fwd then inv of a batch of n-point double-double transforms
+    plans128 = {}
+    for n, batch in ((512, 4096), (2048, 1024), (16384, 128)):
+        fp = cf.fft128.Plan(n)
+        bufs = [torch.rand((batch, n), dtype=torch.float64, device="cuda") for _ in range(4)]
+
+        def step128():
+            fp.fwd(*bufs)
+            fp.inv(*bufs)
+        ms128, _ = timed(torch, step128, max(5, args.steps), args.warmup, local, world)
+        plans128[n] = {"transforms_per_s": world * 2 * batch * max(5, args.steps) / (ms128 * 1e-3), "batch": batch}
     if rank != 0:
         return
     print(json.dumps({
@@ -652,7 +663,7 @@ def run_u128(args):
         "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64x2 (double-double)", "data": "synthetic (seeded numpy PCG64)",
         "config": {"workload": "u128 product, 2048 per launch", "N1024_products_per_s": res[1024],
-                   "N4096_products_per_s": res[4096]},
+                   "N4096_products_per_s": res[4096], "fft128_plan_fwd_inv_by_n": plans128},
         "e2e": {"value": e2e, "unit": "products/s", "h2d_bytes_per_step": count * 1024 * 16,
                 "d2h_bytes_per_step": count * 1024 * 16, "matches_device_result": e2e_ok, "N": 1024},
         "roofline": {"bound": "hbm", "achieved": res[1024] * 49152 / 1e9, "peak": measured_peaks()[0]["hbm_gbs"],

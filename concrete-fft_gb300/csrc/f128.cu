@@ -147,6 +147,99 @@ __global__ void __launch_bounds__(256) u128_prepare_kernel(const int64_t* __rest
   }
 }
 
+
+// ---- u128 products above N = 8192: the same steps as separate kernels around
+// the fft128 plan's transform (global stages + shared-memory blocks), on a
+// workspace of four arrays of count x n f64 (the plan's batch layout).
+
+// a (N (lo, hi) pairs per product) -> f128 points, as u128_product_kernel does.
+__global__ void __launch_bounds__(256) u128_fold_kernel(const uint64_t* __restrict__ a, F128Arrays z, long count,
+                                                       int log2n) {
+  const long n = 1L << log2n;
+  const long total = count << (log2n + 1);
+  for (long g = (long)blockIdx.x * blockDim.x + threadIdx.x; g < total; g += (long)gridDim.x * blockDim.x) {
+    const long p = g >> (log2n + 1), j = g & (2 * n - 1);
+    const uint64_t* ap = a + p * 4 * n;
+    const uint64_t lo = __ldcs(ap + 2 * j), hi = __ldcs(ap + 2 * j + 1);
+    const double xh = i128_to_f64_rne(lo, hi);
+    uint64_t tl, th;
+    double fr;
+    trunc_mod128(xh, tl, th, fr);
+    const uint64_t rl = lo - tl;
+    const uint64_t rh = hi - th - (lo < tl ? 1 : 0);
+    const double xl = i128_to_f64_rne(rl, rh);
+    if (j < n) {
+      z.re0[p * n + j] = xh;
+      z.re1[p * n + j] = xl;
+    } else {
+      z.im0[p * n + j - n] = xh;
+      z.im1[p * n + j - n] = xl;
+    }
+  }
+}
+
+// z <- (z * bhat) * factor, the fused kernel's double-double pointwise step.
+__global__ void __launch_bounds__(256) u128_pointwise_kernel(F128Arrays z, const double* __restrict__ bhat,
+                                                            long bhat_stride, long count, int log2n, double factor) {
+  const long n = 1L << log2n;
+  const long total = count << log2n;
+  for (long g = (long)blockIdx.x * blockDim.x + threadIdx.x; g < total; g += (long)gridDim.x * blockDim.x) {
+    const long p = g >> log2n, k = g & (n - 1);
+    const double* bp = bhat + p * bhat_stride;
+    f128 pr, pi;
+    cplx_mul(f128{z.re0[g], z.re1[g]}, f128{z.im0[g], z.im1[g]}, f128{__ldg(bp + k), __ldg(bp + n + k)},
+             f128{__ldg(bp + 2 * n + k), __ldg(bp + 3 * n + k)}, pr, pi);
+    z.re0[g] = __dmul_rn(pr.hi, factor);
+    z.re1[g] = __dmul_rn(pr.lo, factor);
+    z.im0[g] = __dmul_rn(pi.hi, factor);
+    z.im1[g] = __dmul_rn(pi.lo, factor);
+  }
+}
+
+// f128 points -> N (lo, hi) pairs, floor(x + 1/2) mod 2^128.
+__global__ void __launch_bounds__(256) u128_round_kernel(F128Arrays z, uint64_t* __restrict__ out, long count,
+                                                        int log2n) {
+  const long n = 1L << log2n;
+  const long total = count << (log2n + 1);
+  for (long g = (long)blockIdx.x * blockDim.x + threadIdx.x; g < total; g += (long)gridDim.x * blockDim.x) {
+    const long p = g >> (log2n + 1), j = g & (2 * n - 1);
+    uint64_t rl, rh;
+    if (j < n) round_half_up_mod128(z.re0[p * n + j], z.re1[p * n + j], rl, rh);
+    else round_half_up_mod128(z.im0[p * n + j - n], z.im1[p * n + j - n], rl, rh);
+    __stcs(out + p * 4 * n + 2 * j, rl);
+    __stcs(out + p * 4 * n + 2 * j + 1, rh);
+  }
+}
+
+// digits -> f128(b, 0) points (the operand's fold), and the transformed points
+// -> the operand layout (four arrays of n per operand).
+__global__ void __launch_bounds__(256) u128_prepare_fold_kernel(const int64_t* __restrict__ b, F128Arrays z,
+                                                               long count, int log2n) {
+  const long n = 1L << log2n;
+  const long total = count << log2n;
+  for (long g = (long)blockIdx.x * blockDim.x + threadIdx.x; g < total; g += (long)gridDim.x * blockDim.x) {
+    const long p = g >> log2n, j = g & (n - 1);
+    const int64_t* bp = b + p * 2 * n;
+    z.re0[g] = i64_to_f64_rne(bp[j]);
+    z.re1[g] = 0.0;
+    z.im0[g] = i64_to_f64_rne(bp[j + n]);
+    z.im1[g] = 0.0;
+  }
+}
+__global__ void __launch_bounds__(256) u128_operand_layout_kernel(F128Arrays z, double* __restrict__ bhat,
+                                                                 long count, int log2n) {
+  const long n = 1L << log2n;
+  const long total = count << log2n;
+  for (long g = (long)blockIdx.x * blockDim.x + threadIdx.x; g < total; g += (long)gridDim.x * blockDim.x) {
+    const long p = g >> log2n, k = g & (n - 1);
+    double* op = bhat + p * 4 * n;
+    op[k] = z.re0[g];
+    op[n + k] = z.re1[g];
+    op[2 * n + k] = z.im0[g];
+    op[3 * n + k] = z.im1[g];
+  }
+}
+
 }  // namespace cfft
 
 struct cfft_f128_plan {
@@ -234,6 +327,22 @@ cfft_status run_f128_tw(size_t n, const F128Tw& tw, double* re0, double* re1, do
       CFFT_CHECK_LAUNCH();
     }
   }
+  return CFFT_OK;
+}
+
+int elementwise_grid(long total) {
+  return (int)std::max<long>(1, std::min<long>((total + 255) / 256, (long)sm_count() * 16));
+}
+
+// Four arrays of count x n f64 from the stream-ordered allocator (no device
+// synchronisation; calls on different streams get different blocks).
+cfft_status workspace_alloc(size_t count, size_t n, cudaStream_t s, F128Arrays* z) {
+  void* ptr = nullptr;
+  const size_t per = count * n;
+  if (cudaMallocAsync(&ptr, 4 * per * sizeof(double), s) != cudaSuccess)
+    return fail(CFFT_ERR_OUT_OF_MEMORY, "u128 product workspace");
+  double* d = (double*)ptr;
+  *z = F128Arrays{d, d + per, d + 2 * per, d + 3 * per};
   return CFFT_OK;
 }
 
@@ -342,8 +451,8 @@ cfft_status cfft_f128_negacyclic_inv(size_t n, size_t batch, double* re0, double
 cfft_status cfft_u128_product_plan_create(size_t N, cfft_u128_product_plan** out) {
   if (!out) return fail(CFFT_ERR_INVALID_ARGUMENT, "null output pointer");
   *out = nullptr;
-  if (!is_pow2(N) || N < 64 || ilog2(N) > kF128SmemLog2 + 1)
-    return fail(CFFT_ERR_INVALID_SIZE, "u128 product: N must be a power of two in [64, 8192]");
+  if (!is_pow2(N) || N < 64 || ilog2(N) > 17)
+    return fail(CFFT_ERR_INVALID_SIZE, "u128 product: N must be a power of two in [64, 131072]");
   auto* p = new cfft_u128_product_plan();
   p->N = N;
   cfft_status st = build_f128(&p->f, N / 2);
@@ -367,6 +476,23 @@ cfft_status cfft_u128_prepare_operand(const cfft_u128_product_plan* p, const int
                                       void* stream) {
   if (!p || !b || !bhat4) return fail(CFFT_ERR_INVALID_ARGUMENT, "null argument");
   if (count == 0) return CFFT_OK;
+  if (ilog2(p->f.n) > kF128SmemLog2) {  // fold, the plan's forward transform, operand layout
+    cudaStream_t s = (cudaStream_t)stream;
+    const int log2n = ilog2(p->f.n);
+    F128Arrays z;
+    cfft_status st = workspace_alloc(count, p->f.n, s, &z);
+    if (st != CFFT_OK) return st;
+    const long total = (long)count << log2n;
+    u128_prepare_fold_kernel<<<elementwise_grid(total), 256, 0, s>>>(b, z, (long)count, log2n);
+    CFFT_CHECK_LAUNCH();
+    st = run_f128_tw(p->f.n, p->f.tw(), z.re0, z.re1, z.im0, z.im1, count, true, s);
+    if (st == CFFT_OK) {
+      u128_operand_layout_kernel<<<elementwise_grid(total), 256, 0, s>>>(z, bhat4, (long)count, log2n);
+      st = cudaGetLastError() == cudaSuccess ? CFFT_OK : fail(CFFT_ERR_CUDA, "operand layout launch");
+    }
+    cudaFreeAsync(z.re0, s);
+    return st;
+  }
   const int log2n = ilog2(p->f.n);
   const int threads = f128_threads(log2n);
   const size_t smem = 4 * p->f.n * sizeof(double);
@@ -382,6 +508,29 @@ cfft_status cfft_u128_product(const cfft_u128_product_plan* p, const uint64_t* a
   if (bhat_stride != 0 && bhat_stride != 2 * p->N)
     return fail(CFFT_ERR_INVALID_ARGUMENT, "bhat_stride must be 0 or 2N");
   if (count == 0) return CFFT_OK;
+  if (ilog2(p->f.n) > kF128SmemLog2) {  // fold, forward, pointwise, inverse, round: five launches
+    cudaStream_t s = (cudaStream_t)stream;
+    const int log2n = ilog2(p->f.n);
+    F128Arrays z;
+    cfft_status st = workspace_alloc(count, p->f.n, s, &z);
+    if (st != CFFT_OK) return st;
+    const long total = (long)count << log2n;
+    u128_fold_kernel<<<elementwise_grid(2 * total), 256, 0, s>>>(a, z, (long)count, log2n);
+    CFFT_CHECK_LAUNCH();
+    st = run_f128_tw(p->f.n, p->f.tw(), z.re0, z.re1, z.im0, z.im1, count, true, s);
+    if (st == CFFT_OK) {
+      u128_pointwise_kernel<<<elementwise_grid(total), 256, 0, s>>>(z, bhat4, (long)bhat_stride, (long)count, log2n,
+                                                                    2.0 / (double)p->N);
+      st = cudaGetLastError() == cudaSuccess ? CFFT_OK : fail(CFFT_ERR_CUDA, "pointwise launch");
+    }
+    if (st == CFFT_OK) st = run_f128_tw(p->f.n, p->f.tw(), z.re0, z.re1, z.im0, z.im1, count, false, s);
+    if (st == CFFT_OK) {
+      u128_round_kernel<<<elementwise_grid(2 * total), 256, 0, s>>>(z, out, (long)count, log2n);
+      st = cudaGetLastError() == cudaSuccess ? CFFT_OK : fail(CFFT_ERR_CUDA, "round launch");
+    }
+    cudaFreeAsync(z.re0, s);
+    return st;
+  }
   const int log2n = ilog2(p->f.n);
   const int threads = f128_threads(log2n);
   const size_t smem = 4 * p->f.n * sizeof(double);

@@ -185,6 +185,32 @@ def test_u64_product_cluster_sizes_bit_identical(cuda, N, base):
             assert torch.equal(out, ref), (N, base, algo, ctas)
 
 
+@pytest.mark.parametrize("N", [16384, 32768])
+def test_u128_product_large_N(cuda, oracle, N):
+    """N > 8192: five launches around the fft128 plan, bit-exact against the CPU pipeline
+    (operand preparation included), exact against the schoolbook for small inputs."""
+    import concrete_fft as cf
+    torch = cuda
+    count = 2
+    plan = cf.product.U128ProductPlan(N)
+    a = RNG.integers(0, 2 ** 64, (count, N, 2), dtype=np.uint64)
+    b = RNG.integers(-2 ** 15, 2 ** 15, (count, N))
+    bhat = torch.empty((count, 4, N // 2), dtype=torch.float64, device="cuda")
+    plan.prepare_operand(torch.from_numpy(b).cuda(), bhat)
+    want_bhat = oracle.u128_prepare(N, b)
+    assert np.array_equal(bhat.cpu().numpy().view(np.uint64), want_bhat.view(np.uint64))
+    da = torch.from_numpy(a.view(np.int64)).cuda()
+    out = torch.empty_like(da)
+    plan.product(da, bhat, out)
+    assert np.array_equal(out.cpu().numpy().view(np.uint64), oracle.u128_product(N, a, want_bhat, nthreads=0))
+    if N == 16384:
+        small = RNG.integers(-2 ** 40, 2 ** 40, (1, N)).astype(np.int64)
+        a2 = np.stack([small.view(np.uint64), np.where(small < 0, np.uint64(2 ** 64 - 1), np.uint64(0))], -1)
+        out2 = torch.empty((1, N, 2), dtype=torch.int64, device="cuda")
+        plan.product(torch.from_numpy(a2.view(np.int64)).cuda(), bhat[:1], out2)
+        assert np.array_equal(out2.cpu().numpy().view(np.uint64), oracle.u128_schoolbook(a2, b[:1]))
+
+
 def test_u128_product_host_pipeline(cuda, oracle):
     """Host entry point for u128 products over several pipelined chunks, one operand per
     product, against the device entry point (itself checked against the oracle above)."""

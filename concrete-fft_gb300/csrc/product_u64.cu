@@ -349,8 +349,20 @@ cfft_status cfft_u64_product(const cfft_u64_product_plan* plan, const uint64_t* 
     return fail(CFFT_ERR_INVALID_ARGUMENT, "bhat_stride must be 0 or N/2");
   bool ok = true;
   const int ls = product_split_log2(plan, count, &ok);
-  if (!ok) return fail(CFFT_ERR_INVALID_SIZE, "fused u64 product: N must be at most 65536 (use cfft_product_engine_run)");
   if (count == 0) return CFFT_OK;
+  if (!ok) {  // N = 131072: the five-launch path on a workspace from the stream-ordered allocator
+    cudaStream_t s = (cudaStream_t)stream;
+    void* z = nullptr;
+    if (cudaMallocAsync(&z, count * plan->n * sizeof(double2), s) != cudaSuccess)
+      return fail(CFFT_ERR_OUT_OF_MEMORY, "u64 product workspace");
+    cfft_status st = cfft_u64_fold_twist(plan, a, (double*)z, count, stream);
+    if (st == CFFT_OK) st = cfft_unordered_fwd(plan->fft, (double*)z, count, stream);
+    if (st == CFFT_OK) st = cfft_c64_pointwise(bhat, bhat_stride, (double*)z, plan->n, count, stream);
+    if (st == CFFT_OK) st = cfft_unordered_inv(plan->fft, (double*)z, count, stream);
+    if (st == CFFT_OK) st = cfft_u64_untwist_round(plan, (const double*)z, out, count, stream);
+    cudaFreeAsync(z, s);
+    return st;
+  }
   if (ls > 0) return launch_split_product(plan, ls, a, bhat, bhat_stride, out, count, (cudaStream_t)stream);
   return launch_product(plan, a, bhat, bhat_stride, out, count, (cudaStream_t)stream);
 

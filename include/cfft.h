@@ -204,9 +204,10 @@ cfft_status cfft_f128_negacyclic_inv(size_t n, size_t batch, double* re0, double
  * untwist, exact rounding back to the integer ring.
  *
  * u64: coefficients are read as i64, rounded with floor(x + 1/2) and reduced
- * mod 2^64.  N a power of two, 64 <= N <= 65536 for the fused product: one CTA
- * per product up to N = 8192, a thread-block cluster of 2..8 CTAs per product
- * above (and for small batches, see cfft_u64_product_set_cluster_size).  bhat
+ * mod 2^64.  N a power of two, 64 <= N <= 131072: one CTA per product up to
+ * N = 8192, a thread-block cluster of 2..8 CTAs per product up to 65536 (and
+ * for small batches, see cfft_u64_product_set_cluster_size), and at 131072 the
+ * five-launch path on a workspace from the stream-ordered allocator.  bhat
  * holds N/2 c64 per operand in the plan's permuted order; `bhat_stride` is 0
  * (one operand shared by all products) or N/2 (one operand per product). */
 typedef struct cfft_u64_product_plan cfft_u64_product_plan;

@@ -138,10 +138,12 @@ def test_u128_product_bit_exact(cuda, oracle, N):
     assert np.array_equal(out2.cpu().numpy().view(np.uint64), oracle.u128_schoolbook(a2, b[:1]))
 
 
-@pytest.mark.parametrize("N,algo,base", [(16384, 2, 1024), (16384, 5, 512), (32768, 2, 1024), (65536, 6, 1024)])
-def test_u64_product_large_N_on_a_cluster(cuda, oracle, N, algo, base):
-    """N > 8192: the fused product on a thread-block cluster, bit-exact against the CPU
-    pipeline, exact against the schoolbook when the sums fit in 53 bits."""
+@pytest.mark.parametrize("N,algo,base", [(16384, 2, 1024), (16384, 5, 512), (32768, 2, 1024), (65536, 6, 1024),
+                                         (131072, 2, 1024)])
+def test_u64_product_large_N(cuda, oracle, N, algo, base):
+    """N > 8192: a thread-block cluster per product up to 65536, five launches at 131072;
+    bit-exact against the CPU pipeline, exact against the schoolbook when the sums fit
+    in 53 bits."""
     import concrete_fft as cf
     torch = cuda
     plan = cf.product.U64ProductPlan(N, algo, base)

@@ -102,3 +102,15 @@ def test_f128_init_negacyclic_twiddles_matches_oracle(cfft_lib, oracle):
             assert t[k][0] == 7.0
             assert np.array_equal(t[k][1:].view(np.uint64), want[k][1:].view(np.uint64)), (n, k)
     assert cfft_lib.cfft_f128_init_negacyclic_twiddles(24, *[ctypes.c_void_p(t[0].ctypes.data)] * 4) == -1
+
+
+def test_missing_library_fails_loudly(tmp_path):
+    """No silent fallback: without the built library the package refuses to load."""
+    import concrete_fft._lib as L
+    saved = L._lib
+    L._lib = None
+    try:
+        with pytest.raises(ImportError, match="not built"):
+            L.load(str(tmp_path / "libcfft_gb300.so"))
+    finally:
+        L._lib = saved

@@ -248,8 +248,7 @@ cfft_status cfft_u64_product_sum(const cfft_u64_product_plan* plan, const uint64
  * Fourier-domain data themselves; bit-identical to cfft_u64_product):
  *   cfft_u64_fold_twist -> cfft_unordered_fwd(cfft_u64_product_fft(plan)) ->
  *   cfft_c64_pointwise -> cfft_unordered_inv -> cfft_u64_untwist_round.
- * z holds count * N/2 c64.  Plans of N up to 131072 may be created for these
- * entry points; the fused cfft_u64_product takes N <= 8192. */
+ * z holds count * N/2 c64.  Every plan size (N up to 131072) works here. */
 cfft_status cfft_u64_fold_twist(const cfft_u64_product_plan* plan, const uint64_t* a, double* z, size_t count,
                                 void* stream);
 /* z[p][k] = bhat[p*bhat_stride + k] * z[p][k] (the reference's FMA complex product). */

@@ -645,6 +645,15 @@ def run_u128(args):
                 plan.product(ha, bhat, hout)
             e2e = world * count * max(3, args.steps // 10) / (time.perf_counter() - t0)
             e2e_ok = bool(torch.equal(hout, out.cpu()))
+    prof = profiled_traffic("u128_product_n1024") or {}
+    fp64_u128 = None
+    if prof.get("fp64_thread_inst_per_product"):
+        peak = fp64_peak(cf)
+        ach = prof["fp64_thread_inst_per_product"] * res[1024]
+        fp64_u128 = {"achieved_ops_per_s": ach, "peak_ops_per_s": peak, "frac": ach / peak,
+                     "ops_per_product": prof["fp64_thread_inst_per_product"],
+                     "note": "DADD/DFMA/DMUL per product counted by ncu (N=1024); the FP64 pipe also issues the "
+                             "double-double code's comparisons and conversions"}
     # fft128::Plan itself: fwd then inv of a batch of n-point double-double transforms
     plans128 = {}
     for n, batch in ((512, 4096), (2048, 1024), (16384, 128)):
@@ -669,6 +678,7 @@ def run_u128(args):
         "roofline": {"bound": "hbm", "achieved": res[1024] * 49152 / 1e9, "peak": measured_peaks()[0]["hbm_gbs"],
                      "unit": "GB/s", "frac": res[1024] * 49152 / 1e9 / measured_peaks()[0]["hbm_gbs"],
                      "traffic": (profiled_traffic("u128_product_n1024") or {}).get("dram_bytes_per_launch"),
+                     "fp64": fp64_u128,
                      "note": "N=1024: 49,152 algorithmic bytes per product; bound by the FP64 pipe "
                              "(double-double arithmetic), see profiles/u128_product_n1024.md"},
         "clocks": clocks, "gpu_launches": 2 * args.steps,

@@ -4,7 +4,7 @@
 // Same module and method names as the Rust crate (zama-ai/concrete-fft v0.5.1):
 //   concrete_fft::ordered::{FftAlgo, Method, Plan}      (src/ordered.rs)
 //   concrete_fft::unordered::{Method, Plan}             (src/unordered.rs)
-//   concrete_fft::fft128::Plan                          (src/fft128/mod.rs)
+//   concrete_fft::fft128::{Plan, f128}                  (src/fft128/mod.rs, f128_ops.rs)
 // Where the crate panics (assert! on sizes, base sizes, buffer lengths), these
 // classes throw concrete_fft::Error carrying the cfft_status.  Slices become
 // (pointer, length) pairs; host buffers go through the *_host entry points,
@@ -20,6 +20,7 @@
 #include <vector>
 
 #include "../../include/cfft.h"
+#include "f128.hpp"
 
 namespace concrete_fft {
 
@@ -178,9 +179,7 @@ class Plan {
 
 namespace fft128 {
 
-struct f128 {  // src/fft128/mod.rs:7
-  double hi, lo;
-};
+// f128 (src/fft128/mod.rs:7, src/fft128/f128_ops.rs): see f128.hpp
 
 class Plan {
  public:

@@ -209,6 +209,23 @@ class Plan {
   cfft_f128_plan* raw_ = nullptr;
 };
 
+// The crate's #[doc(hidden)] free functions (src/fft128/mod.rs:1041-1104, 1805-1828).
+// init_negacyclic_twiddles fills positions 1..n-1 of four host slices of n; the
+// transforms take DEVICE arrays (`batch` transforms of n back to back) and a stream.
+inline void init_negacyclic_twiddles(double* re0, double* re1, double* im0, double* im1, std::size_t n) {
+  check(cfft_f128_init_negacyclic_twiddles(n, re0, re1, im0, im1));
+}
+inline void negacyclic_fwd_fft(double* re0, double* re1, double* im0, double* im1, const double* twid_re0,
+                               const double* twid_re1, const double* twid_im0, const double* twid_im1,
+                               std::size_t n, std::size_t batch = 1, void* stream = nullptr) {
+  check(cfft_f128_negacyclic_fwd(n, batch, re0, re1, im0, im1, twid_re0, twid_re1, twid_im0, twid_im1, stream));
+}
+inline void negacyclic_inv_fft(double* re0, double* re1, double* im0, double* im1, const double* twid_re0,
+                               const double* twid_re1, const double* twid_im0, const double* twid_im1,
+                               std::size_t n, std::size_t batch = 1, void* stream = nullptr) {
+  check(cfft_f128_negacyclic_inv(n, batch, re0, re1, im0, im1, twid_re0, twid_re1, twid_im0, twid_im1, stream));
+}
+
 }  // namespace fft128
 
 }  // namespace concrete_fft

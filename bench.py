@@ -656,7 +656,7 @@ def run_u128(args):
                              "double-double code's comparisons and conversions"}
     # fft128::Plan itself: fwd then inv of a batch of n-point double-double transforms
     plans128 = {}
-    for n, batch in ((512, 4096), (2048, 1024), (16384, 128)):
+    for n, batch in ((512, 4096), (2048, 1024), (4096, 512), (16384, 128)):
         fp = cf.fft128.Plan(n)
         bufs = [torch.rand((batch, n), dtype=torch.float64, device="cuda") for _ in range(4)]
 
@@ -664,7 +664,14 @@ def run_u128(args):
             fp.fwd(*bufs)
             fp.inv(*bufs)
         ms128, _ = timed(torch, step128, max(5, args.steps), args.warmup, local, world)
-        plans128[n] = {"transforms_per_s": world * 2 * batch * max(5, args.steps) / (ms128 * 1e-3), "batch": batch}
+        one = [bb[:1].clone() for bb in bufs]
+
+        def step1():
+            fp.fwd(*one)
+            fp.inv(*one)
+        ms1, _ = timed(torch, step1, max(10, args.steps), args.warmup, local, world)
+        plans128[n] = {"transforms_per_s": world * 2 * batch * max(5, args.steps) / (ms128 * 1e-3), "batch": batch,
+                       "batch1_us_per_fwd_inv": round(ms1 * 1e3 / max(10, args.steps), 2)}
     if rank != 0:
         return
     print(json.dumps({

@@ -303,10 +303,15 @@ cfft_status run_f128_tw(size_t n, const F128Tw& tw, double* re0, double* re1, do
   cfft_status ast = f128_attrs();
   if (ast != CFFT_OK) return ast;
   const int log2n = ilog2(n);
-  const int log2c = std::min(log2n, kF128SmemLog2);
+  int log2c = std::min(log2n, kF128SmemLog2);
+  // small batches: smaller shared-memory blocks after more global stages, so that
+  // one transform spreads over several SMs (same butterflies, same results)
+  const bool few = ((long)batch << (log2n - log2c)) < (long)sm_count() / 2;
+  while (log2c > 8 && ((long)batch << (log2n - log2c)) < (long)sm_count() / 2) --log2c;
   F128Arrays g{re0, re1, im0, im1};
   const long nblocks = (long)batch << (log2n - log2c);
-  const int threads = f128_threads(log2c);
+  // few blocks: a thread per butterfly of a stage (latency); many: fewer threads, more CTAs per SM
+  const int threads = few ? std::min(256, 1 << (log2c - 1)) : f128_threads(log2c);
   const size_t smem = (size_t)4 * (size_t(1) << log2c) * sizeof(double);
   const int grid = product_grid(fwd ? (const void*)f128_smem_kernel<true> : (const void*)f128_smem_kernel<false>,
                                 threads, smem, nblocks);

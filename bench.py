@@ -624,6 +624,7 @@ def run_u128(args):
     import numpy as np
     torch, cf, rank, world, local = gpu_setup()
     res = {}
+    lat1 = {}
     clocks = None
     for N in (1024, 4096):
         plan = cf.product.U128ProductPlan(N)
@@ -636,6 +637,9 @@ def run_u128(args):
         out = torch.empty_like(a)
         ms, clocks = timed(torch, lambda: plan.product(a, bhat, out), args.steps, args.warmup, local, world)
         res[N] = world * count * args.steps / (ms * 1e-3)
+        a1, b1, o1 = a[:1].clone(), bhat[:1].clone(), out[:1].clone()
+        ms1, _ = timed(torch, lambda: plan.product(a1, b1, o1), max(10, args.steps), args.warmup, local, world)
+        lat1[N] = round(ms1 * 1e3 / max(10, args.steps), 2)
         if N == 1024:  # end to end: pinned host A in and results out through the host entry point
             ha = a.cpu().pin_memory()
             hout = torch.empty_like(ha).pin_memory()
@@ -679,7 +683,8 @@ def run_u128(args):
         "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64x2 (double-double)", "data": "synthetic (seeded numpy PCG64)",
         "config": {"workload": "u128 product, 2048 per launch", "N1024_products_per_s": res[1024],
-                   "N4096_products_per_s": res[4096], "fft128_plan_fwd_inv_by_n": plans128},
+                   "N4096_products_per_s": res[4096], "one_product_us_by_N": lat1,
+                   "fft128_plan_fwd_inv_by_n": plans128},
         "e2e": {"value": e2e, "unit": "products/s", "h2d_bytes_per_step": count * 1024 * 16,
                 "d2h_bytes_per_step": count * 1024 * 16, "matches_device_result": e2e_ok, "N": 1024},
         "roofline": {"bound": "hbm", "achieved": res[1024] * 49152 / 1e9, "peak": measured_peaks()[0]["hbm_gbs"],

@@ -513,7 +513,11 @@ cfft_status cfft_u128_product(const cfft_u128_product_plan* p, const uint64_t* a
   if (bhat_stride != 0 && bhat_stride != 2 * p->N)
     return fail(CFFT_ERR_INVALID_ARGUMENT, "bhat_stride must be 0 or 2N");
   if (count == 0) return CFFT_OK;
-  if (ilog2(p->f.n) > kF128SmemLog2) {  // fold, forward, pointwise, inverse, round: five launches
+  // Above N = 8192, and for a few products of N >= 1024 (their transforms then spread
+  // over many SMs instead of one CTA each): fold, forward, pointwise, inverse, round
+  // as five launches around the plan's transform.  Bit-identical to the fused kernel.
+  const bool few = (long)count < (long)sm_count() / 2;
+  if (ilog2(p->f.n) > kF128SmemLog2 || (few && p->f.n >= 512)) {
     cudaStream_t s = (cudaStream_t)stream;
     const int log2n = ilog2(p->f.n);
     F128Arrays z;
@@ -537,7 +541,8 @@ cfft_status cfft_u128_product(const cfft_u128_product_plan* p, const uint64_t* a
     return st;
   }
   const int log2n = ilog2(p->f.n);
-  const int threads = f128_threads(log2n);
+  // few products: a thread per butterfly (latency); many: fewer threads, more CTAs per SM
+  const int threads = few ? std::min(256, 1 << (log2n - 1)) : f128_threads(log2n);
   const size_t smem = 4 * p->f.n * sizeof(double);
   const int grid = product_grid((const void*)u128_product_kernel, threads, smem, (long)count);
   u128_product_kernel<<<grid, threads, smem, (cudaStream_t)stream>>>(

@@ -295,6 +295,11 @@ def run_gb300(args):
     per_launch_s = ms * 1e-3 / args.steps
     value = world * count * args.steps / (ms * 1e-3)
 
+    # one product alone (latency of the fused path), and through the five-launch path
+    a1, bh1, o1 = a[:1].clone(), bhat[:1].clone(), out[:1].clone()
+    ms_one, _ = timed(torch, lambda: plan.product(a1, bh1, o1), 50, 5, local, world)
+    z1 = torch.empty((1, N_POLY // 2), dtype=torch.complex128, device="cuda")
+    ms_one_u, _ = timed(torch, lambda: plan.product_unfused(a1, bh1, o1, z1), 50, 5, local, world)
     # the plain Plan path on the same products: five launches (fold+twist, forward FFT, pointwise,
     # inverse FFT, untwist+round) per batch, and per product (one launch per transform)
     z = torch.empty((count, N_POLY // 2), dtype=torch.complex128, device="cuda")
@@ -310,7 +315,8 @@ def run_gb300(args):
     ms_pp, _ = timed(torch, per_product, 2, 1, local, world)
     plain = {"batched_5_launches_products_per_s": world * count * plain_steps / (ms_pb * 1e-3),
              "per_product_5_launches_products_per_s": world * sample * 2 / (ms_pp * 1e-3),
-             "per_product_sample": sample, "matches_fused_result": plain_ok}
+             "per_product_sample": sample, "matches_fused_result": plain_ok,
+             "one_product_us_fused": round(ms_one * 1e3 / 50, 2), "one_product_us_5_launches": round(ms_one_u * 1e3 / 50, 2)}
 
     # end to end: pinned host A in, pinned host result out, through the C ABI host entry point
     ha = torch.from_numpy(a_np.view(np.int64)).pin_memory()

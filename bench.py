@@ -629,6 +629,14 @@ def run_u128(args):
     """u128 negacyclic products N = 1024 and 4096, 2048 per launch, B digits in [-2^15, 2^15)."""
     import numpy as np
     torch, cf, rank, world, local = gpu_setup()
+    if args.profile_case:  # for ncu: four forward calls of the fft128 plan, n = 512, batch 4096
+        fp = cf.fft128.Plan(512)
+        bufs = [torch.rand((4096, 512), dtype=torch.float64, device="cuda") for _ in range(4)]
+        for _ in range(4):
+            fp.fwd(*bufs)
+        torch.cuda.synchronize()
+        print(json.dumps({"profile_case": "fft128 plan n=512 batch 4096 forward"}))
+        return
     res = {}
     lat1 = {}
     clocks = None

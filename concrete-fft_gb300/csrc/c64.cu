@@ -526,7 +526,7 @@ cfft_status cfft_unordered_plan_create(size_t n, cfft_algo base_algo, size_t bas
   if (!out) return fail(CFFT_ERR_INVALID_ARGUMENT, "null output pointer");
   *out = nullptr;
   if (!is_pow2(n)) return fail(CFFT_ERR_INVALID_SIZE, "unordered plan: n must be a power of two");
-  if (ilog2(n) > 20) return fail(CFFT_ERR_INVALID_SIZE, "unordered plan: n must be at most 2^20");
+  if (ilog2(n) > kUnorderedMaxLog2) return fail(CFFT_ERR_INVALID_SIZE, "unordered plan: n must be at most 2^28");
   if (!is_pow2(base_n)) return fail(CFFT_ERR_INVALID_ARGUMENT, "base_n must be a power of two");
   if (base_n > n) return fail(CFFT_ERR_INVALID_ARGUMENT, "base_n must not exceed n");
   if (base_n != n && base_n < 32) return fail(CFFT_ERR_INVALID_ARGUMENT, "base_n must be >= 32 when base_n != n");
@@ -548,7 +548,8 @@ cfft_status cfft_unordered_plan_create(size_t n, cfft_algo base_algo, size_t bas
 cfft_status cfft_unordered_plan_create_measure(size_t n, double seconds, cfft_unordered_plan** out) {
   if (!out) return fail(CFFT_ERR_INVALID_ARGUMENT, "null output pointer");
   *out = nullptr;
-  if (!is_pow2(n) || ilog2(n) > 20) return fail(CFFT_ERR_INVALID_SIZE, "unordered plan: n must be 2^k, k <= 20");
+  if (!is_pow2(n) || ilog2(n) > kUnorderedMaxLog2)
+    return fail(CFFT_ERR_INVALID_SIZE, "unordered plan: n must be 2^k, k <= 28");
   TuneVal tv;
   if (tune_lookup(1, n, &tv)) {  // measured before on this GPU model
     cfft_status st = cfft_unordered_plan_create(n, (cfft_algo)tv.algo, tv.base_n, out);

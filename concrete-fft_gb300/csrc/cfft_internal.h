@@ -23,6 +23,18 @@ void unordered_twiddles(size_t n, size_t base_n, int base_r, c64h* w, c64h* w_in
 void monomial_twiddles(size_t n, c64h* tw);
 // src/fft128/mod.rs:1805-1828: n entries each
 void f128_twiddles(size_t n, double* re0, double* re1, double* im0, double* im1);
+// u64 product twist tables: tw[j] = exp(i pi j / N), itw[j] = conj(tw[j]) / (N/2), j < N/2
+void product_twist_tables(size_t N, c64h* tw, c64h* itw);
+// Runs f(begin, end) over [0, count) on up to 16 host threads for large tables
+// (every entry is computed independently, so the bits do not depend on the split).
+void parallel_range(size_t count, void (*f)(size_t, size_t, void*), void* ctx);
+
+// Largest transforms accepted (the reference has no upper bound): 2^28 c64
+// points (4 GiB) per unordered transform, 2^24 points (512 MiB) per fft128
+// transform.  The level descriptors hold 8 outer levels, enough for 2^28 over
+// the smallest base (32 points).
+constexpr int kUnorderedMaxLog2 = 28;
+constexpr int kF128MaxLog2 = 24;
 
 inline bool is_pow2(size_t n) { return n != 0 && (n & (n - 1)) == 0; }
 inline int ilog2(size_t n) {

@@ -386,7 +386,7 @@ cfft_status cfft_f128_plan_create(size_t n, cfft_f128_plan** out) {
   if (!out) return fail(CFFT_ERR_INVALID_ARGUMENT, "null output pointer");
   *out = nullptr;
   if (!is_pow2(n) || n < 32) return fail(CFFT_ERR_INVALID_SIZE, "fft128 plan: n must be a power of two >= 32");
-  if (ilog2(n) > 16) return fail(CFFT_ERR_INVALID_SIZE, "fft128 plan: n must be at most 65536");
+  if (ilog2(n) > kF128MaxLog2) return fail(CFFT_ERR_INVALID_SIZE, "fft128 plan: n must be at most 2^24");
   auto* p = new cfft_f128_plan();
   cfft_status st = build_f128(p, n);
   if (st != CFFT_OK) {
@@ -424,7 +424,7 @@ cfft_status cfft_f128_inv_host(const cfft_f128_plan* p, double* re0, double* re1
 
 cfft_status cfft_f128_init_negacyclic_twiddles(size_t n, double* re0, double* re1, double* im0, double* im1) {
   if (!re0 || !re1 || !im0 || !im1) return fail(CFFT_ERR_INVALID_ARGUMENT, "null argument");
-  if (!is_pow2(n) || ilog2(n) > 16) return fail(CFFT_ERR_INVALID_SIZE, "n must be a power of two <= 65536");
+  if (!is_pow2(n) || ilog2(n) > kF128MaxLog2) return fail(CFFT_ERR_INVALID_SIZE, "n must be a power of two <= 2^24");
   if (n < 2) return CFFT_OK;
   std::vector<double> tw(4 * n);
   f128_twiddles(n, tw.data(), tw.data() + n, tw.data() + 2 * n, tw.data() + 3 * n);
@@ -438,8 +438,8 @@ static cfft_status raw_f128(size_t n, size_t batch, double* re0, double* re1, do
                             const double* t0, const double* t1, const double* t2, const double* t3, bool fwd,
                             void* stream) {
   if (!t0 || !t1 || !t2 || !t3) return fail(CFFT_ERR_INVALID_ARGUMENT, "null twiddle array");
-  if (!is_pow2(n) || n < 2 || ilog2(n) > 16)
-    return fail(CFFT_ERR_INVALID_SIZE, "n must be a power of two in [2, 65536]");
+  if (!is_pow2(n) || n < 2 || ilog2(n) > kF128MaxLog2)
+    return fail(CFFT_ERR_INVALID_SIZE, "n must be a power of two in [2, 2^24]");
   return run_f128_tw(n, F128Tw{t0, t1, t2, t3}, re0, re1, im0, im1, batch, fwd, (cudaStream_t)stream);
 }
 cfft_status cfft_f128_negacyclic_fwd(size_t n, size_t batch, double* re0, double* re1, double* im0, double* im1,
@@ -456,8 +456,8 @@ cfft_status cfft_f128_negacyclic_inv(size_t n, size_t batch, double* re0, double
 cfft_status cfft_u128_product_plan_create(size_t N, cfft_u128_product_plan** out) {
   if (!out) return fail(CFFT_ERR_INVALID_ARGUMENT, "null output pointer");
   *out = nullptr;
-  if (!is_pow2(N) || N < 64 || ilog2(N) > 17)
-    return fail(CFFT_ERR_INVALID_SIZE, "u128 product: N must be a power of two in [64, 131072]");
+  if (!is_pow2(N) || N < 64 || ilog2(N) > kF128MaxLog2 + 1)
+    return fail(CFFT_ERR_INVALID_SIZE, "u128 product: N must be a power of two in [64, 2^25]");
   auto* p = new cfft_u128_product_plan();
   p->N = N;
   cfft_status st = build_f128(&p->f, N / 2);

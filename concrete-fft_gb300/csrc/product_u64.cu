@@ -61,6 +61,23 @@ __global__ void pointwise_kernel(const double2* __restrict__ bhat, long bhat_str
     st(z + g, cmul(ldg(bhat + p * bhat_stride + k), ld(z + g)));
   }
 }
+// acc[g] = sum over t of bhat[g, t] * z[g, t] (terms back to back per group),
+// the first product assigned and the others added in term order, as the fused
+// sum kernels do.
+__global__ void fourier_sum_kernel(const double2* __restrict__ bhat, const double2* __restrict__ z,
+                                   double2* __restrict__ acc, int terms, long total, int log2n) {
+  const long n = 1L << log2n;
+  for (long g = (long)blockIdx.x * blockDim.x + threadIdx.x; g < total; g += (long)gridDim.x * blockDim.x) {
+    const long grp = g >> log2n, k = g & (n - 1);
+    const long base = ((grp * terms) << log2n) + k;
+    c64 s = cmul(ldg(bhat + base), ld(z + base));
+    for (int t = 1; t < terms; ++t) {
+      const long o = base + ((long)t << log2n);
+      s = cadd(s, cmul(ldg(bhat + o), ld(z + o)));
+    }
+    st(acc + g, s);
+  }
+}
 __global__ void untwist_round_kernel(const double2* __restrict__ z, uint64_t* __restrict__ out, long total, int log2n,
                                      const double2* __restrict__ itw) {
   const long n = 1L << log2n;
@@ -107,6 +124,37 @@ DevLevels dev_levels(const LevelDesc& l) {
 int grid_for(const void* kernel, int threads, size_t smem, long count) {
   if (count <= (1L << 20)) return (int)std::max<long>(1, count);
   return (int)((long)sm_count() * max_blocks_per_sm(kernel, threads, smem));
+}
+
+// Sums of products too large for a cluster (N > 65536), unfused: fold and twist
+// every term, the plan's forward transforms, the Fourier-domain sum per group,
+// one inverse per group, untwist and round.  Groups run in chunks whose
+// workspace (terms + 1 transforms per group) stays within 1 GiB.
+cfft_status product_sum_unfused(const cfft_u64_product_plan* plan, const uint64_t* a, const double* bhat,
+                                size_t terms, uint64_t* out, size_t count, cudaStream_t s) {
+  const size_t n = plan->n, per_group = (terms + 1) * n * sizeof(double2);
+  const size_t chunk = std::min(count, std::max<size_t>(1, (size_t(1) << 30) / per_group));
+  void* ws = nullptr;
+  if (cudaMallocAsync(&ws, chunk * per_group, s) != cudaSuccess)
+    return fail(CFFT_ERR_OUT_OF_MEMORY, "product sum workspace");
+  double2* z = (double2*)ws;
+  double2* acc = z + chunk * terms * n;
+  cfft_status st = CFFT_OK;
+  for (size_t g0 = 0; g0 < count && st == CFFT_OK; g0 += chunk) {
+    const size_t g = std::min(chunk, count - g0);
+    st = cfft_u64_fold_twist(plan, a + g0 * terms * plan->N, (double*)z, g * terms, s);
+    if (st == CFFT_OK) st = cfft_unordered_fwd(plan->fft, (double*)z, g * terms, s);
+    if (st == CFFT_OK) {
+      const long total = (long)(g * n);
+      fourier_sum_kernel<<<ew_grid(total), 256, 0, s>>>((const double2*)bhat + g0 * terms * n, z, acc, (int)terms,
+                                                         total, ilog2(n));
+      st = cudaGetLastError() == cudaSuccess ? CFFT_OK : fail(CFFT_ERR_CUDA, "fourier_sum_kernel launch");
+    }
+    if (st == CFFT_OK) st = cfft_unordered_inv(plan->fft, (double*)acc, g, s);
+    if (st == CFFT_OK) st = cfft_u64_untwist_round(plan, (const double*)acc, out + g0 * plan->N, g, s);
+  }
+  cudaFreeAsync(ws, s);
+  return st;
 }
 
 cfft_status launch_product(const cfft_u64_product_plan* plan, const uint64_t* a, const double* bhat,
@@ -234,9 +282,10 @@ cfft_status cfft_u64_product_sum(const cfft_u64_product_plan* plan, const uint64
   if (plan->N > (size_t(2) << kSmemLog2Max)) {  // one output per thread-block cluster
     bool ok = true;
     const int ls = product_split_log2(plan, count, &ok);
-    if (!ok) return fail(CFFT_ERR_INVALID_SIZE, "product sum: N must be at most 65536");
     if (count == 0) return CFFT_OK;
-    return launch_split_product(plan, ls, a, bhat, plan->n, out, count, (cudaStream_t)stream, nullptr, (int)terms);
+    if (ok) return launch_split_product(plan, ls, a, bhat, plan->n, out, count, (cudaStream_t)stream, nullptr,
+                                        (int)terms);
+    return product_sum_unfused(plan, a, bhat, terms, out, count, (cudaStream_t)stream);
   }
   if (count == 0) return CFFT_OK;
   const bool reg_acc = plan->n <= (size_t)(kSumRegAcc * kProdThreads);
@@ -273,8 +322,8 @@ int cfft_u64_product_int_adds(const cfft_u64_product_plan* plan) {
 cfft_status cfft_u64_product_plan_create(size_t N, cfft_algo base_algo, size_t base_n, cfft_u64_product_plan** out) {
   if (!out) return fail(CFFT_ERR_INVALID_ARGUMENT, "null output pointer");
   *out = nullptr;
-  if (!is_pow2(N) || N < 64 || ilog2(N) > 17)
-    return fail(CFFT_ERR_INVALID_SIZE, "u64 product: N must be a power of two in [64, 131072]");
+  if (!is_pow2(N) || N < 64 || ilog2(N) > kUnorderedMaxLog2 + 1)
+    return fail(CFFT_ERR_INVALID_SIZE, "u64 product: N must be a power of two in [64, 2^29]");
   const size_t n = N / 2;
   if (!is_pow2(base_n) || base_n > n || (base_n != n && base_n < 32) || ilog2(base_n) > 10)
     return fail(CFFT_ERR_INVALID_ARGUMENT, "u64 product: invalid base_n");
@@ -289,13 +338,7 @@ cfft_status cfft_u64_product_plan_create(size_t N, cfft_algo base_algo, size_t b
   p->dlv = dev_levels(p->lv);
   std::vector<c64h> w(n + base_n), wi(n + base_n), tw(n), itw(n);
   unordered_twiddles(n, base_n, algo_radix(base_algo), w.data(), wi.data());
-  const double inv_n = 1.0 / (double)n;
-  for (size_t j = 0; j < n; ++j) {
-    double s, c;
-    sincospi64((double)j / (double)N, &s, &c);
-    tw[j] = c64h{c, s};
-    itw[j] = c64h{c * inv_n, -s * inv_n};  // exact: inv_n is a power of two
-  }
+  product_twist_tables(N, tw.data(), itw.data());
   st = upload((const double2*)w.data(), n + base_n, &p->d_w);
   if (st == CFFT_OK) st = cfft_unordered_plan_create(n, base_algo, base_n, &p->fft);
   if (st == CFFT_OK) st = upload((const double2*)wi.data(), n + base_n, &p->d_winv);
@@ -350,7 +393,7 @@ cfft_status cfft_u64_product(const cfft_u64_product_plan* plan, const uint64_t* 
   bool ok = true;
   const int ls = product_split_log2(plan, count, &ok);
   if (count == 0) return CFFT_OK;
-  // The five-launch path on a workspace from the stream-ordered allocator: N = 131072
+  // The five-launch path on a workspace from the stream-ordered allocator: N > 65536
   // (no cluster holds it), and large batches of N >= 32768, where it measured faster
   // than one cluster per product (304 vs 280 k products/s at 32768, 129 vs 102 k at 65536)
   const bool many = (long)count >= (long)sm_count() / 2 && plan->cluster == 0;
@@ -379,8 +422,8 @@ cfft_status cfft_u64_product(const cfft_u64_product_plan* plan, const uint64_t* 
 cfft_status cfft_u64_product_plan_create_measure(size_t N, double seconds, cfft_u64_product_plan** out) {
   if (!out) return fail(CFFT_ERR_INVALID_ARGUMENT, "null output pointer");
   *out = nullptr;
-  if (!is_pow2(N) || N < 64 || ilog2(N) > 16)
-    return fail(CFFT_ERR_INVALID_SIZE, "u64 product: N must be a power of two in [64, 65536]");
+  if (!is_pow2(N) || N < 64 || ilog2(N) > kUnorderedMaxLog2 + 1)
+    return fail(CFFT_ERR_INVALID_SIZE, "u64 product: N must be a power of two in [64, 2^29]");
   const size_t n = N / 2;
   TuneVal tv;
   if (tune_lookup(2, N, &tv)) {  // measured before on this GPU model
@@ -393,8 +436,10 @@ cfft_status cfft_u64_product_plan_create_measure(size_t N, double seconds, cfft_
   else
     for (size_t b : {size_t(512), size_t(1024)})
       if (b <= n) bases.push_back(b);
-  // eight products per SM up to N = 8192, the same number of CTAs for larger N
-  const size_t count = (size_t)sm_count() * std::max<size_t>(1, 8 * 8192 / std::max<size_t>(N, 8192));
+  // eight products per SM up to N = 8192, the same number of CTAs for larger N,
+  // within 2 GiB of operands, results and workspace (32 N bytes per product)
+  const size_t per_sm = std::max<size_t>(1, 8 * 8192 / std::max<size_t>(N, 8192));
+  const size_t count = std::max<size_t>(1, std::min((size_t)sm_count() * per_sm, (size_t(1) << 31) / (32 * N)));
   uint64_t *da = nullptr, *dout = nullptr;
   double* dbhat = nullptr;
   CFFT_CUDA_TRY(cudaMalloc(&da, count * N * sizeof(uint64_t)));

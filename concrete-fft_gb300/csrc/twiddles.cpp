@@ -6,8 +6,11 @@
 // -ffp-contract=off: std::fma appears only where the reference calls mul_add.
 #include <cmath>
 #include <cstring>
+#include <algorithm>
 #include <mutex>
 #include <string>
+#include <thread>
+#include <vector>
 
 #include "cfft_internal.h"
 #include "tune_cache.h"
@@ -70,6 +73,26 @@ void init_wt(int r, size_t n, c64h* w, c64h* w_inv) {
   }
 }
 
+void parallel_range(size_t count, void (*f)(size_t, size_t, void*), void* ctx) {
+  const size_t hw = std::max<size_t>(1, std::thread::hardware_concurrency());
+  const size_t nt = std::min<size_t>({hw, 16, count >> 16});  // below 2^17 entries: this thread
+  if (nt <= 1) {
+    f(0, count, ctx);
+    return;
+  }
+  std::vector<std::thread> ts;
+  for (size_t t = 0; t < nt; ++t) ts.emplace_back(f, count * t / nt, count * (t + 1) / nt, ctx);
+  for (auto& t : ts) t.join();
+}
+
+namespace {
+template <class F>
+void for_range(size_t count, F&& body) {
+  parallel_range(
+      count, [](size_t b, size_t e, void* c) { (*(F*)c)(b, e); }, (void*)&body);
+}
+}  // namespace
+
 static void unordered_rec(size_t n, size_t base_n, int base_r, c64h* w, c64h* w_inv, size_t len) {
   if (n <= base_n) {
     init_wt(base_r, n, w, w_inv);
@@ -80,15 +103,17 @@ static void unordered_rec(size_t n, size_t base_n, int base_r, c64h* w, c64h* w_
   const size_t head = (size_t)(r - 1) * m;
   const double theta = 2.0 / (double)n;
   c64h* w_inv_cur = w_inv + (len - head);
-  for (size_t p = 0; p < m; ++p) {
-    for (int k = 1; k < r; ++k) {
-      double sk, ck;
-      sincospi64(theta * (double)((size_t)k * p), &sk, &ck);
-      const size_t idx = (size_t)(r - 1) * p + (size_t)(k - 1);
-      w[idx] = c64h{ck, -sk};
-      w_inv_cur[idx] = c64h{ck, sk};
+  for_range(m, [&](size_t b, size_t e) {
+    for (size_t p = b; p < e; ++p) {
+      for (int k = 1; k < r; ++k) {
+        double sk, ck;
+        sincospi64(theta * (double)((size_t)k * p), &sk, &ck);
+        const size_t idx = (size_t)(r - 1) * p + (size_t)(k - 1);
+        w[idx] = c64h{ck, -sk};
+        w_inv_cur[idx] = c64h{ck, sk};
+      }
     }
-  }
+  });
   unordered_rec(n / (size_t)r, base_n, base_r, w + head, w_inv, len - head);
 }
 
@@ -98,11 +123,26 @@ void unordered_twiddles(size_t n, size_t base_n, int base_r, c64h* w, c64h* w_in
 
 void monomial_twiddles(size_t n, c64h* tw) {
   const double theta = -2.0 / (double)n;
-  for (size_t i = 0; i < n; ++i) {
-    double s, c;
-    sincospi64(theta * (double)i, &s, &c);
-    tw[i] = c64h{c, s};
-  }
+  for_range(n, [&](size_t b, size_t e) {
+    for (size_t i = b; i < e; ++i) {
+      double s, c;
+      sincospi64(theta * (double)i, &s, &c);
+      tw[i] = c64h{c, s};
+    }
+  });
+}
+
+void product_twist_tables(size_t N, c64h* tw, c64h* itw) {
+  const size_t n = N / 2;
+  const double inv_n = 1.0 / (double)n;
+  for_range(n, [&](size_t b, size_t e) {
+    for (size_t j = b; j < e; ++j) {
+      double s, c;
+      sincospi64((double)j / (double)N, &s, &c);
+      tw[j] = c64h{c, s};
+      itw[j] = c64h{c * inv_n, -s * inv_n};  // exact: inv_n is a power of two
+    }
+  });
 }
 
 LevelDesc make_levels(size_t n, size_t base_n) {
@@ -245,19 +285,22 @@ void f128_sincospi(f128 x, f128* s_out, f128* c_out) {
 void f128_twiddles(size_t n, double* re0, double* re1, double* im0, double* im1) {
   re0[0] = re1[0] = im0[0] = im1[0] = 0.0;
   const int logn2 = ilog2(2 * n);
-  for (size_t m = 1; m < n; m *= 2) {
-    for (size_t i = 0; i < m; ++i) {
-      const size_t k = 2 * m + i;
+  // entry m + i (m a power of two, i < m) holds the twiddle of k = 2m + i
+  for_range(n, [&](size_t b, size_t e) {
+    for (size_t pos = std::max<size_t>(b, 1); pos < e; ++pos) {
+      size_t m = 1;
+      while (2 * m <= pos) m *= 2;
+      const size_t k = pos + m;
       size_t br = 0;
-      for (int b = 0; b < logn2; ++b) br |= ((k >> b) & 1u) << (logn2 - 1 - b);
+      for (int bit = 0; bit < logn2; ++bit) br |= ((k >> bit) & 1u) << (logn2 - 1 - bit);
       f128 s, c;
       f128_sincospi(f128{(double)br / (double)(2 * n), 0.0}, &s, &c);
-      re0[m + i] = c.hi;
-      re1[m + i] = c.lo;
-      im0[m + i] = s.hi;
-      im1[m + i] = s.lo;
+      re0[pos] = c.hi;
+      re1[pos] = c.lo;
+      im0[pos] = s.hi;
+      im1[pos] = s.lo;
     }
-  }
+  });
 }
 
 // ---------------------------------------------------------------- errors

@@ -117,7 +117,7 @@ int cfft_ordered_int_adds(const cfft_ordered_plan* plan);
 cfft_status cfft_ordered_set_cluster_size(cfft_ordered_plan* plan, int ctas);
 
 /* ===================================================== unordered::Plan ====
- * Replaces src/unordered.rs:496-1036.  Any power-of-two n up to 2^20 with a
+ * Replaces src/unordered.rs:496-1036.  Any power-of-two n up to 2^28 with a
  * base (internal ordered) size base_n <= 1024, base_n >= 32 unless base_n == n
  * (src/unordered.rs:660-670). */
 typedef struct cfft_unordered_plan cfft_unordered_plan;
@@ -162,7 +162,7 @@ cfft_status cfft_unordered_set_cluster_size(cfft_unordered_plan* plan, int ctas)
 int cfft_unordered_int_adds(const cfft_unordered_plan* plan);
 
 /* ======================================================== fft128::Plan ====
- * Replaces src/fft128/mod.rs:1832-1960.  n a power of two, 32 <= n <= 8192.
+ * Replaces src/fft128/mod.rs:1832-1960.  n a power of two, 32 <= n <= 2^24.
  * Split double-double storage: four f64 arrays (re0, re1, im0, im1), each
  * batch * n long; forward output is in bit-reversed order, inverse is
  * unnormalised. */
@@ -185,7 +185,7 @@ cfft_status cfft_f128_inv_host(const cfft_f128_plan* plan, double* re0, double* 
  * negacyclic_fwd_fft / negacyclic_inv_fft (src/fft128/mod.rs:1041-1104, one
  * entry for the _scalar/_avxfma/_avx512 variants, whose results are equal)
  * transform `batch` sets of n points with explicit twiddle arrays.  Data and
- * twiddles are DEVICE arrays here; n is a power of two in [2, 65536]. */
+ * twiddles are DEVICE arrays here; n is a power of two in [2, 2^24]. */
 cfft_status cfft_f128_init_negacyclic_twiddles(size_t n, double* twid_re0, double* twid_re1, double* twid_im0,
                                                double* twid_im1);
 cfft_status cfft_f128_negacyclic_fwd(size_t n, size_t batch, double* re0, double* re1, double* im0, double* im1,
@@ -204,10 +204,10 @@ cfft_status cfft_f128_negacyclic_inv(size_t n, size_t batch, double* re0, double
  * untwist, exact rounding back to the integer ring.
  *
  * u64: coefficients are read as i64, rounded with floor(x + 1/2) and reduced
- * mod 2^64.  N a power of two, 64 <= N <= 131072: one CTA per product up to
+ * mod 2^64.  N a power of two, 64 <= N <= 2^29: one CTA per product up to
  * N = 8192, a thread-block cluster of 2..8 CTAs per product up to 65536 (and
- * for small batches, see cfft_u64_product_set_cluster_size), and at 131072 the
- * five-launch path on a workspace from the stream-ordered allocator.  bhat
+ * for small batches, see cfft_u64_product_set_cluster_size), and above 65536
+ * the five-launch path on a workspace from the stream-ordered allocator.  bhat
  * holds N/2 c64 per operand in the plan's permuted order; `bhat_stride` is 0
  * (one operand shared by all products) or N/2 (one operand per product). */
 typedef struct cfft_u64_product_plan cfft_u64_product_plan;
@@ -240,7 +240,9 @@ cfft_status cfft_u64_product_host(const cfft_u64_product_plan* plan, const uint6
  * mod (X^N + 1), every term transformed forward, multiplied and accumulated
  * in term order, then one inverse per group instead of one per term.
  * a: count * terms * N u64; bhat: count * terms * N/2 c64; out: count * N u64.
- * N <= 65536 (one output per thread-block cluster above 8192). */
+ * N <= 2^29: one output per CTA up to 8192, per thread-block cluster up to
+ * 65536, and above that the unfused steps on a stream-ordered workspace of at
+ * most 1 GiB (groups in chunks). */
 cfft_status cfft_u64_product_sum(const cfft_u64_product_plan* plan, const uint64_t* a, const double* bhat,
                                  size_t terms, uint64_t* out, size_t count, void* stream);
 
@@ -248,7 +250,7 @@ cfft_status cfft_u64_product_sum(const cfft_u64_product_plan* plan, const uint64
  * Fourier-domain data themselves; bit-identical to cfft_u64_product):
  *   cfft_u64_fold_twist -> cfft_unordered_fwd(cfft_u64_product_fft(plan)) ->
  *   cfft_c64_pointwise -> cfft_unordered_inv -> cfft_u64_untwist_round.
- * z holds count * N/2 c64.  Every plan size (N up to 131072) works here. */
+ * z holds count * N/2 c64.  Every plan size (N up to 2^29) works here. */
 cfft_status cfft_u64_fold_twist(const cfft_u64_product_plan* plan, const uint64_t* a, double* z, size_t count,
                                 void* stream);
 /* z[p][k] = bhat[p*bhat_stride + k] * z[p][k] (the reference's FMA complex product). */
@@ -343,7 +345,7 @@ cfft_status cfft_server_run_alone(cfft_server* server, const cfft_serve_config* 
 
 /* u128: coefficients as little-endian (lo, hi) u64 pairs read as i128,
  * double-double arithmetic around fft128::Plan(N/2), floor(x + 1/2) mod 2^128.
- * 64 <= N <= 131072: one fused kernel up to N = 8192; above, five launches
+ * 64 <= N <= 2^25: one fused kernel up to N = 8192; above, five launches
  * around the plan's transform on a workspace from the stream-ordered allocator
  * (2N f64 per product, freed on the stream).  bhat holds 4 arrays of N/2 f64
  * (re0, re1, im0, im1) per operand; bhat_stride is 0 or 2N (doubles). */

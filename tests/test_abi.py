@@ -41,7 +41,10 @@ def test_argument_errors_without_device(cfft_lib):
     assert L.cfft_f128_plan_create(16, ctypes.byref(h)) == -1                # n < 32 (fft128/mod.rs:1866)
     assert L.cfft_u64_product_plan_create(2048, 6, 4096, ctypes.byref(h)) == -2
     assert L.cfft_u64_product_plan_create(100, 6, 32, ctypes.byref(h)) == -1
-    assert L.cfft_u128_product_plan_create(262144, ctypes.byref(h)) == -1      # N > 2^17
+    assert L.cfft_u128_product_plan_create(1 << 26, ctypes.byref(h)) == -1     # N > 2^25
+    assert L.cfft_unordered_plan_create(1 << 29, 2, 1024, ctypes.byref(h)) == -1  # n > 2^28
+    assert L.cfft_f128_plan_create(1 << 25, ctypes.byref(h)) == -1            # n > 2^24
+    assert L.cfft_u64_product_plan_create(1 << 30, 2, 1024, ctypes.byref(h)) == -1  # N > 2^29
     assert b"power of two" in L.cfft_last_error()
     buf = (ctypes.c_double * 8)()
     assert L.cfft_batch_run_host(None, buf, buf, None) == -2                 # null batch

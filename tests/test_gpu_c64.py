@@ -98,7 +98,7 @@ def test_unordered_golden_vector_on_gpu(cuda):
 
 
 CASES = [(32, 32), (64, 32), (256, 32), (1024, 32), (1024, 512), (1024, 1024), (2048, 1024), (4096, 64),
-         (8192, 1024), (16384, 512), (65536, 1024), (65536, 32), (1 << 20, 1024)]
+         (8192, 1024), (16384, 512), (65536, 1024), (65536, 32), (1 << 20, 1024), (1 << 22, 1024), (1 << 22, 32)]
 
 
 @pytest.mark.parametrize("n,base", CASES)

@@ -139,9 +139,9 @@ def test_u128_product_bit_exact(cuda, oracle, N):
 
 
 @pytest.mark.parametrize("N,algo,base", [(16384, 2, 1024), (16384, 5, 512), (32768, 2, 1024), (65536, 6, 1024),
-                                         (131072, 2, 1024)])
+                                         (131072, 2, 1024), (1 << 22, 6, 1024)])
 def test_u64_product_large_N(cuda, oracle, N, algo, base):
-    """N > 8192: a thread-block cluster per product up to 65536, five launches at 131072;
+    """N > 8192: a thread-block cluster per product up to 65536, five launches above;
     bit-exact against the CPU pipeline, exact against the schoolbook when the sums fit
     in 53 bits."""
     import concrete_fft as cf
@@ -187,7 +187,7 @@ def test_u64_product_cluster_sizes_bit_identical(cuda, N, base):
             assert torch.equal(out, ref), (N, base, algo, ctas)
 
 
-@pytest.mark.parametrize("N", [16384, 32768])
+@pytest.mark.parametrize("N", [16384, 32768, 1 << 21])
 def test_u128_product_large_N(cuda, oracle, N):
     """N > 8192: five launches around the fft128 plan, bit-exact against the CPU pipeline
     (operand preparation included), exact against the schoolbook for small inputs."""
@@ -236,7 +236,8 @@ def test_u128_product_host_pipeline(cuda, oracle):
 
 
 @pytest.mark.parametrize("N,algo,base,terms", [(2048, 2, 1024, 8), (1024, 4, 512, 3), (4096, 6, 1024, 1),
-                                               (8192, 3, 1024, 2), (16384, 2, 1024, 3), (32768, 6, 1024, 2)])
+                                               (8192, 3, 1024, 2), (16384, 2, 1024, 3), (32768, 6, 1024, 2),
+                                               (1 << 18, 2, 1024, 3)])
 def test_u64_product_sum_bit_exact(cuda, oracle, N, algo, base, terms):
     """Fourier-domain accumulation of `terms` products, one inverse per group."""
     import concrete_fft as cf
@@ -252,5 +253,27 @@ def test_u64_product_sum_bit_exact(cuda, oracle, N, algo, base, terms):
     want_bhat = oracle.u64_prepare(N, algo, base, b).reshape(count, terms, N // 2)
     want = oracle.u64_product_sum(N, algo, base, a, want_bhat, nthreads=0)
     assert np.array_equal(out.cpu().numpy().view(np.uint64), want)
-    exact = sum(oracle.u64_schoolbook(a[0, t], b[t]) for t in range(terms))
-    assert torus_err_bits(want[0], exact.astype(np.uint64)) < 30
+    if N <= 32768:  # the schoolbook is quadratic in N
+        exact = sum(oracle.u64_schoolbook(a[0, t], b[t]) for t in range(terms))
+        assert torus_err_bits(want[0], exact.astype(np.uint64)) < 30
+
+
+def test_u64_product_sum_unfused_chunks(cuda, oracle):
+    """Above N = 65536 the sum runs unfused, its groups in chunks within a 1 GiB
+    workspace: N = 2^21, 2 terms (96 MiB a group), 23 groups -> chunks of 21 and 2."""
+    import concrete_fft as cf
+    torch = cuda
+    N, terms, count = 1 << 21, 2, 23
+    plan = cf.product.U64ProductPlan(N, 2, 1024)
+    a = RNG.integers(0, 2 ** 64, (count, terms, N), dtype=np.uint64)
+    b = RNG.integers(-2 ** 7, 2 ** 7, (count * terms, N))
+    bhat = torch.empty((count, terms, N // 2), dtype=torch.complex128, device="cuda")
+    plan.prepare_operand(torch.from_numpy(b).cuda(), bhat)
+    out = torch.empty((count, N), dtype=torch.int64, device="cuda")
+    plan.product_sum(torch.from_numpy(a.view(np.int64)).cuda(), bhat, out)
+    sel = [0, 20, 21, 22]  # both sides of the chunk boundary
+    want_bhat = oracle.u64_prepare(N, 2, 1024, b.reshape(count, terms, N)[sel].reshape(-1, N))
+    want_bhat = want_bhat.reshape(len(sel), terms, N // 2)
+    assert np.array_equal(bhat[sel].cpu().numpy().view(np.uint64), want_bhat.view(np.uint64))
+    want = oracle.u64_product_sum(N, 2, 1024, a[sel], want_bhat, nthreads=0)
+    assert np.array_equal(out.cpu().numpy().view(np.uint64)[sel], want)

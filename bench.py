@@ -790,14 +790,15 @@ def run_serving(args):
 
 
 def run_u64_large(args):
-    """Fused u64 products above N = 8192 (one product per thread-block cluster) against the
-    plain five-launch path on the same products: N = 16384, 32768, 65536."""
+    """Fused u64 products from N = 8192 (one product per thread-block cluster) against the
+    plain five-launch path on the same products: N = 8192 (also against one CTA per
+    product), 16384, 32768, 65536."""
     import numpy as np
     torch, cf, rank, world, local = gpu_setup()
     peak = fp64_peak(cf)
     rows = {}
     clocks = None
-    for N in ((16384,) if args.profile_case else (16384, 32768, 65536)):
+    for N in ((16384,) if args.profile_case else (8192, 16384, 32768, 65536)):
         count = 8192 * 2048 // N
         plan = cf.product.U64ProductPlan(N, cf.FftAlgo.Dif4, 1024)
         rng = np.random.default_rng(N)
@@ -810,6 +811,12 @@ def run_u64_large(args):
         plan.set_cluster_size(8)  # one cluster per product, whatever the batch
         out3 = torch.empty_like(a)
         ms_c, _ = timed(torch, lambda: plan.product(a, bhat, out3), args.steps, args.warmup, local, world)
+        ms_1 = None
+        if N <= 8192:  # one CTA per product (4096 points: one CTA per SM)
+            plan.set_cluster_size(1)
+            out4 = torch.empty_like(a)
+            ms_1, _ = timed(torch, lambda: plan.product(a, bhat, out4), args.steps, args.warmup, local, world)
+            assert torch.equal(out4, out)
         plan.set_cluster_size(0)
         z = torch.empty((count, N // 2), dtype=torch.complex128, device="cuda")
         out2 = torch.empty_like(a)
@@ -821,14 +828,16 @@ def run_u64_large(args):
                    "cluster_products_per_s": world * count * args.steps / (ms_c * 1e-3),
                    "unfused_products_per_s": world * count * max(3, args.steps // 4) / (ms_u * 1e-3),
                    "matches_unfused": bool(torch.equal(out, out2) and torch.equal(out3, out2)), "count": count}
+        if ms_1 is not None:
+            rows[N]["one_cta_products_per_s"] = world * count * args.steps / (ms_1 * 1e-3)
     if rank != 0:
         return
     print(json.dumps({
-        "metric": "u64 products/s above N=8192 (automatic path: clusters, or five launches for large batches of N >= 32768)",
+        "metric": "u64 products/s at N=16384 (automatic path: clusters, or five launches for large batches of N >= 32768)",
         "value": rows[16384]["products_per_s"], "unit": "products/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
         "data": "synthetic (seeded numpy PCG64)",
-        "config": {"workload": "u64 products N=16384/32768/65536, Dif4 base 1024, 16 MiB of A per launch",
+        "config": {"workload": "u64 products N=8192/16384/32768/65536, Dif4 base 1024, 16 MiB of A per launch",
                    "by_N": rows},
         "clocks": clocks, "gpu_launches": 3 * args.steps,
     }))

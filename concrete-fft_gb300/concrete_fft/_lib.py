@@ -57,6 +57,8 @@ _SIGS = [
     ("cfft_ordered_set_int_adds", c_int, [vp, c_int]),
     ("cfft_ordered_set_cluster_size", c_int, [vp, c_int]),
     ("cfft_unordered_set_cluster_size", c_int, [vp, c_int]),
+    ("cfft_unordered_set_block_points", c_int, [vp, c_size]),
+    ("cfft_unordered_block_points", c_size, [vp]),
     ("cfft_ordered_int_adds", c_int, [vp]),
     ("cfft_unordered_set_int_adds", c_int, [vp, c_int]),
     ("cfft_unordered_int_adds", c_int, [vp]),
@@ -79,6 +81,9 @@ _SIGS = [
     ("cfft_f128_plan_create", c_int, [c_size, pp]),
     ("cfft_f128_plan_destroy", None, [vp]),
     ("cfft_f128_fft_size", c_size, [vp]),
+    ("cfft_f128_set_block_points", c_int, [vp, c_size]),
+    ("cfft_f128_block_points", c_size, [vp]),
+    ("cfft_u128_product_fft", vp, [vp]),
     ("cfft_f128_fwd", c_int, [vp, vp, vp, vp, vp, c_size, vp]),
     ("cfft_f128_inv", c_int, [vp, vp, vp, vp, vp, c_size, vp]),
     ("cfft_f128_fwd_host", c_int, [vp, vp, vp, vp, vp, c_size]),

@@ -22,6 +22,14 @@ class Plan:
     def fft_size(self):
         return self._lib.cfft_f128_fft_size(self._h)
 
+    def set_block_points(self, points):
+        """Points per shared-memory block: 0 automatic, else a power of two in [256, 4096];
+        results unchanged."""
+        check(self._lib.cfft_f128_set_block_points(self._h, int(points)))
+
+    def block_points(self):
+        return self._lib.cfft_f128_block_points(self._h)
+
     def _run(self, re0, re1, im0, im1, fwd):
         bufs = (re0, re1, im0, im1)
         for b in bufs:

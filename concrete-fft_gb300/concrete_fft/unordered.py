@@ -56,6 +56,14 @@ class Plan:
         """CTAs per transform: 0 automatic, 1 one CTA, 2/4/8 a thread-block cluster; results unchanged."""
         check(self._lib.cfft_unordered_set_cluster_size(self._h, int(ctas)))
 
+    def set_block_points(self, points):
+        """Sub-transform size one CTA holds in shared memory: 0 automatic, else one of the
+        plan's level sizes of at most 4096 points; results unchanged."""
+        check(self._lib.cfft_unordered_set_block_points(self._h, int(points)))
+
+    def block_points(self):
+        return self._lib.cfft_unordered_block_points(self._h)
+
     def int_adds(self):
         return self._lib.cfft_unordered_int_adds(self._h)
 

@@ -159,6 +159,14 @@ cfft_status cfft_unordered_from_standard_host(const cfft_unordered_plan* plan, c
 cfft_status cfft_unordered_set_int_adds(cfft_unordered_plan* plan, int eighths);
 /* CTAs per transform, as cfft_ordered_set_cluster_size. */
 cfft_status cfft_unordered_set_cluster_size(cfft_unordered_plan* plan, int ctas);
+/* Points per shared-memory block (no counterpart in the reference): the
+ * sub-transform one CTA holds after the levels above it ran in global memory
+ * (forward; the inverse runs them after).  0 = automatic (the first level of
+ * at most 4096 points); otherwise the size of one of the plan's levels (n, its
+ * outer-level sizes, base_n) of at most 4096 points.  Resets the launch shape
+ * that Method::Measure chose.  Results are bit-identical for every value. */
+cfft_status cfft_unordered_set_block_points(cfft_unordered_plan* plan, size_t points);
+size_t cfft_unordered_block_points(const cfft_unordered_plan* plan);
 int cfft_unordered_int_adds(const cfft_unordered_plan* plan);
 
 /* ======================================================== fft128::Plan ====
@@ -170,6 +178,15 @@ typedef struct cfft_f128_plan cfft_f128_plan;
 cfft_status cfft_f128_plan_create(size_t n, cfft_f128_plan** out);
 void cfft_f128_plan_destroy(cfft_f128_plan* plan);
 size_t cfft_f128_fft_size(const cfft_f128_plan* plan);
+/* Points per shared-memory block (no counterpart in the reference): 0 =
+ * automatic (512 for large batches; for small ones 4096 and fewer until the
+ * blocks cover half the SMs), else a power of two in
+ * [256, 4096]; the stages above the block run in global memory.  The u128
+ * product plan's transforms use their fft128 plan's value.  Results are
+ * bit-identical for every value.  cfft_f128_block_points returns 0 when
+ * automatic. */
+cfft_status cfft_f128_set_block_points(cfft_f128_plan* plan, size_t points);
+size_t cfft_f128_block_points(const cfft_f128_plan* plan);
 cfft_status cfft_f128_fwd(const cfft_f128_plan* plan, double* re0, double* re1, double* im0, double* im1,
                           size_t batch, void* stream);
 cfft_status cfft_f128_inv(const cfft_f128_plan* plan, double* re0, double* re1, double* im0, double* im1,
@@ -353,6 +370,8 @@ typedef struct cfft_u128_product_plan cfft_u128_product_plan;
 cfft_status cfft_u128_product_plan_create(size_t N, cfft_u128_product_plan** out);
 void cfft_u128_product_plan_destroy(cfft_u128_product_plan* plan);
 size_t cfft_u128_product_poly_size(const cfft_u128_product_plan* plan);
+/* The plan's fft128::Plan(N/2) (owned by the product plan; do not destroy it). */
+cfft_f128_plan* cfft_u128_product_fft(cfft_u128_product_plan* plan);
 cfft_status cfft_u128_prepare_operand(const cfft_u128_product_plan* plan, const int64_t* b, double* bhat4,
                                       size_t count, void* stream);
 cfft_status cfft_u128_product(const cfft_u128_product_plan* plan, const uint64_t* a, const double* bhat4,

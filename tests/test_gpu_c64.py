@@ -120,6 +120,35 @@ def test_unordered_bit_exact(cuda, oracle, n, base):
         assert np.abs(d.cpu().numpy() / n - x).max() < 1e-12
 
 
+@pytest.mark.parametrize("n,base", [(4096, 1024), (4096, 512), (32768, 1024), (16384, 64), (1 << 18, 1024)])
+def test_block_points_bit_exact(cuda, oracle, n, base):
+    """Every shared-memory block size a plan allows (its level sizes of at most 4096
+    points; the levels above run in global memory) gives the oracle's bits."""
+    import concrete_fft as cf
+    torch = cuda
+    plan = cf.unordered.Plan(n, cf.unordered.Method.UserProvided(6, base))
+    auto = plan.block_points()
+    x = rand_c64(2, n)
+    want_f = oracle.unordered_fwd(6, base, x, nthreads=0)
+    want_i = oracle.unordered_inv(6, base, want_f, nthreads=0)
+    sizes, cur = [n], n
+    while cur > base:
+        cur //= 2 if cur == 2 * base else (4 if cur == 4 * base else 8)
+        sizes.append(cur)
+    for pts in [s for s in sizes if s <= 4096]:
+        plan.set_block_points(pts)
+        assert plan.block_points() == pts
+        d = on_gpu(torch, x)
+        plan.fwd(d)
+        assert np.array_equal(bits(d.cpu().numpy()), bits(want_f)), (n, base, pts)
+        plan.inv(d)
+        assert np.array_equal(bits(d.cpu().numpy()), bits(want_i)), (n, base, pts)
+    with pytest.raises(cf.CfftError):
+        plan.set_block_points(2 * n if n <= 2048 else 8192)
+    plan.set_block_points(0)
+    assert plan.block_points() == auto
+
+
 @pytest.mark.parametrize("ctas", [1, 2, 4, 8, 0])
 def test_cluster_sizes_bit_exact(cuda, oracle, ctas):
     """One transform spread over a thread-block cluster (distributed shared memory)

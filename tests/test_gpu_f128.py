@@ -34,6 +34,33 @@ def test_f128_fwd_inv_bit_exact(cuda, oracle, n):
         assert np.array_equal(bits(h), bits(w))
 
 
+@pytest.mark.parametrize("n", [1024, 4096, 16384])
+def test_f128_block_points_bit_exact(cuda, oracle, n):
+    """Every shared-memory block size (the stages above it in global memory) gives the
+    oracle's bits, for the plan and for a u128 product plan's transforms."""
+    import concrete_fft as cf
+    torch = cuda
+    hi = [RNG.standard_normal((4, n)) for _ in range(2)]
+    host = [hi[0], hi[0] * 2.0 ** -60, hi[1], hi[1] * 2.0 ** -60]
+    want_f = oracle.f128_fwd(*host)
+    want_i = oracle.f128_inv(*want_f)
+    plan = cf.fft128.Plan(n)
+    for pts in (256, 512, 1024, 2048, 4096, 0):
+        if pts > n:
+            continue
+        plan.set_block_points(pts)
+        assert plan.block_points() == pts
+        d = [torch.from_numpy(np.ascontiguousarray(a)).cuda() for a in host]
+        plan.fwd(*d)
+        for x, w in zip(d, want_f):
+            assert np.array_equal(bits(x.cpu().numpy()), bits(w)), (n, pts)
+        plan.inv(*d)
+        for x, w in zip(d, want_i):
+            assert np.array_equal(bits(x.cpu().numpy()), bits(w)), (n, pts)
+    with pytest.raises(cf.CfftError):
+        plan.set_block_points(8192)
+
+
 @pytest.mark.parametrize("n", [2, 4, 16, 64, 1024, 8192])
 def test_f128_raw_negacyclic_functions(cuda, oracle, n):
     """negacyclic_fwd_fft / negacyclic_inv_fft with caller-owned twiddle arrays

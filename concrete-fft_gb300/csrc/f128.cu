@@ -579,6 +579,8 @@ cfft_status cfft_u128_product_host(const cfft_u128_product_plan* p, const uint64
   constexpr int kSlots = 4;
   const size_t poly_bytes = p->N * 2 * sizeof(uint64_t);
   const size_t chunk = std::min(count, std::max((size_t)sm_count() * 2, (count + 15) / 16));
+  // page-locked `out`: the kernels store the results there themselves (no copy out)
+  uint64_t* mapped_out = (uint64_t*)mapped_host_range(out, count * poly_bytes);
   PipeSlot slot[kSlots];
   cfft_status st = host_pipeline(kSlots, 2 * chunk * poly_bytes, slot);
   if (st != CFFT_OK) return st;
@@ -587,12 +589,13 @@ cfft_status cfft_u128_product_host(const cfft_u128_product_plan* p, const uint64
     const size_t c = std::min(chunk, count - first);
     const PipeSlot& sl = slot[i % kSlots];
     uint64_t* da = (uint64_t*)sl.dev;
-    uint64_t* dout = da + chunk * 2 * p->N;
+    uint64_t* dout = mapped_out ? mapped_out + first * 2 * p->N : da + chunk * 2 * p->N;
     CFFT_CUDA_TRY(cudaMemcpyAsync(da, a + first * 2 * p->N, c * poly_bytes, cudaMemcpyHostToDevice, sl.stream));
     const double* bh = bhat4 + (bhat_stride ? first * bhat_stride : 0);
     st = cfft_u128_product(p, da, bh, bhat_stride, dout, c, sl.stream);
     if (st != CFFT_OK) return st;
-    CFFT_CUDA_TRY(cudaMemcpyAsync(out + first * 2 * p->N, dout, c * poly_bytes, cudaMemcpyDeviceToHost, sl.stream));
+    if (!mapped_out)
+      CFFT_CUDA_TRY(cudaMemcpyAsync(out + first * 2 * p->N, dout, c * poly_bytes, cudaMemcpyDeviceToHost, sl.stream));
   }
   for (int k = 0; k < kSlots; ++k) CFFT_CUDA_TRY(cudaStreamSynchronize(slot[k].stream));
   return CFFT_OK;

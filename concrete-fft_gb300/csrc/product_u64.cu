@@ -545,11 +545,17 @@ cfft_status cfft_u64_product_host(const cfft_u64_product_plan* plan, const uint6
   if (count == 0) return CFFT_OK;
   // About 24 chunks per call on 6 streams: the first copy in and the last
   // copy out, which nothing overlaps, are then 1/24 of the data each, and 6
-  // chunks in flight keep kernels of several chunks resident at once.
+  // chunks in flight keep kernels of several chunks resident at once.  When
+  // `out` is page-locked the kernels store the results there themselves (no
+  // copy out, no drain): 6.56 vs 6.40 M products/s at N = 2048, 8192 per call.
+  // The operands still come in by copy: kernels reading them from host memory
+  // wait on every product's first loads (6.60 M/s for one launch with both
+  // sides in host memory, against 6.94 M/s on device buffers).
   constexpr int kSlots = 6;
   const size_t poly_bytes = plan->N * sizeof(uint64_t);
   const size_t min_chunk = (size_t)sm_count() * 2;
   const size_t chunk = std::min(count, std::max(min_chunk, (count + 23) / 24));
+  uint64_t* mapped_out = (uint64_t*)mapped_host_range(out, count * poly_bytes);
   PipeSlot slot[kSlots];
   cfft_status st = host_pipeline(kSlots, 2 * chunk * poly_bytes, slot);
   if (st != CFFT_OK) return st;
@@ -558,12 +564,13 @@ cfft_status cfft_u64_product_host(const cfft_u64_product_plan* plan, const uint6
     const size_t c = std::min(chunk, count - first);
     const PipeSlot& sl = slot[i % kSlots];
     uint64_t* da = (uint64_t*)sl.dev;
-    uint64_t* dout = da + chunk * plan->N;
+    uint64_t* dout = mapped_out ? mapped_out + first * plan->N : da + chunk * plan->N;
     CFFT_CUDA_TRY(cudaMemcpyAsync(da, a + first * plan->N, c * poly_bytes, cudaMemcpyHostToDevice, sl.stream));
     const double* bh = bhat + (bhat_stride ? first * bhat_stride * 2 : 0);
     st = cfft_u64_product(plan, da, bh, bhat_stride, dout, c, sl.stream);
     if (st != CFFT_OK) return st;
-    CFFT_CUDA_TRY(cudaMemcpyAsync(out + first * plan->N, dout, c * poly_bytes, cudaMemcpyDeviceToHost, sl.stream));
+    if (!mapped_out)
+      CFFT_CUDA_TRY(cudaMemcpyAsync(out + first * plan->N, dout, c * poly_bytes, cudaMemcpyDeviceToHost, sl.stream));
   }
   for (int k = 0; k < kSlots; ++k) CFFT_CUDA_TRY(cudaStreamSynchronize(slot[k].stream));
   return CFFT_OK;

@@ -163,6 +163,20 @@ cfft_status host_pipeline(int nslots, size_t bytes, PipeSlot* slots) {
   return CFFT_OK;
 }
 
+void* mapped_host_range(const void* p, size_t bytes) {
+  if (!p || bytes == 0) return nullptr;
+  cudaPointerAttributes first{}, last{};
+  const char* end = (const char*)p + bytes - 1;
+  if (cudaPointerGetAttributes(&first, p) != cudaSuccess || cudaPointerGetAttributes(&last, end) != cudaSuccess) {
+    cudaGetLastError();  // pageable memory on older drivers reports an error: clear it
+    return nullptr;
+  }
+  if (first.type != cudaMemoryTypeHost || last.type != cudaMemoryTypeHost) return nullptr;
+  if (!first.devicePointer || !last.devicePointer) return nullptr;
+  if ((const char*)last.devicePointer - (const char*)first.devicePointer != (long)(bytes - 1)) return nullptr;
+  return first.devicePointer;
+}
+
 }  // namespace cfft
 
 extern "C" {

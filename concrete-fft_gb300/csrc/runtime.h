@@ -66,4 +66,10 @@ struct PipeSlot {
 };
 cfft_status host_pipeline(int nslots, size_t bytes, PipeSlot* slots);
 
+// The device address of `bytes` of page-locked host memory starting at p, or
+// nullptr when the range is not one page-locked, device-mapped allocation
+// (pageable memory, device memory).  Kernels then write results there
+// directly: on a Grace host they cross NVLink-C2C as the kernel stores them.
+void* mapped_host_range(const void* p, size_t bytes);
+
 }  // namespace cfft

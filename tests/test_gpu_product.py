@@ -106,6 +106,47 @@ def test_u64_product_host_pipeline_chunks(cuda, oracle):
     assert np.array_equal(out, want)
 
 
+@pytest.mark.parametrize("N,count", [(2048, 2000), (65536, 80)])
+def test_u64_product_host_page_locked_out(cuda, oracle, N, count):
+    """Host entry point with page-locked host buffers: the kernels store the results
+    into host memory themselves (no copy out).  Same bits as the copy path."""
+    import concrete_fft as cf
+    torch = cuda
+    plan = cf.product.U64ProductPlan(N, 2, 1024)
+    a = RNG.integers(0, 2 ** 64, (count, N), dtype=np.uint64)
+    b = RNG.integers(-2 ** 7, 2 ** 7, (count, N))
+    bhat = torch.empty((count, N // 2), dtype=torch.complex128, device="cuda")
+    plan.prepare_operand(torch.from_numpy(b).cuda(), bhat)
+    ha = torch.from_numpy(a.view(np.int64)).pin_memory()
+    hout = torch.full_like(ha, -1).pin_memory()
+    plan.product(ha, bhat, hout)
+    copied = np.zeros_like(a)
+    plan.product(a, bhat, copied)  # pageable: copies in and out
+    assert np.array_equal(hout.numpy().view(np.uint64), copied)
+    sel = [0, count // 2, count - 1]
+    want = oracle.u64_product(N, 2, 1024, a[sel], bhat[sel].cpu().numpy(), nthreads=0)
+    assert np.array_equal(copied[sel], want)
+
+
+def test_u128_product_host_page_locked_out(cuda, oracle):
+    import concrete_fft as cf
+    torch = cuda
+    N, count = 1024, 700
+    plan = cf.product.U128ProductPlan(N)
+    a = RNG.integers(0, 2 ** 64, (count, N, 2), dtype=np.uint64)
+    b = RNG.integers(-2 ** 15, 2 ** 15, (count, N))
+    bhat = torch.empty((count, 4, N // 2), dtype=torch.float64, device="cuda")
+    plan.prepare_operand(torch.from_numpy(b).cuda(), bhat)
+    ha = torch.from_numpy(a.view(np.int64)).pin_memory()
+    hout = torch.full_like(ha, -1).pin_memory()
+    plan.product(ha, bhat, hout)
+    copied = np.zeros_like(a)
+    plan.product(a, bhat, copied)
+    assert np.array_equal(hout.numpy().view(np.uint64), copied)
+    want = oracle.u128_product(N, a[[0, 699]], bhat[[0, 699]].cpu().numpy(), nthreads=0)
+    assert np.array_equal(copied[[0, 699]], want)
+
+
 def test_u64_measure_plan(cuda, oracle):
     import concrete_fft as cf
     plan = cf.product.U64ProductPlan(2048, measure_seconds=0.001)

@@ -25,6 +25,7 @@ template <bool FWD>
 __global__ void __launch_bounds__(256) c64_level_kernel(double2* data, long total, int log2r, int log2nl,
                                                         const double2* __restrict__ wl) {
   const int lm = log2nl - log2r;
+  grid_dependency_wait();
   for (long g = (long)blockIdx.x * blockDim.x + threadIdx.x; g < total; g += (long)gridDim.x * blockDim.x) {
     double2* zc = data + ((g >> lm) << log2nl);
     const int i = (int)(g & ((1L << lm) - 1));
@@ -197,7 +198,7 @@ cfft_status launch_smem(const C64Plan& p, bool fwd, int blocks, size_t smem, cud
   DevLevels L = p.dlv;
   int tpc = p.tpc, d0 = p.d0;
   void* args[] = {&data, &nsub, &tpc, &L, &d0, (void*)&w};
-  return launch_kernel(c64_kernel(p.base_algo, p.emu, fwd), blocks, p.threads, args, smem, stream);
+  return launch_kernel(c64_kernel(p.base_algo, p.emu, fwd), blocks, p.threads, args, smem, stream, true);
 }
 
 cfft_status build_plan(C64Plan& p, size_t n, size_t base_n, int algo, bool unordered) {
@@ -271,7 +272,15 @@ cfft_status launch_split(const C64Plan& p, bool fwd, int ls, int mode, long nsub
   void* args[] = {&data, &L, (void*)&w};
   if ((nsub << ls) > 0x7fffffffL) return fail(CFFT_ERR_INVALID_SIZE, "batch too large");
   const int grid = (int)(nsub << ls);
-  return launch_kernel_cluster(fn, grid, threads, 1 << ls, args, smem, stream);
+  return launch_kernel_cluster(fn, grid, threads, 1 << ls, args, smem, stream, true);
+}
+
+cfft_status launch_level(bool fwd, double2* data, long total, int log2r, int log2nl, const double2* wl, int nsm,
+                         cudaStream_t stream) {
+  const int grid = (int)std::min<long>((total + 255) / 256, (long)nsm * 16);
+  void* args[] = {&data, &total, &log2r, &log2nl, (void*)&wl};
+  const void* fn = fwd ? (const void*)c64_level_kernel<true> : (const void*)c64_level_kernel<false>;
+  return launch_kernel(fn, grid, 256, args, 0, stream, true);
 }
 
 cfft_status run_plan(const C64Plan& p, double* buf, size_t batch, bool fwd, cudaStream_t stream) {
@@ -291,10 +300,9 @@ cfft_status run_plan(const C64Plan& p, double* buf, size_t batch, bool fwd, cuda
   const int nsm = sm_count();
   if (fwd) {
     for (int l = 0; l < p.d0; ++l) {
-      const long total = ((long)batch << log2n) >> p.lv.log2r[l];
-      const int grid = (int)std::min<long>((total + 255) / 256, (long)nsm * 16);
-      c64_level_kernel<true><<<grid, 256, 0, stream>>>(data, total, p.lv.log2r[l], p.lv.log2n[l], p.d_w + p.lv.w_off[l]);
-      CFFT_CHECK_LAUNCH();
+      cfft_status st = launch_level(true, data, ((long)batch << log2n) >> p.lv.log2r[l], p.lv.log2r[l],
+                                    p.lv.log2n[l], p.d_w + p.lv.w_off[l], nsm, stream);
+      if (st != CFFT_OK) return st;
     }
     cfft_status st = launch_smem(p, true, blocks, smem, stream, data, (int)nsub, p.d_w);
     if (st != CFFT_OK) return st;
@@ -302,11 +310,9 @@ cfft_status run_plan(const C64Plan& p, double* buf, size_t batch, bool fwd, cuda
     cfft_status st = launch_smem(p, false, blocks, smem, stream, data, (int)nsub, p.d_winv);
     if (st != CFFT_OK) return st;
     for (int l = p.d0 - 1; l >= 0; --l) {
-      const long total = ((long)batch << log2n) >> p.lv.log2r[l];
-      const int grid = (int)std::min<long>((total + 255) / 256, (long)nsm * 16);
-      c64_level_kernel<false>
-          <<<grid, 256, 0, stream>>>(data, total, p.lv.log2r[l], p.lv.log2n[l], p.d_winv + p.lv.winv_off[l]);
-      CFFT_CHECK_LAUNCH();
+      st = launch_level(false, data, ((long)batch << log2n) >> p.lv.log2r[l], p.lv.log2r[l], p.lv.log2n[l],
+                        p.d_winv + p.lv.winv_off[l], nsm, stream);
+      if (st != CFFT_OK) return st;
     }
   }
   return CFFT_OK;

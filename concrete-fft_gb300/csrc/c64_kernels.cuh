@@ -16,6 +16,7 @@ template <int ALGO, int E, bool FWD>
 __global__ void __launch_bounds__(256) c64_smem_kernel(double2* data, int count, int tpc, DevLevels L, int d0,
                                                        const double2* __restrict__ w) {
   extern __shared__ double2 smem[];
+  grid_dependency_wait();
   const int log2sub = L.log2n[d0];
   const long first = (long)blockIdx.x * tpc;
   const int nch = (int)min((long)tpc, (long)count - first);

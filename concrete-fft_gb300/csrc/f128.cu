@@ -29,6 +29,7 @@ __global__ void __launch_bounds__(256) f128_smem_kernel(F128Arrays g, int log2n,
   F128Arrays s{sm, sm + c, sm + 2 * c, sm + 3 * c};
   const int tid = threadIdx.x, nth = blockDim.x;
   const long per_transform = 1L << (log2n - log2c);
+  grid_dependency_wait();
   for (long blk = blockIdx.x; blk < nblocks; blk += gridDim.x) {
     const long off = blk << log2c;
     const long sb = blk % per_transform;  // sub-block index inside its transform
@@ -54,6 +55,7 @@ __global__ void __launch_bounds__(256) f128_smem_kernel(F128Arrays g, int log2n,
 template <bool FWD>
 __global__ void __launch_bounds__(256) f128_stage_kernel(F128Arrays g, int log2n, int log2t, long total, F128Tw tw) {
   const long m = 1L << (log2n - 1 - log2t);
+  grid_dependency_wait();
   for (long b = (long)blockIdx.x * blockDim.x + threadIdx.x; b < total; b += (long)gridDim.x * blockDim.x) {
     const long tr = b >> (log2n - 1);                 // transform index
     const long bb = b & ((1L << (log2n - 1)) - 1);    // butterfly within transform
@@ -322,22 +324,26 @@ cfft_status run_f128_tw(size_t n, const F128Tw& tw, double* re0, double* re1, do
                                 threads, smem, nblocks);
   const long total = (long)batch << (log2n - 1);
   const int sgrid = (int)std::min<long>((total + 255) / 256, (long)sm_count() * 16);
+  // programmatic dependent launches: each kernel is launched as the previous one's CTAs exit
+  F128Tw t = tw;
+  long tot = total, nb = nblocks;
+  int ln = log2n, lc = log2c;
+  auto stage = [&](int lt) {
+    void* args[] = {&g, &ln, &lt, &tot, &t};
+    return launch_kernel(fwd ? (const void*)f128_stage_kernel<true> : (const void*)f128_stage_kernel<false>, sgrid,
+                         256, args, 0, stream, true);
+  };
+  void* sargs[] = {&g, &ln, &lc, &nb, &t};
+  const void* sfn = fwd ? (const void*)f128_smem_kernel<true> : (const void*)f128_smem_kernel<false>;
+  cfft_status st = CFFT_OK;
   if (fwd) {
-    for (int lt = log2n - 1; lt >= log2c; --lt) {
-      f128_stage_kernel<true><<<sgrid, 256, 0, stream>>>(g, log2n, lt, total, tw);
-      CFFT_CHECK_LAUNCH();
-    }
-    f128_smem_kernel<true><<<grid, threads, smem, stream>>>(g, log2n, log2c, nblocks, tw);
-    CFFT_CHECK_LAUNCH();
+    for (int lt = log2n - 1; lt >= log2c && st == CFFT_OK; --lt) st = stage(lt);
+    if (st == CFFT_OK) st = launch_kernel(sfn, grid, threads, sargs, smem, stream, true);
   } else {
-    f128_smem_kernel<false><<<grid, threads, smem, stream>>>(g, log2n, log2c, nblocks, tw);
-    CFFT_CHECK_LAUNCH();
-    for (int lt = log2c; lt <= log2n - 1; ++lt) {
-      f128_stage_kernel<false><<<sgrid, 256, 0, stream>>>(g, log2n, lt, total, tw);
-      CFFT_CHECK_LAUNCH();
-    }
+    st = launch_kernel(sfn, grid, threads, sargs, smem, stream, true);
+    for (int lt = log2c; lt <= log2n - 1 && st == CFFT_OK; ++lt) st = stage(lt);
   }
-  return CFFT_OK;
+  return st;
 }
 
 int elementwise_grid(long total) {

@@ -88,16 +88,31 @@ cfft_status ensure_smem_attr(const void* fn, size_t smem) {
 }
 }  // namespace
 
-cfft_status launch_kernel(const void* fn, int grid, int block, void** args, size_t smem, cudaStream_t stream) {
+cfft_status launch_kernel(const void* fn, int grid, int block, void** args, size_t smem, cudaStream_t stream,
+                          bool pdl) {
   if (!fn) return fail(CFFT_ERR_INVALID_ARGUMENT, "no kernel instantiated for this configuration");
   cfft_status st = ensure_smem_attr(fn, smem);
   if (st != CFFT_OK) return st;
-  CFFT_CUDA_TRY(cudaLaunchKernel(fn, dim3(grid), dim3(block), args, smem, stream));
+  if (!pdl) {
+    CFFT_CUDA_TRY(cudaLaunchKernel(fn, dim3(grid), dim3(block), args, smem, stream));
+    return CFFT_OK;
+  }
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3((unsigned)grid);
+  cfg.blockDim = dim3((unsigned)block);
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = stream;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  attr[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  CFFT_CUDA_TRY(cudaLaunchKernelExC(&cfg, fn, args));
   return CFFT_OK;
 }
 
 cfft_status launch_kernel_cluster(const void* fn, int grid, int block, int cluster, void** args, size_t smem,
-                                  cudaStream_t stream) {
+                                  cudaStream_t stream, bool pdl) {
   if (!fn) return fail(CFFT_ERR_INVALID_ARGUMENT, "no kernel instantiated for this configuration");
   if (cluster < 1 || cluster > 8 || grid % cluster != 0) return fail(CFFT_ERR_INVALID_ARGUMENT, "bad cluster shape");
   cfft_status st = ensure_smem_attr(fn, smem);
@@ -107,13 +122,15 @@ cfft_status launch_kernel_cluster(const void* fn, int grid, int block, int clust
   cfg.blockDim = dim3((unsigned)block);
   cfg.dynamicSmemBytes = smem;
   cfg.stream = stream;
-  cudaLaunchAttribute attr[1];
+  cudaLaunchAttribute attr[2];
   attr[0].id = cudaLaunchAttributeClusterDimension;
   attr[0].val.clusterDim.x = (unsigned)cluster;
   attr[0].val.clusterDim.y = 1;
   attr[0].val.clusterDim.z = 1;
+  attr[1].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  attr[1].val.programmaticStreamSerializationAllowed = 1;
   cfg.attrs = attr;
-  cfg.numAttrs = 1;
+  cfg.numAttrs = pdl ? 2 : 1;
   CFFT_CUDA_TRY(cudaLaunchKernelExC(&cfg, fn, args));
   return CFFT_OK;
 }

@@ -45,14 +45,17 @@ cfft_status upload(const T* host, size_t count, T** dev) {
 int sm_count();
 
 // Launch a kernel through its pointer, raising its dynamic shared-memory limit
-// the first time it is used with more than 48 KiB.
-cfft_status launch_kernel(const void* fn, int grid, int block, void** args, size_t smem, cudaStream_t stream);
+// the first time it is used with more than 48 KiB.  `pdl`: programmatic stream
+// serialization (the kernel may start while the previous one drains; it must
+// call grid_dependency_wait() before its first global access).
+cfft_status launch_kernel(const void* fn, int grid, int block, void** args, size_t smem, cudaStream_t stream,
+                          bool pdl = false);
 // Raises a kernel's dynamic shared-memory limit to `smem` on the current
 // device, once (thread-safe); a no-op up to 48 KiB.
 cfft_status ensure_smem(const void* fn, size_t smem);
 // The same with a thread-block cluster of `cluster` CTAs (grid a multiple of it).
 cfft_status launch_kernel_cluster(const void* fn, int grid, int block, int cluster, void** args, size_t smem,
-                                  cudaStream_t stream);
+                                  cudaStream_t stream, bool pdl = false);
 int max_blocks_per_sm(const void* fn, int block, size_t smem);
 
 // Persistent scratch for the *_host convenience entry points (one per thread).

@@ -165,6 +165,7 @@ __global__ void __launch_bounds__(256) c64_split_kernel(double2* data, DevLevels
   constexpr int S = 1 << LS;
   constexpr bool LAST = MODE == 0 ? AlgoInfo<ALGO>::DIT : !FWD;
   extern __shared__ double2 smem[];
+  grid_dependency_wait();
   const int log2n = L.log2n[0];
   const int log2c = log2n - LS;
   const int c = (int)(blockIdx.x & (S - 1));

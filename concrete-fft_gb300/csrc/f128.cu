@@ -158,6 +158,7 @@ __global__ void __launch_bounds__(256) u128_prepare_kernel(const int64_t* __rest
 // a (N (lo, hi) pairs per product) -> f128 points, as u128_product_kernel does.
 __global__ void __launch_bounds__(256) u128_fold_kernel(const uint64_t* __restrict__ a, F128Arrays z, long count,
                                                        int log2n) {
+  grid_dependency_wait();
   const long n = 1L << log2n;
   const long total = count << (log2n + 1);
   for (long g = (long)blockIdx.x * blockDim.x + threadIdx.x; g < total; g += (long)gridDim.x * blockDim.x) {
@@ -184,6 +185,7 @@ __global__ void __launch_bounds__(256) u128_fold_kernel(const uint64_t* __restri
 // z <- (z * bhat) * factor, the fused kernel's double-double pointwise step.
 __global__ void __launch_bounds__(256) u128_pointwise_kernel(F128Arrays z, const double* __restrict__ bhat,
                                                             long bhat_stride, long count, int log2n, double factor) {
+  grid_dependency_wait();
   const long n = 1L << log2n;
   const long total = count << log2n;
   for (long g = (long)blockIdx.x * blockDim.x + threadIdx.x; g < total; g += (long)gridDim.x * blockDim.x) {
@@ -202,6 +204,7 @@ __global__ void __launch_bounds__(256) u128_pointwise_kernel(F128Arrays z, const
 // f128 points -> N (lo, hi) pairs, floor(x + 1/2) mod 2^128.
 __global__ void __launch_bounds__(256) u128_round_kernel(F128Arrays z, uint64_t* __restrict__ out, long count,
                                                         int log2n) {
+  grid_dependency_wait();
   const long n = 1L << log2n;
   const long total = count << (log2n + 1);
   for (long g = (long)blockIdx.x * blockDim.x + threadIdx.x; g < total; g += (long)gridDim.x * blockDim.x) {
@@ -218,6 +221,7 @@ __global__ void __launch_bounds__(256) u128_round_kernel(F128Arrays z, uint64_t*
 // -> the operand layout (four arrays of n per operand).
 __global__ void __launch_bounds__(256) u128_prepare_fold_kernel(const int64_t* __restrict__ b, F128Arrays z,
                                                                long count, int log2n) {
+  grid_dependency_wait();
   const long n = 1L << log2n;
   const long total = count << log2n;
   for (long g = (long)blockIdx.x * blockDim.x + threadIdx.x; g < total; g += (long)gridDim.x * blockDim.x) {
@@ -231,6 +235,7 @@ __global__ void __launch_bounds__(256) u128_prepare_fold_kernel(const int64_t* _
 }
 __global__ void __launch_bounds__(256) u128_operand_layout_kernel(F128Arrays z, double* __restrict__ bhat,
                                                                  long count, int log2n) {
+  grid_dependency_wait();
   const long n = 1L << log2n;
   const long total = count << log2n;
   for (long g = (long)blockIdx.x * blockDim.x + threadIdx.x; g < total; g += (long)gridDim.x * blockDim.x) {
@@ -511,12 +516,14 @@ cfft_status cfft_u128_prepare_operand(const cfft_u128_product_plan* p, const int
     cfft_status st = workspace_alloc(count, p->f.n, s, &z);
     if (st != CFFT_OK) return st;
     const long total = (long)count << log2n;
-    u128_prepare_fold_kernel<<<elementwise_grid(total), 256, 0, s>>>(b, z, (long)count, log2n);
-    CFFT_CHECK_LAUNCH();
+    CFFT_CUDA_TRY(launch_dependent(u128_prepare_fold_kernel, elementwise_grid(total), 256, 0, s, b, z, (long)count,
+                                   log2n));
     st = run_f128_tw(p->f.n, p->f.tw(), z.re0, z.re1, z.im0, z.im1, count, true, s, p->f.block_log2);
     if (st == CFFT_OK) {
-      u128_operand_layout_kernel<<<elementwise_grid(total), 256, 0, s>>>(z, bhat4, (long)count, log2n);
-      st = cudaGetLastError() == cudaSuccess ? CFFT_OK : fail(CFFT_ERR_CUDA, "operand layout launch");
+      st = launch_dependent(u128_operand_layout_kernel, elementwise_grid(total), 256, 0, s, z, bhat4, (long)count,
+                            log2n) == cudaSuccess
+               ? CFFT_OK
+               : fail(CFFT_ERR_CUDA, "operand layout launch");
     }
     cudaFreeAsync(z.re0, s);
     return st;
@@ -547,19 +554,21 @@ cfft_status cfft_u128_product(const cfft_u128_product_plan* p, const uint64_t* a
     cfft_status st = workspace_alloc(count, p->f.n, s, &z);
     if (st != CFFT_OK) return st;
     const long total = (long)count << log2n;
-    u128_fold_kernel<<<elementwise_grid(2 * total), 256, 0, s>>>(a, z, (long)count, log2n);
-    CFFT_CHECK_LAUNCH();
+    CFFT_CUDA_TRY(launch_dependent(u128_fold_kernel, elementwise_grid(2 * total), 256, 0, s, a, z, (long)count, log2n));
     st = run_f128_tw(p->f.n, p->f.tw(), z.re0, z.re1, z.im0, z.im1, count, true, s, p->f.block_log2);
     if (st == CFFT_OK) {
-      u128_pointwise_kernel<<<elementwise_grid(total), 256, 0, s>>>(z, bhat4, (long)bhat_stride, (long)count, log2n,
-                                                                    2.0 / (double)p->N);
-      st = cudaGetLastError() == cudaSuccess ? CFFT_OK : fail(CFFT_ERR_CUDA, "pointwise launch");
+      st = launch_dependent(u128_pointwise_kernel, elementwise_grid(total), 256, 0, s, z, bhat4, (long)bhat_stride,
+                            (long)count, log2n, 2.0 / (double)p->N) == cudaSuccess
+               ? CFFT_OK
+               : fail(CFFT_ERR_CUDA, "pointwise launch");
     }
     if (st == CFFT_OK)
       st = run_f128_tw(p->f.n, p->f.tw(), z.re0, z.re1, z.im0, z.im1, count, false, s, p->f.block_log2);
     if (st == CFFT_OK) {
-      u128_round_kernel<<<elementwise_grid(2 * total), 256, 0, s>>>(z, out, (long)count, log2n);
-      st = cudaGetLastError() == cudaSuccess ? CFFT_OK : fail(CFFT_ERR_CUDA, "round launch");
+      st = launch_dependent(u128_round_kernel, elementwise_grid(2 * total), 256, 0, s, z, out, (long)count, log2n) ==
+                   cudaSuccess
+               ? CFFT_OK
+               : fail(CFFT_ERR_CUDA, "round launch");
     }
     cudaFreeAsync(z.re0, s);
     return st;

@@ -45,6 +45,7 @@ namespace cfft {
 // The product pipeline's elementwise steps as separate kernels (the unfused path).
 __global__ void fold_twist_kernel(const uint64_t* __restrict__ a, double2* __restrict__ z, long total, int log2n,
                                   const double2* __restrict__ tw) {
+  grid_dependency_wait();
   const long n = 1L << log2n;
   for (long g = (long)blockIdx.x * blockDim.x + threadIdx.x; g < total; g += (long)gridDim.x * blockDim.x) {
     const long p = g >> log2n, j = g & (n - 1);
@@ -55,6 +56,7 @@ __global__ void fold_twist_kernel(const uint64_t* __restrict__ a, double2* __res
 }
 __global__ void pointwise_kernel(const double2* __restrict__ bhat, long bhat_stride, double2* __restrict__ z,
                                  long total, int log2n) {
+  grid_dependency_wait();
   const long n = 1L << log2n;
   for (long g = (long)blockIdx.x * blockDim.x + threadIdx.x; g < total; g += (long)gridDim.x * blockDim.x) {
     const long p = g >> log2n, k = g & (n - 1);
@@ -66,6 +68,7 @@ __global__ void pointwise_kernel(const double2* __restrict__ bhat, long bhat_str
 // sum kernels do.
 __global__ void fourier_sum_kernel(const double2* __restrict__ bhat, const double2* __restrict__ z,
                                    double2* __restrict__ acc, int terms, long total, int log2n) {
+  grid_dependency_wait();
   const long n = 1L << log2n;
   for (long g = (long)blockIdx.x * blockDim.x + threadIdx.x; g < total; g += (long)gridDim.x * blockDim.x) {
     const long grp = g >> log2n, k = g & (n - 1);
@@ -80,6 +83,7 @@ __global__ void fourier_sum_kernel(const double2* __restrict__ bhat, const doubl
 }
 __global__ void untwist_round_kernel(const double2* __restrict__ z, uint64_t* __restrict__ out, long total, int log2n,
                                      const double2* __restrict__ itw) {
+  grid_dependency_wait();
   const long n = 1L << log2n;
   for (long g = (long)blockIdx.x * blockDim.x + threadIdx.x; g < total; g += (long)gridDim.x * blockDim.x) {
     const long p = g >> log2n, j = g & (n - 1);
@@ -146,9 +150,10 @@ cfft_status product_sum_unfused(const cfft_u64_product_plan* plan, const uint64_
     if (st == CFFT_OK) st = cfft_unordered_fwd(plan->fft, (double*)z, g * terms, s);
     if (st == CFFT_OK) {
       const long total = (long)(g * n);
-      fourier_sum_kernel<<<ew_grid(total), 256, 0, s>>>((const double2*)bhat + g0 * terms * n, z, acc, (int)terms,
-                                                         total, ilog2(n));
-      st = cudaGetLastError() == cudaSuccess ? CFFT_OK : fail(CFFT_ERR_CUDA, "fourier_sum_kernel launch");
+      st = launch_dependent(fourier_sum_kernel, ew_grid(total), 256, 0, s, (const double2*)bhat + g0 * terms * n, z,
+                            acc, (int)terms, total, ilog2(n)) == cudaSuccess
+               ? CFFT_OK
+               : fail(CFFT_ERR_CUDA, "fourier_sum_kernel launch");
     }
     if (st == CFFT_OK) st = cfft_unordered_inv(plan->fft, (double*)acc, g, s);
     if (st == CFFT_OK) st = cfft_u64_untwist_round(plan, (const double*)acc, out + g0 * plan->N, g, s);
@@ -248,9 +253,8 @@ cfft_status cfft_u64_fold_twist(const cfft_u64_product_plan* plan, const uint64_
   if (!plan || !a || !z) return fail(CFFT_ERR_INVALID_ARGUMENT, "null argument");
   if (count == 0) return CFFT_OK;
   const long total = (long)(count * plan->n);
-  fold_twist_kernel<<<ew_grid(total), 256, 0, (cudaStream_t)stream>>>(a, (double2*)z, total, ilog2(plan->n),
-                                                                      plan->d_tw);
-  CFFT_CHECK_LAUNCH();
+  CFFT_CUDA_TRY(launch_dependent(fold_twist_kernel, ew_grid(total), 256, 0, (cudaStream_t)stream, a, (double2*)z,
+                                 total, ilog2(plan->n), (const double2*)plan->d_tw));
   return CFFT_OK;
 }
 
@@ -260,9 +264,8 @@ cfft_status cfft_c64_pointwise(const double* bhat, size_t bhat_stride, double* z
   if (!is_pow2(n)) return fail(CFFT_ERR_INVALID_SIZE, "n must be a power of two");
   if (count == 0) return CFFT_OK;
   const long total = (long)(count * n);
-  pointwise_kernel<<<ew_grid(total), 256, 0, (cudaStream_t)stream>>>((const double2*)bhat, (long)bhat_stride,
-                                                                     (double2*)z, total, ilog2(n));
-  CFFT_CHECK_LAUNCH();
+  CFFT_CUDA_TRY(launch_dependent(pointwise_kernel, ew_grid(total), 256, 0, (cudaStream_t)stream, (const double2*)bhat,
+                                 (long)bhat_stride, (double2*)z, total, ilog2(n)));
   return CFFT_OK;
 }
 
@@ -271,9 +274,8 @@ cfft_status cfft_u64_untwist_round(const cfft_u64_product_plan* plan, const doub
   if (!plan || !z || !out) return fail(CFFT_ERR_INVALID_ARGUMENT, "null argument");
   if (count == 0) return CFFT_OK;
   const long total = (long)(count * plan->n);
-  untwist_round_kernel<<<ew_grid(total), 256, 0, (cudaStream_t)stream>>>((const double2*)z, out, total,
-                                                                         ilog2(plan->n), plan->d_itw);
-  CFFT_CHECK_LAUNCH();
+  CFFT_CUDA_TRY(launch_dependent(untwist_round_kernel, ew_grid(total), 256, 0, (cudaStream_t)stream,
+                                 (const double2*)z, out, total, ilog2(plan->n), (const double2*)plan->d_itw));
   return CFFT_OK;
 }
 
@@ -400,7 +402,12 @@ cfft_status cfft_u64_product(const cfft_u64_product_plan* plan, const uint64_t* 
   // (no cluster holds it), and large batches of N >= 32768, where it measured faster
   // than one cluster per product (304 vs 280 k products/s at 32768, 129 vs 102 k at 65536)
   const bool many = (long)count >= (long)sm_count() / 2 && plan->cluster == 0;
-  if (!ok || (plan->N >= 32768 && many)) {
+  // A few products whose transform has no outer level (n = base_n), so no cluster
+  // can split the fused kernel, also take the five launches: their transforms
+  // split over 2-8 CTAs each, and the launches follow one another without gaps
+  // (one product at N = 2048, base 1024: 20 vs 31 us; 76 products: 26 vs 31 us)
+  const bool few_unsplit = ls == 0 && plan->cluster == 0 && plan->N >= 2048 && !many;
+  if (!ok || (plan->N >= 32768 && many) || few_unsplit) {
     cudaStream_t s = (cudaStream_t)stream;
     void* z = nullptr;
     if (cudaMallocAsync(&z, count * plan->n * sizeof(double2), s) != cudaSuccess)

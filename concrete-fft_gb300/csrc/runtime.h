@@ -58,6 +58,24 @@ cfft_status launch_kernel_cluster(const void* fn, int grid, int block, int clust
                                   cudaStream_t stream, bool pdl = false);
 int max_blocks_per_sm(const void* fn, int block, size_t smem);
 
+// kernel<<<grid, block, smem, stream>>>(args...) as a programmatic dependent
+// launch (the kernel calls grid_dependency_wait() before its first global access).
+template <typename... Params, typename... Args>
+cudaError_t launch_dependent(void (*kernel)(Params...), int grid, int block, size_t smem, cudaStream_t stream,
+                             Args... args) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3((unsigned)grid);
+  cfg.blockDim = dim3((unsigned)block);
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = stream;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  attr[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  return cudaLaunchKernelEx(&cfg, kernel, static_cast<Params>(args)...);
+}
+
 // Persistent scratch for the *_host convenience entry points (one per thread).
 cfft_status host_staging(size_t bytes, void** dev_ptr, cudaStream_t* stream);
 

@@ -283,7 +283,8 @@ cfft_status launch_level(bool fwd, double2* data, long total, int log2r, int log
   return launch_kernel(fn, grid, 256, args, 0, stream, true);
 }
 
-cfft_status run_plan(const C64Plan& p, double* buf, size_t batch, bool fwd, cudaStream_t stream) {
+cfft_status run_plan(const C64Plan& p, double* buf, size_t batch, bool fwd, cudaStream_t stream,
+                     bool allow_split = true) {
   if (batch == 0) return CFFT_OK;
   if (buf == nullptr) return fail(CFFT_ERR_INVALID_ARGUMENT, "null buffer");
   if (p.n == 1) return CFFT_OK;
@@ -293,7 +294,7 @@ cfft_status run_plan(const C64Plan& p, double* buf, size_t batch, bool fwd, cuda
   const long nsub = (long)batch << (log2n - log2sub);
   if (nsub > 0x7fffffffL * (long)p.tpc) return fail(CFFT_ERR_INVALID_SIZE, "batch too large");
   int mode = 0;
-  const int ls = split_log2(p, (long)batch, &mode);
+  const int ls = allow_split ? split_log2(p, (long)batch, &mode) : 0;
   if (ls > 0) return launch_split(p, fwd, ls, mode, (long)batch, stream, data);
   const int blocks = (int)((nsub + p.tpc - 1) / p.tpc);
   const size_t smem = smem_bytes(p);
@@ -323,6 +324,21 @@ cfft_status run_host(const C64Plan& p, double* buf, size_t batch, bool fwd) {
   const size_t bytes = batch * p.n * sizeof(double2);
   void* d = nullptr;
   cudaStream_t s;
+  // A page-locked buffer, and a transform that one kernel does whole (no level in
+  // global memory): the kernel reads and writes the caller's memory in place,
+  // across NVLink-C2C on a Grace host, with no staging copy.  From 16 transforms
+  // on, one CTA per transform: the parts of a split transform each read the
+  // whole transform, which over the link costs more than the split gains.
+  if (p.d0 == 0) {
+    if (void* mapped = mapped_host_range(buf, bytes)) {
+      cfft_status st = host_staging(0, &d, &s);
+      if (st != CFFT_OK) return st;
+      st = run_plan(p, (double*)mapped, batch, fwd, s, batch < 16);
+      if (st != CFFT_OK) return st;
+      CFFT_CUDA_TRY(cudaStreamSynchronize(s));
+      return CFFT_OK;
+    }
+  }
   cfft_status st = host_staging(bytes, &d, &s);
   if (st != CFFT_OK) return st;
   CFFT_CUDA_TRY(cudaMemcpyAsync(d, buf, bytes, cudaMemcpyHostToDevice, s));

@@ -101,6 +101,29 @@ CASES = [(32, 32), (64, 32), (256, 32), (1024, 32), (1024, 512), (1024, 1024), (
          (8192, 1024), (16384, 512), (65536, 1024), (65536, 32), (1 << 20, 1024), (1 << 22, 1024), (1 << 22, 32)]
 
 
+@pytest.mark.parametrize("batch", [1, 5, 64])
+def test_host_entry_page_locked_in_place(cuda, oracle, batch):
+    """Host entry points on page-locked buffers: one-kernel transforms read and write
+    the caller's memory in place (split over a cluster below 16 transforms, one CTA
+    per transform above).  Bits equal the oracle's."""
+    import concrete_fft as cf
+    torch = cuda
+    for algo in (2, 3, 6):
+        plan = cf.ordered.Plan(1024, cf.ordered.Method.UserProvided(algo))
+        x = rand_c64(batch, 1024)
+        h = torch.from_numpy(x.copy()).pin_memory()
+        plan.fwd(h)
+        want = oracle.ordered_fwd(algo, x)
+        assert np.array_equal(bits(h.numpy()), bits(want)), (algo, batch)
+        plan.inv(h)
+        assert np.array_equal(bits(h.numpy()), bits(oracle.ordered_inv(algo, want))), (algo, batch)
+    plan = cf.unordered.Plan(2048, cf.unordered.Method.UserProvided(2, 256))
+    x = rand_c64(batch, 2048)
+    h = torch.from_numpy(x.copy()).pin_memory()
+    plan.fwd(h)
+    assert np.array_equal(bits(h.numpy()), bits(oracle.unordered_fwd(2, 256, x, nthreads=0)))
+
+
 @pytest.mark.parametrize("n,base", CASES)
 def test_unordered_bit_exact(cuda, oracle, n, base):
     import concrete_fft as cf

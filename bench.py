@@ -774,6 +774,8 @@ def run_serving(args):
         clk.mark(t1, time.time())
     # the same stream with every product on the engine (no clusters for N >= 8192)
     no_cluster = srv.run(srv.config(rate=args.rate, duration_s=args.serve_seconds, cluster_log2N=32))
+    # the same stream with item records copied in and results copied out per launch
+    staged = srv.run(srv.config(rate=args.rate, duration_s=args.serve_seconds, staged_io=True))
     # capacity: the continuous-batching loop at higher arrival rates (same request mix)
     sweep = {}
     for rate in (50000.0, 100000.0, 150000.0, 200000.0):
@@ -792,7 +794,7 @@ def run_serving(args):
         "config": {"workload": "serving, (k+1)*l products per request, k in 1..2, l in 1..4, N in 2^10..2^14, "
                                "digits b in 4..10 bits", "duration_s": args.serve_seconds,
                    "resident_setup_s": setup_s},
-        "batched": batched, "batched_without_clusters": no_cluster, "plain": plain,
+        "batched": batched, "batched_without_clusters": no_cluster, "batched_staged_io": staged, "plain": plain,
         "capacity_sweep_req_per_s": sweep,
         "p99_speedup_vs_plain": plain["p99_ms"] / batched["p99_ms"] if batched["p99_ms"] else None,
         "clocks": clk.summary(), "gpu_launches": batched["launches"],

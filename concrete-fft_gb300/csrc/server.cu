@@ -77,7 +77,8 @@ struct Slot {
   unsigned int* counter = nullptr;
   double* ws = nullptr;
   cfft_product_item* d_items = nullptr;
-  cfft_product_item* h_items = nullptr;
+  cfft_product_item* h_items = nullptr;      // page-locked
+  cfft_product_item* h_items_dev = nullptr;  // the device address of h_items
   size_t item_cap = 0;
   bool busy = false;
   std::vector<size_t> reqs;  // indices into the request table
@@ -99,6 +100,7 @@ struct cfft_server {
   // output ring (device) and its pinned host mirror
   uint8_t* d_ring = nullptr;
   uint8_t* h_ring = nullptr;
+  uint8_t* h_ring_dev = nullptr;  // the device address of h_ring (page-locked)
   uint64_t ring_cap = 0;
   std::map<uint64_t, std::vector<uint64_t>> recorded;
   std::vector<double> last_latency;
@@ -155,6 +157,7 @@ cfft_status ensure_items(Slot& sl, size_t n) {
   sl.h_items = nullptr;
   CFFT_CUDA_TRY(cudaMalloc(&sl.d_items, cap * sizeof(cfft_product_item)));
   CFFT_CUDA_TRY(cudaMallocHost(&sl.h_items, cap * sizeof(cfft_product_item)));
+  CFFT_CUDA_TRY(cudaHostGetDevicePointer((void**)&sl.h_items_dev, sl.h_items, 0));
   sl.item_cap = cap;
   return CFFT_OK;
 }
@@ -291,7 +294,8 @@ cfft_status cfft_server_create(const cfft_product_engine* engine, const uint32_t
     size_t free_b = 0, total_b = 0;
     cudaMemGetInfo(&free_b, &total_b);
     s->ring_cap = ring_bytes ? ring_bytes : std::min<uint64_t>(free_b / 4, uint64_t(4) << 30);
-    if (cudaMalloc(&s->d_ring, s->ring_cap) != cudaSuccess || cudaMallocHost(&s->h_ring, s->ring_cap) != cudaSuccess)
+    if (cudaMalloc(&s->d_ring, s->ring_cap) != cudaSuccess || cudaMallocHost(&s->h_ring, s->ring_cap) != cudaSuccess ||
+        cudaHostGetDevicePointer((void**)&s->h_ring_dev, s->h_ring, 0) != cudaSuccess)
       st = fail(CFFT_ERR_OUT_OF_MEMORY, "server output ring");
   }
   cudaStreamDestroy(prep);
@@ -400,6 +404,11 @@ cfft_status cfft_server_run(cfft_server* s, const cfft_serve_config* cfg, cfft_s
     }
     if (z) cudaFree(z);
   } else {
+    // direct mode: the kernels read the item records from the slot's page-locked
+    // array and store the results into the page-locked host ring (across
+    // NVLink-C2C on a Grace host); no copy in either direction
+    const bool direct = c.staged_io == 0;
+    uint8_t* out_ring = direct ? s->h_ring_dev : s->d_ring;
     for (;;) {
       const double now = now_s(t0);
       while (next < reqs.size() && reqs[next].d.arrival <= now) waiting.push_back(next++);
@@ -428,7 +437,7 @@ cfft_status cfft_server_run(cfft_server* s, const cfft_serve_config* cfg, cfft_s
           size_t at = 0;
           for (size_t ri : batch)
             if (!on_cluster[reqs[ri].d.log2N]) {
-              fill_items(s, reqs[ri].d, s->d_ring + reqs[ri].ring_off, sl.h_items + at);
+              fill_items(s, reqs[ri].d, out_ring + reqs[ri].ring_off, sl.h_items + at);
               at += reqs[ri].d.nprod;
             }
           const size_t nsmall = at;
@@ -438,50 +447,57 @@ cfft_status cfft_server_run(cfft_server* s, const cfft_serve_config* cfg, cfft_s
             group_first[lN] = at;
             for (size_t ri : batch)
               if (reqs[ri].d.log2N == lN) {
-                fill_items(s, reqs[ri].d, s->d_ring + reqs[ri].ring_off, sl.h_items + at);
+                fill_items(s, reqs[ri].d, out_ring + reqs[ri].ring_off, sl.h_items + at);
                 at += reqs[ri].d.nprod;
               }
             group_count[lN] = at - group_first[lN];
           }
-          CFFT_CUDA_TRY(cudaMemcpyAsync(sl.d_items, sl.h_items, nitems * sizeof(cfft_product_item),
-                                        cudaMemcpyHostToDevice, sl.stream));
+          const cfft_product_item* items = direct ? sl.h_items_dev : sl.d_items;
+          if (!direct)
+            CFFT_CUDA_TRY(cudaMemcpyAsync(sl.d_items, sl.h_items, nitems * sizeof(cfft_product_item),
+                                          cudaMemcpyHostToDevice, sl.stream));
           if (nsmall < nitems) {
-            CFFT_CUDA_TRY(cudaEventRecord(sl.items_ready, sl.stream));
-            CFFT_CUDA_TRY(cudaStreamWaitEvent(sl.stream2, sl.items_ready, 0));
+            if (!direct) {
+              CFFT_CUDA_TRY(cudaEventRecord(sl.items_ready, sl.stream));
+              CFFT_CUDA_TRY(cudaStreamWaitEvent(sl.stream2, sl.items_ready, 0));
+            }
             for (uint32_t lN = 0; lN <= 17; ++lN) {
               if (!group_count[lN]) continue;
-              st = u64_product_split_items(cfft_product_engine_plan(s->engine, lN), sl.d_items + group_first[lN],
+              st = u64_product_split_items(cfft_product_engine_plan(s->engine, lN), items + group_first[lN],
                                            group_count[lN], sl.stream2);
               if (st != CFFT_OK) return st;
             }
             CFFT_CUDA_TRY(cudaEventRecord(sl.big_done, sl.stream2));
           }
           if (nsmall) {
-            st = cfft_product_engine_run(s->engine, sl.d_items, nsmall, sl.counter, sl.ws, sl.stream);
+            st = cfft_product_engine_run(s->engine, items, nsmall, sl.counter, sl.ws, sl.stream);
             if (st != CFFT_OK) return st;
           }
           if (nsmall < nitems) CFFT_CUDA_TRY(cudaStreamWaitEvent(sl.stream, sl.big_done, 0));
-          // results back to the pinned host ring: the batch's requests were allocated in
-          // admission order, so they are contiguous (256-byte aligned) except across the
-          // wrap; one copy per contiguous run
-          uint64_t run_off = 0, run_end = 0;
-          bool have_run = false;
-          for (size_t ri : batch) {
-            const uint64_t off = reqs[ri].ring_off, end = off + reqs[ri].ring_bytes;
-            if (have_run && off == ((run_end + 255) & ~uint64_t(255))) {
+          // staged mode: results back to the pinned host ring (in direct mode the kernels
+          // stored them there).  The batch's requests were allocated in admission order,
+          // so they are contiguous (256-byte aligned) except across the wrap; one copy
+          // per contiguous run
+          if (!direct) {
+            uint64_t run_off = 0, run_end = 0;
+            bool have_run = false;
+            for (size_t ri : batch) {
+              const uint64_t off = reqs[ri].ring_off, end = off + reqs[ri].ring_bytes;
+              if (have_run && off == ((run_end + 255) & ~uint64_t(255))) {
+                run_end = end;
+                continue;
+              }
+              if (have_run)
+                CFFT_CUDA_TRY(cudaMemcpyAsync(s->h_ring + run_off, s->d_ring + run_off, run_end - run_off,
+                                              cudaMemcpyDeviceToHost, sl.stream));
+              run_off = off;
               run_end = end;
-              continue;
+              have_run = true;
             }
             if (have_run)
               CFFT_CUDA_TRY(cudaMemcpyAsync(s->h_ring + run_off, s->d_ring + run_off, run_end - run_off,
                                             cudaMemcpyDeviceToHost, sl.stream));
-            run_off = off;
-            run_end = end;
-            have_run = true;
           }
-          if (have_run)
-            CFFT_CUDA_TRY(cudaMemcpyAsync(s->h_ring + run_off, s->d_ring + run_off, run_end - run_off,
-                                          cudaMemcpyDeviceToHost, sl.stream));
           CFFT_CUDA_TRY(cudaEventRecord(sl.done, sl.stream));
           sl.busy = true;
           sl.reqs = batch;

@@ -335,6 +335,9 @@ typedef struct cfft_serve_config {
   uint32_t record_every; /* keep the outputs of every k-th request (0: none) */
   uint32_t cluster_log2N; /* batched mode: products with N >= 2^cluster_log2N run one per
                              thread-block cluster beside the engine launch (0: 13; > 17: never) */
+  uint32_t staged_io;    /* batched mode: 0 = the kernels read the item records from and store
+                            the results into page-locked host memory; 1 = item records copied
+                            in and results copied out per launch */
 } cfft_serve_config;
 typedef struct cfft_serve_stats {
   uint64_t requests, products, launches, deferred_admissions;

@@ -124,6 +124,37 @@ def test_host_entry_page_locked_in_place(cuda, oracle, batch):
     assert np.array_equal(bits(h.numpy()), bits(oracle.unordered_fwd(2, 256, x, nthreads=0)))
 
 
+def test_host_entry_registered_memory(cuda, oracle):
+    """Host memory page-locked by cudaHostRegister (its device address is looked up,
+    not assumed equal to the host pointer): in-place transforms and product results."""
+    import concrete_fft as cf
+    torch = cuda
+    rt = torch.cuda.cudart()
+    x = rand_c64(40, 1024)
+    h = np.ascontiguousarray(x.copy())
+    assert int(rt.cudaHostRegister(h.ctypes.data, h.nbytes, 0)) == 0
+    try:
+        plan = cf.ordered.Plan(1024, cf.ordered.Method.UserProvided(2))
+        plan.fwd(h)
+        assert np.array_equal(bits(h), bits(oracle.ordered_fwd(2, x)))
+    finally:
+        rt.cudaHostUnregister(h.ctypes.data)
+    N, count = 2048, 300
+    pp = cf.product.U64ProductPlan(N, 2, 1024)
+    a = RNG.integers(0, 2 ** 64, (count, N), dtype=np.uint64)
+    b = RNG.integers(-2 ** 7, 2 ** 7, (count, N))
+    bhat = torch.empty((count, N // 2), dtype=torch.complex128, device="cuda")
+    pp.prepare_operand(torch.from_numpy(b).cuda(), bhat)
+    out = np.zeros_like(a)
+    assert int(rt.cudaHostRegister(out.ctypes.data, out.nbytes, 0)) == 0
+    try:
+        pp.product(a, bhat, out)
+    finally:
+        rt.cudaHostUnregister(out.ctypes.data)
+    want = oracle.u64_product(N, 2, 1024, a[[0, 299]], bhat[[0, 299]].cpu().numpy(), nthreads=0)
+    assert np.array_equal(out[[0, 299]], want)
+
+
 @pytest.mark.parametrize("n,base", CASES)
 def test_unordered_bit_exact(cuda, oracle, n, base):
     import concrete_fft as cf

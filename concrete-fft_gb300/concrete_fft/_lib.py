@@ -101,6 +101,7 @@ _SIGS = [
     ("cfft_c64_pointwise", c_int, [vp, c_size, vp, c_size, c_size, vp]),
     ("cfft_u64_untwist_round", c_int, [vp, vp, vp, c_size, vp]),
     ("cfft_u64_product_fft", vp, [vp]),
+    ("cfft_u64_fourier_mul_monomial", c_int, [vp, ctypes.c_ulonglong, vp, c_size, vp]),
     ("cfft_u64_product_set_int_adds", c_int, [vp, c_int]),
     ("cfft_u64_product_set_cluster_size", c_int, [vp, c_int]),
     ("cfft_u64_product_int_adds", c_int, [vp]),

@@ -76,6 +76,15 @@ class U64ProductPlan:
         check(self._lib.cfft_u64_untwist_round(self._h, B.ptr(z), B.ptr(out), count, s))
         return out
 
+    def fourier_mul_monomial(self, degree, z):
+        """z: (count, N/2) complex128 device tensor in the plan's Fourier layout (a prepared
+        operand, or a folded, twisted and forward-transformed polynomial); multiplied in place
+        by the Fourier form of X^degree mod (X^N + 1), degree taken mod 2N."""
+        count = B.batch_of(z, self.N // 2, 16)
+        check(self._lib.cfft_u64_fourier_mul_monomial(self._h, int(degree) % (2 * self.N), B.ptr(z), count,
+                                                      B.stream_of(z)))
+        return z
+
     def product_sum(self, a, bhat, out):
         """a: (count, terms, N) device int64/uint64; bhat: (count, terms, N/2) complex128;
         out: (count, N).  out[g] = sum_t a[g, t] * B[g, t], accumulated in the Fourier domain."""

@@ -81,6 +81,14 @@ __global__ void fourier_sum_kernel(const double2* __restrict__ bhat, const doubl
     st(acc + g, s);
   }
 }
+// digits of the monomial X^degree mod (X^N + 1): one coefficient +-1 (X^N = -1)
+__global__ void monomial_digits_kernel(int64_t* __restrict__ b, long N, unsigned long long degree) {
+  grid_dependency_wait();
+  const long pos = (long)(degree % (unsigned long long)N);
+  const int64_t sign = ((degree / (unsigned long long)N) & 1) ? -1 : 1;
+  for (long j = (long)blockIdx.x * blockDim.x + threadIdx.x; j < N; j += (long)gridDim.x * blockDim.x)
+    b[j] = j == pos ? sign : 0;
+}
 __global__ void untwist_round_kernel(const double2* __restrict__ z, uint64_t* __restrict__ out, long total, int log2n,
                                      const double2* __restrict__ itw) {
   grid_dependency_wait();
@@ -277,6 +285,29 @@ cfft_status cfft_u64_untwist_round(const cfft_u64_product_plan* plan, const doub
   CFFT_CUDA_TRY(launch_dependent(untwist_round_kernel, ew_grid(total), 256, 0, (cudaStream_t)stream,
                                  (const double2*)z, out, total, ilog2(plan->n), (const double2*)plan->d_itw));
   return CFFT_OK;
+}
+
+cfft_status cfft_u64_fourier_mul_monomial(const cfft_u64_product_plan* plan, unsigned long long degree, double* z,
+                                          size_t count, void* stream) {
+  if (!plan || !z) return fail(CFFT_ERR_INVALID_ARGUMENT, "null argument");
+  if (count == 0) return CFFT_OK;
+  cudaStream_t s = (cudaStream_t)stream;
+  // the monomial's digits, its operand (the plan's own preparation), then the pointwise
+  // product with every polynomial: the same bits as preparing X^degree and multiplying
+  void* ws = nullptr;
+  const size_t digit_bytes = plan->N * sizeof(int64_t);
+  if (cudaMallocAsync(&ws, digit_bytes + plan->n * sizeof(double2), s) != cudaSuccess)
+    return fail(CFFT_ERR_OUT_OF_MEMORY, "monomial workspace");
+  int64_t* digits = (int64_t*)ws;
+  double* mono = (double*)((char*)ws + digit_bytes);
+  cfft_status st = launch_dependent(monomial_digits_kernel, ew_grid((long)plan->N), 256, 0, s, digits, (long)plan->N,
+                                    degree) == cudaSuccess
+                       ? CFFT_OK
+                       : fail(CFFT_ERR_CUDA, "monomial digits launch");
+  if (st == CFFT_OK) st = cfft_u64_prepare_operand(plan, digits, mono, 1, stream);
+  if (st == CFFT_OK) st = cfft_c64_pointwise(mono, 0, z, plan->n, count, stream);
+  cudaFreeAsync(ws, s);
+  return st;
 }
 
 cfft_status cfft_u64_product_sum(const cfft_u64_product_plan* plan, const uint64_t* a, const double* bhat,

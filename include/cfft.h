@@ -277,6 +277,14 @@ cfft_status cfft_u64_untwist_round(const cfft_u64_product_plan* plan, const doub
                                    void* stream);
 /* The plan's N/2-point unordered transform (owned by the product plan). */
 cfft_unordered_plan* cfft_u64_product_fft(const cfft_u64_product_plan* plan);
+/* z[p] <- Fourier form of X^degree mod (X^N + 1) times z[p], p < count, in place
+ * (z: count * N/2 c64 in the plan's Fourier layout: a prepared operand or a
+ * forward-transformed, twisted polynomial).  degree is taken mod 2N, X^N = -1.
+ * The monomial's Fourier form is cfft_u64_prepare_operand of its digits, so the
+ * result is bit-identical to preparing X^degree and calling cfft_c64_pointwise
+ * (the blind-rotation step: rotate a Fourier-domain polynomial by a monomial). */
+cfft_status cfft_u64_fourier_mul_monomial(const cfft_u64_product_plan* plan, unsigned long long degree, double* z,
+                                          size_t count, void* stream);
 
 /* Mixed-size product engine: one persistent launch over a DEVICE array of
  * items of any configured N (2^6..2^17), each with its own operand, result

@@ -1164,6 +1164,13 @@ int oracle_u64_prepare_b(size_t N, int base_algo, size_t base_n, const int64_t* 
   return 0;
 }
 
+void oracle_c64_pointwise(size_t n, size_t count, const double* bhat, double* z) {
+  const c64* b = (const c64*)bhat;
+  c64* v = (c64*)z;
+  for (size_t p = 0; p < count; ++p)
+    for (size_t k = 0; k < n; ++k) v[p * n + k] = mul(b[k], v[p * n + k]);
+}
+
 int oracle_u64_product(size_t N, int base_algo, size_t base_n, const uint64_t* a, const double* bhat, uint64_t* out) {
   return oracle_u64_product_batch(N, base_algo, base_n, 1, a, bhat, out, 1);
 }

@@ -68,6 +68,9 @@ int oracle_negacyclic_u128_schoolbook(size_t N, const uint64_t* a, const int64_t
  * (fold, twist, fwd, pointwise, inv, untwist, exact round mod 2^64).
  * bhat: N/2 c64 in the plan's permuted order (from oracle_u64_prepare_b). */
 int oracle_u64_prepare_b(size_t N, int base_algo, size_t base_n, const int64_t* b, double* bhat);
+/* z[p][k] = bhat[k] * z[p][k] for count rows of n c64 (the product pipeline's
+ * pointwise step: the reference's FMA complex product, src/fft_simd.rs:164-234). */
+void oracle_c64_pointwise(size_t n, size_t count, const double* bhat, double* z);
 int oracle_u64_product(size_t N, int base_algo, size_t base_n, const uint64_t* a,
                        const double* bhat, uint64_t* out);
 /* batched + threaded version for the CPU baseline (nthreads <= 0: all cores) */

@@ -190,6 +190,16 @@ def u64_prepare(N, base_algo, base_n, b):
     return out
 
 
+def c64_pointwise(bhat, z):
+    """bhat: (n,) complex128; z: (count, n) complex128 -> bhat * z per row (the reference's
+    FMA complex product)."""
+    b = np.ascontiguousarray(bhat, dtype=np.complex128)
+    out = np.array(z, dtype=np.complex128, copy=True, order="C")
+    n = b.shape[-1]
+    lib().oracle_c64_pointwise(S(n), S(out.size // n), P(b), P(out))
+    return out
+
+
 def u64_product(N, base_algo, base_n, a, bhat, nthreads=1):
     a = np.ascontiguousarray(a, dtype=np.uint64)
     bhat = np.ascontiguousarray(bhat, dtype=np.complex128)

@@ -3,6 +3,8 @@ pipeline, and torus error against the exact wrapping-integer schoolbook."""
 import numpy as np
 import pytest
 
+from conftest import bits
+
 pytestmark = pytest.mark.gpu
 RNG = np.random.default_rng(3)
 
@@ -145,6 +147,46 @@ def test_u128_product_host_page_locked_out(cuda, oracle):
     assert np.array_equal(hout.numpy().view(np.uint64), copied)
     want = oracle.u128_product(N, a[[0, 699]], bhat[[0, 699]].cpu().numpy(), nthreads=0)
     assert np.array_equal(copied[[0, 699]], want)
+
+
+def negacyclic_shift(c, d):
+    """c * X^d mod (X^N + 1) for integer rows c (int64, wrapping)."""
+    N = c.shape[-1]
+    d %= 2 * N
+    out = np.roll(c, d % N, axis=-1)
+    j = np.arange(N)
+    flip = (j < d % N) ^ (d >= N)
+    return np.where(flip, -out, out)
+
+
+@pytest.mark.parametrize("N,algo,base", [(2048, 2, 1024), (2048, 6, 256), (16384, 2, 1024), (131072, 2, 1024)])
+def test_u64_fourier_mul_monomial(cuda, oracle, N, algo, base):
+    """Fourier-domain multiplication by X^d (the blind-rotation step): bit-identical to the
+    oracle's prepared monomial times the operand, and a product with the rotated operand is
+    the rotated product, exactly, for small inputs."""
+    import concrete_fft as cf
+    torch = cuda
+    plan = cf.product.U64ProductPlan(N, algo, base)
+    count = 2
+    b = RNG.integers(-2 ** 7, 2 ** 7, (count, N))
+    bhat = torch.empty((count, N // 2), dtype=torch.complex128, device="cuda")
+    plan.prepare_operand(torch.from_numpy(b).cuda(), bhat)
+    a = RNG.integers(-2 ** 10, 2 ** 10, (count, N)).astype(np.int64)
+    base_out = torch.empty((count, N), dtype=torch.int64, device="cuda")
+    plan.product(torch.from_numpy(a).cuda(), bhat, base_out)
+    base_out = base_out.cpu().numpy()
+    for d in (0, 1, N - 1, N, N + 7, 2 * N - 1, 5 * N + 3):
+        z = bhat.clone()
+        plan.fourier_mul_monomial(d, z)
+        dm = d % (2 * N)
+        digits = np.zeros((1, N), dtype=np.int64)
+        digits[0, dm % N] = -1 if dm >= N else 1
+        mono = oracle.u64_prepare(N, algo, base, digits)[0]
+        want = oracle.c64_pointwise(mono, bhat.cpu().numpy())
+        assert np.array_equal(bits(z.cpu().numpy()), bits(want)), (N, d)
+        out = torch.empty((count, N), dtype=torch.int64, device="cuda")
+        plan.product(torch.from_numpy(a).cuda(), z, out)
+        assert np.array_equal(out.cpu().numpy(), negacyclic_shift(base_out, d)), (N, d)
 
 
 def test_u64_measure_plan(cuda, oracle):

@@ -870,6 +870,15 @@ def run_serde(args):
     nbytes = 2 * batch * n * 16
     gbs_to = nbytes * args.steps / (ms_to * 1e-3) / 1e9
     gbs_from = nbytes * args.steps / (ms_from * 1e-3) / 1e9
+    # the wire format across the host link: page-locked standard-order host data straight into
+    # the device's permuted order and back, the permutation kernel reading (writing) host memory
+    wire = torch.empty((batch, n), dtype=torch.complex128).pin_memory()
+    ms_h2d, _ = timed(torch, lambda: plan.from_standard(wire, src), max(3, args.steps // 4), 2, local, world)
+    ms_d2h, _ = timed(torch, lambda: plan.to_standard(src, wire), max(3, args.steps // 4), 2, local, world)
+    link_bytes = batch * n * 16  # each direction crosses the link once per call
+    gbs_h2d = link_bytes * max(3, args.steps // 4) / (ms_h2d * 1e-3) / 1e9
+    gbs_d2h = link_bytes * max(3, args.steps // 4) / (ms_d2h * 1e-3) / 1e9
+    del wire
     peaks, peak_kind = measured_peaks()
     prof = profiled_traffic("permute_tile_n1024")
     traffic = prof["dram_bytes_per_point"] * batch * n if prof else None
@@ -882,7 +891,11 @@ def run_serde(args):
         "dtype": "c64 copy", "data": "synthetic (torch.randn)",
         "config": {"workload": "to_standard / from_standard, %d x 1024 points, base 32, %.2f GiB per call"
                                % (batch, nbytes / 2 ** 30),
-                   "from_standard_gbs": world * gbs_from, "l2": "inputs larger than L2"},
+                   "from_standard_gbs": world * gbs_from, "l2": "inputs larger than L2",
+                   "from_standard_h2d_gbs": world * gbs_h2d, "to_standard_d2h_gbs": world * gbs_d2h,
+                   "host_side": "page-locked, read or written by the permutation kernel across the link"},
+        "e2e": {"value": world * gbs_d2h, "unit": "GB/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": link_bytes,
+                "note": "device permuted order -> serialized standard order in host memory (to_standard_d2h)"},
         "roofline": {"bound": "hbm", "achieved": gbs_to, "peak": peaks["hbm_gbs"], "unit": "GB/s",
                      "frac": gbs_to / peaks["hbm_gbs"], "traffic": traffic, "peak_kind": peak_kind,
                      "algorithmic_bytes_per_launch": nbytes,

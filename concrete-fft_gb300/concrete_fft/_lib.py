@@ -78,6 +78,8 @@ _SIGS = [
     ("cfft_unordered_from_standard", c_int, [vp, vp, vp, c_size, vp]),
     ("cfft_unordered_to_standard_host", c_int, [vp, vp, vp, c_size]),
     ("cfft_unordered_from_standard_host", c_int, [vp, vp, vp, c_size]),
+    ("cfft_unordered_from_standard_h2d", c_int, [vp, vp, vp, c_size, vp]),
+    ("cfft_unordered_to_standard_d2h", c_int, [vp, vp, vp, c_size, vp]),
     ("cfft_f128_plan_create", c_int, [c_size, pp]),
     ("cfft_f128_plan_destroy", None, [vp]),
     ("cfft_f128_fft_size", c_size, [vp]),

@@ -112,12 +112,19 @@ class Plan:
         batch = B.batch_of(src, self.fft_size(), 16)
         if B.batch_of(dst, self.fft_size(), 16) != batch:
             raise ValueError("source and destination sizes differ")
-        if B.is_device(src):
+        sd, dd = B.is_device(src), B.is_device(dst)
+        if sd and dd:
             fn = self._lib.cfft_unordered_to_standard if to_std else self._lib.cfft_unordered_from_standard
             check(fn(self._h, B.ptr(src), B.ptr(dst), batch, B.stream_of(src)))
-        else:
+        elif not sd and not dd:
             fn = self._lib.cfft_unordered_to_standard_host if to_std else self._lib.cfft_unordered_from_standard_host
             check(fn(self._h, B.ptr(src), B.ptr(dst), batch))
+        elif not to_std and dd:  # serialized host data straight into a device Fourier buffer
+            check(self._lib.cfft_unordered_from_standard_h2d(self._h, B.ptr(src), B.ptr(dst), batch, B.stream_of(dst)))
+        elif to_std and sd:  # a device Fourier buffer straight into serialized host data
+            check(self._lib.cfft_unordered_to_standard_d2h(self._h, B.ptr(src), B.ptr(dst), batch, B.stream_of(src)))
+        else:
+            raise ValueError("permuted data must be on the device when the standard-order side is on the host")
         return dst
 
     def serialize_fourier_buffer(self, buf):

@@ -770,4 +770,45 @@ cfft_status cfft_unordered_from_standard_host(const cfft_unordered_plan* plan, c
   return permute_host(plan, standard, permuted, batch, false);
 }
 
+// Host standard order <-> device permuted order in one call.  Page-locked host
+// memory is read (or written) by the permutation kernel itself, on `stream`,
+// asynchronously; pageable memory is staged through a device buffer on
+// `stream` and the call returns when the copy is done.
+cfft_status cfft_unordered_from_standard_h2d(const cfft_unordered_plan* plan, const double* standard,
+                                             double* permuted, size_t batch, void* stream) {
+  if (!plan || !standard || !permuted) return fail(CFFT_ERR_INVALID_ARGUMENT, "null argument");
+  if (batch == 0) return CFFT_OK;
+  cudaStream_t s = (cudaStream_t)stream;
+  const size_t bytes = batch * plan->p.n * sizeof(double2);
+  if (const void* m = mapped_host_range(standard, bytes)) return permute(plan, (const double*)m, permuted, batch, s, false);
+  void* d;
+  cudaStream_t own;
+  cfft_status st = host_staging(bytes, &d, &own);
+  if (st != CFFT_OK) return st;
+  CFFT_CUDA_TRY(cudaStreamSynchronize(own));
+  CFFT_CUDA_TRY(cudaMemcpyAsync(d, standard, bytes, cudaMemcpyHostToDevice, s));
+  st = permute(plan, (const double*)d, permuted, batch, s, false);
+  if (st != CFFT_OK) return st;
+  CFFT_CUDA_TRY(cudaStreamSynchronize(s));  // the staging buffer is free again
+  return CFFT_OK;
+}
+cfft_status cfft_unordered_to_standard_d2h(const cfft_unordered_plan* plan, const double* permuted, double* standard,
+                                           size_t batch, void* stream) {
+  if (!plan || !standard || !permuted) return fail(CFFT_ERR_INVALID_ARGUMENT, "null argument");
+  if (batch == 0) return CFFT_OK;
+  cudaStream_t s = (cudaStream_t)stream;
+  const size_t bytes = batch * plan->p.n * sizeof(double2);
+  if (void* m = mapped_host_range(standard, bytes)) return permute(plan, permuted, (double*)m, batch, s, true);
+  void* d;
+  cudaStream_t own;
+  cfft_status st = host_staging(bytes, &d, &own);
+  if (st != CFFT_OK) return st;
+  CFFT_CUDA_TRY(cudaStreamSynchronize(own));
+  st = permute(plan, permuted, (double*)d, batch, s, true);
+  if (st != CFFT_OK) return st;
+  CFFT_CUDA_TRY(cudaMemcpyAsync(standard, d, bytes, cudaMemcpyDeviceToHost, s));
+  CFFT_CUDA_TRY(cudaStreamSynchronize(s));
+  return CFFT_OK;
+}
+
 }  // extern "C"

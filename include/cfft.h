@@ -154,6 +154,16 @@ cfft_status cfft_unordered_to_standard_host(const cfft_unordered_plan* plan, con
                                             double* standard, size_t batch);
 cfft_status cfft_unordered_from_standard_host(const cfft_unordered_plan* plan, const double* standard,
                                               double* permuted, size_t batch);
+/* Serialized (standard-order) host data straight into device Fourier buffers in
+ * the plan's permuted order, and back: the wire format loads into resident
+ * operands (for a u64 product plan, through cfft_u64_product_fft) for any
+ * base_n.  With page-locked host memory the permutation kernel reads (writes)
+ * it directly and the call is asynchronous on `stream`; pageable memory is
+ * staged and the call returns when done. */
+cfft_status cfft_unordered_from_standard_h2d(const cfft_unordered_plan* plan, const double* standard_host,
+                                             double* permuted, size_t batch, void* stream);
+cfft_status cfft_unordered_to_standard_d2h(const cfft_unordered_plan* plan, const double* permuted,
+                                           double* standard_host, size_t batch, void* stream);
 
 /* Integer-pipe share of the butterfly additions, as cfft_ordered_set_int_adds. */
 cfft_status cfft_unordered_set_int_adds(cfft_unordered_plan* plan, int eighths);

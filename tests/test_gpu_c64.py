@@ -301,6 +301,44 @@ def test_serde_tiles_and_batches(cuda, oracle, batch):
         assert np.array_equal(bits(back.cpu().numpy()), bits(x)), (n, base, batch)
 
 
+@pytest.mark.parametrize("pinned", [False, True])
+def test_serde_host_device_in_one_call(cuda, oracle, pinned):
+    """Serialized (standard-order) host data straight into device Fourier buffers and
+    back, page-locked (read and written by the permutation kernel) or pageable (staged)."""
+    import concrete_fft as cf
+    torch = cuda
+    for n, base in [(64, 32), (1024, 32), (2048, 1024), (8192, 1024), (65536, 64)]:
+        plan = cf.unordered.Plan(n, cf.unordered.Method.UserProvided(2, base))
+        x = rand_c64(3, n)
+        std = torch.from_numpy(x.copy())
+        if pinned:
+            std = std.pin_memory()
+        dev = torch.empty((3, n), dtype=torch.complex128, device="cuda")
+        plan.from_standard(std, dev)
+        torch.cuda.synchronize()
+        assert np.array_equal(bits(dev.cpu().numpy()), bits(oracle.from_standard(n, base, x))), (n, base)
+        back = torch.zeros_like(std)
+        if pinned:
+            back = back.pin_memory()
+        plan.to_standard(dev, back)
+        torch.cuda.synchronize()
+        assert np.array_equal(bits(back.numpy()), bits(x)), (n, base)
+    # a serialized product operand loads straight into the product plan's Fourier layout
+    L = cf.load()
+    N = 4096
+    pp = cf.product.U64ProductPlan(N, 2, 512)
+    b = RNG.integers(-2 ** 7, 2 ** 7, (2, N))
+    want = oracle.u64_prepare(N, 2, 512, b)
+    wire = torch.from_numpy(oracle.to_standard(N // 2, 512, want))
+    if pinned:
+        wire = wire.pin_memory()
+    bhat = torch.empty((2, N // 2), dtype=torch.complex128, device="cuda")
+    cf.check(L.cfft_unordered_from_standard_h2d(L.cfft_u64_product_fft(pp._h), wire.data_ptr(), bhat.data_ptr(), 2,
+                                                torch.cuda.current_stream().cuda_stream))
+    torch.cuda.synchronize()
+    assert np.array_equal(bits(bhat.cpu().numpy()), bits(want))
+
+
 def test_serde_roundtrip_across_bases(cuda, oracle):
     """src/unordered.rs:9399-9466 on the GPU: base-32 forward, standard order, base-64 inverse."""
     import concrete_fft as cf

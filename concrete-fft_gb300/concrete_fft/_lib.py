@@ -44,6 +44,7 @@ _SIGS = [
     ("cfft_diag_dadd_check", c_int, [ctypes.c_uint64, ctypes.c_uint64, ctypes.POINTER(ctypes.c_uint64),
                                      ctypes.POINTER(ctypes.c_uint64)]),
     ("cfft_diag_dadd_int_rate", c_int, [ctypes.POINTER(c_dbl)]),
+    ("cfft_diag_host_mapping", c_int, [vp, c_size, vp]),
     ("cfft_ordered_plan_create", c_int, [c_size, c_int, pp]),
     ("cfft_ordered_plan_create_measure", c_int, [c_size, c_dbl, pp]),
     ("cfft_ordered_plan_destroy", None, [vp]),
@@ -122,6 +123,11 @@ _SIGS = [
     ("cfft_product_engine_workspace_bytes", c_size, [vp]),
     ("cfft_product_engine_plan", vp, [vp, ctypes.c_uint32]),
     ("cfft_product_engine_run", c_int, [vp, vp, c_size, vp, vp, vp]),
+    ("cfft_product_queue_create", c_int, [vp, vp, vp]),
+    ("cfft_product_queue_destroy", None, [vp]),
+    ("cfft_product_queue_submit", c_int, [vp, vp, c_size, vp]),
+    ("cfft_product_queue_poll", c_int, [vp, ctypes.c_uint64]),
+    ("cfft_product_queue_wait", c_int, [vp, ctypes.c_uint64]),
     ("cfft_product_engine_run_static", c_int, [vp, vp, c_size, vp]),
     ("cfft_server_create", c_int, [vp, vp, c_size, ctypes.c_uint64, ctypes.c_uint64, ctypes.c_uint64, pp]),
     ("cfft_server_destroy", None, [vp]),

@@ -59,6 +59,49 @@ class ProductEngine:
                                                        ctypes.c_void_p(stream)))
 
 
+class QueueConfig(ctypes.Structure):
+    _fields_ = [("max_inflight", ctypes.c_uint32), ("cluster_log2N", ctypes.c_uint32)]
+
+
+class ProductQueue:
+    """The engine behind a work queue: submit groups of products from any thread, then poll or
+    wait on the returned ticket.  Item buffers are device tensors or page-locked host tensors."""
+
+    def __init__(self, engine, max_inflight=0, cluster_log2N=0):
+        self._lib = load()
+        self.engine = engine  # keep the engine alive
+        h = ctypes.c_void_p()
+        cfg = QueueConfig(max_inflight, cluster_log2N)
+        check(self._lib.cfft_product_queue_create(engine._h, ctypes.byref(cfg), ctypes.byref(h)))
+        self._h = h
+
+    def close(self):
+        """Runs everything submitted, then releases the queue."""
+        if getattr(self, "_h", None):
+            self._lib.cfft_product_queue_destroy(self._h)
+            self._h = None
+
+    __del__ = close
+
+    def submit(self, items):
+        """items: numpy array of ITEM_DTYPE records (a, bhat, out addresses, log2N); returns a ticket."""
+        arr = np.ascontiguousarray(items, dtype=ITEM_DTYPE)
+        t = ctypes.c_uint64()
+        check(self._lib.cfft_product_queue_submit(self._h, ctypes.c_void_p(arr.ctypes.data), len(arr),
+                                                  ctypes.byref(t)))
+        return t.value
+
+    def poll(self, ticket):
+        """True when the ticket's products are complete (raises if its launch failed)."""
+        r = self._lib.cfft_product_queue_poll(self._h, ticket)
+        if r < 0:
+            check(r)
+        return r == 1
+
+    def wait(self, ticket):
+        check(self._lib.cfft_product_queue_wait(self._h, ticket))
+
+
 class ServeConfig(ctypes.Structure):
     _fields_ = [("rate", ctypes.c_double), ("duration_s", ctypes.c_double), ("log2N_min", ctypes.c_uint32),
                 ("log2N_max", ctypes.c_uint32), ("k_max", ctypes.c_uint32), ("l_max", ctypes.c_uint32),

@@ -180,8 +180,17 @@ cfft_status host_pipeline(int nslots, size_t bytes, PipeSlot* slots) {
   return CFFT_OK;
 }
 
+void bind_device_context() {
+  // a thread's first runtime call does not always make the device's primary
+  // context current, and pointer queries then miss page-locked host memory;
+  // cudaSetDevice makes it current (a no-op once it is)
+  int dev = 0;
+  if (cudaGetDevice(&dev) == cudaSuccess) cudaSetDevice(dev);
+}
+
 void* mapped_host_range(const void* p, size_t bytes) {
   if (!p || bytes == 0) return nullptr;
+  bind_device_context();
   cudaPointerAttributes first{}, last{};
   const char* end = (const char*)p + bytes - 1;
   if (cudaPointerGetAttributes(&first, p) != cudaSuccess || cudaPointerGetAttributes(&last, end) != cudaSuccess) {
@@ -410,5 +419,11 @@ extern "C" cfft_status cfft_diag_dadd_int_rate(double* adds_per_second) {
   cudaFree(d);
   CFFT_CHECK_LAUNCH();
   *adds_per_second = (double)reps * blocks * threads * kIntIters * 4 / (ms * 1e-3);
+  return CFFT_OK;
+}
+
+extern "C" cfft_status cfft_diag_host_mapping(const void* p, size_t bytes, void** device_address) {
+  if (!device_address) return cfft::fail(CFFT_ERR_INVALID_ARGUMENT, "null output pointer");
+  *device_address = cfft::mapped_host_range(p, bytes);
   return CFFT_OK;
 }

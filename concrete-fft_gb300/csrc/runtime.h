@@ -92,5 +92,7 @@ cfft_status host_pipeline(int nslots, size_t bytes, PipeSlot* slots);
 // (pageable memory, device memory).  Kernels then write results there
 // directly: on a Grace host they cross NVLink-C2C as the kernel stores them.
 void* mapped_host_range(const void* p, size_t bytes);
+// Makes the current device's primary context current on the calling thread.
+void bind_device_context();
 
 }  // namespace cfft

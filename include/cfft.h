@@ -318,6 +318,32 @@ size_t cfft_product_engine_workspace_bytes(const cfft_product_engine* engine);
 const cfft_u64_product_plan* cfft_product_engine_plan(const cfft_product_engine* engine, uint32_t log2N);
 cfft_status cfft_product_engine_run(const cfft_product_engine* engine, const cfft_product_item* items, size_t count,
                                     unsigned int* counter, double* workspace, void* stream);
+/* The engine behind a work queue (the submit / poll API; no counterpart in the
+ * reference, whose callers run one product per call): callers on any thread
+ * submit groups of items and get a ticket; one worker thread per queue gathers
+ * everything pending into the next launch on a free slot (the engine over the
+ * small products and, beside it, one thread-block cluster per product of
+ * N >= 2^cluster_log2N), at most max_inflight launches at once.  Item buffers
+ * are device memory or page-locked host memory (results are then stored
+ * straight into host memory); pageable host memory is refused.  Buffers must
+ * stay valid until the ticket is done.  poll returns 1 when the ticket's
+ * products are complete, 0 while they are queued or running, a negative
+ * cfft_status if its launch failed; a ticket reported done once reads as done
+ * afterwards.  destroy runs everything submitted, then returns. */
+typedef struct cfft_product_queue_config {
+  uint32_t max_inflight;  /* concurrent launches, 1..4 (0: 3) */
+  uint32_t cluster_log2N; /* products with N >= 2^cluster_log2N run one per thread-block cluster
+                             (0: 13; > 17: never) */
+} cfft_product_queue_config;
+typedef struct cfft_product_queue cfft_product_queue;
+cfft_status cfft_product_queue_create(const cfft_product_engine* engine, const cfft_product_queue_config* config,
+                                      cfft_product_queue** out);
+void cfft_product_queue_destroy(cfft_product_queue* queue);
+cfft_status cfft_product_queue_submit(cfft_product_queue* queue, const cfft_product_item* items, size_t count,
+                                      uint64_t* ticket);
+int cfft_product_queue_poll(cfft_product_queue* queue, uint64_t ticket);
+cfft_status cfft_product_queue_wait(cfft_product_queue* queue, uint64_t ticket);
+
 /* cfft_product_engine_run without any allocation (no counterpart in the
  * reference): for callers that cannot allocate device memory on their call
  * path -- code inside a framework whose own allocator has reserved the device

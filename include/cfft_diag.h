@@ -30,6 +30,12 @@ cfft_status cfft_diag_dadd_check(uint64_t count, uint64_t seed, uint64_t* mismat
 /* Issue rate of the integer-pipe double addition alone (additions per second). */
 cfft_status cfft_diag_dadd_int_rate(double* adds_per_second);
 
+/* Whether `bytes` at p are page-locked host memory that kernels can reach
+ * directly (the in-place and direct-store host paths use it): *device_address
+ * receives the address kernels use, or NULL when the range takes the staged
+ * copies (pageable or device memory). */
+cfft_status cfft_diag_host_mapping(const void* p, size_t bytes, void** device_address);
+
 #ifdef __cplusplus
 }
 #endif

@@ -124,6 +124,34 @@ def test_host_entry_page_locked_in_place(cuda, oracle, batch):
     assert np.array_equal(bits(h.numpy()), bits(oracle.unordered_fwd(2, 256, x, nthreads=0)))
 
 
+def test_host_mapping_seen_from_any_thread(cuda):
+    """The zero-copy host paths engage for page-locked memory, from the main thread and
+    from other threads, and not for device or pageable memory."""
+    import ctypes
+    import threading
+    import concrete_fft as cf
+    torch = cuda
+    L = cf.load()
+
+    def mapped(ptr, n):
+        d = ctypes.c_void_p()
+        cf.check(L.cfft_diag_host_mapping(ctypes.c_void_p(ptr), n, ctypes.byref(d)))
+        return d.value is not None
+
+    pinned = torch.zeros(1 << 16, dtype=torch.int64).pin_memory()
+    dev = torch.zeros(1 << 16, dtype=torch.int64, device="cuda")
+    pageable = np.zeros(1 << 16, dtype=np.int64)
+    assert mapped(pinned.data_ptr(), pinned.numel() * 8)
+    assert mapped(pinned.data_ptr() + 4096, 4096)
+    assert not mapped(dev.data_ptr(), 8)
+    assert not mapped(pageable.ctypes.data, 8)
+    seen = []
+    t = threading.Thread(target=lambda: seen.append(mapped(pinned.data_ptr(), pinned.numel() * 8)))
+    t.start()
+    t.join()
+    assert seen == [True]
+
+
 def test_host_entry_registered_memory(cuda, oracle):
     """Host memory page-locked by cudaHostRegister (its device address is looked up,
     not assumed equal to the host pointer): in-place transforms and product results."""

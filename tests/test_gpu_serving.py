@@ -121,3 +121,95 @@ def test_server_memory_gate(cuda, engine):
     assert len(srv.recorded_ids()) == stats["requests"]
     with pytest.raises(cf.CfftError):
         srv.run(srv.config(rate=100, duration_s=0.01, log2N_min=12, log2N_max=14))  # sizes without pools
+
+
+def _queue_requests(torch, engine, rng, nreq, host_out=False):
+    """nreq requests of 1..6 products of random configured sizes, each with its own
+    operand; returns (items per request, buffers to keep, expected results)."""
+    import concrete_fft as cf
+    reqs = []
+    for _ in range(nreq):
+        lN = int(rng.choice(SIZES))
+        N = 1 << lN
+        k = int(rng.integers(1, 7))
+        a = rng.integers(0, 2 ** 64, (k, N), dtype=np.uint64)
+        b = rng.integers(-2 ** 7, 2 ** 7, (k, N))
+        bhat = torch.empty((k, N // 2), dtype=torch.complex128, device="cuda")
+        engine.prepare_operand(lN, torch.from_numpy(b).cuda(), bhat)
+        da = torch.from_numpy(a.view(np.int64)).cuda()
+        out = torch.full((k, N), -1, dtype=torch.int64)
+        out = out.pin_memory() if host_out else out.cuda()
+        items = np.array([(da[p].data_ptr(), bhat[p].data_ptr(), out[p].data_ptr(), lN, 0) for p in range(k)],
+                         dtype=cf.serving.ITEM_DTYPE)
+        reqs.append((items, (lN, da, bhat, out)))
+    return reqs
+
+
+@pytest.mark.parametrize("host_out", [False, True])
+def test_product_queue_threads(cuda, engine, host_out):
+    """The submit / poll / wait API: four threads submit requests concurrently; every
+    result equals the same products run alone through cfft_u64_product."""
+    import threading
+    import concrete_fft as cf
+    torch = cuda
+    q = cf.serving.ProductQueue(engine)
+    rng = np.random.default_rng(31)
+    per_thread = [_queue_requests(torch, engine, rng, 40, host_out) for _ in range(4)]
+    torch.cuda.synchronize()
+    errors = []
+
+    def worker(reqs):
+        try:
+            tickets = [q.submit(items) for items, _ in reqs]
+            for t in tickets[::2]:
+                q.wait(t)
+            for t in tickets[1::2]:
+                while not q.poll(t):
+                    pass
+            assert all(q.poll(t) for t in tickets)  # done tickets stay done
+        except Exception as e:  # reported by the main thread
+            errors.append(repr(e))
+
+    ts = [threading.Thread(target=worker, args=(r,)) for r in per_thread]
+    for t in ts:
+        t.start()
+    for t in ts:
+        t.join()
+    assert not errors, errors
+    for reqs in per_thread:
+        for items, (lN, da, bhat, out) in reqs:
+            want = torch.empty_like(da)
+            cf.check(cf.load().cfft_u64_product(engine.plan(lN), da.data_ptr(), bhat.data_ptr(), (1 << lN) // 2,
+                                                want.data_ptr(), len(items), torch.cuda.current_stream().cuda_stream))
+            torch.cuda.synchronize()
+            assert torch.equal(out.cpu(), want.cpu()), lN
+    q.close()
+
+
+def test_product_queue_errors_and_shutdown(cuda, engine):
+    """Unconfigured sizes and pageable buffers are refused at submit; unknown tickets
+    fail; closing the queue runs everything submitted first."""
+    import concrete_fft as cf
+    torch = cuda
+    q = cf.serving.ProductQueue(engine, max_inflight=1)
+    rng = np.random.default_rng(32)
+    reqs = _queue_requests(torch, engine, rng, 30)
+    torch.cuda.synchronize()
+    bad = reqs[0][0].copy()
+    bad["log2N"] = 20
+    with pytest.raises(cf.CfftError):
+        q.submit(bad)
+    pageable = np.zeros((1, 1 << SIZES[0]), dtype=np.uint64)
+    bad = reqs[0][0][:1].copy()
+    bad["log2N"] = SIZES[0]
+    bad["out"] = pageable.ctypes.data
+    with pytest.raises(cf.CfftError):
+        q.submit(bad)
+    with pytest.raises(cf.CfftError):
+        q.poll(10 ** 9)
+    assert q.poll(q.submit(np.zeros(0, dtype=cf.serving.ITEM_DTYPE)))  # an empty group is done at once
+    for items, _ in reqs:
+        q.submit(items)
+    q.close()  # returns after the 30 requests ran
+    for items, (lN, da, bhat, out) in reqs:
+        assert int((out == -1).all(dim=1).sum()) == 0, lN

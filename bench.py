@@ -76,6 +76,11 @@ class ClockSampler:
                                          stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self.t = threading.Thread(target=self._read, daemon=True)
             self.t.start()
+            # nvidia-smi's start-up (NVML initialisation) takes driver locks: let it finish
+            # before the timed region, so that it does not stall the first timed launches
+            deadline = time.time() + 3.0
+            while not self.lines and time.time() < deadline and self.proc.poll() is None:
+                time.sleep(0.01)
         except OSError:
             self.proc = None
         return self
@@ -776,6 +781,8 @@ def run_serving(args):
     no_cluster = srv.run(srv.config(rate=args.rate, duration_s=args.serve_seconds, cluster_log2N=32))
     # the same stream with item records copied in and results copied out per launch
     staged = srv.run(srv.config(rate=args.rate, duration_s=args.serve_seconds, staged_io=True))
+    # the same stream through the public submit / poll work queue (cfft_product_queue_*)
+    queued = srv.run(srv.config(rate=args.rate, duration_s=args.serve_seconds, via_queue=True))
     # capacity: the continuous-batching loop at higher arrival rates (same request mix)
     sweep = {}
     for rate in (50000.0, 100000.0, 150000.0, 200000.0):
@@ -794,7 +801,7 @@ def run_serving(args):
         "config": {"workload": "serving, (k+1)*l products per request, k in 1..2, l in 1..4, N in 2^10..2^14, "
                                "digits b in 4..10 bits", "duration_s": args.serve_seconds,
                    "resident_setup_s": setup_s},
-        "batched": batched, "batched_without_clusters": no_cluster, "batched_staged_io": staged, "plain": plain,
+        "batched": batched, "batched_without_clusters": no_cluster, "batched_staged_io": staged, "batched_via_queue": queued, "plain": plain,
         "capacity_sweep_req_per_s": sweep,
         "p99_speedup_vs_plain": plain["p99_ms"] / batched["p99_ms"] if batched["p99_ms"] else None,
         "clocks": clk.summary(), "gpu_launches": batched["launches"],

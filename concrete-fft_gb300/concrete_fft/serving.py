@@ -106,7 +106,7 @@ class ServeConfig(ctypes.Structure):
     _fields_ = [("rate", ctypes.c_double), ("duration_s", ctypes.c_double), ("log2N_min", ctypes.c_uint32),
                 ("log2N_max", ctypes.c_uint32), ("k_max", ctypes.c_uint32), ("l_max", ctypes.c_uint32),
                 ("plain", ctypes.c_uint32), ("max_inflight", ctypes.c_uint32), ("record_every", ctypes.c_uint32),
-                ("cluster_log2N", ctypes.c_uint32), ("staged_io", ctypes.c_uint32)]
+                ("cluster_log2N", ctypes.c_uint32), ("staged_io", ctypes.c_uint32), ("via_queue", ctypes.c_uint32)]
 
 
 class ServeStats(ctypes.Structure):
@@ -138,9 +138,9 @@ class Server:
 
     @staticmethod
     def config(rate, duration_s, log2N_min=10, log2N_max=14, k_max=2, l_max=4, plain=False, max_inflight=3,
-               record_every=0, cluster_log2N=0, staged_io=False):
+               record_every=0, cluster_log2N=0, staged_io=False, via_queue=False):
         return ServeConfig(rate, duration_s, log2N_min, log2N_max, k_max, l_max, int(plain), max_inflight,
-                           record_every, cluster_log2N, int(staged_io))
+                           record_every, cluster_log2N, int(staged_io), int(via_queue))
 
     def run(self, cfg):
         st = ServeStats()

@@ -88,6 +88,7 @@ struct Live {
   ReqDesc d;
   uint64_t ring_off = 0, ring_bytes = 0, ring_end = 0;  // offset in the ring; end in the monotonic byte count
   double t_done = -1;
+  uint64_t ticket = 0;  // via the work queue
 };
 
 }  // namespace
@@ -403,6 +404,60 @@ cfft_status cfft_server_run(cfft_server* s, const cfft_serve_config* cfg, cfft_s
       ++done_count;
     }
     if (z) cudaFree(z);
+  } else if (c.via_queue) {
+    // the same stream through the public work queue: each admitted request is
+    // submitted on arrival; its ticket is polled until done
+    cfft_product_queue_config qc{std::min<uint32_t>(nslots, 4), big_log2N};
+    cfft_product_queue* q = nullptr;
+    cfft_status st = cfft_product_queue_create(s->engine, &qc, &q);
+    if (st != CFFT_OK) return st;
+    std::vector<size_t> inflight;
+    std::vector<cfft_product_item> its;
+    for (;;) {
+      const double now = now_s(t0);
+      while (next < reqs.size() && reqs[next].d.arrival <= now) waiting.push_back(next++);
+      while (!waiting.empty()) {
+        Live& r = reqs[waiting.front()];
+        r.ring_bytes = (uint64_t)r.d.nprod << (r.d.log2N + 3);
+        if (!ring.alloc(r.ring_bytes, &r.ring_off, &r.ring_end)) {
+          ++deferred;
+          break;
+        }
+        its.resize(r.d.nprod);
+        fill_items(s, r.d, s->h_ring_dev + r.ring_off, its.data());
+        st = cfft_product_queue_submit(q, its.data(), its.size(), &r.ticket);
+        if (st != CFFT_OK) break;
+        ring_order.push_back(waiting.front());
+        inflight.push_back(waiting.front());
+        waiting.pop_front();
+      }
+      if (st != CFFT_OK) break;
+      for (size_t k = 0; k < inflight.size();) {
+        const int pr = cfft_product_queue_poll(q, reqs[inflight[k]].ticket);
+        if (pr < 0) {
+          st = (cfft_status)pr;
+          break;
+        }
+        if (pr == 0) {
+          ++k;
+          continue;
+        }
+        reqs[inflight[k]].t_done = now_s(t0);
+        record(inflight[k]);
+        ++done_count;
+        inflight[k] = inflight.back();
+        inflight.pop_back();
+      }
+      if (st != CFFT_OK) break;
+      while (!ring_order.empty() && reqs[ring_order.front()].t_done >= 0) {
+        ring.tail = reqs[ring_order.front()].ring_end;
+        ring_order.pop_front();
+      }
+      if (done_count == reqs.size()) break;
+    }
+    cfft_product_queue_destroy(q);
+    if (st != CFFT_OK) return st;
+    launches = 0;  // counted by the queue, not here
   } else {
     // direct mode: the kernels read the item records from the slot's page-locked
     // array and store the results into the page-locked host ring (across

@@ -382,6 +382,8 @@ typedef struct cfft_serve_config {
   uint32_t staged_io;    /* batched mode: 0 = the kernels read the item records from and store
                             the results into page-locked host memory; 1 = item records copied
                             in and results copied out per launch */
+  uint32_t via_queue;    /* batched mode through the public work queue (cfft_product_queue_*):
+                            each request submitted on arrival, its ticket polled */
 } cfft_serve_config;
 typedef struct cfft_serve_stats {
   uint64_t requests, products, launches, deferred_admissions;

@@ -137,6 +137,7 @@ struct C64Plan {
   int tpc = 1;       // sub-transforms per CTA
   int emu = 0;       // eighths of the butterfly additions issued on the integer pipe
   int cluster = 0;   // CTAs per transform: 0 automatic, 1 one CTA, 2/4/8 a cluster of that size
+  bool block_set = false;  // block size chosen by the caller (no per-call change)
 };
 
 struct cfft_ordered_plan {
@@ -283,22 +284,37 @@ cfft_status launch_level(bool fwd, double2* data, long total, int log2r, int log
   return launch_kernel(fn, grid, 256, args, 0, stream, true);
 }
 
-cfft_status run_plan(const C64Plan& p, double* buf, size_t batch, bool fwd, cudaStream_t stream,
+cfft_status run_plan(const C64Plan& plan, double* buf, size_t batch, bool fwd, cudaStream_t stream,
                      bool allow_split = true) {
   if (batch == 0) return CFFT_OK;
   if (buf == nullptr) return fail(CFFT_ERR_INVALID_ARGUMENT, "null buffer");
-  if (p.n == 1) return CFFT_OK;
+  if (plan.n == 1) return CFFT_OK;
   double2* data = (double2*)buf;
-  const int log2n = p.lv.log2n[0];
+  const int log2n = plan.lv.log2n[0];
+  int mode = 0;
+  const int ls = allow_split ? split_log2(plan, (long)batch, &mode) : 0;
+  if (ls > 0) return launch_split(plan, fwd, ls, mode, (long)batch, stream, data);
+  const int nsm = sm_count();
+  // A plan with levels in global memory and a batch whose blocks would cover
+  // fewer than half the SMs takes smaller blocks for this call (one more level
+  // in global memory, blocks of at least 512 points): one transform of 16384
+  // points runs on 16 CTAs of 1024 points instead of 8 of 2048.
+  int d = plan.d0;
+  while (!plan.block_set && d > 0 && d < plan.lv.nlevels && plan.lv.log2n[d + 1] >= 9 &&
+         ((long)batch << (log2n - plan.lv.log2n[d])) < nsm / 2)
+    ++d;
+  C64Plan deeper;
+  if (d != plan.d0) {
+    deeper = plan;
+    deeper.d0 = d;
+    default_launch(deeper);
+  }
+  const C64Plan& p = d != plan.d0 ? deeper : plan;
   const int log2sub = p.lv.log2n[p.d0];
   const long nsub = (long)batch << (log2n - log2sub);
   if (nsub > 0x7fffffffL * (long)p.tpc) return fail(CFFT_ERR_INVALID_SIZE, "batch too large");
-  int mode = 0;
-  const int ls = allow_split ? split_log2(p, (long)batch, &mode) : 0;
-  if (ls > 0) return launch_split(p, fwd, ls, mode, (long)batch, stream, data);
   const int blocks = (int)((nsub + p.tpc - 1) / p.tpc);
   const size_t smem = smem_bytes(p);
-  const int nsm = sm_count();
   if (fwd) {
     for (int l = 0; l < p.d0; ++l) {
       cfft_status st = launch_level(true, data, ((long)batch << log2n) >> p.lv.log2r[l], p.lv.log2r[l],
@@ -554,6 +570,7 @@ cfft_status cfft_unordered_set_block_points(cfft_unordered_plan* plan, size_t po
     if ((size_t(1) << p.lv.log2n[l]) == points && p.lv.log2n[l] <= kSmemLog2Max) d = l;
   if (d < 0) return fail(CFFT_ERR_INVALID_ARGUMENT, "block points must be 0 or a level size of at most 4096 points");
   p.d0 = d;
+  p.block_set = points != 0;
   default_launch(p);
   return CFFT_OK;
 }

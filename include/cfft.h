@@ -173,8 +173,10 @@ cfft_status cfft_unordered_set_cluster_size(cfft_unordered_plan* plan, int ctas)
  * sub-transform one CTA holds after the levels above it ran in global memory
  * (forward; the inverse runs them after).  0 = automatic (the first level of
  * at most 4096 points); otherwise the size of one of the plan's levels (n, its
- * outer-level sizes, base_n) of at most 4096 points.  Resets the launch shape
- * that Method::Measure chose.  Results are bit-identical for every value. */
+ * outer-level sizes, base_n) of at most 4096 points.  Automatic blocks shrink
+ * for a call whose blocks would cover fewer than half the SMs; a block set
+ * here is used for every call.  Resets the launch shape that Method::Measure
+ * chose.  Results are bit-identical for every value. */
 cfft_status cfft_unordered_set_block_points(cfft_unordered_plan* plan, size_t points);
 size_t cfft_unordered_block_points(const cfft_unordered_plan* plan);
 int cfft_unordered_int_adds(const cfft_unordered_plan* plan);

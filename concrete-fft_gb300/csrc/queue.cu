@@ -139,6 +139,12 @@ void worker_main(cfft_product_queue* q) {
       for (const auto& p : batch) sl.tickets.push_back(p.ticket);
       lk.unlock();
       const cfft_status st = launch_slot(q, sl, batch);
+      if (st != CFFT_OK) {
+        // part of the launch may be running (the clusters on the second stream):
+        // let it end before the slot's records can be rewritten
+        cudaStreamSynchronize(sl.stream2);
+        cudaStreamSynchronize(sl.stream);
+      }
       lk.lock();
       if (st == CFFT_OK) {
         sl.busy = true;

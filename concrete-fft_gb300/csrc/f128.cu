@@ -306,7 +306,7 @@ int f128_threads(int log2c) { return std::min(256, std::max(64, (1 << log2c) / 8
 // `batch` negacyclic transforms of n points stored back to back in each of
 // the four arrays, with the twiddle arrays tw (init_negacyclic_twiddles).
 cfft_status run_f128_tw(size_t n, const F128Tw& tw, double* re0, double* re1, double* im0, double* im1, size_t batch,
-                        bool fwd, cudaStream_t stream, int block_log2 = 0) {
+                        bool fwd, cudaStream_t stream, int block_log2 = 0, bool one_kernel = false) {
   if (!re0 || !re1 || !im0 || !im1) return fail(CFFT_ERR_INVALID_ARGUMENT, "null argument");
   if (batch == 0) return CFFT_OK;
   cfft_status ast = f128_attrs();
@@ -318,8 +318,8 @@ cfft_status run_f128_tw(size_t n, const F128Tw& tw, double* re0, double* re1, do
   const bool few = ((long)batch << (log2n - log2c)) < (long)sm_count() / 2;
   // large batches: 512-point blocks (more CTAs per SM) measured 1-3% faster than
   // 4096 (fwd+inv, 2^22 points per call, n = 1024..16384)
-  if (block_log2 == 0 && !few) log2c = std::min(log2c, kF128BlockLog2Auto);
-  while (log2c > 8 && ((long)batch << (log2n - log2c)) < (long)sm_count() / 2) --log2c;
+  if (block_log2 == 0 && !few && !one_kernel) log2c = std::min(log2c, kF128BlockLog2Auto);
+  while (!one_kernel && log2c > 8 && ((long)batch << (log2n - log2c)) < (long)sm_count() / 2) --log2c;
   F128Arrays g{re0, re1, im0, im1};
   const long nblocks = (long)batch << (log2n - log2c);
   // few blocks: a thread per butterfly of a stage (latency); many: fewer threads, more CTAs per SM
@@ -379,6 +379,20 @@ cfft_status run_f128_host(const cfft_f128_plan* p, double* re0, double* re1, dou
   const size_t bytes = batch * p->n * sizeof(double);
   void* d;
   cudaStream_t s;
+  // page-locked arrays and a transform that one shared-memory block holds: one
+  // kernel works on the caller's memory in place, across the host link
+  if (ilog2(p->n) <= kF128SmemLog2 && batch > 0) {
+    double* m[4] = {(double*)mapped_host_range(re0, bytes), (double*)mapped_host_range(re1, bytes),
+                    (double*)mapped_host_range(im0, bytes), (double*)mapped_host_range(im1, bytes)};
+    if (m[0] && m[1] && m[2] && m[3]) {
+      cfft_status st = host_staging(0, &d, &s);
+      if (st != CFFT_OK) return st;
+      st = run_f128_tw(p->n, p->tw(), m[0], m[1], m[2], m[3], batch, fwd, s, ilog2(p->n), true);
+      if (st != CFFT_OK) return st;
+      CFFT_CUDA_TRY(cudaStreamSynchronize(s));
+      return CFFT_OK;
+    }
+  }
   cfft_status st = host_staging(4 * bytes, &d, &s);
   if (st != CFFT_OK) return st;
   double* dd[4];

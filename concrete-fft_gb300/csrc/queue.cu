@@ -287,7 +287,17 @@ cfft_status cfft_product_queue_submit(cfft_product_queue* queue, const cfft_prod
                                       uint64_t* ticket) {
   if (!queue || !ticket || (count && !items)) return fail(CFFT_ERR_INVALID_ARGUMENT, "null argument");
   *ticket = 0;
-  cudaSetDevice(queue->device);  // this thread's pointer queries need the queue's context
+  // this thread's pointer queries need the queue's device context; the caller's
+  // current device is put back on return
+  int caller_dev = -1;
+  cudaGetDevice(&caller_dev);
+  cudaSetDevice(queue->device);
+  struct Restore {
+    int dev, mine;
+    ~Restore() {
+      if (dev >= 0 && dev != mine) cudaSetDevice(dev);
+    }
+  } restore{caller_dev, queue->device};
   Pending p;
   p.items.reserve(count);
   for (size_t i = 0; i < count; ++i) {

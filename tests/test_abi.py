@@ -54,6 +54,21 @@ def test_argument_errors_without_device(cfft_lib):
     assert L.cfft_f128_negacyclic_inv(2048, 1, *[buf] * 4, None, buf, buf, buf, None) == -2  # null twiddles
     assert L.cfft_ordered_set_cluster_size(None, 4) == -2
     assert L.cfft_unordered_set_cluster_size(None, 3) == -2
+    assert L.cfft_unordered_set_block_points(None, 1024) == -2
+    assert L.cfft_f128_set_block_points(None, 1024) == -2
+    assert L.cfft_unordered_block_points(None) == 0 and L.cfft_f128_block_points(None) == 0
+    assert L.cfft_unordered_from_standard_h2d(None, buf, buf, 1, None) == -2
+    assert L.cfft_unordered_to_standard_d2h(None, buf, buf, 1, None) == -2
+    assert L.cfft_u64_fourier_mul_monomial(None, 3, buf, 1, None) == -2
+    assert L.cfft_u128_product_fft(None) is None
+    q = ctypes.c_void_p()
+    assert L.cfft_product_queue_create(None, None, ctypes.byref(q)) == -2    # null engine
+    assert L.cfft_product_queue_submit(None, None, 0, ctypes.byref(q)) == -2
+    assert L.cfft_product_queue_poll(None, 1) == -2
+    assert L.cfft_product_queue_wait(None, 1) == -2
+    L.cfft_product_queue_destroy(None)  # no-op
+    mapped = ctypes.c_void_p(1)
+    assert L.cfft_diag_host_mapping(None, 8, ctypes.byref(mapped)) == 0 and mapped.value is None
 
 
 def test_no_device_is_reported(cfft_lib):

@@ -1,6 +1,7 @@
 // runtime.cu -- library-wide state: errors, device checks, staging buffers.
 #include <cuda_runtime.h>
 
+#include <atomic>
 #include <mutex>
 #include <string>
 #include <vector>
@@ -111,6 +112,11 @@ cfft_status launch_kernel(const void* fn, int grid, int block, void** args, size
   return CFFT_OK;
 }
 
+// Cluster scheduling policy of every cluster launch (cfft_diag_set_cluster_policy):
+// load balancing by default (N = 16384 products on 8-CTA clusters: 661 vs 649 k/s
+// with the driver's default; the split transforms are unchanged).
+static std::atomic<int> g_cluster_policy{(int)cudaClusterSchedulingPolicyLoadBalancing};
+
 cfft_status launch_kernel_cluster(const void* fn, int grid, int block, int cluster, void** args, size_t smem,
                                   cudaStream_t stream, bool pdl) {
   if (!fn) return fail(CFFT_ERR_INVALID_ARGUMENT, "no kernel instantiated for this configuration");
@@ -122,15 +128,26 @@ cfft_status launch_kernel_cluster(const void* fn, int grid, int block, int clust
   cfg.blockDim = dim3((unsigned)block);
   cfg.dynamicSmemBytes = smem;
   cfg.stream = stream;
-  cudaLaunchAttribute attr[2];
-  attr[0].id = cudaLaunchAttributeClusterDimension;
-  attr[0].val.clusterDim.x = (unsigned)cluster;
-  attr[0].val.clusterDim.y = 1;
-  attr[0].val.clusterDim.z = 1;
-  attr[1].id = cudaLaunchAttributeProgrammaticStreamSerialization;
-  attr[1].val.programmaticStreamSerializationAllowed = 1;
+  cudaLaunchAttribute attr[3];
+  unsigned na = 0;
+  attr[na].id = cudaLaunchAttributeClusterDimension;
+  attr[na].val.clusterDim.x = (unsigned)cluster;
+  attr[na].val.clusterDim.y = 1;
+  attr[na].val.clusterDim.z = 1;
+  ++na;
+  if (pdl) {
+    attr[na].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[na].val.programmaticStreamSerializationAllowed = 1;
+    ++na;
+  }
+  const int policy = g_cluster_policy.load(std::memory_order_relaxed);
+  if (policy) {
+    attr[na].id = cudaLaunchAttributeClusterSchedulingPolicyPreference;
+    attr[na].val.clusterSchedulingPolicyPreference = (cudaClusterSchedulingPolicy)policy;
+    ++na;
+  }
   cfg.attrs = attr;
-  cfg.numAttrs = pdl ? 2 : 1;
+  cfg.numAttrs = na;
   CFFT_CUDA_TRY(cudaLaunchKernelExC(&cfg, fn, args));
   return CFFT_OK;
 }
@@ -425,5 +442,11 @@ extern "C" cfft_status cfft_diag_dadd_int_rate(double* adds_per_second) {
 extern "C" cfft_status cfft_diag_host_mapping(const void* p, size_t bytes, void** device_address) {
   if (!device_address) return cfft::fail(CFFT_ERR_INVALID_ARGUMENT, "null output pointer");
   *device_address = cfft::mapped_host_range(p, bytes);
+  return CFFT_OK;
+}
+
+extern "C" cfft_status cfft_diag_set_cluster_policy(int policy) {
+  if (policy < 0 || policy > 2) return cfft::fail(CFFT_ERR_INVALID_ARGUMENT, "policy must be 0, 1 or 2");
+  cfft::g_cluster_policy.store(policy, std::memory_order_relaxed);
   return CFFT_OK;
 }

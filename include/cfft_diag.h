@@ -36,6 +36,11 @@ cfft_status cfft_diag_dadd_int_rate(double* adds_per_second);
  * copies (pageable or device memory). */
 cfft_status cfft_diag_host_mapping(const void* p, size_t bytes, void** device_address);
 
+/* Cluster scheduling policy requested for every thread-block-cluster launch of
+ * the library: 0 the driver's default, 1 spread, 2 load balancing (the
+ * library's default).  Process-wide; for measurement. */
+cfft_status cfft_diag_set_cluster_policy(int policy);
+
 #ifdef __cplusplus
 }
 #endif

@@ -331,7 +331,8 @@ cfft_status cfft_product_engine_run(const cfft_product_engine* engine, const cff
  * stay valid until the ticket is done.  poll returns 1 when the ticket's
  * products are complete, 0 while they are queued or running, a negative
  * cfft_status if its launch failed; a ticket reported done once reads as done
- * afterwards.  destroy runs everything submitted, then returns. */
+ * afterwards.  destroy runs everything submitted, then returns; no other call
+ * on the queue may run or start meanwhile. */
 typedef struct cfft_product_queue_config {
   uint32_t max_inflight;  /* concurrent launches, 1..4 (0: 3) */
   uint32_t cluster_log2N; /* products with N >= 2^cluster_log2N run one per thread-block cluster

@@ -81,7 +81,7 @@ def test_f128_block_points_bit_exact(cuda, oracle, n):
         plan.set_block_points(8192)
 
 
-@pytest.mark.parametrize("n", [2, 4, 16, 64, 1024, 8192])
+@pytest.mark.parametrize("n", [2, 4, 16, 64, 1024, 8192, 65536])
 def test_f128_raw_negacyclic_functions(cuda, oracle, n):
     """negacyclic_fwd_fft / negacyclic_inv_fft with caller-owned twiddle arrays
     (src/fft128/mod.rs:1041-1104), batched, against the oracle."""

@@ -130,10 +130,10 @@ def test_u64_product_host_page_locked_out(cuda, oracle, N, count):
     assert np.array_equal(copied[sel], want)
 
 
-def test_u128_product_host_page_locked_out(cuda, oracle):
+@pytest.mark.parametrize("N,count", [(1024, 700), (16384, 100)])
+def test_u128_product_host_page_locked_out(cuda, oracle, N, count):
     import concrete_fft as cf
     torch = cuda
-    N, count = 1024, 700
     plan = cf.product.U128ProductPlan(N)
     a = RNG.integers(0, 2 ** 64, (count, N, 2), dtype=np.uint64)
     b = RNG.integers(-2 ** 15, 2 ** 15, (count, N))
@@ -145,8 +145,9 @@ def test_u128_product_host_page_locked_out(cuda, oracle):
     copied = np.zeros_like(a)
     plan.product(a, bhat, copied)
     assert np.array_equal(hout.numpy().view(np.uint64), copied)
-    want = oracle.u128_product(N, a[[0, 699]], bhat[[0, 699]].cpu().numpy(), nthreads=0)
-    assert np.array_equal(copied[[0, 699]], want)
+    sel = [0, count - 1]
+    want = oracle.u128_product(N, a[sel], bhat[sel].cpu().numpy(), nthreads=0)
+    assert np.array_equal(copied[sel], want)
 
 
 def negacyclic_shift(c, d):

@@ -587,6 +587,14 @@ def run_ordered(args):
     with torch.cuda.graph(graph):
         step1()
     ms1g, _ = timed(torch, graph.replay, args.steps, args.warmup, local, world)
+    # device-side batch-1 latency: 20 fwd+inv pairs captured in one graph, so that no host
+    # call (Python, ctypes) sits between the launches
+    graph20 = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(graph20):
+        for _ in range(20):
+            step1()
+    reps20 = max(5, args.steps // 10)
+    ms1g20, _ = timed(torch, graph20.replay, reps20, args.warmup, local, world)
     # CTAs per transform (1 = one CTA, 2/4/8 = split over a cluster) at a few batch sizes, fwd then inv,
     # for a DIT algorithm (one exchange through distributed shared memory) and a DIF one (none)
     sweep = {}
@@ -628,6 +636,7 @@ def run_ordered(args):
         "config": {"workload": "ordered::Plan n=1024 batch 256", "algo": plan.algo().name,
                    "batch1_us_per_fwd_inv": ms1 * 1e3 / args.steps,
                    "batch1_us_per_fwd_inv_graph_replay": ms1g * 1e3 / args.steps,
+                   "batch1_us_per_fwd_inv_device": ms1g20 * 1e3 / (reps20 * 20),
                    "unordered_batch1_us_per_fwd_inv_by_n": large,
                    "us_per_fwd_inv_by_batch_and_ctas_per_transform": sweep},
         "roofline": {"bound": "hbm", "achieved": 256 * 65536 / per / 1e9, "peak": measured_peaks()[0]["hbm_gbs"],

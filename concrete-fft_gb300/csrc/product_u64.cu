@@ -438,7 +438,11 @@ cfft_status cfft_u64_product(const cfft_u64_product_plan* plan, const uint64_t* 
   // split over 2-8 CTAs each, and the launches follow one another without gaps
   // (one product at N = 2048, base 1024: 20 vs 31 us; 76 products: 26 vs 31 us)
   const bool few_unsplit = ls == 0 && plan->cluster == 0 && plan->N >= 2048 && !many;
-  if (!ok || (plan->N >= 32768 && many) || few_unsplit) {
+  // Fewer than SMs/4 products of N = 4096 or 8192 as well (one product: 34 vs 37 us at
+  // 4096, 37 vs 39 us at 8192; from SMs/4 products of N = 8192 the cluster kernel is faster)
+  const bool few_mid = plan->cluster == 0 && plan->N >= 4096 && plan->N <= 8192 &&
+                       (long)count < (long)sm_count() / 4;
+  if (!ok || (plan->N >= 32768 && many) || few_unsplit || few_mid) {
     cudaStream_t s = (cudaStream_t)stream;
     void* z = nullptr;
     if (cudaMallocAsync(&z, count * plan->n * sizeof(double2), s) != cudaSuccess)

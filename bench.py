@@ -238,6 +238,25 @@ def run_reference(args):
     }))
 
 
+def torus_error(np, got, a, b, rows):
+    """Per-coefficient torus error of sampled products against the exact product mod
+    (X^N + 1, 2^64), computed here with wrapping uint64 arithmetic (not the oracle):
+    the largest |got - exact| as a signed 64-bit difference, in bits."""
+    worst = 0
+    exact_coeffs = 0
+    for r in rows:
+        n = a.shape[-1]
+        conv = np.convolve(a[r].astype(np.uint64), b[r].astype(np.int64).view(np.uint64))  # wraps mod 2^64
+        exact = conv[:n].copy()
+        exact[: n - 1] -= conv[n:]  # X^N = -1
+        diff = (got[r] - exact).view(np.int64)
+        worst = max(worst, int(np.abs(diff.astype(np.float64)).max()))
+        exact_coeffs += int((diff == 0).sum())
+    return {"sample_products": len(rows), "max_torus_error_bits": float(np.log2(worst)) if worst else 0.0,
+            "exact_coefficient_fraction": exact_coeffs / (len(rows) * a.shape[-1]),
+            "against": "exact wrapping-integer negacyclic product (numpy, uint64)"}
+
+
 def run_gb300(args):
     import numpy as np
     import torch
@@ -298,6 +317,7 @@ def run_gb300(args):
         clk.mark(t_start, time.time())
     ms = replicas.max_over_ranks(e0.elapsed_time(e1), "cuda")
     per_launch_s = ms * 1e-3 / args.steps
+    accuracy = torus_error(np, out.cpu().numpy().view(np.uint64), a_np, b_np, [0, count // 2, count - 1])
     value = world * count * args.steps / (ms * 1e-3)
 
     # one product alone: the automatic path (five launches for a lone product of this plan),
@@ -401,6 +421,7 @@ def run_gb300(args):
                               "note": "binding roof: FP64 pipe (best DFMA/DADD/DMUL/mix issue rate, measured live)"}},
         "plain_path": plain,
         "cpu_baseline": cpu,
+        "accuracy": accuracy,
         "e2e": {"value": e2e, "unit": "products/s", "h2d_bytes_per_step": count * N_POLY * 8,
                 "d2h_bytes_per_step": count * N_POLY * 8, "steps": e2e_steps, "matches_device_result": ok,
                 "copy_only_gbs": copy_gbs},

@@ -22,26 +22,38 @@ namespace cfft {
 constexpr int kF128SmemLog2 = 12;  // 4096 points x 32 B = 128 KiB
 constexpr int kF128BlockLog2Auto = 9;
 
+// Blocks of 2^log2c points; 2^log2t consecutive blocks per CTA iteration (whole
+// transforms of fewer than 128 points are packed so that a stage's butterflies
+// fill whole warps: a group of threads per block, every group through the same
+// barriers).
 template <bool FWD>
-__global__ void __launch_bounds__(256) f128_smem_kernel(F128Arrays g, int log2n, int log2c, long nblocks, F128Tw tw) {
+__global__ void __launch_bounds__(256) f128_smem_kernel(F128Arrays g, int log2n, int log2c, long nblocks, F128Tw tw,
+                                                        int log2t) {
   extern __shared__ double sm[];
   const int c = 1 << log2c;
-  F128Arrays s{sm, sm + c, sm + 2 * c, sm + 3 * c};
+  const int tc = c << log2t;  // points per CTA iteration
+  F128Arrays s{sm, sm + tc, sm + 2 * tc, sm + 3 * tc};
   const int tid = threadIdx.x, nth = blockDim.x;
+  const int gsize = nth >> log2t;  // threads per block
+  const int grp = tid / gsize, gtid = tid - grp * gsize;
   const long per_transform = 1L << (log2n - log2c);
+  const long total = nblocks << log2c;
   grid_dependency_wait();
-  for (long blk = blockIdx.x; blk < nblocks; blk += gridDim.x) {
-    const long off = blk << log2c;
-    const long sb = blk % per_transform;  // sub-block index inside its transform
-    for (int i = tid; i < c; i += nth) {
+  for (long first = (long)blockIdx.x << log2t; first < nblocks; first += (long)gridDim.x << log2t) {
+    const long off = first << log2c;
+    for (int i = tid; i < tc; i += nth) {
+      if (off + i >= total) break;
       s.re0[i] = g.re0[off + i];
       s.re1[i] = g.re1[off + i];
       s.im0[i] = g.im0[off + i];
       s.im1[i] = g.im1[off + i];
     }
     __syncthreads();
-    f128_stages_smem<FWD>(s, log2n, log2c, sb, tw, tid, nth);
-    for (int i = tid; i < c; i += nth) {
+    const long sb = (first + grp) % per_transform;  // sub-block index inside its transform
+    const F128Arrays sg{s.re0 + grp * c, s.re1 + grp * c, s.im0 + grp * c, s.im1 + grp * c};
+    f128_stages_smem<FWD>(sg, log2n, log2c, sb, tw, gtid, gsize);  // past the batch's end: unused values
+    for (int i = tid; i < tc; i += nth) {
+      if (off + i >= total) break;
       g.re0[off + i] = s.re0[i];
       g.re1[off + i] = s.re1[i];
       g.im0[off + i] = s.im0[i];
@@ -323,10 +335,17 @@ cfft_status run_f128_tw(size_t n, const F128Tw& tw, double* re0, double* re1, do
   F128Arrays g{re0, re1, im0, im1};
   const long nblocks = (long)batch << (log2n - log2c);
   // few blocks: a thread per butterfly of a stage (latency); many: fewer threads, more CTAs per SM
-  const int threads = few ? std::min(256, 1 << (log2c - 1)) : f128_threads(log2c);
-  const size_t smem = (size_t)4 * (size_t(1) << log2c) * sizeof(double);
+  int threads = few ? std::min(256, 1 << (log2c - 1)) : f128_threads(log2c);
+  // whole transforms of fewer than 128 points: 128 points per CTA iteration, 64 threads,
+  // one butterfly per thread and stage (n = 32 alone would fill half a warp)
+  int log2t = 0;
+  if (log2c == log2n && log2c < 7) {
+    log2t = 7 - log2c;
+    threads = 64;
+  }
+  const size_t smem = (size_t)4 * (size_t(1) << (log2c + log2t)) * sizeof(double);
   const int grid = product_grid(fwd ? (const void*)f128_smem_kernel<true> : (const void*)f128_smem_kernel<false>,
-                                threads, smem, nblocks);
+                                threads, smem, (nblocks + (1L << log2t) - 1) >> log2t);
   const long total = (long)batch << (log2n - 1);
   const int sgrid = (int)std::min<long>((total + 255) / 256, (long)sm_count() * 16);
   // programmatic dependent launches: each kernel is launched as the previous one's CTAs exit
@@ -338,7 +357,7 @@ cfft_status run_f128_tw(size_t n, const F128Tw& tw, double* re0, double* re1, do
     return launch_kernel(fwd ? (const void*)f128_stage_kernel<true> : (const void*)f128_stage_kernel<false>, sgrid,
                          256, args, 0, stream, true);
   };
-  void* sargs[] = {&g, &ln, &lc, &nb, &t};
+  void* sargs[] = {&g, &ln, &lc, &nb, &t, &log2t};
   const void* sfn = fwd ? (const void*)f128_smem_kernel<true> : (const void*)f128_smem_kernel<false>;
   cfft_status st = CFFT_OK;
   if (fwd) {

@@ -40,31 +40,40 @@ __global__ void __launch_bounds__(THREADS) u64_product_kernel(const uint64_t* __
                                                              const double2* __restrict__ w,
                                                              const double2* __restrict__ winv,
                                                              const double2* __restrict__ tw,
-                                                             const double2* __restrict__ itw) {
+                                                             const double2* __restrict__ itw, int log2p) {
+  // 2^log2p products per CTA iteration, back to back in shared memory (small N: a pass's
+  // butterflies then fill whole warps; the products stay independent, so the bits do not
+  // depend on the packing)
   extern __shared__ double2 smem[];
   const int log2n = L.log2n[0];
   const int n = 1 << log2n;
   double2* x = smem;
-  double2* y = smem + n;
+  double2* y = smem + ((long)n << log2p);
   const int tid = threadIdx.x;
-  for (long prod = blockIdx.x; prod < count; prod += gridDim.x) {
-    const uint64_t* ap = a + (prod << (log2n + 1));
-    for (int j = tid; j < n; j += THREADS) {
-      const c64 v{i64_to_f64_rne((int64_t)__ldcs(ap + j)), i64_to_f64_rne((int64_t)__ldcs(ap + j + n))};
-      st(x + j, cmul(ldg(tw + j), v));
+  for (long first = (long)blockIdx.x << log2p; first < count; first += (long)gridDim.x << log2p) {
+    const int np = (int)min((long)1 << log2p, count - first);
+    const int pts = np << log2n;
+    for (int j = tid; j < pts; j += THREADS) {
+      const int jj = j & (n - 1);
+      const uint64_t* ap = a + ((first + (j >> log2n)) << (log2n + 1));
+      const c64 v{i64_to_f64_rne((int64_t)__ldcs(ap + jj)), i64_to_f64_rne((int64_t)__ldcs(ap + jj + n))};
+      st(x + j, cmul(ldg(tw + jj), v));
     }
     __syncthreads();
-    double2* r = unordered_smem<true, E, ALGO>(L, 0, 1, x, y, w, tid, THREADS);
-    const double2* bp = bhat + prod * bhat_stride;
-    for (int k = tid; k < n; k += THREADS) st(r + k, cmul(ldg(bp + k), ld(r + k)));
+    double2* r = unordered_smem<true, E, ALGO>(L, 0, np, x, y, w, tid, THREADS);
+    for (int k = tid; k < pts; k += THREADS) {
+      const double2* bp = bhat + (first + (k >> log2n)) * bhat_stride;
+      st(r + k, cmul(ldg(bp + (k & (n - 1))), ld(r + k)));
+    }
     __syncthreads();
     double2* o = (r == x) ? y : x;
-    double2* s = unordered_smem<false, E, ALGO>(L, 0, 1, r, o, winv, tid, THREADS);
-    uint64_t* op = out + (prod << (log2n + 1));
-    for (int j = tid; j < n; j += THREADS) {
-      const c64 t = cmul(ldg(itw + j), ld(s + j));
-      __stcs(op + j, round_half_up_mod64(t.re));
-      __stcs(op + j + n, round_half_up_mod64(t.im));
+    double2* s = unordered_smem<false, E, ALGO>(L, 0, np, r, o, winv, tid, THREADS);
+    for (int j = tid; j < pts; j += THREADS) {
+      const int jj = j & (n - 1);
+      uint64_t* op = out + ((first + (j >> log2n)) << (log2n + 1));
+      const c64 t = cmul(ldg(itw + jj), ld(s + j));
+      __stcs(op + jj, round_half_up_mod64(t.re));
+      __stcs(op + jj + n, round_half_up_mod64(t.im));
     }
     __syncthreads();
   }

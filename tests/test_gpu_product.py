@@ -222,6 +222,29 @@ def test_u128_product_bit_exact(cuda, oracle, N):
     assert np.array_equal(out2.cpu().numpy().view(np.uint64), oracle.u128_schoolbook(a2, b[:1]))
 
 
+@pytest.mark.parametrize("N,algo,base", [(64, 2, 32), (128, 6, 64), (128, 3, 32)])
+def test_u64_product_small_N_packed(cuda, oracle, N, algo, base):
+    """N <= 128: several products per CTA iteration (512 points); 1003 products, so the
+    last group is ragged.  Every product equals the oracle's."""
+    import concrete_fft as cf
+    torch = cuda
+    count = 1003
+    plan = cf.product.U64ProductPlan(N, algo, base)
+    a = RNG.integers(0, 2 ** 64, (count, N), dtype=np.uint64)
+    b = RNG.integers(-2 ** 7, 2 ** 7, (count, N))
+    bhat = torch.empty((count, N // 2), dtype=torch.complex128, device="cuda")
+    plan.prepare_operand(torch.from_numpy(b).cuda(), bhat)
+    want_bhat = oracle.u64_prepare(N, algo, base, b)
+    da = torch.from_numpy(a.view(np.int64)).cuda()
+    out = torch.empty_like(da)
+    plan.product(da, bhat, out)
+    assert np.array_equal(out.cpu().numpy().view(np.uint64), oracle.u64_product(N, algo, base, a, want_bhat, nthreads=0))
+    shared = torch.empty_like(da)
+    plan.product(da, bhat[:1], shared, shared_operand=True)
+    want = oracle.u64_product(N, algo, base, a, np.repeat(want_bhat[:1], count, axis=0), nthreads=0)
+    assert np.array_equal(shared.cpu().numpy().view(np.uint64), want)
+
+
 @pytest.mark.parametrize("N,algo,base", [(16384, 2, 1024), (16384, 5, 512), (32768, 2, 1024), (65536, 6, 1024),
                                          (131072, 2, 1024), (1 << 22, 6, 1024)])
 def test_u64_product_large_N(cuda, oracle, N, algo, base):

@@ -238,22 +238,41 @@ def run_reference(args):
     }))
 
 
-def torus_error(np, got, a, b, rows):
-    """Per-coefficient torus error of sampled products against the exact product mod
-    (X^N + 1, 2^64), computed here with wrapping uint64 arithmetic (not the oracle):
-    the largest |got - exact| as a signed 64-bit difference, in bits."""
-    worst = 0
-    exact_coeffs = 0
-    for r in rows:
-        n = a.shape[-1]
+def exact_u64_products(np, a, b, rows):
+    """The exact products a[r] * b[r] mod (X^N + 1, 2^64) of the sampled rows, computed here with
+    wrapping uint64 numpy arithmetic (independent of the oracle)."""
+    n = a.shape[-1]
+    out = np.zeros((len(rows), n), dtype=np.uint64)
+    for i, r in enumerate(rows):
         conv = np.convolve(a[r].astype(np.uint64), b[r].astype(np.int64).view(np.uint64))  # wraps mod 2^64
-        exact = conv[:n].copy()
-        exact[: n - 1] -= conv[n:]  # X^N = -1
-        diff = (got[r] - exact).view(np.int64)
-        worst = max(worst, int(np.abs(diff.astype(np.float64)).max()))
-        exact_coeffs += int((diff == 0).sum())
-    return {"sample_products": len(rows), "max_torus_error_bits": float(np.log2(worst)) if worst else 0.0,
-            "exact_coefficient_fraction": exact_coeffs / (len(rows) * a.shape[-1]),
+        out[i] = conv[:n]
+        out[i, : n - 1] -= conv[n:]  # X^N = -1
+    return out
+
+
+def headline_accuracy(np, got, a, b, algo, base_n, sample=64):
+    """Torus error of `sample` products of the timed launch (spread over it) against the exact
+    product, beside the restated reference pipeline's error on the same products: with the same
+    base algorithm as the GPU plan, and with the algorithm the reference's Method::Measure picks
+    on this host."""
+    po = _oracle()
+    threads = host_threads()
+    count, N = a.shape
+    rows = np.linspace(0, count - 1, sample).astype(np.int64)
+    exact = exact_u64_products(np, a, b, rows)
+    gbits, gex = torus_bits_u64(got[rows], exact)
+    ref = po.u64_product(N, algo, base_n, a[rows], po.u64_prepare(N, algo, base_n, b[rows]), nthreads=threads)
+    rbits, rex = torus_bits_u64(ref, exact)
+    calgo, cbase = cpu_fastest_algo(threads)
+    ref_h = po.u64_product(N, calgo, cbase, a[rows], po.u64_prepare(N, calgo, cbase, b[rows]), nthreads=threads)
+    hbits, hex_ = torus_bits_u64(ref_h, exact)
+    return {"sample_products": sample, "max_torus_error_bits": gbits, "exact_coefficient_fraction": gex,
+            "reference_pipeline_same_algo": {"max_torus_error_bits": rbits, "exact_coefficient_fraction": rex,
+                                             "algo": "%s base %d" % (ALGO_NAMES[algo], base_n),
+                                             "gpu_bit_identical": bool(np.array_equal(got[rows], ref))},
+            "reference_pipeline_host_measure": {"max_torus_error_bits": hbits, "exact_coefficient_fraction": hex_,
+                                                "algo": "%s base %d" % (ALGO_NAMES[calgo], cbase)},
+            "gpu_bits_le_reference_bits": gbits <= min(rbits, hbits),
             "against": "exact wrapping-integer negacyclic product (numpy, uint64)"}
 
 
@@ -317,7 +336,7 @@ def run_gb300(args):
         clk.mark(t_start, time.time())
     ms = replicas.max_over_ranks(e0.elapsed_time(e1), "cuda")
     per_launch_s = ms * 1e-3 / args.steps
-    accuracy = torus_error(np, out.cpu().numpy().view(np.uint64), a_np, b_np, [0, count // 2, count - 1])
+    accuracy = headline_accuracy(np, out.cpu().numpy().view(np.uint64), a_np, b_np, int(algo), base_n)
     value = world * count * args.steps / (ms * 1e-3)
 
     # one product alone: the automatic path (five launches for a lone product of this plan),
@@ -392,6 +411,23 @@ def run_gb300(args):
     fp64_ops = fp64_ops_per_product(N_POLY, base_n, int(algo))
     fp64_achieved = fp64_ops * count / per_launch_s
 
+    del z, out_plain, ha, hout
+    # the other benchmark configurations, each with its own clocks, roofline, e2e, accuracy and
+    # CPU baseline (one GPU only)
+    configs = None
+    if world == 1 and not args.no_configs:
+        configs = {}
+        for name, fn in (("ordered_c64_n1024", lambda: measure_ordered(torch, cf, 50, 3, local, world)),
+                         ("u128_product", lambda: measure_u128(torch, cf, 10, 3, local, world)),
+                         ("mixed_batch_100k", lambda: measure_mixed(torch, cf, 3, 3, local, world)),
+                         ("serving_20k_req_s", lambda: measure_serving(torch, cf, local, world))):
+            t_cfg = time.perf_counter()
+            try:
+                configs[name] = fn()
+            except Exception as exc:  # recorded in the line, not hidden
+                configs[name] = {"error": "%s: %s" % (type(exc).__name__, exc)}
+            configs[name]["wall_s"] = round(time.perf_counter() - t_cfg, 1)
+            torch.cuda.empty_cache()
     if rank != 0:
         return
     cpu = None
@@ -399,9 +435,12 @@ def run_gb300(args):
         threads = os.cpu_count() or 1
         rate, done, el = cpu_product_rate(threads, args.cpu_seconds, BASE_SEED)
         calgo, cbase = cpu_fastest_algo(threads)
+        rate1, done1, el1 = cpu_product_rate(1, args.cpu_seconds / 5, BASE_SEED)
         cpu = {"value": rate, "unit": "products/s", "cores": threads, "kind": "port",
-               "sample": "%d products (N=2048) in %.1f s on %d host threads, %s base %d (fastest there)"
-                         % (done, el, threads, ALGO_NAMES[calgo], cbase)}
+               "single_thread_us_per_product": el1 / done1 * 1e6,
+               "sample": "%d products (N=2048) in %.1f s on %d host threads, %s base %d (Method::Measure's pick "
+                         "there); one thread: %d products in %.1f s"
+                         % (done, el, threads, ALGO_NAMES[calgo], cbase, done1, el1)}
     line = {
         "metric": METRIC, "value": value, "unit": "products/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
@@ -427,6 +466,7 @@ def run_gb300(args):
                 "copy_only_gbs": copy_gbs},
         "clocks": clk.summary(),
         "gpu_launches": args.steps,
+        "configs": configs,
     }
     print(json.dumps(line))
 
@@ -487,94 +527,140 @@ def fp64_peak(cf):
     return max(fp64_rates(cf).values())
 
 
-def run_mixed(args):
-    """100,000 c64 transforms, sizes 2^k with k uniform in 8..16, half ordered and half unordered,
-    forward then inverse, one persistent launch per step (CUDA graph replay)."""
-    import numpy as np
-    torch, cf, rank, world, local = gpu_setup()
-    count = args.mixed_items
-    rng = np.random.default_rng(3 + rank)
-    log2n = rng.integers(8, 17, count)
-    kind = rng.integers(0, 2, count)
-    kind = np.where(log2n > 10, 1, kind)  # the reference has no ordered plan above 1024 points
-    sizes = (1 << log2n).astype(np.int64)
-    offs = np.concatenate([[0], np.cumsum(sizes)[:-1]]).astype(np.uint64)
-    items = np.zeros(count, dtype=cf.batch.ITEM_DTYPE)
-    items["offset"], items["log2n"], items["kind"], items["direction"] = offs, log2n, kind, 3
-    total = int(sizes.sum())
-    t0 = time.perf_counter()
-    b = cf.batch.Batch(items, tune_seconds=args.tune_seconds)
-    tune_s = time.perf_counter() - t0
-    g = torch.Generator(device="cuda")
-    g.manual_seed(3 + rank)
-    data = (torch.rand((total, 2), dtype=torch.float64, device="cuda", generator=g) * 2 - 1)
-    stream = torch.cuda.Stream()
-    with torch.cuda.stream(stream):
-        ms, clocks = timed(torch, lambda: b.run(data), args.steps, args.warmup, local, world)
-    transforms = 2 * count  # forward and inverse of every item
-    value = world * transforms * args.steps / (ms * 1e-3)
-    per_launch = ms * 1e-3 / args.steps
-    ops = 0
-    sched = {}
-    for k in range(8, 17):
-        for kd in (0, 1):
-            sel = (log2n == k) & (kind == kd)
-            if not sel.any():
-                continue
-            algo, base, tpc = b.schedule(kd, k, 3)
-            sched["%s%d" % ("o" if kd == 0 else "u", k)] = [algo.name, base, tpc]
-            ops += int(sel.sum()) * 2 * fp64_ops_per_transform(1 << k, base, int(algo))
-    peak = fp64_peak(cf)
-    bytes_alg = total * 32
-    peaks, kindp = measured_peaks()
-    # end to end: pinned host data in and out, chunks of items pipelined (cfft_batch_run_host)
-    host = data.cpu().pin_memory()
-    with torch.cuda.stream(stream):
-        b.run_host(host, data)  # builds the chunk tables
-        torch.cuda.current_stream().synchronize()
-        t1 = time.perf_counter()
-        e2e_steps = 3
-        for _ in range(e2e_steps):
-            b.run_host(host, data)
-        torch.cuda.current_stream().synchronize()
-    e2e_s = time.perf_counter() - t1
-    if rank != 0:
-        return
-    print(json.dumps({
-        "metric": "mixed-size c64 transforms/s (100k items, n=2^8..2^16, fwd then inv)", "value": value,
-        "unit": "transforms/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
-        "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-        "dtype": "f64", "data": "synthetic (seeded)",
-        "config": {"workload": "mixed batch, %d items, %d points, one persistent launch per step (graph)" % (count, total),
-                   "schedule": sched, "units": b.units(), "tune_seconds_total": tune_s,
-                   "ordered_items": int((kind == 0).sum())},
-        "roofline": {"bound": "hbm", "achieved": bytes_alg / per_launch / 1e9, "peak": peaks["hbm_gbs"],
-                     "unit": "GB/s", "frac": bytes_alg / per_launch / 1e9 / peaks["hbm_gbs"], "traffic": None,
-                     "fp64": {"achieved_ops_per_s": ops / per_launch, "peak_ops_per_s": peak,
-                              "frac": ops / per_launch / peak}},
-        "e2e": {"value": world * transforms * e2e_steps / e2e_s, "unit": "transforms/s",
-                "h2d_bytes_per_step": total * 16, "d2h_bytes_per_step": total * 16},
-        "clocks": clocks, "gpu_launches": args.steps,
-    }))
+def _oracle():
+    p = os.path.join(ROOT, "oracle")
+    if p not in sys.path:
+        sys.path.insert(0, p)
+    import pyoracle
+    return pyoracle
 
 
-def run_ordered(args):
-    """ordered::Plan n = 1024, fwd then inv, batch 256 (throughput) and batch 1 (latency)."""
+def host_threads():
+    return os.cpu_count() or 1
+
+
+def rel_l2(got, want):
     import numpy as np
-    torch, cf, rank, world, local = gpu_setup()
+    got, want = np.asarray(got), np.asarray(want)
+    den = float(np.linalg.norm(want.ravel()))
+    return float(np.linalg.norm((got - want).ravel())) / den if den else 0.0
+
+
+def same_bits(got, want):
+    import numpy as np
+    return bool(np.array_equal(np.ascontiguousarray(got).view(np.uint64), np.ascontiguousarray(want).view(np.uint64)))
+
+
+def cpu_loop(fn, seconds, min_reps=2):
+    """Calls fn until `seconds` have passed (at least min_reps times); returns (reps, elapsed)."""
+    fn()  # warm
+    reps, t0 = 0, time.perf_counter()
+    while True:
+        fn()
+        reps += 1
+        el = time.perf_counter() - t0
+        if el >= seconds and reps >= min_reps:
+            return reps, el
+
+
+_CPU_MEASURE = {}
+
+
+def cpu_measure_ordered(po, n):
+    """ordered::Plan's Method::Measure on the host (src/ordered.rs:99-180): the fastest of the 8
+    algorithms for one n-point forward transform, single-threaded, on the restatement."""
+    key = ("o", n)
+    if key not in _CPU_MEASURE:
+        import numpy as np
+        x = np.random.default_rng(n).uniform(-1, 1, (max(1, 4096 // n), n)).astype(np.complex128)
+        best = None
+        for algo in range(8):
+            w, _ = po.ordered_twiddles(po.radix(algo), n)
+            reps, el = cpu_loop(lambda: po.ordered_batch_inplace(1, algo, x, w, 1), 0.02)
+            if best is None or el / reps < best[0]:
+                best = (el / reps, algo)
+        _CPU_MEASURE[key] = best[1]
+    return _CPU_MEASURE[key]
+
+
+def cpu_measure_unordered(po, n):
+    """unordered::Plan's Method::Measure on the host (src/unordered.rs:553-640): n <= 256 takes
+    the ordered winner at n; otherwise bases 512 and 1024 (<= n), each with the ordered winner at
+    the base, and the faster forward transform wins."""
+    key = ("u", n)
+    if key not in _CPU_MEASURE:
+        import numpy as np
+        if n <= 256:
+            _CPU_MEASURE[key] = (cpu_measure_ordered(po, n), n)
+        else:
+            best = None
+            for base in (512, 1024):
+                if n < base:
+                    break
+                algo = cpu_measure_ordered(po, base)
+                w, _ = po.unordered_twiddles(n, base, algo)
+                x = np.random.default_rng(n).uniform(-1, 1, (max(1, 8192 // n), n)).astype(np.complex128)
+                reps, el = cpu_loop(lambda: po.unordered_batch_inplace(1, algo, base, x, w, 1), 0.03)
+                if best is None or el / reps < best[0]:
+                    best = (el / reps, algo, base)
+            _CPU_MEASURE[key] = best[1:]
+    return _CPU_MEASURE[key]
+
+
+def torus_bits_u128(got, exact):
+    """Largest |got - exact| mod 2^128 (as a signed 128-bit difference) in bits, and the
+    fraction of exact coefficients; arrays (..., N, 2) uint64 holding (lo, hi)."""
+    import numpy as np
+    g = np.ascontiguousarray(got, dtype=np.uint64).reshape(-1, 2)
+    e = np.ascontiguousarray(exact, dtype=np.uint64).reshape(-1, 2)
+    lo = g[:, 0] - e[:, 0]
+    borrow = (g[:, 0] < e[:, 0]).astype(np.uint64)
+    hi = (g[:, 1] - e[:, 1] - borrow).view(np.int64)
+    small_pos = hi == 0
+    small_neg = hi == -1
+    mag = np.where(small_pos, lo.astype(np.float64), 0.0)
+    mag = np.where(small_neg, (np.uint64(0) - lo).astype(np.float64), mag)
+    big = ~(small_pos | small_neg)
+    mag = np.where(big, np.abs(hi.astype(np.float64) + lo.astype(np.float64) / 2.0 ** 64) * 2.0 ** 64, mag)
+    worst = float(mag.max()) if mag.size else 0.0
+    exact_frac = float(((lo == 0) & (hi == 0)).mean()) if mag.size else 1.0
+    return (float(np.log2(worst)) if worst > 0 else 0.0), exact_frac
+
+
+def torus_bits_u64(got, exact):
+    import numpy as np
+    diff = (np.ascontiguousarray(got, dtype=np.uint64) - np.ascontiguousarray(exact, dtype=np.uint64)).view(np.int64)
+    worst = float(np.abs(diff.astype(np.float64)).max()) if diff.size else 0.0
+    return (float(np.log2(worst)) if worst > 0 else 0.0), float((diff == 0).mean()) if diff.size else 1.0
+
+
+# ---------------------------------------------------------------- config 1: ordered c64
+def measure_ordered(torch, cf, steps, warmup, local, world, full=False, cpu_seconds=2.0, cpu=True):
+    """ordered::Plan n = 1024, forward then inverse: batch 256 (throughput) and batch 1
+    (latency), accuracy against the oracle and numpy, e2e through the host entry points on a
+    page-locked buffer, and the reference's CPU algorithm on the host cores."""
+    import numpy as np
+    po = _oracle()
     rng = np.random.default_rng(1)
     x = rng.uniform(-1, 1, (256, 1024)) + 1j * rng.uniform(-1, 1, (256, 1024))
-    d = torch.from_numpy(x).cuda()
-    if args.profile_case:  # for ncu: 4 forward calls of batch 256 split over 4 CTAs per transform
-        algo = cf.FftAlgo[args.base_algo] if args.base_algo else cf.FftAlgo.Dit4
-        plan = cf.ordered.Plan(1024, cf.ordered.Method.UserProvided(algo))
-        plan.set_cluster_size(4)
-        for _ in range(4):
-            plan.fwd(d)
-        torch.cuda.synchronize()
-        print(json.dumps({"profile_case": "ordered n=1024 batch 256, 4 CTAs per transform", "algo": algo.name}))
-        return
     plan = cf.ordered.Plan(1024, cf.ordered.Method.Measure(0.002))
+    algo = plan.algo()
+    d = torch.from_numpy(x).cuda()
+    # accuracy: one forward and one inverse of all 256 transforms against the oracle's
+    # restatement of the same algorithm, and the forward against numpy's FFT
+    plan.fwd(d)
+    got_f = d.cpu().numpy()
+    plan.inv(d)
+    got_i = d.cpu().numpy()
+    want_f = po.ordered_fwd(int(algo), x)
+    want_i = po.ordered_inv(int(algo), want_f)
+    accuracy = {"sample_transforms": 256, "rel_l2_fwd_vs_oracle": rel_l2(got_f, want_f),
+                "rel_l2_inv_vs_oracle": rel_l2(got_i, want_i),
+                "bit_identical_to_oracle": same_bits(got_f, want_f) and same_bits(got_i, want_i),
+                "rel_l2_fwd_vs_numpy_fft": rel_l2(got_f, np.fft.fft(x, axis=-1)),
+                "roundtrip_rel_l2": rel_l2(got_i / 1024, x),
+                "bound": "c64 relative L2 <= 1e-13 against the reference (the oracle: same algorithm, same bits)"}
+    d.copy_(torch.from_numpy(x))  # fwd+inv multiplies by n each step: start from the inputs
     one = d[:1].clone()
 
     def step256():
@@ -585,10 +671,88 @@ def run_ordered(args):
         plan.fwd(one)
         plan.inv(one)
 
-    ms256, clocks = timed(torch, step256, args.steps, args.warmup, local, world)
-    ms1, _ = timed(torch, step1, args.steps, args.warmup, local, world)
-    # one unordered transform of 4096..32768 points (base 1024), fwd then inv: split over a
-    # cluster (automatic) against one CTA / the global-level path
+    ms256, clocks = timed(torch, step256, steps, warmup, local, world)
+    d.copy_(torch.from_numpy(x))
+    ms1, _ = timed(torch, step1, steps, warmup, local, world)
+    # device-side batch-1 latency: 20 fwd+inv pairs in one CUDA graph (no host call between)
+    graph20 = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(graph20):
+        for _ in range(20):
+            step1()
+    reps20 = max(5, steps // 10)
+    ms1g20, _ = timed(torch, graph20.replay, reps20, warmup, local, world)
+    per = ms256 * 1e-3 / steps
+    ops = 256 * 2 * fp64_ops_ordered(1024, int(algo))
+    peak = fp64_peak(cf)
+    peaks, peak_kind = measured_peaks()
+    bytes_step = 256 * 2 * 32768  # each of the 512 calls reads and writes 16 KiB
+    prof = profiled_traffic("split_kernel_ordered_n1024_b256") or {}
+    # end to end through the host entry points on a page-locked buffer (in place across the link)
+    h = torch.from_numpy(x.copy()).pin_memory()
+    plan.fwd(h)
+    plan.inv(h)
+    h.copy_(torch.from_numpy(x))
+    e2e_steps = max(3, steps // 5)
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        plan.fwd(h)
+        plan.inv(h)
+    e2e = world * 512 * e2e_steps / (time.perf_counter() - t0)
+    entry = {
+        "metric": "ordered c64 n=1024 transforms/s (batch 256, fwd then inv)",
+        "value": world * 512 * steps / (ms256 * 1e-3), "unit": "transforms/s", "steps": steps, "warmup": warmup,
+        "ms_per_step": ms256 / steps, "higher_is_better": True, "dtype": "f64",
+        "config": {"workload": "ordered::Plan n=1024, batch 256 and batch 1, fwd then inv (in place)",
+                   "algo": algo.name, "l2": "8 MiB batch, L2-resident between calls (as in the reference's loop)",
+                   "batch1_us_per_fwd_inv": ms1 * 1e3 / steps,
+                   "batch1_us_per_fwd_inv_device": ms1g20 * 1e3 / (reps20 * 20)},
+        "roofline": {"bound": "hbm", "achieved": bytes_step / per / 1e9, "peak": peaks["hbm_gbs"], "unit": "GB/s",
+                     "frac": bytes_step / per / 1e9 / peaks["hbm_gbs"], "peak_kind": peak_kind,
+                     "traffic": prof.get("dram_bytes_per_launch"),
+                     "algorithmic_bytes_per_launch": 256 * 32768,
+                     "fp64": {"achieved_ops_per_s": ops / per, "peak_ops_per_s": peak, "frac": ops / per / peak,
+                              "ops_per_transform": fp64_ops_ordered(1024, int(algo)),
+                              "note": "binding roof: FP64 pipe"}},
+        "e2e": {"value": e2e, "unit": "transforms/s", "h2d_bytes_per_step": 2 * 256 * 1024 * 16,
+                "d2h_bytes_per_step": 2 * 256 * 1024 * 16, "steps": e2e_steps,
+                "path": "cfft_ordered_fwd_host / _inv_host on a page-locked buffer, in place"},
+        "accuracy": accuracy, "clocks": clocks, "gpu_launches": 2 * steps,
+    }
+    if full:
+        entry["config"].update(ordered_sweeps(torch, cf, plan, d, one, step1, steps, warmup, local, world, rng))
+    if cpu and world == 1:
+        threads = host_threads()
+        calgo = cpu_measure_ordered(po, 1024)
+        w, wi = po.ordered_twiddles(po.radix(calgo), 1024)
+        x1 = np.ascontiguousarray(x[:1])
+
+        def one_call():
+            po.ordered_batch_inplace(1, calgo, x1, w, 1)
+            po.ordered_batch_inplace(0, calgo, x1, wi, 1)
+        reps1, el1 = cpu_loop(one_call, cpu_seconds / 4)
+        xb = np.ascontiguousarray(np.tile(x, (max(1, threads // 4), 1)))
+
+        def all_core():
+            po.ordered_batch_inplace(1, calgo, xb, w, threads)
+            po.ordered_batch_inplace(0, calgo, xb, wi, threads)
+        repsb, elb = cpu_loop(all_core, cpu_seconds)
+        entry["cpu_baseline"] = {
+            "value": 2 * xb.shape[0] * repsb / elb, "unit": "transforms/s", "cores": threads, "kind": "port",
+            "single_thread_us_per_fwd_inv": el1 / reps1 * 1e6,
+            "single_thread_transforms_per_s": 2 * reps1 / el1, "algo": ALGO_NAMES[calgo],
+            "sample": "%d x (fwd+inv of %d transforms, n=1024) on %d threads in %.1f s; batch 1 on one thread "
+                      "(%s: Method::Measure's pick on this host, scalar restatement)"
+                      % (repsb, xb.shape[0], threads, elb, ALGO_NAMES[calgo])}
+    return entry
+
+
+def ordered_sweeps(torch, cf, plan, d, one, step1, steps, warmup, local, world, rng):
+    """The ordered workload's diagnostics: caller-captured graph replay, unordered batch-1
+    latency by n, and the CTAs-per-transform sweep."""
+    graph = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(graph):
+        step1()
+    ms1g, _ = timed(torch, graph.replay, steps, warmup, local, world)
     large = {}
     for lgn in (12, 13, 14, 15):
         up = cf.unordered.Plan(1 << lgn, cf.unordered.Method.UserProvided(cf.FftAlgo.Dif4, 1024))
@@ -600,24 +764,9 @@ def run_ordered(args):
         row = {}
         for ctas, name in ((0, "split"), (1, "one_cta_or_levels")):
             up.set_cluster_size(ctas)
-            msu, _ = timed(torch, stepu, max(10, args.steps // 4), args.warmup, local, world)
-            row[name] = round(msu * 1e3 / max(10, args.steps // 4), 2)
+            msu, _ = timed(torch, stepu, max(10, steps // 4), warmup, local, world)
+            row[name] = round(msu * 1e3 / max(10, steps // 4), 2)
         large[1 << lgn] = row
-    # the same batch-1 fwd+inv captured by the caller into a CUDA graph and replayed
-    graph = torch.cuda.CUDAGraph()
-    with torch.cuda.graph(graph):
-        step1()
-    ms1g, _ = timed(torch, graph.replay, args.steps, args.warmup, local, world)
-    # device-side batch-1 latency: 20 fwd+inv pairs captured in one graph, so that no host
-    # call (Python, ctypes) sits between the launches
-    graph20 = torch.cuda.CUDAGraph()
-    with torch.cuda.graph(graph20):
-        for _ in range(20):
-            step1()
-    reps20 = max(5, args.steps // 10)
-    ms1g20, _ = timed(torch, graph20.replay, reps20, args.warmup, local, world)
-    # CTAs per transform (1 = one CTA, 2/4/8 = split over a cluster) at a few batch sizes, fwd then inv,
-    # for a DIT algorithm (one exchange through distributed shared memory) and a DIF one (none)
     sweep = {}
     for aname in ("Dit4", "Dif4"):
         sp = cf.ordered.Plan(1024, cf.ordered.Method.UserProvided(cf.FftAlgo[aname]))
@@ -629,50 +778,463 @@ def run_ordered(args):
                 sp.fwd(sub)
                 sp.inv(sub)
             row = {}
-            for ctas in (1, 2, 4, 8):
+            for ctas in (0, 1, 2, 4, 8):
                 sp.set_cluster_size(ctas)
-                ms_b, _ = timed(torch, step_b, max(10, args.steps // 4), args.warmup, local, world)
-                row[ctas] = round(ms_b * 1e3 / max(10, args.steps // 4), 2)
+                ms_b, _ = timed(torch, step_b, max(10, steps // 4), warmup, local, world)
+                row["auto" if ctas == 0 else ctas] = round(ms_b * 1e3 / max(10, steps // 4), 2)
             sweep[aname][batch] = row
-    per = ms256 * 1e-3 / args.steps
-    ops = 256 * 2 * fp64_ops_ordered(1024, int(plan.algo()))
-    peak = fp64_peak(cf)
-    # end to end through the host entry points on a page-locked buffer: the kernel reads and
-    # writes it in place across the host link (each call moves the batch in and out)
-    h = torch.from_numpy(x.copy()).pin_memory()
-    plan.fwd(h)
-    plan.inv(h)
+    return {"batch1_us_per_fwd_inv_graph_replay": ms1g * 1e3 / steps,
+            "unordered_batch1_us_per_fwd_inv_by_n": large,
+            "us_per_fwd_inv_by_batch_and_ctas_per_transform": sweep}
+
+
+# ---------------------------------------------------------------- config 3: mixed batch
+def mixed_items(cf, count, seed):
+    import numpy as np
+    rng = np.random.default_rng(seed)
+    log2n = rng.integers(8, 17, count)
+    kind = rng.integers(0, 2, count)
+    kind = np.where(log2n > 10, 1, kind)  # the reference has no ordered plan above 1024 points
+    sizes = (1 << log2n).astype(np.int64)
+    offs = np.concatenate([[0], np.cumsum(sizes)[:-1]]).astype(np.uint64)
+    items = np.zeros(count, dtype=cf.batch.ITEM_DTYPE)
+    items["offset"], items["log2n"], items["kind"], items["direction"] = offs, log2n, kind, 3
+    return items, log2n, kind, sizes, offs, rng
+
+
+def measure_mixed(torch, cf, steps, warmup, local, world, count=100000, tune_seconds=0.0005, seed=3,
+                  cpu_seconds=3.0, cpu=True, e2e_steps=3):
+    """100,000 c64 transforms, sizes 2^k with k uniform in 8..16, half ordered and half unordered,
+    forward then inverse, one persistent launch per step (CUDA graph replay)."""
+    import numpy as np
+    po = _oracle()
+    items, log2n, kind, sizes, offs, rng = mixed_items(cf, count, seed)
+    total = int(sizes.sum())
     t0 = time.perf_counter()
-    for _ in range(max(3, args.steps // 10)):
-        plan.fwd(h)
-        plan.inv(h)
-    e2e = world * 512 * max(3, args.steps // 10) / (time.perf_counter() - t0)
-    if rank != 0:
+    b = cf.batch.Batch(items, tune_seconds=tune_seconds)
+    tune_s = time.perf_counter() - t0
+    g = torch.Generator(device="cuda")
+    g.manual_seed(seed)
+    data = (torch.rand((total, 2), dtype=torch.float64, device="cuda", generator=g) * 2 - 1)
+    sample = rng.choice(count, 64, replace=False)
+    saved = {int(i): data[int(offs[i]):int(offs[i]) + int(sizes[i])].clone() for i in sample}
+    stream = torch.cuda.Stream()
+    with torch.cuda.stream(stream):
+        ms, clocks = timed(torch, lambda: b.run(data), steps, warmup, local, world)
+        # accuracy: the sampled items from their inputs again, one launch, against the oracle
+        for i, v in saved.items():
+            data[int(offs[i]):int(offs[i]) + int(sizes[i])].copy_(v)
+        b.run(data)
+        torch.cuda.current_stream().synchronize()
+    worst_rel, identical, rt = 0.0, True, 0.0
+    for i, v in saved.items():
+        n = int(sizes[i])
+        xs = v.cpu().numpy()
+        xi = xs[:, 0] + 1j * xs[:, 1]
+        got = data[int(offs[i]):int(offs[i]) + n].cpu().numpy()
+        got = got[:, 0] + 1j * got[:, 1]
+        algo, base, _ = b.schedule(int(kind[i]), int(log2n[i]), 3)
+        if kind[i] == 0:
+            want = po.ordered_inv(int(algo), po.ordered_fwd(int(algo), xi))
+        else:
+            want = po.unordered_inv(int(algo), base, po.unordered_fwd(int(algo), base, xi))
+        worst_rel = max(worst_rel, rel_l2(got, want))
+        identical = identical and same_bits(got, want)
+        rt = max(rt, rel_l2(got / n, xi))
+    accuracy = {"sample_items": len(saved), "max_rel_l2_vs_oracle": worst_rel, "bit_identical_to_oracle": identical,
+                "max_roundtrip_rel_l2": rt,
+                "against": "oracle restatement of the reference's ordered/unordered plans with the scheduled algorithm"}
+    transforms = 2 * count
+    value = world * transforms * steps / (ms * 1e-3)
+    per_launch = ms * 1e-3 / steps
+    ops = 0
+    sched = {}
+    for k in range(8, 17):
+        for kd in (0, 1):
+            sel = (log2n == k) & (kind == kd)
+            if not sel.any():
+                continue
+            algo, base, tpc = b.schedule(kd, k, 3)
+            sched["%s%d" % ("o" if kd == 0 else "u", k)] = [algo.name, base, tpc]
+            ops += int(sel.sum()) * 2 * fp64_ops_per_transform(1 << k, base, int(algo))
+    peak = fp64_peak(cf)
+    bytes_alg = total * 32 * 2  # forward and inverse each read and write every point
+    peaks, peak_kind = measured_peaks()
+    prof = profiled_traffic("batch_kernel_mixed") or {}
+    # end to end: pinned host data in and out, chunks of items pipelined (cfft_batch_run_host)
+    host = data.cpu().pin_memory()
+    with torch.cuda.stream(stream):
+        b.run_host(host, data)  # builds the chunk tables
+        torch.cuda.current_stream().synchronize()
+        t1 = time.perf_counter()
+        for _ in range(e2e_steps):
+            b.run_host(host, data)
+        torch.cuda.current_stream().synchronize()
+    e2e_s = time.perf_counter() - t1
+    del host, data
+    entry = {
+        "metric": "mixed-size c64 transforms/s (100k items, n=2^8..2^16, fwd then inv)", "value": value,
+        "unit": "transforms/s", "steps": steps, "warmup": warmup, "ms_per_step": ms / steps,
+        "higher_is_better": True, "dtype": "f64",
+        "config": {"workload": "mixed batch, %d items, %d points, one persistent launch per step (graph)"
+                               % (count, total),
+                   "schedule": sched, "units": b.units(), "tune_seconds_total": tune_s,
+                   "ordered_items": int((kind == 0).sum()), "l2": "23 GB of data > L2"},
+        "roofline": {"bound": "hbm", "achieved": bytes_alg / per_launch / 1e9, "peak": peaks["hbm_gbs"],
+                     "unit": "GB/s", "frac": bytes_alg / per_launch / 1e9 / peaks["hbm_gbs"], "peak_kind": peak_kind,
+                     "traffic": (prof.get("dram_bytes_per_point") * total) if prof.get("dram_bytes_per_point") else None,
+                     "algorithmic_bytes_per_launch": bytes_alg,
+                     "fp64": {"achieved_ops_per_s": ops / per_launch, "peak_ops_per_s": peak,
+                              "frac": ops / per_launch / peak, "note": "binding roof: FP64 pipe"}},
+        "e2e": {"value": world * transforms * e2e_steps / e2e_s, "unit": "transforms/s",
+                "h2d_bytes_per_step": total * 16, "d2h_bytes_per_step": total * 16, "steps": e2e_steps,
+                "path": "cfft_batch_run_host from page-locked host memory, 16 pipelined chunks"},
+        "accuracy": accuracy, "clocks": clocks, "gpu_launches": steps,
+    }
+    if cpu and world == 1:
+        entry["cpu_baseline"] = cpu_mixed_rate(po, log2n, kind, cpu_seconds)
+    return entry
+
+
+def cpu_mixed_rate(po, log2n, kind, seconds):
+    """The reference's CPU path over the mixed items, in item order, on every host thread (one
+    Python thread per core driving the single-threaded restatement; ctypes releases the GIL),
+    each size with the algorithm Method::Measure picks on this host."""
+    import numpy as np
+    from concurrent.futures import ThreadPoolExecutor
+    threads = host_threads()
+    tables = {}
+    for k in range(8, 17):
+        for kd in (0, 1):
+            n = 1 << k
+            if kd == 0 and k <= 10:
+                a = cpu_measure_ordered(po, n)
+                tables[(kd, k)] = (a, n, *po.ordered_twiddles(po.radix(a), n))
+            elif kd == 1:
+                a, base = cpu_measure_unordered(po, n)
+                tables[(kd, k)] = (a, base, *po.unordered_twiddles(n, base, a))
+    rng = np.random.default_rng(11)
+    bufs = {k: rng.uniform(-1, 1, (threads, 1 << k)).astype(np.complex128) for k in range(8, 17)}
+    stop_at = [None]
+    done = [0] * threads
+
+    def worker(t):
+        i = t
+        while time.perf_counter() < stop_at[0]:
+            k, kd = int(log2n[i % len(log2n)]), int(kind[i % len(kind)])
+            a, base, w, wi = tables[(kd, k)]
+            buf = bufs[k][t:t + 1]
+            if kd == 0:
+                po.ordered_batch_inplace(1, a, buf, w, 1)
+                po.ordered_batch_inplace(0, a, buf, wi, 1)
+            else:
+                po.unordered_batch_inplace(1, a, base, buf, w, 1)
+                po.unordered_batch_inplace(0, a, base, buf, wi, 1)
+            buf *= 1.0 / (1 << k)
+            done[t] += 1
+            i += threads
+    t0 = time.perf_counter()
+    stop_at[0] = t0 + seconds
+    with ThreadPoolExecutor(threads) as ex:
+        list(ex.map(worker, range(threads)))
+    el = time.perf_counter() - t0
+    items_done = sum(done)
+    return {"value": 2 * items_done / el, "unit": "transforms/s", "cores": threads, "kind": "port",
+            "sample": "the first %d items of the 100k list (same size/kind mix), fwd+inv each, %d host threads, "
+                      "%.1f s; per size the algorithm Method::Measure picks on this host (scalar restatement)"
+                      % (items_done, threads, el),
+            "host_algorithms": {("o%d" % k if kd == 0 else "u%d" % k): [ALGO_NAMES[v[0]], v[1]]
+                                for (kd, k), v in sorted(tables.items())}}
+
+
+# ---------------------------------------------------------------- config 4: u128 products
+def measure_u128(torch, cf, steps, warmup, local, world, full=False, cpu_seconds=2.0, cpu=True, sample=64):
+    """u128 negacyclic products N = 1024 and 4096, 2048 per launch, A uniform u128, B digits in
+    [-2^15, 2^15); per N: device rate, accuracy on `sample` products against the exact
+    wrapping-u128 schoolbook beside the restated reference pipeline's, and the CPU rate."""
+    import numpy as np
+    po = _oracle()
+    threads = host_threads()
+    by_n = {}
+    clocks = None
+    e2e = None
+    count = 2048
+    for N in (1024, 4096):
+        plan = cf.product.U128ProductPlan(N)
+        rng = np.random.default_rng(4)
+        a_np = rng.integers(0, 2 ** 64, (count, N, 2), dtype=np.uint64)
+        b_np = rng.integers(-2 ** 15, 2 ** 15, (count, N))
+        a = torch.from_numpy(a_np.view(np.int64)).cuda()
+        b = torch.from_numpy(b_np).cuda()
+        bhat = torch.empty((count, 4, N // 2), dtype=torch.float64, device="cuda")
+        plan.prepare_operand(b, bhat)
+        out = torch.empty_like(a)
+        ms, clk = timed(torch, lambda: plan.product(a, bhat, out), steps, warmup, local, world)
+        clocks = clocks or clk
+        a1, b1, o1 = a[:1].clone(), bhat[:1].clone(), out[:1].clone()
+        ms1, _ = timed(torch, lambda: plan.product(a1, b1, o1), max(10, steps), warmup, local, world)
+        rows = np.linspace(0, count - 1, sample).astype(np.int64)
+        got = out.cpu().numpy().view(np.uint64)[rows]
+        exact = po.schoolbook_batch(a_np[rows], b_np[rows], threads)
+        ref = po.u128_product(N, a_np[rows], po.u128_prepare(N, b_np[rows]), nthreads=threads)
+        gbits, gex = torus_bits_u128(got, exact)
+        rbits, rex = torus_bits_u128(ref, exact)
+        row = {"products_per_s": world * count * steps / (ms * 1e-3), "ms_per_launch": ms / steps,
+               "one_product_us": round(ms1 * 1e3 / max(10, steps), 2),
+               "accuracy": {"sample_products": sample, "gpu_max_torus_error_bits": gbits,
+                            "gpu_exact_coefficient_fraction": gex,
+                            "reference_pipeline_max_torus_error_bits": rbits,
+                            "reference_pipeline_exact_coefficient_fraction": rex,
+                            "gpu_equals_reference_pipeline": bool(np.array_equal(got, ref)),
+                            "gpu_bits_le_reference_bits": gbits <= rbits,
+                            "against": "exact wrapping-u128 schoolbook (oracle, unsigned __int128)"}}
+        if N == 1024:  # end to end: pinned host A in and results out through the host entry point
+            ha = a.cpu().pin_memory()
+            hout = torch.empty_like(ha).pin_memory()
+            plan.product(ha, bhat, hout)
+            e2e_steps = max(3, steps // 3)
+            t0 = time.perf_counter()
+            for _ in range(e2e_steps):
+                plan.product(ha, bhat, hout)
+            e2e = {"value": world * count * e2e_steps / (time.perf_counter() - t0), "unit": "products/s",
+                   "h2d_bytes_per_step": count * N * 16, "d2h_bytes_per_step": count * N * 16, "steps": e2e_steps,
+                   "matches_device_result": bool(torch.equal(hout, out.cpu())), "N": N,
+                   "path": "cfft_u128_product_host, page-locked A and result"}
+        if cpu and world == 1:
+            cs = max(64, 8 * threads)
+            ca, cb = a_np[:cs], po.u128_prepare(N, b_np[:cs])
+            reps, el = cpu_loop(lambda: po.u128_product(N, ca, cb, nthreads=threads), cpu_seconds / 2)
+            reps1, el1 = cpu_loop(lambda: po.u128_product(N, ca[:1], cb[:1], nthreads=1), cpu_seconds / 8)
+            row["cpu_products_per_s"] = cs * reps / el
+            row["cpu_single_thread_us_per_product"] = el1 / reps1 * 1e6
+            row["cpu_sample"] = "%d x %d products on %d threads in %.1f s" % (reps, cs, threads, el)
+        by_n[N] = row
+        del a, b, bhat, out
+    prof = profiled_traffic("u128_product_n1024") or {}
+    peak = fp64_peak(cf)
+    peaks, peak_kind = measured_peaks()
+    v = by_n[1024]["products_per_s"]
+    fp64 = None
+    if prof.get("fp64_thread_inst_per_product"):
+        ach = prof["fp64_thread_inst_per_product"] * v
+        fp64 = {"achieved_ops_per_s": ach, "peak_ops_per_s": peak, "frac": ach / peak,
+                "ops_per_product": prof["fp64_thread_inst_per_product"],
+                "note": "DADD/DFMA/DMUL per product counted by ncu (N=1024); the FP64 pipe also issues the "
+                        "double-double code's comparisons and conversions"}
+    # fft128::Plan itself at n = 512 (batch 4096 and batch 1), GPU and the host's restatement
+    plans128 = {}
+    for n, batch in (((512, 4096), (2048, 1024), (4096, 512), (16384, 128)) if full else ((512, 4096),)):
+        fp = cf.fft128.Plan(n)
+        bufs = [torch.rand((batch, n), dtype=torch.float64, device="cuda") for _ in range(4)]
+
+        def step128():
+            fp.fwd(*bufs)
+            fp.inv(*bufs)
+        s128 = max(5, steps)
+        ms128, _ = timed(torch, step128, s128, warmup, local, world)
+        one = [bb[:1].clone() for bb in bufs]
+
+        def step1():
+            fp.fwd(*one)
+            fp.inv(*one)
+        ms1, _ = timed(torch, step1, max(10, steps), warmup, local, world)
+        row = {"transforms_per_s": world * 2 * batch * s128 / (ms128 * 1e-3), "batch": batch,
+               "batch1_us_per_fwd_inv": round(ms1 * 1e3 / max(10, steps), 2)}
+        if cpu and world == 1 and n == 512:
+            t = po.f128_twiddles(n)
+            rng = np.random.default_rng(12)
+            hb = [rng.uniform(-1, 1, (4 * threads, n)) for _ in range(4)]
+
+            def cpu_all():
+                po.f128_batch_inplace(1, hb, t, threads)
+                po.f128_batch_inplace(0, hb, t, threads)
+                for v_ in hb:
+                    v_ *= 1.0 / n
+            reps, el = cpu_loop(cpu_all, cpu_seconds / 2)
+            h1 = [v_[:1].copy() for v_ in hb]
+
+            def cpu_one():
+                po.f128_batch_inplace(1, h1, t, 1)
+                po.f128_batch_inplace(0, h1, t, 1)
+                for v_ in h1:
+                    v_ *= 1.0 / n
+            reps1, el1 = cpu_loop(cpu_one, cpu_seconds / 8)
+            row["cpu_transforms_per_s"] = 2 * 4 * threads * reps / el
+            row["cpu_single_thread_us_per_fwd_inv"] = el1 / reps1 * 1e6
+        plans128[n] = row
+        del bufs
+    entry = {
+        "metric": "u128 negacyclic polymul/s (double-double), N=1024", "value": v, "unit": "products/s",
+        "steps": steps, "warmup": warmup, "ms_per_step": by_n[1024]["ms_per_launch"], "higher_is_better": True,
+        "dtype": "f64x2 (double-double)",
+        "config": {"workload": "u128 products N=1024 and N=4096, 2048 per launch, A uniform u128, "
+                               "B digits in [-2^15, 2^15)", "by_N": by_n, "fft128_plan_fwd_inv_by_n": plans128,
+                   "l2": "N=1024: 96 MiB per launch (A, Bhat, out); N=4096: 384 MiB"},
+        "roofline": {"bound": "hbm", "achieved": v * 49152 / 1e9, "peak": peaks["hbm_gbs"], "unit": "GB/s",
+                     "frac": v * 49152 / 1e9 / peaks["hbm_gbs"], "peak_kind": peak_kind,
+                     "traffic": prof.get("dram_bytes_per_launch"),
+                     "algorithmic_bytes_per_launch": 49152 * count, "fp64": fp64,
+                     "note": "N=1024: 49,152 algorithmic bytes per product; bound by the FP64 pipe"},
+        "e2e": e2e,
+        "accuracy": {"N%d" % N: r["accuracy"] for N, r in by_n.items()},
+        "clocks": clocks, "gpu_launches": 4 * steps,
+    }
+    if cpu and world == 1:
+        entry["cpu_baseline"] = {
+            "value": by_n[1024]["cpu_products_per_s"], "unit": "products/s", "cores": threads, "kind": "port",
+            "N4096_products_per_s": by_n[4096]["cpu_products_per_s"],
+            "single_thread_us_per_product": {N: r["cpu_single_thread_us_per_product"] for N, r in by_n.items()},
+            "fft128_n512": {k: plans128[512][k] for k in ("cpu_transforms_per_s", "cpu_single_thread_us_per_fwd_inv")},
+            "sample": "N=1024: %s; restated reference pipeline (fft128 double-double, scalar)"
+                      % by_n[1024]["cpu_sample"]}
+    return entry
+
+
+# ---------------------------------------------------------------- config 5: serving
+SERVE_SIZES = [10, 11, 12, 13, 14]
+
+
+def measure_serving(torch, cf, local, world, rate=20000.0, seconds=1.0, operand_gb=8, full=False, cpu=True,
+                    cpu_seconds=2.0, seed=5, check_requests=64):
+    """Poisson stream of (k+1)*l-product requests, N in 2^10..2^14, 8 GiB of resident Fourier
+    operands: continuous batching against the plain one-launch-per-step loop on the same
+    seeded stream, and a sample of served results against the same requests run alone."""
+    import numpy as np
+    eng = cf.serving.ProductEngine(SERVE_SIZES)
+    t0 = time.perf_counter()
+    srv = cf.serving.Server(eng, SERVE_SIZES, operand_bytes=operand_gb << 30, seed=seed)
+    setup_s = time.perf_counter() - t0
+    srv.run(srv.config(rate=rate, duration_s=0.05))  # warm-up
+    record_every = 50
+    cfg = srv.config(rate=rate, duration_s=seconds, record_every=record_every)
+    with ClockSampler(local) as clk:
+        t1 = time.time()
+        batched = srv.run(cfg)
+        clk.mark(t1, time.time())
+    ids = srv.recorded_ids()[:check_requests]
+    same = all(np.array_equal(srv.recorded_output(cfg, int(r)), srv.run_alone(cfg, int(r))) for r in ids)
+    extra = {}
+    if full:
+        extra["batched_without_clusters"] = srv.run(srv.config(rate=rate, duration_s=seconds, cluster_log2N=32))
+        extra["batched_staged_io"] = srv.run(srv.config(rate=rate, duration_s=seconds, staged_io=True))
+        extra["batched_via_queue"] = srv.run(srv.config(rate=rate, duration_s=seconds, via_queue=True))
+        sweep = {}
+        for r in (50000.0, 100000.0, 150000.0, 200000.0):
+            st = srv.run(srv.config(rate=r, duration_s=0.5))
+            sweep["%d" % r] = {k: st[k] for k in ("products_per_s", "p50_ms", "p99_ms", "max_ms", "launches",
+                                                  "mean_batch", "deferred_admissions") if k in st}
+        extra["capacity_sweep_req_per_s"] = sweep
+    # the comparator last: it saturates and queues for seconds
+    plain = srv.run(srv.config(rate=rate, duration_s=seconds, plain=True))
+    out_bytes = batched.get("output_bytes", 0)
+    entry = {
+        "metric": "serving: products/s and p50/p99 latency, Poisson %g req/s" % rate,
+        "value": batched["products_per_s"], "unit": "products/s", "steps": 1, "warmup": 1,
+        "higher_is_better": True, "dtype": "f64",
+        "config": {"workload": "serving, (k+1)*l products per request, k in 1..2, l in 1..4, N in 2^10..2^14, "
+                               "digits b in 4..10 bits, resident operands %d GiB" % operand_gb,
+                   "duration_s": seconds, "resident_setup_s": setup_s},
+        "value_note": "the offered load is served in full: products/s equals the arrival rate's products; the "
+                      "serving workload's capacity sweep gives the loop's ceiling",
+        "p50_ms": batched["p50_ms"], "p99_ms": batched["p99_ms"],
+        "plain_p50_ms": plain["p50_ms"], "plain_p99_ms": plain["p99_ms"],
+        "p99_speedup_vs_plain": plain["p99_ms"] / batched["p99_ms"] if batched["p99_ms"] else None,
+        "batched": batched, "plain": plain,
+        "accuracy": {"checked_requests": len(ids), "same_alone_and_in_the_mix": bool(same),
+                     "against": "each recorded request recomputed alone (outside any mix), bit for bit"},
+        "e2e": {"value": batched["products_per_s"], "unit": "products/s", "h2d_bytes_per_step": batched.get("input_bytes"),
+                "d2h_bytes_per_step": out_bytes,
+                "path": "requests admitted on the host as they arrive; item records read from and results stored "
+                        "into page-locked host memory by the kernels; latency from arrival to completion on the "
+                        "host clock"},
+        "clocks": clk.summary(), "gpu_launches": batched["launches"],
+    }
+    entry.update(extra)
+    if cpu and world == 1:
+        entry["cpu_baseline"] = cpu_serving_rate(srv, cfg, cpu_seconds)
+    del srv, eng
+    return entry
+
+
+def cpu_serving_rate(srv, cfg, seconds):
+    """The restated reference pipeline on the host cores over the served requests' products
+    (each request's digit rows times its Fourier operands, per size with the plan's algorithm),
+    in request order until `seconds` have passed: products/s."""
+    import numpy as np
+    from concurrent.futures import ThreadPoolExecutor
+    po = _oracle()
+    threads = host_threads()
+    reqs = []
+    for rid in range(4096):
+        lN, npd = srv.shape(cfg, rid)
+        digits, bhat = srv.inputs(cfg, rid)
+        algo, base = srv.engine.algo(lN)
+        reqs.append((1 << lN, algo, base, digits.view(np.uint64), bhat))
+    stop_at = [None]
+    done = [0] * threads
+
+    def worker(t):
+        i = t
+        while time.perf_counter() < stop_at[0]:
+            N, algo, base, a, bh = reqs[i % len(reqs)]
+            po.u64_product(N, algo, base, a, bh, nthreads=1)
+            done[t] += a.shape[0]
+            i += threads
+    t0 = time.perf_counter()
+    stop_at[0] = t0 + seconds
+    with ThreadPoolExecutor(threads) as ex:
+        list(ex.map(worker, range(threads)))
+    el = time.perf_counter() - t0
+    return {"value": sum(done) / el, "unit": "products/s", "cores": threads, "kind": "port",
+            "sample": "%d products of the first 4096 requests of the same seeded stream (N in 2^10..2^14), in "
+                      "request order and repeated, on %d host threads in %.1f s, the restated reference pipeline "
+                      "with each size's plan algorithm; a capacity (all requests present), not a served rate"
+                      % (sum(done), threads, el)}
+
+
+def print_line(entry, world, data="synthetic (seeded)"):
+    line = {"metric": entry["metric"], "value": entry["value"], "unit": entry["unit"], "n_gpus": world,
+            "steps": entry.get("steps"), "warmup": entry.get("warmup"), "ms_per_step": entry.get("ms_per_step"),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": entry.get("dtype", "f64"),
+            "data": data}
+    line.update({k: v for k, v in entry.items() if k not in line})
+    print(json.dumps(line))
+
+
+def run_mixed(args):
+    """The mixed-size batch (100,000 items) as its own JSON line."""
+    torch, cf, rank, world, local = gpu_setup()
+    entry = measure_mixed(torch, cf, args.steps, args.warmup, local, world, count=args.mixed_items,
+                          tune_seconds=args.tune_seconds, seed=3 + rank, cpu=not args.no_cpu_baseline and rank == 0,
+                          cpu_seconds=args.cpu_seconds)
+    if rank == 0:
+        print_line(entry, world)
+
+
+def run_ordered(args):
+    """ordered::Plan n = 1024 with the full set of latency diagnostics, as its own JSON line."""
+    import numpy as np
+    torch, cf, rank, world, local = gpu_setup()
+    if args.profile_case:  # for ncu: 4 forward calls of batch 256 split over 4 CTAs per transform
+        rng = np.random.default_rng(1)
+        x = rng.uniform(-1, 1, (256, 1024)) + 1j * rng.uniform(-1, 1, (256, 1024))
+        d = torch.from_numpy(x).cuda()
+        algo = cf.FftAlgo[args.base_algo] if args.base_algo else cf.FftAlgo.Dit4
+        plan = cf.ordered.Plan(1024, cf.ordered.Method.UserProvided(algo))
+        plan.set_cluster_size(args.cluster_size if args.cluster_size is not None else 4)
+        for _ in range(4):
+            plan.fwd(d)
+        torch.cuda.synchronize()
+        print(json.dumps({"profile_case": "ordered n=1024 batch 256", "algo": algo.name}))
         return
-    print(json.dumps({
-        "metric": "ordered c64 n=1024 transforms/s (batch 256, fwd then inv)",
-        "value": world * 512 * args.steps / (ms256 * 1e-3), "unit": "transforms/s", "n_gpus": world,
-        "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms256 / args.steps, "higher_is_better": True,
-        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded numpy PCG64)",
-        "config": {"workload": "ordered::Plan n=1024 batch 256", "algo": plan.algo().name,
-                   "batch1_us_per_fwd_inv": ms1 * 1e3 / args.steps,
-                   "batch1_us_per_fwd_inv_graph_replay": ms1g * 1e3 / args.steps,
-                   "batch1_us_per_fwd_inv_device": ms1g20 * 1e3 / (reps20 * 20),
-                   "unordered_batch1_us_per_fwd_inv_by_n": large,
-                   "us_per_fwd_inv_by_batch_and_ctas_per_transform": sweep},
-        "roofline": {"bound": "hbm", "achieved": 256 * 65536 / per / 1e9, "peak": measured_peaks()[0]["hbm_gbs"],
-                     "unit": "GB/s", "frac": 256 * 65536 / per / 1e9 / measured_peaks()[0]["hbm_gbs"],
-                     "traffic": None, "fp64": {"achieved_ops_per_s": ops / per, "peak_ops_per_s": peak,
-                                               "frac": ops / per / peak}},
-        "e2e": {"value": e2e, "unit": "transforms/s", "h2d_bytes_per_step": 2 * 256 * 1024 * 16,
-                "d2h_bytes_per_step": 2 * 256 * 1024 * 16},
-        "clocks": clocks, "gpu_launches": 2 * args.steps,
-    }))
+    entry = measure_ordered(torch, cf, args.steps, args.warmup, local, world, full=True,
+                            cpu=not args.no_cpu_baseline and rank == 0, cpu_seconds=args.cpu_seconds)
+    if rank == 0:
+        print_line(entry, world)
 
 
 def run_u128(args):
-    """u128 negacyclic products N = 1024 and 4096, 2048 per launch, B digits in [-2^15, 2^15)."""
-    import numpy as np
+    """u128 negacyclic products N = 1024 and 4096 and the fft128 plan, as its own JSON line."""
     torch, cf, rank, world, local = gpu_setup()
     if args.profile_case:  # for ncu: four forward calls of the fft128 plan, n = 512, batch 4096
         fp = cf.fft128.Plan(512)
@@ -682,78 +1244,10 @@ def run_u128(args):
         torch.cuda.synchronize()
         print(json.dumps({"profile_case": "fft128 plan n=512 batch 4096 forward"}))
         return
-    res = {}
-    lat1 = {}
-    clocks = None
-    for N in (1024, 4096):
-        plan = cf.product.U128ProductPlan(N)
-        rng = np.random.default_rng(4)
-        count = 2048
-        a = torch.from_numpy(rng.integers(0, 2 ** 64, (count, N, 2), dtype=np.uint64).view(np.int64)).cuda()
-        b = torch.from_numpy(rng.integers(-2 ** 15, 2 ** 15, (count, N))).cuda()
-        bhat = torch.empty((count, 4, N // 2), dtype=torch.float64, device="cuda")
-        plan.prepare_operand(b, bhat)
-        out = torch.empty_like(a)
-        ms, clocks = timed(torch, lambda: plan.product(a, bhat, out), args.steps, args.warmup, local, world)
-        res[N] = world * count * args.steps / (ms * 1e-3)
-        a1, b1, o1 = a[:1].clone(), bhat[:1].clone(), out[:1].clone()
-        ms1, _ = timed(torch, lambda: plan.product(a1, b1, o1), max(10, args.steps), args.warmup, local, world)
-        lat1[N] = round(ms1 * 1e3 / max(10, args.steps), 2)
-        if N == 1024:  # end to end: pinned host A in and results out through the host entry point
-            ha = a.cpu().pin_memory()
-            hout = torch.empty_like(ha).pin_memory()
-            plan.product(ha, bhat, hout)
-            t0 = time.perf_counter()
-            for _ in range(max(3, args.steps // 10)):
-                plan.product(ha, bhat, hout)
-            e2e = world * count * max(3, args.steps // 10) / (time.perf_counter() - t0)
-            e2e_ok = bool(torch.equal(hout, out.cpu()))
-    prof = profiled_traffic("u128_product_n1024") or {}
-    fp64_u128 = None
-    if prof.get("fp64_thread_inst_per_product"):
-        peak = fp64_peak(cf)
-        ach = prof["fp64_thread_inst_per_product"] * res[1024]
-        fp64_u128 = {"achieved_ops_per_s": ach, "peak_ops_per_s": peak, "frac": ach / peak,
-                     "ops_per_product": prof["fp64_thread_inst_per_product"],
-                     "note": "DADD/DFMA/DMUL per product counted by ncu (N=1024); the FP64 pipe also issues the "
-                             "double-double code's comparisons and conversions"}
-    # fft128::Plan itself: fwd then inv of a batch of n-point double-double transforms
-    plans128 = {}
-    for n, batch in ((512, 4096), (2048, 1024), (4096, 512), (16384, 128)):
-        fp = cf.fft128.Plan(n)
-        bufs = [torch.rand((batch, n), dtype=torch.float64, device="cuda") for _ in range(4)]
-
-        def step128():
-            fp.fwd(*bufs)
-            fp.inv(*bufs)
-        ms128, _ = timed(torch, step128, max(5, args.steps), args.warmup, local, world)
-        one = [bb[:1].clone() for bb in bufs]
-
-        def step1():
-            fp.fwd(*one)
-            fp.inv(*one)
-        ms1, _ = timed(torch, step1, max(10, args.steps), args.warmup, local, world)
-        plans128[n] = {"transforms_per_s": world * 2 * batch * max(5, args.steps) / (ms128 * 1e-3), "batch": batch,
-                       "batch1_us_per_fwd_inv": round(ms1 * 1e3 / max(10, args.steps), 2)}
-    if rank != 0:
-        return
-    print(json.dumps({
-        "metric": "u128 negacyclic polymul/s (double-double)", "value": res[1024], "unit": "products/s",
-        "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "f64x2 (double-double)", "data": "synthetic (seeded numpy PCG64)",
-        "config": {"workload": "u128 product, 2048 per launch", "N1024_products_per_s": res[1024],
-                   "N4096_products_per_s": res[4096], "one_product_us_by_N": lat1,
-                   "fft128_plan_fwd_inv_by_n": plans128},
-        "e2e": {"value": e2e, "unit": "products/s", "h2d_bytes_per_step": count * 1024 * 16,
-                "d2h_bytes_per_step": count * 1024 * 16, "matches_device_result": e2e_ok, "N": 1024},
-        "roofline": {"bound": "hbm", "achieved": res[1024] * 49152 / 1e9, "peak": measured_peaks()[0]["hbm_gbs"],
-                     "unit": "GB/s", "frac": res[1024] * 49152 / 1e9 / measured_peaks()[0]["hbm_gbs"],
-                     "traffic": (profiled_traffic("u128_product_n1024") or {}).get("dram_bytes_per_launch"),
-                     "fp64": fp64_u128,
-                     "note": "N=1024: 49,152 algorithmic bytes per product; bound by the FP64 pipe "
-                             "(double-double arithmetic), see profiles/u128_product_n1024.md"},
-        "clocks": clocks, "gpu_launches": 2 * args.steps,
-    }))
+    entry = measure_u128(torch, cf, args.steps, args.warmup, local, world, full=True,
+                         cpu=not args.no_cpu_baseline and rank == 0, cpu_seconds=args.cpu_seconds)
+    if rank == 0:
+        print_line(entry, world)
 
 
 def run_product_sum(args):
@@ -789,53 +1283,20 @@ def run_product_sum(args):
 
 
 def run_serving(args):
-    """Poisson stream of (k+1)*l-product requests, N in 2^10..2^14, 8 GB of resident operands:
-    continuous batching vs the plain one-launch-per-step path, same seeded stream."""
+    """The Poisson request loop with the full set of variants and the capacity sweep."""
     torch, cf, rank, world, local = gpu_setup()
-    sizes = [10, 11, 12, 13, 14]
-    eng = cf.serving.ProductEngine(sizes)
-    t0 = time.perf_counter()
-    srv = cf.serving.Server(eng, sizes, operand_bytes=args.operand_gb << 30, seed=5 + rank)
-    setup_s = time.perf_counter() - t0
-    cfg = srv.config(rate=args.rate, duration_s=args.serve_seconds)
-    srv.run(srv.config(rate=args.rate, duration_s=0.05))  # warm-up
     if args.profile_case:  # for ncu: a short batched run only
+        eng = cf.serving.ProductEngine(SERVE_SIZES)
+        srv = cf.serving.Server(eng, SERVE_SIZES, operand_bytes=args.operand_gb << 30, seed=5 + rank)
+        srv.run(srv.config(rate=args.rate, duration_s=0.05))
         st = srv.run(srv.config(rate=args.rate, duration_s=0.1))
         print(json.dumps({"profile_case": "serving 0.1 s", "launches": st.get("launches")}))
         return
-    with ClockSampler(local) as clk:
-        t1 = time.time()
-        batched = srv.run(cfg)
-        clk.mark(t1, time.time())
-    # the same stream with every product on the engine (no clusters for N >= 8192)
-    no_cluster = srv.run(srv.config(rate=args.rate, duration_s=args.serve_seconds, cluster_log2N=32))
-    # the same stream with item records copied in and results copied out per launch
-    staged = srv.run(srv.config(rate=args.rate, duration_s=args.serve_seconds, staged_io=True))
-    # the same stream through the public submit / poll work queue (cfft_product_queue_*)
-    queued = srv.run(srv.config(rate=args.rate, duration_s=args.serve_seconds, via_queue=True))
-    # capacity: the continuous-batching loop at higher arrival rates (same request mix)
-    sweep = {}
-    for rate in (50000.0, 100000.0, 150000.0, 200000.0):
-        st = srv.run(srv.config(rate=rate, duration_s=0.5))
-        sweep["%d" % rate] = {k: st[k] for k in ("products_per_s", "p50_ms", "p99_ms", "max_ms", "launches",
-                                                 "mean_batch", "deferred_admissions") if k in st}
-    # the comparator last: it saturates and queues for seconds
-    plain = srv.run(srv.config(rate=args.rate, duration_s=args.serve_seconds, plain=True))
-    if rank != 0:
-        return
-    print(json.dumps({
-        "metric": "serving: products/s and p99 latency, Poisson %g req/s" % args.rate,
-        "value": batched["products_per_s"], "unit": "products/s", "n_gpus": world, "steps": 1,
-        "warmup": 1, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
-        "data": "synthetic (seeded Poisson stream, resident operands %d GiB)" % args.operand_gb,
-        "config": {"workload": "serving, (k+1)*l products per request, k in 1..2, l in 1..4, N in 2^10..2^14, "
-                               "digits b in 4..10 bits", "duration_s": args.serve_seconds,
-                   "resident_setup_s": setup_s},
-        "batched": batched, "batched_without_clusters": no_cluster, "batched_staged_io": staged, "batched_via_queue": queued, "plain": plain,
-        "capacity_sweep_req_per_s": sweep,
-        "p99_speedup_vs_plain": plain["p99_ms"] / batched["p99_ms"] if batched["p99_ms"] else None,
-        "clocks": clk.summary(), "gpu_launches": batched["launches"],
-    }))
+    entry = measure_serving(torch, cf, local, world, rate=args.rate, seconds=args.serve_seconds,
+                            operand_gb=args.operand_gb, full=True, cpu=not args.no_cpu_baseline and rank == 0,
+                            cpu_seconds=args.cpu_seconds, seed=5 + rank)
+    if rank == 0:
+        print_line(entry, world, data="synthetic (seeded Poisson stream, resident operands %d GiB)" % args.operand_gb)
 
 
 def run_u64_large(args):
@@ -965,6 +1426,9 @@ def main():
                     default="u64_product",
                     help="u64_product (default headline) or one of the other benchmark configurations")
     ap.add_argument("--mixed-items", type=int, default=100000)
+    ap.add_argument("--no-configs", action="store_true",
+                    help="headline only: skip the other benchmark configurations in the default line")
+    ap.add_argument("--cluster-size", type=int, default=None, help="--profile-case of the ordered workload: CTAs per transform")
     ap.add_argument("--tune-seconds", type=float, default=0.0005)
     args = ap.parse_args()
     if args.warmup < 3:

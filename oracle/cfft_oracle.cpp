@@ -1306,4 +1306,35 @@ int oracle_unordered_batch(int fwd, int base_algo, size_t n, size_t base_n, size
   return 0;
 }
 
+int oracle_f128_batch(int fwd, size_t n, size_t count, double* re0, double* re1, double* im0, double* im1,
+                      const double* t_re0, const double* t_re1, const double* t_im0, const double* t_im1,
+                      int nthreads) {
+  if (!is_pow2(n) || n < 2) return -1;
+  parallel_for(count, nthreads, [&](size_t b, size_t e) {
+    for (size_t i = b; i < e; ++i) {
+      const size_t o = i * n;
+      if (fwd)
+        f128_fwd(n, re0 + o, re1 + o, im0 + o, im1 + o, t_re0, t_re1, t_im0, t_im1);
+      else
+        f128_inv(n, re0 + o, re1 + o, im0 + o, im1 + o, t_re0, t_re1, t_im0, t_im1);
+    }
+  });
+  return 0;
+}
+
+int oracle_schoolbook_batch(int words, size_t N, size_t count, const uint64_t* a, const int64_t* b, uint64_t* out,
+                            int nthreads) {
+  if (!is_pow2(N) || (words != 1 && words != 2)) return -1;
+  int bad = 0;
+  parallel_for(count, nthreads, [&](size_t lo, size_t hi) {
+    for (size_t i = lo; i < hi; ++i) {
+      const int rc = words == 1
+                         ? oracle_negacyclic_u64_schoolbook(N, a + i * N, b + i * N, out + i * N)
+                         : oracle_negacyclic_u128_schoolbook(N, a + 2 * i * N, b + i * N, out + 2 * i * N);
+      if (rc) bad = 1;
+    }
+  });
+  return bad ? -1 : 0;
+}
+
 }  // extern "C"

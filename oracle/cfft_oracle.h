@@ -99,6 +99,13 @@ int oracle_ordered_batch(int fwd, int algo, size_t n, size_t count, double* bufs
                          const double* twiddles, int nthreads);
 int oracle_unordered_batch(int fwd, int base_algo, size_t n, size_t base_n, size_t count,
                            double* bufs, const double* tw, int nthreads);
+/* batched fft128 transforms: re0/re1/im0/im1 each hold count x n doubles (SoA per word) */
+int oracle_f128_batch(int fwd, size_t n, size_t count, double* re0, double* re1, double* im0, double* im1,
+                      const double* t_re0, const double* t_re1, const double* t_im0, const double* t_im1,
+                      int nthreads);
+/* exact schoolbook products over a batch (words = 1: u64, words = 2: u128 as lo/hi u64 pairs), threaded */
+int oracle_schoolbook_batch(int words, size_t N, size_t count, const uint64_t* a, const int64_t* b, uint64_t* out,
+                            int nthreads);
 
 #ifdef __cplusplus
 }

@@ -258,3 +258,37 @@ def stdrng_uniform01(seed, count):
 
 def round_mod64(x):
     return lib().oracle_round_mod64(float(x))
+
+
+# ---- in-place batch calls for the timed CPU baseline (no copies around the call) ----
+def ordered_batch_inplace(fwd, algo, flat, tw, nthreads=1):
+    """flat: (count, n) complex128, C-contiguous, transformed in place; tw: the init_wt table
+    of the direction (ordered_twiddles)."""
+    n = flat.shape[-1]
+    _ok(lib().oracle_ordered_batch(int(bool(fwd)), int(algo), S(n), S(flat.size // n), P(flat), P(tw), nthreads))
+
+
+def unordered_batch_inplace(fwd, base_algo, base_n, flat, tw, nthreads=1):
+    n = flat.shape[-1]
+    _ok(lib().oracle_unordered_batch(int(bool(fwd)), int(base_algo), S(n), S(base_n), S(flat.size // n), P(flat),
+                                     P(tw), nthreads))
+
+
+def f128_batch_inplace(fwd, bufs, t, nthreads=1):
+    """bufs: four (count, n) float64 arrays (re0, re1, im0, im1), transformed in place;
+    t: f128_twiddles(n)."""
+    n = bufs[0].shape[-1]
+    _ok(lib().oracle_f128_batch(int(bool(fwd)), S(n), S(bufs[0].size // n), *[P(x) for x in bufs],
+                                *[P(np.ascontiguousarray(x)) for x in t], nthreads))
+
+
+def schoolbook_batch(a, b, nthreads=0):
+    """Exact negacyclic products of a batch, threaded: a (count, N) uint64 (u64) or
+    (count, N, 2) uint64 (u128 as lo, hi); b (count, N) int64."""
+    a = np.ascontiguousarray(a, dtype=np.uint64)
+    b = np.ascontiguousarray(b, dtype=np.int64)
+    N = b.shape[-1]
+    words = 2 if a.ndim == 3 else 1
+    out = np.zeros_like(a)
+    _ok(lib().oracle_schoolbook_batch(words, S(N), S(b.size // N), P(a), P(b), P(out), nthreads))
+    return out

@@ -260,12 +260,20 @@ cfft_status cfft_product_engine_run(const cfft_product_engine* e, const cfft_pro
 //
 // Limits and sharing: the array holds 256 bytes of counter and 24 MiB of
 // workspace, and every GPU that loads this library keeps it until the process
-// exits.  Sizes whose per-CTA workspace does not fit one CTA per SM in 24 MiB
-// (N/2 > 8192, i.e. N > 16384 on GB300) are rejected with
-// CFFT_ERR_INVALID_SIZE.  All calls share the array: calls whose executions
-// overlap on the GPU (different streams, or several threads) race on it and
-// must be serialised by the caller.  The counter is cleared by every call; the
-// workspace needs no clearing (each product writes before it reads).
+// exits.  Under CUDA's lazy module loading the 24 MiB is committed when this
+// file's kernels are first loaded on a device, which happens at
+// cfft_product_engine_create.  Engines with a size above N = 16384 (128 KiB of
+// workspace per CTA) are rejected with CFFT_ERR_INVALID_SIZE, on every device.
+// The launch is capped at 24 MiB / per-CTA workspace CTAs (192 at N = 16384,
+// 384 at N = 8192); that cap holds for the whole launch, including the items
+// of an engine's smaller sizes, which then run on fewer CTAs than
+// cfft_product_engine_run would give them.  All calls share the array: calls
+// whose executions overlap on the GPU (different streams, or several threads)
+// race on it and must be serialised by the caller.  The counter is cleared by
+// every call; the workspace needs no clearing (each product writes before it
+// reads).  The looked-up device address is kept per device ordinal for the
+// life of the process; it does not survive cudaDeviceReset.
+constexpr int kStaticMaxLog2N = 14;
 constexpr size_t kStaticCounterBytes = 256;
 constexpr size_t kStaticWorkspaceBytes = size_t(24) << 20;
 static __device__ __align__(256) unsigned char g_engine_scratch[kStaticCounterBytes + kStaticWorkspaceBytes];
@@ -303,15 +311,14 @@ extern "C" cfft_status cfft_product_engine_run_static(const cfft_product_engine*
   int grid = (int)std::min<size_t>((size_t)e->grid, count);
   long ws_points = 0;
   if (e->ws_log2n) {
-    ws_points = 1L << e->ws_log2n;
-    const size_t per_cta = (size_t)ws_points * sizeof(double2);
-    const size_t fit = kStaticWorkspaceBytes / per_cta;
-    if (fit < (size_t)sm_count())
+    if (e->ws_log2n + 1 > kStaticMaxLog2N)
       return fail(CFFT_ERR_INVALID_SIZE,
                   "cfft_product_engine_run_static: N = 2^" + std::to_string(e->ws_log2n + 1) +
-                      " needs " + std::to_string(per_cta >> 10) + " KiB of workspace per CTA, more than the 24 MiB "
-                      "static scratch holds for one CTA per SM (largest N: 16384); use cfft_product_engine_run "
-                      "with a caller workspace");
+                      " is above the largest size (N = 16384) whose workspace the 24 MiB static scratch holds; "
+                      "use cfft_product_engine_run with a caller workspace");
+    ws_points = 1L << e->ws_log2n;
+    const size_t per_cta = (size_t)ws_points * sizeof(double2);
+    const size_t fit = kStaticWorkspaceBytes / per_cta;  // >= 192 for N <= 16384
     grid = (int)std::min<size_t>((size_t)grid, fit);
   }
   void* base = nullptr;

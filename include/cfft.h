@@ -352,10 +352,17 @@ cfft_status cfft_product_queue_wait(cfft_product_queue* queue, uint64_t ticket);
  * path -- code inside a framework whose own allocator has reserved the device
  * memory budget, or latency-critical loops where cudaMalloc/cudaFree would
  * synchronise the device.  The counter and the workspace come from a static
- * device array (256 B + 24 MiB, held on every GPU that loads the library until
- * exit) instead of caller buffers.  Limit: engines with N > 16384 are
- * rejected with CFFT_ERR_INVALID_SIZE.  The first call on a device looks up the
- * array's device address; make it before any stream capture.  All calls share
+ * device array (256 B + 24 MiB) instead of caller buffers.  Every GPU that
+ * loads the library holds that array until exit; under CUDA's lazy module
+ * loading it is committed at the first cfft_product_engine_create on a device,
+ * so a caller that hands the device budget to its own allocator creates its
+ * engines first (or leaves 24 MiB free).  Limit: engines with a size above
+ * N = 16384 are rejected with CFFT_ERR_INVALID_SIZE, on any device.  The
+ * launch runs on at most 24 MiB / (N_max / 2 x 16 B) CTAs (192 when the
+ * engine's largest N is 16384), and that cap applies to all items of the call,
+ * small N included.  The first call on a device looks up the array's device
+ * address; make it before any stream capture.  The address is kept for the
+ * life of the process and does not survive cudaDeviceReset.  All calls share
  * the array, so calls that overlap on the GPU race: serialise them.  Results
  * are bit-identical to cfft_product_engine_run. */
 cfft_status cfft_product_engine_run_static(const cfft_product_engine* engine, const cfft_product_item* items,
@@ -365,8 +372,9 @@ cfft_status cfft_product_engine_run_static(const cfft_product_engine* engine, co
  * A request is (k+1)*l products of one size N: signed b-bit digit polynomials
  * times device-resident Fourier operands (the TFHE external-product shape);
  * its content is a function of (seed, request id).  cfft_server_run serves a
- * seeded Poisson stream in real time: admission gated by the device output
- * ring (memory), everything admitted since the last launch batched into one
+ * seeded Poisson stream in real time: admission gated by the output ring and
+ * by the device's free memory read during the run (mem_reserve_bytes),
+ * everything admitted since the last launch batched into one
  * product-engine run, up to max_inflight runs overlapping on the device.  With
  * plain = 1 it serves the same stream one request at a time through the
  * unfused pipeline (one launch per step), the comparator. */

@@ -18,11 +18,10 @@ import pytest
 pytestmark = pytest.mark.gpu
 
 
-def _items(torch, cf, engine, sizes, rng):
+def _items(torch, cf, engine, sizes, rng, count=3):
     items, outs, keep = [], [], []
     for lN in sizes:
         N = 1 << lN
-        count = 3
         a = torch.from_numpy(rng.integers(0, 2 ** 64, (count, N), dtype=np.uint64).view(np.int64)).cuda()
         b = torch.from_numpy(rng.integers(-2 ** 7, 2 ** 7, (count, N))).cuda()
         bhat = torch.empty((count, N // 2), dtype=torch.complex128, device="cuda")
@@ -60,6 +59,34 @@ def test_no_alloc_entry_point_matches_regular_run(cuda):
             assert torch.equal(got, want)
 
 
+def test_no_alloc_entry_point_caps_its_grid_to_the_static_workspace(cuda):
+    """320 products of N = 16384 (128 KiB of workspace each) and 64 of N = 2048: more CTAs
+    than the 24 MiB array holds slices for (192), so the call runs on the capped grid, and
+    the small items of the same call share it."""
+    import concrete_fft as cf
+    torch = cuda
+    engine = cf.serving.ProductEngine([11, 14])
+    rng = np.random.default_rng(321)
+    d_big, n_big, outs_big, keep_big = _items(torch, cf, engine, [14], rng, count=320)
+    d_small, n_small, outs_small, keep_small = _items(torch, cf, engine, [11], rng, count=64)
+    d_items = torch.cat([d_big, d_small])
+    count = n_big + n_small
+    outs = outs_big + outs_small
+    stream = torch.cuda.current_stream().cuda_stream
+    counter = torch.zeros(4, dtype=torch.int32, device="cuda")
+    ws = torch.empty(engine.workspace_bytes(), dtype=torch.uint8, device="cuda")
+    engine.run(d_items, count, counter, ws, stream)
+    torch.cuda.synchronize()
+    ref = [o.clone() for o in outs]
+    for _ in range(2):
+        for o in outs:
+            o.zero_()
+        engine.run_static(d_items, count, stream)
+        torch.cuda.synchronize()
+        for got, want in zip(outs, ref):
+            assert torch.equal(got, want)
+
+
 def test_no_alloc_entry_point_rejects_sizes_beyond_its_limit(cuda):
     import concrete_fft as cf
     torch = cuda
@@ -68,4 +95,4 @@ def test_no_alloc_entry_point_rejects_sizes_beyond_its_limit(cuda):
     with pytest.raises(cf.CfftError) as err:
         engine.run_static(dummy, 1, torch.cuda.current_stream().cuda_stream)
     assert err.value.status == -1
-    assert "24 MiB" in str(err.value)
+    assert "24 MiB" in str(err.value) and "16384" in str(err.value)

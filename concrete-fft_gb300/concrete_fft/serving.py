@@ -106,14 +106,17 @@ class ServeConfig(ctypes.Structure):
     _fields_ = [("rate", ctypes.c_double), ("duration_s", ctypes.c_double), ("log2N_min", ctypes.c_uint32),
                 ("log2N_max", ctypes.c_uint32), ("k_max", ctypes.c_uint32), ("l_max", ctypes.c_uint32),
                 ("plain", ctypes.c_uint32), ("max_inflight", ctypes.c_uint32), ("record_every", ctypes.c_uint32),
-                ("cluster_log2N", ctypes.c_uint32), ("staged_io", ctypes.c_uint32), ("via_queue", ctypes.c_uint32)]
+                ("cluster_log2N", ctypes.c_uint32), ("staged_io", ctypes.c_uint32), ("via_queue", ctypes.c_uint32),
+                ("mem_reserve_bytes", ctypes.c_uint64), ("mem_free_override", ctypes.c_uint64)]
 
 
 class ServeStats(ctypes.Structure):
     _fields_ = [("requests", ctypes.c_uint64), ("products", ctypes.c_uint64), ("launches", ctypes.c_uint64),
                 ("deferred_admissions", ctypes.c_uint64), ("products_per_s", ctypes.c_double),
                 ("p50_ms", ctypes.c_double), ("p99_ms", ctypes.c_double), ("max_ms", ctypes.c_double),
-                ("mean_batch", ctypes.c_double), ("span_s", ctypes.c_double)]
+                ("mean_batch", ctypes.c_double), ("span_s", ctypes.c_double),
+                ("memory_deferrals", ctypes.c_uint64), ("input_bytes", ctypes.c_uint64),
+                ("output_bytes", ctypes.c_uint64), ("min_memory_budget_mib", ctypes.c_double)]
 
     def as_dict(self):
         return {f: getattr(self, f) for f, _ in self._fields_}
@@ -138,9 +141,13 @@ class Server:
 
     @staticmethod
     def config(rate, duration_s, log2N_min=10, log2N_max=14, k_max=2, l_max=4, plain=False, max_inflight=3,
-               record_every=0, cluster_log2N=0, staged_io=False, via_queue=False):
+               record_every=0, cluster_log2N=0, staged_io=False, via_queue=False, mem_reserve_bytes=0,
+               mem_free_override=0):
+        """mem_reserve_bytes: device memory the admission gate leaves free; mem_free_override: a
+        stand-in for the device's free bytes (tests fake a small device with it)."""
         return ServeConfig(rate, duration_s, log2N_min, log2N_max, k_max, l_max, int(plain), max_inflight,
-                           record_every, cluster_log2N, int(staged_io), int(via_queue))
+                           record_every, cluster_log2N, int(staged_io), int(via_queue), int(mem_reserve_bytes),
+                           int(mem_free_override))
 
     def run(self, cfg):
         st = ServeStats()

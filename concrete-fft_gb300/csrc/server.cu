@@ -8,7 +8,8 @@
 // (seed, request id) and can be recomputed alone for checking.
 //
 // Batched mode: every loop iteration admits the requests that have arrived
-// while the device output ring has room (the memory gate), and as soon as one
+// while the device memory gate (the output bytes in flight against the
+// device's free memory, read live) and the output ring allow, and as soon as one
 // of `max_inflight` launch slots is free, launches everything admitted since
 // the previous launch as one product-engine run on that slot's stream,
 // followed by the copy of the results into a pinned host ring.  Products of
@@ -180,6 +181,35 @@ struct RingAlloc {
   }
 };
 
+// Device memory gate: admitted, unfinished requests hold their output bytes,
+// and their sum stays within the device's free memory less a reserve.  Free
+// memory is read with cudaMemGetInfo at most once per millisecond, so memory
+// that other users of the device take or release during the run moves the
+// gate; mem_free_override replaces that reading (tests fake a small device).
+// When nothing is in flight a request is admitted whatever the budget, so a
+// budget smaller than one request slows the stream but cannot stall it.
+struct MemGate {
+  uint64_t reserve, override_free;
+  double next_refresh = -1;
+  uint64_t budget = 0;
+  uint64_t inflight = 0;
+  uint64_t min_budget = ~uint64_t(0);
+  MemGate(uint64_t r, uint64_t o) : reserve(r), override_free(o) {}
+  void refresh(double now) {
+    if (now < next_refresh) return;
+    next_refresh = now + 1e-3;
+    size_t free_b = 0, total_b = 0;
+    if (override_free) {
+      free_b = override_free;
+    } else if (cudaMemGetInfo(&free_b, &total_b) != cudaSuccess) {
+      return;  // keep the previous budget
+    }
+    budget = free_b > reserve ? free_b - reserve : 0;
+    min_budget = std::min(min_budget, budget);
+  }
+  bool admits(uint64_t bytes) const { return inflight == 0 || inflight + bytes <= budget; }
+};
+
 void free_server(cfft_server* s) {
   for (auto& p : s->pools) {
     if (p.digits) cudaFree(p.digits);
@@ -345,7 +375,8 @@ cfft_status cfft_server_run(cfft_server* s, const cfft_serve_config* cfg, cfft_s
   std::deque<size_t> waiting;
   std::vector<size_t> batch;
   std::vector<cfft_product_item> items;
-  uint64_t deferred = 0, launches = 0;
+  uint64_t deferred = 0, launches = 0, mem_deferred = 0;
+  MemGate gate(c.mem_reserve_bytes, c.mem_free_override);
   const auto t0 = std::chrono::steady_clock::now();
   const uint32_t nslots = std::max<uint32_t>(1, std::min<uint32_t>(c.max_inflight ? c.max_inflight : kSlots, kSlots));
   // products of at least this size run one per thread-block cluster (only sizes whose
@@ -416,13 +447,19 @@ cfft_status cfft_server_run(cfft_server* s, const cfft_serve_config* cfg, cfft_s
     for (;;) {
       const double now = now_s(t0);
       while (next < reqs.size() && reqs[next].d.arrival <= now) waiting.push_back(next++);
+      if (!waiting.empty()) gate.refresh(now);
       while (!waiting.empty()) {
         Live& r = reqs[waiting.front()];
         r.ring_bytes = (uint64_t)r.d.nprod << (r.d.log2N + 3);
+        if (!gate.admits(r.ring_bytes)) {
+          ++mem_deferred;
+          break;
+        }
         if (!ring.alloc(r.ring_bytes, &r.ring_off, &r.ring_end)) {
           ++deferred;
           break;
         }
+        gate.inflight += r.ring_bytes;
         its.resize(r.d.nprod);
         fill_items(s, r.d, s->h_ring_dev + r.ring_off, its.data());
         st = cfft_product_queue_submit(q, its.data(), its.size(), &r.ticket);
@@ -443,6 +480,7 @@ cfft_status cfft_server_run(cfft_server* s, const cfft_serve_config* cfg, cfft_s
           continue;
         }
         reqs[inflight[k]].t_done = now_s(t0);
+        gate.inflight -= reqs[inflight[k]].ring_bytes;
         record(inflight[k]);
         ++done_count;
         inflight[k] = inflight.back();
@@ -467,14 +505,20 @@ cfft_status cfft_server_run(cfft_server* s, const cfft_serve_config* cfg, cfft_s
     for (;;) {
       const double now = now_s(t0);
       while (next < reqs.size() && reqs[next].d.arrival <= now) waiting.push_back(next++);
-      // admission: output ring space is the memory gate
+      // admission: the device memory gate, then output ring space
+      if (!waiting.empty()) gate.refresh(now);
       while (!waiting.empty()) {
         Live& r = reqs[waiting.front()];
         r.ring_bytes = (uint64_t)r.d.nprod << (r.d.log2N + 3);
+        if (!gate.admits(r.ring_bytes)) {
+          ++mem_deferred;
+          break;
+        }
         if (!ring.alloc(r.ring_bytes, &r.ring_off, &r.ring_end)) {
           ++deferred;
           break;
         }
+        gate.inflight += r.ring_bytes;
         ring_order.push_back(waiting.front());
         batch.push_back(waiting.front());
         waiting.pop_front();
@@ -572,6 +616,7 @@ cfft_status cfft_server_run(cfft_server* s, const cfft_serve_config* cfg, cfft_s
         const double t = now_s(t0);
         for (size_t ri : sl.reqs) {
           reqs[ri].t_done = t;
+          gate.inflight -= reqs[ri].ring_bytes;
           record(ri);
           ++done_count;
         }
@@ -589,12 +634,13 @@ cfft_status cfft_server_run(cfft_server* s, const cfft_serve_config* cfg, cfft_s
   // statistics
   std::vector<double> lat;
   double first = 1e30, last = 0;
-  uint64_t prods = 0;
+  uint64_t prods = 0, out_bytes = 0;
   for (const auto& r : reqs) {
     lat.push_back(r.t_done - r.d.arrival);
     first = std::min(first, r.d.arrival);
     last = std::max(last, r.t_done);
     prods += r.d.nprod;
+    out_bytes += (uint64_t)r.d.nprod << (r.d.log2N + 3);
   }
   std::sort(lat.begin(), lat.end());
   auto pct = [&](double q) { return lat.empty() ? 0.0 : lat[std::min(lat.size() - 1, (size_t)(q * lat.size()))]; };
@@ -607,7 +653,11 @@ cfft_status cfft_server_run(cfft_server* s, const cfft_serve_config* cfg, cfft_s
   stats->p99_ms = pct(0.99) * 1e3;
   stats->max_ms = lat.empty() ? 0 : lat.back() * 1e3;
   stats->mean_batch = launches && !c.plain ? stats->mean_batch / launches : 1.0;
-  stats->deferred_admissions = deferred;
+  stats->deferred_admissions = deferred + mem_deferred;
+  stats->memory_deferrals = mem_deferred;
+  stats->input_bytes = prods * sizeof(cfft_product_item);
+  stats->output_bytes = out_bytes;
+  stats->min_memory_budget_mib = gate.min_budget == ~uint64_t(0) ? -1.0 : gate.min_budget / 1048576.0;
   (void)ring;
   s->last_latency = lat;
   return CFFT_OK;

@@ -395,10 +395,20 @@ typedef struct cfft_serve_config {
                             in and results copied out per launch */
   uint32_t via_queue;    /* batched mode through the public work queue (cfft_product_queue_*):
                             each request submitted on arrival, its ticket polled */
+  uint64_t mem_reserve_bytes; /* batched mode, device memory gate: the output bytes of admitted,
+                                 unfinished requests stay within the device's free memory less
+                                 this reserve, read with cudaMemGetInfo at most once per
+                                 millisecond during the run (a request is always admitted when
+                                 nothing is in flight, so the stream makes progress) */
+  uint64_t mem_free_override; /* nonzero: stands in for cudaMemGetInfo's free bytes (tests) */
 } cfft_serve_config;
 typedef struct cfft_serve_stats {
   uint64_t requests, products, launches, deferred_admissions;
   double products_per_s, p50_ms, p99_ms, max_ms, mean_batch, span_s;
+  uint64_t memory_deferrals; /* admissions held back by the device memory gate (the others by ring space) */
+  uint64_t input_bytes;      /* item records the launches read (32 B per product) */
+  uint64_t output_bytes;     /* results delivered to host memory */
+  double min_memory_budget_mib; /* smallest device memory budget the gate saw */
 } cfft_serve_stats;
 typedef struct cfft_server cfft_server;
 /* Resident state: digit pools and Fourier operands (operand_bytes in total) for

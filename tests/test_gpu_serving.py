@@ -124,6 +124,32 @@ def test_server_memory_gate(cuda, engine):
         srv.run(srv.config(rate=100, duration_s=0.01, log2N_min=12, log2N_max=14))  # sizes without pools
 
 
+@pytest.mark.parametrize("staged_io,via_queue", [(False, False), (True, False), (False, True)])
+def test_server_device_memory_gate(cuda, engine, staged_io, via_queue):
+    """Admission is gated on the device's free memory, read during the run: with a faked free
+    memory of 1.5 MiB (the output of the largest request, 12 products at N = 2^14) requests are
+    held back by the gate, every request is still served, and every recorded result equals the
+    request run alone.  A generous reserve against the real free
+    memory defers as well; none does with the real reading and no reserve."""
+    import concrete_fft as cf
+    srv = cf.serving.Server(engine, SIZES, operand_bytes=64 << 20, ring_bytes=256 << 20, seed=4)
+    cfg = srv.config(rate=40000, duration_s=0.03, record_every=1, staged_io=staged_io, via_queue=via_queue,
+                     mem_free_override=3 << 19)
+    stats = srv.run(cfg)
+    assert stats["memory_deferrals"] > 0
+    assert 0 < stats["min_memory_budget_mib"] <= 1.5
+    ids = srv.recorded_ids()
+    assert len(ids) == stats["requests"] > 100
+    assert stats["output_bytes"] == sum(srv.shape(cfg, int(r))[1] << (srv.shape(cfg, int(r))[0] + 3) for r in ids)
+    for rid in ids[:: max(1, len(ids) // 30)]:
+        assert np.array_equal(srv.recorded_output(cfg, rid), srv.run_alone(cfg, rid)), rid
+    free = cuda.cuda.mem_get_info()[0]
+    tight = srv.run(srv.config(rate=40000, duration_s=0.01, mem_reserve_bytes=free - (1 << 20)))
+    assert tight["memory_deferrals"] > 0 and tight["min_memory_budget_mib"] < 8
+    loose = srv.run(srv.config(rate=40000, duration_s=0.01))
+    assert loose["memory_deferrals"] == 0 and loose["min_memory_budget_mib"] > 1024
+
+
 def _queue_requests(torch, engine, rng, nreq, host_out=False):
     """nreq requests of 1..6 products of random configured sizes, each with its own
     operand; returns (items per request, buffers to keep, expected results)."""

@@ -95,6 +95,9 @@ _SIGS = [
     ("cfft_f128_init_negacyclic_twiddles", c_int, [c_size, vp, vp, vp, vp]),
     ("cfft_f128_negacyclic_fwd", c_int, [c_size, c_size, vp, vp, vp, vp, vp, vp, vp, vp, vp]),
     ("cfft_f128_negacyclic_inv", c_int, [c_size, c_size, vp, vp, vp, vp, vp, vp, vp, vp, vp]),
+    ("cfft_f128_negacyclic_fwd_host", c_int, [c_size, c_size, vp, vp, vp, vp, vp, vp, vp, vp]),
+    ("cfft_f128_negacyclic_inv_host", c_int, [c_size, c_size, vp, vp, vp, vp, vp, vp, vp, vp]),
+    ("cfft_f128_sincospi", c_int, [c_dbl, c_dbl, vp, vp]),
     ("cfft_u64_product_plan_create", c_int, [c_size, c_int, c_size, pp]),
     ("cfft_u64_product_plan_create_measure", c_int, [c_size, c_dbl, pp]),
     ("cfft_u64_product_plan_destroy", None, [vp]),

@@ -67,24 +67,39 @@ def init_negacyclic_twiddles(twid_re0, twid_re1, twid_im0, twid_im1):
 
 
 def _raw(data, twid, fwd):
+    on_device = [B.is_device(a) for a in (*data, *twid)]
+    if any(on_device) and not all(on_device):
+        raise TypeError("negacyclic_fwd_fft/inv_fft: all eight arrays on the device, or all in host memory")
     for a in (*data, *twid):
         B.check_dtype(a, ("float64",))
-        if not B.is_device(a):
-            raise TypeError("negacyclic_fwd_fft/inv_fft take CUDA tensors")
-    n = twid[0].numel()
+    n = B.points(twid[0], 8)
     batch = B.batch_of(data[0], n, 8)
-    if any(B.batch_of(d, n, 8) != batch for d in data) or any(t.numel() != n for t in twid):
+    if any(B.batch_of(d, n, 8) != batch for d in data) or any(B.points(t, 8) != n for t in twid):
         raise ValueError("data arrays must hold the same whole number of transforms of the twiddles' length")
     lib = load()
-    fn = lib.cfft_f128_negacyclic_fwd if fwd else lib.cfft_f128_negacyclic_inv
-    check(fn(n, batch, *[B.ptr(d) for d in data], *[B.ptr(t) for t in twid], B.stream_of(data[0])))
+    if all(on_device):
+        fn = lib.cfft_f128_negacyclic_fwd if fwd else lib.cfft_f128_negacyclic_inv
+        check(fn(n, batch, *[B.ptr(d) for d in data], *[B.ptr(t) for t in twid], B.stream_of(data[0])))
+    else:  # the reference's slice form: host arrays, transformed in place
+        fn = lib.cfft_f128_negacyclic_fwd_host if fwd else lib.cfft_f128_negacyclic_inv_host
+        check(fn(n, batch, *[B.ptr(d) for d in data], *[B.ptr(t) for t in twid]))
 
 
 def negacyclic_fwd_fft(data_re0, data_re1, data_im0, data_im1, twid_re0, twid_re1, twid_im0, twid_im1):
-    """src/fft128/mod.rs:1041-1071 on device tensors (batched over whole multiples of n)."""
+    """src/fft128/mod.rs:1041-1071, batched over whole multiples of n: device tensors (on their
+    stream) or host arrays (the reference's slices; returns when done)."""
     _raw((data_re0, data_re1, data_im0, data_im1), (twid_re0, twid_re1, twid_im0, twid_im1), True)
 
 
 def negacyclic_inv_fft(data_re0, data_re1, data_im0, data_im1, twid_re0, twid_re1, twid_im0, twid_im1):
-    """src/fft128/mod.rs:1073-1104 on device tensors (unnormalised)."""
+    """src/fft128/mod.rs:1073-1104 (unnormalised), device tensors or host arrays."""
     _raw((data_re0, data_re1, data_im0, data_im1), (twid_re0, twid_re1, twid_im0, twid_im1), False)
+
+
+def sincospi(x_hi, x_lo=0.0):
+    """f128::sincospi (src/fft128/f128_ops.rs:534-575) on the host: ((sin_hi, sin_lo),
+    (cos_hi, cos_lo)) of pi * (x_hi + x_lo), for inputs in [-1, 1]."""
+    s = (ctypes.c_double * 2)()
+    c = (ctypes.c_double * 2)()
+    check(load().cfft_f128_sincospi(float(x_hi), float(x_lo), s, c))
+    return (s[0], s[1]), (c[0], c[1])

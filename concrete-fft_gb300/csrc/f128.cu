@@ -513,6 +513,46 @@ cfft_status cfft_f128_negacyclic_inv(size_t n, size_t batch, double* re0, double
   return raw_f128(n, batch, re0, re1, im0, im1, twid_re0, twid_re1, twid_im0, twid_im1, false, stream);
 }
 
+// The same free functions on host slices (the reference's signatures take
+// &mut [f64] / &[f64]): data and twiddles are staged through device memory.
+static cfft_status raw_f128_host(size_t n, size_t batch, double* re0, double* re1, double* im0, double* im1,
+                                 const double* t0, const double* t1, const double* t2, const double* t3, bool fwd) {
+  if (!re0 || !re1 || !im0 || !im1 || !t0 || !t1 || !t2 || !t3) return fail(CFFT_ERR_INVALID_ARGUMENT, "null argument");
+  if (!is_pow2(n) || n < 2 || ilog2(n) > kF128MaxLog2)
+    return fail(CFFT_ERR_INVALID_SIZE, "n must be a power of two in [2, 2^24]");
+  if (batch == 0) return CFFT_OK;
+  const size_t bytes = batch * n * sizeof(double), tw_bytes = n * sizeof(double);
+  void* d;
+  cudaStream_t s;
+  cfft_status st = host_staging(4 * bytes + 4 * tw_bytes, &d, &s);
+  if (st != CFFT_OK) return st;
+  double* hh[4] = {re0, re1, im0, im1};
+  const double* th[4] = {t0, t1, t2, t3};
+  double* dd[4];
+  double* dt[4];
+  for (int i = 0; i < 4; ++i) {
+    dd[i] = (double*)((char*)d + i * bytes);
+    dt[i] = (double*)((char*)d + 4 * bytes + i * tw_bytes);
+    CFFT_CUDA_TRY(cudaMemcpyAsync(dd[i], hh[i], bytes, cudaMemcpyHostToDevice, s));
+    CFFT_CUDA_TRY(cudaMemcpyAsync(dt[i], th[i], tw_bytes, cudaMemcpyHostToDevice, s));
+  }
+  st = run_f128_tw(n, F128Tw{dt[0], dt[1], dt[2], dt[3]}, dd[0], dd[1], dd[2], dd[3], batch, fwd, s);
+  if (st != CFFT_OK) return st;
+  for (int i = 0; i < 4; ++i) CFFT_CUDA_TRY(cudaMemcpyAsync(hh[i], dd[i], bytes, cudaMemcpyDeviceToHost, s));
+  CFFT_CUDA_TRY(cudaStreamSynchronize(s));
+  return CFFT_OK;
+}
+cfft_status cfft_f128_negacyclic_fwd_host(size_t n, size_t batch, double* re0, double* re1, double* im0, double* im1,
+                                          const double* twid_re0, const double* twid_re1, const double* twid_im0,
+                                          const double* twid_im1) {
+  return raw_f128_host(n, batch, re0, re1, im0, im1, twid_re0, twid_re1, twid_im0, twid_im1, true);
+}
+cfft_status cfft_f128_negacyclic_inv_host(size_t n, size_t batch, double* re0, double* re1, double* im0, double* im1,
+                                          const double* twid_re0, const double* twid_re1, const double* twid_im0,
+                                          const double* twid_im1) {
+  return raw_f128_host(n, batch, re0, re1, im0, im1, twid_re0, twid_re1, twid_im0, twid_im1, false);
+}
+
 cfft_status cfft_u128_product_plan_create(size_t N, cfft_u128_product_plan** out) {
   if (!out) return fail(CFFT_ERR_INVALID_ARGUMENT, "null output pointer");
   *out = nullptr;

@@ -303,6 +303,23 @@ void f128_twiddles(size_t n, double* re0, double* re1, double* im0, double* im1)
   });
 }
 
+// ---------------------------------------------------------------- f128::sincospi on the host
+// src/fft128/f128_ops.rs:534-575: panics for inputs above 1 or below -1 in
+// f128's lexicographic order (NaN compares as unordered and goes through).
+extern "C" cfft_status cfft_f128_sincospi(double x_hi, double x_lo, double* sin_out, double* cos_out) {
+  if (!sin_out || !cos_out) return fail_status(CFFT_ERR_INVALID_ARGUMENT, "null argument");
+  const bool above = x_hi > 1.0 || (x_hi == 1.0 && x_lo > 0.0);
+  const bool below = x_hi < -1.0 || (x_hi == -1.0 && x_lo < 0.0);
+  if (above || below) return fail_status(CFFT_ERR_INVALID_ARGUMENT, "f128::sincospi: input outside [-1, 1]");
+  f128 s, c;
+  f128_sincospi(f128{x_hi, x_lo}, &s, &c);
+  sin_out[0] = s.hi;
+  sin_out[1] = s.lo;
+  cos_out[0] = c.hi;
+  cos_out[1] = c.lo;
+  return CFFT_OK;
+}
+
 // ---------------------------------------------------------------- errors
 static std::mutex g_err_mu;
 static std::string g_err;

@@ -223,6 +223,19 @@ cfft_status cfft_f128_negacyclic_fwd(size_t n, size_t batch, double* re0, double
 cfft_status cfft_f128_negacyclic_inv(size_t n, size_t batch, double* re0, double* re1, double* im0, double* im1,
                                      const double* twid_re0, const double* twid_re1, const double* twid_im0,
                                      const double* twid_im1, void* stream);
+/* The same on HOST arrays, the reference's slice signatures (staged through
+ * device memory; returns when the result is back in host memory). */
+cfft_status cfft_f128_negacyclic_fwd_host(size_t n, size_t batch, double* re0, double* re1, double* im0, double* im1,
+                                          const double* twid_re0, const double* twid_re1, const double* twid_im0,
+                                          const double* twid_im1);
+cfft_status cfft_f128_negacyclic_inv_host(size_t n, size_t batch, double* re0, double* re1, double* im0, double* im1,
+                                          const double* twid_re0, const double* twid_re1, const double* twid_im0,
+                                          const double* twid_im1);
+/* f128::sincospi -- src/fft128/f128_ops.rs:534-575, on the host: sin(pi x) and
+ * cos(pi x) of the double-double x = x_hi + x_lo as (hi, lo) pairs, bit-identical
+ * to the crate.  Inputs above 1 or below -1 (f128's lexicographic order) give
+ * CFFT_ERR_INVALID_ARGUMENT where the crate panics. */
+cfft_status cfft_f128_sincospi(double x_hi, double x_lo, double* sin_out2, double* cos_out2);
 
 /* ================================================ negacyclic products ====
  * The reference's caller (TFHE-rs) builds polynomial products mod X^N + 1 on

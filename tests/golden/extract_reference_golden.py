@@ -1,8 +1,9 @@
 """Build the golden fixtures in tests/golden/ from the reference crate's own tests.
 
-Run in the development container, where the reference sources are mounted:
+Run it where the reference crate's sources are checked out, giving their root
+directory as the argument or in CFFT_REFERENCE_ROOT:
 
-    python tests/golden/extract_reference_golden.py /root/reference
+    python tests/golden/extract_reference_golden.py <path to concrete-fft v0.5.1>
 
 It reads the reference's Rust test sources as text (nothing is compiled or run)
 and writes:
@@ -112,4 +113,7 @@ def main(ref_root):
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    root = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("CFFT_REFERENCE_ROOT")
+    if not root:
+        sys.exit("usage: extract_reference_golden.py <reference crate root> (or set CFFT_REFERENCE_ROOT)")
+    main(root)

@@ -23,6 +23,30 @@ def test_every_declared_symbol_is_exported(cfft_lib):
         assert hasattr(cfft_lib, name), name
 
 
+def rust_ffi_functions():
+    """The `extern "C"` functions the Rust drop-in crate declares (concrete-fft_gb300/rust)."""
+    txt = open(os.path.join(ROOT, "concrete-fft_gb300", "rust", "src", "ffi.rs")).read()
+    block = txt[txt.index('extern "C" {'):]
+    block = block[:block.index("\n}\n")]
+    return sorted(set(re.findall(r"pub fn (cfft_\w+)\s*\(", block)))
+
+
+def test_rust_crate_binds_only_declared_exported_symbols(cfft_lib):
+    """Every function of the Rust crate's FFI module is declared in include/*.h and
+    exported by the library; the crate wraps every entry point of the reference's API."""
+    names = rust_ffi_functions()
+    declared = set(declared_functions())
+    assert len(names) >= 50
+    for name in names:
+        assert name in declared, name
+        assert hasattr(cfft_lib, name), name
+    for needed in ("cfft_ordered_plan_create_measure", "cfft_unordered_fwd_monomial_host",
+                   "cfft_unordered_to_standard_host", "cfft_unordered_from_standard_host", "cfft_f128_fwd_host",
+                   "cfft_f128_init_negacyclic_twiddles", "cfft_f128_negacyclic_fwd_host",
+                   "cfft_f128_negacyclic_inv_host", "cfft_f128_sincospi"):
+        assert needed in names, needed
+
+
 def test_python_signatures_cover_the_header(cfft_lib):
     import concrete_fft
     assert sorted(concrete_fft.EXPORTED) == declared_functions()
@@ -120,6 +144,26 @@ def test_f128_init_negacyclic_twiddles_matches_oracle(cfft_lib, oracle):
             assert t[k][0] == 7.0
             assert np.array_equal(t[k][1:].view(np.uint64), want[k][1:].view(np.uint64)), (n, k)
     assert cfft_lib.cfft_f128_init_negacyclic_twiddles(24, *[ctypes.c_void_p(t[0].ctypes.data)] * 4) == -1
+
+
+def test_f128_sincospi_entry_point_matches_oracle(cfft_lib, oracle):
+    """f128::sincospi through the C ABI is host code: bit-identical to the oracle's restatement
+    of src/fft128/f128_ops.rs:534-575, and inputs outside [-1, 1] are refused (the crate
+    panics there)."""
+    import numpy as np
+    import concrete_fft as cf
+    rng = np.random.default_rng(21)
+    xs = list(rng.uniform(-1, 1, 200)) + [0.0, 0.5, -0.5, 1.0, -1.0, 0.25, 1 / 16, -3 / 16]
+    for x in xs:
+        lo = -x * rng.uniform(0, 1) * 2.0 ** -54
+        got = cf.fft128.sincospi(x, lo)
+        want = oracle.f128_sincospi((x, lo))
+        assert np.array_equal(np.array(got).view(np.uint64), np.array(want).view(np.uint64)), (x, lo)
+    s = (ctypes.c_double * 2)()
+    c = (ctypes.c_double * 2)()
+    assert cfft_lib.cfft_f128_sincospi(1.0, 1e-30, s, c) == -2
+    assert cfft_lib.cfft_f128_sincospi(-1.5, 0.0, s, c) == -2
+    assert cfft_lib.cfft_f128_sincospi(1.0, 0.0, s, c) == 0
 
 
 def test_missing_library_fails_loudly(tmp_path):

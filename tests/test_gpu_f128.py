@@ -99,9 +99,17 @@ def test_f128_raw_negacyclic_functions(cuda, oracle, n):
     for k in range(4):
         assert np.array_equal(d[k].cpu().numpy().view(np.uint64), want[k].view(np.uint64)), (n, k)
     cf.fft128.negacyclic_inv_fft(*d, *dtw)
-    want = oracle.f128_inv(*want)
+    want_i = oracle.f128_inv(*want)
     for k in range(4):
-        assert np.array_equal(d[k].cpu().numpy().view(np.uint64), want[k].view(np.uint64)), (n, k)
+        assert np.array_equal(d[k].cpu().numpy().view(np.uint64), want_i[k].view(np.uint64)), (n, k)
+    # the reference's slice form: host arrays in place, same bits
+    h = [np.ascontiguousarray(x).copy() for x in data]
+    cf.fft128.negacyclic_fwd_fft(*h, *tw)
+    for k in range(4):
+        assert np.array_equal(h[k].view(np.uint64), want[k].view(np.uint64)), (n, k)
+    cf.fft128.negacyclic_inv_fft(*h, *tw)
+    for k in range(4):
+        assert np.array_equal(h[k].view(np.uint64), want_i[k].view(np.uint64)), (n, k)
 
 
 def test_f128_invalid_size(cuda):

@@ -783,7 +783,28 @@ def ordered_sweeps(torch, cf, plan, d, one, step1, steps, warmup, local, world, 
                 ms_b, _ = timed(torch, step_b, max(10, steps // 4), warmup, local, world)
                 row["auto" if ctas == 0 else ctas] = round(ms_b * 1e3 / max(10, steps // 4), 2)
             sweep[aname][batch] = row
+    # the same at batch 256 without spreading one-wave grids over every SM (cfft_diag_set_spread)
+    lib = cf.load()
+    no_spread = {}
+    lib.cfft_diag_set_spread(0)
+    try:
+        for aname in ("Dit4", "Dif4"):
+            sp = cf.ordered.Plan(1024, cf.ordered.Method.UserProvided(cf.FftAlgo[aname]))
+            sub = d[:256].clone()
+
+            def step_b():
+                sp.fwd(sub)
+                sp.inv(sub)
+            row = {}
+            for ctas in (0, 1, 2, 4, 8):
+                sp.set_cluster_size(ctas)
+                ms_b, _ = timed(torch, step_b, max(10, steps // 4), warmup, local, world)
+                row["auto" if ctas == 0 else ctas] = round(ms_b * 1e3 / max(10, steps // 4), 2)
+            no_spread[aname] = row
+    finally:
+        lib.cfft_diag_set_spread(1)
     return {"batch1_us_per_fwd_inv_graph_replay": ms1g * 1e3 / steps,
+            "batch256_us_per_fwd_inv_without_spread": no_spread,
             "unordered_batch1_us_per_fwd_inv_by_n": large,
             "us_per_fwd_inv_by_batch_and_ctas_per_transform": sweep}
 
@@ -1236,13 +1257,25 @@ def run_ordered(args):
 def run_u128(args):
     """u128 negacyclic products N = 1024 and 4096 and the fft128 plan, as its own JSON line."""
     torch, cf, rank, world, local = gpu_setup()
-    if args.profile_case:  # for ncu: four forward calls of the fft128 plan, n = 512, batch 4096
+    if args.profile_case:  # for ncu: four forward calls of the fft128 plan (n = 512, batch 4096),
+        # then two launches of 2048 u128 products at N = 1024 (the timed shape)
+        import numpy as np
         fp = cf.fft128.Plan(512)
         bufs = [torch.rand((4096, 512), dtype=torch.float64, device="cuda") for _ in range(4)]
         for _ in range(4):
             fp.fwd(*bufs)
+        N, count = 1024, 2048
+        plan = cf.product.U128ProductPlan(N)
+        rng = np.random.default_rng(4)
+        a = torch.from_numpy(rng.integers(0, 2 ** 64, (count, N, 2), dtype=np.uint64).view(np.int64)).cuda()
+        b = torch.from_numpy(rng.integers(-2 ** 15, 2 ** 15, (count, N))).cuda()
+        bhat = torch.empty((count, 4, N // 2), dtype=torch.float64, device="cuda")
+        plan.prepare_operand(b, bhat)
+        out = torch.empty_like(a)
+        for _ in range(2):
+            plan.product(a, bhat, out)
         torch.cuda.synchronize()
-        print(json.dumps({"profile_case": "fft128 plan n=512 batch 4096 forward"}))
+        print(json.dumps({"profile_case": "fft128 plan n=512 batch 4096 forward x4; u128 products N=1024 x2048 x2"}))
         return
     entry = measure_u128(torch, cf, args.steps, args.warmup, local, world, full=True,
                          cpu=not args.no_cpu_baseline and rank == 0, cpu_seconds=args.cpu_seconds)
@@ -1263,6 +1296,12 @@ def run_product_sum(args):
     bhat = torch.empty((groups, T, N // 2), dtype=torch.complex128, device="cuda")
     plan.prepare_operand(b, bhat)
     out = torch.empty((groups, N), dtype=torch.int64, device="cuda")
+    if args.profile_case:  # for ncu: two launches of the timed shape
+        for _ in range(2):
+            plan.product_sum(a, bhat, out)
+        torch.cuda.synchronize()
+        print(json.dumps({"profile_case": "product_sum 1024 groups x 8 terms, N=2048, x2"}))
+        return
     ms, clocks = timed(torch, lambda: plan.product_sum(a, bhat, out), args.steps, args.warmup, local, world)
     per = ms * 1e-3 / args.steps
     n = N // 2
@@ -1363,6 +1402,12 @@ def run_serde(args):
     plan = cf.unordered.Plan(n, cf.unordered.Method.UserProvided(2, base))
     src = torch.randn(batch, n, dtype=torch.complex128, device="cuda")
     dst = torch.empty_like(src)
+    if args.profile_case:  # for ncu: two to_standard calls of the batch
+        for _ in range(2):
+            plan.to_standard(src, dst)
+        torch.cuda.synchronize()
+        print(json.dumps({"profile_case": "to_standard %d x 1024 points, base 32, x2" % batch}))
+        return
     ms_to, clocks = timed(torch, lambda: plan.to_standard(src, dst), args.steps, args.warmup, local, world)
     ms_from, _ = timed(torch, lambda: plan.from_standard(dst, src), args.steps, args.warmup, local, world)
     nbytes = 2 * batch * n * 16

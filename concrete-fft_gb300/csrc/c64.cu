@@ -199,7 +199,8 @@ cfft_status launch_smem(const C64Plan& p, bool fwd, int blocks, size_t smem, cud
   DevLevels L = p.dlv;
   int tpc = p.tpc, d0 = p.d0;
   void* args[] = {&data, &nsub, &tpc, &L, &d0, (void*)&w};
-  return launch_kernel(c64_kernel(p.base_algo, p.emu, fwd), blocks, p.threads, args, smem, stream, true);
+  const void* fn = c64_kernel(p.base_algo, p.emu, fwd);
+  return launch_kernel(fn, blocks, p.threads, args, spread_smem(fn, blocks, p.threads, 1, smem), stream, true);
 }
 
 cfft_status build_plan(C64Plan& p, size_t n, size_t base_n, int algo, bool unordered) {
@@ -266,14 +267,18 @@ cfft_status launch_split(const C64Plan& p, bool fwd, int ls, int mode, long nsub
   const void* fn = c64_split_kernel_ptr(p.base_algo, fwd, ls, mode);
   const size_t part = p.n >> ls;
   const size_t smem = 2 * part * sizeof(double2);
-  // one thread per butterfly of a pass over the part (more would idle at the barriers)
-  const int threads = (int)std::min<size_t>(256, std::max<size_t>(32, part / (size_t)algo_radix(p.base_algo)));
+  // one thread per butterfly of a pass over the part (more would idle at the barriers);
+  // two for the DIF radix-2/4 algorithms, whose passes split each butterfly into halves
+  const int R = algo_radix(p.base_algo);
+  const bool halves = (p.base_algo & 1) == 0 && R <= 4;
+  const int threads = (int)std::min<size_t>(256, std::max<size_t>(32, (halves ? 2 : 1) * part / (size_t)R));
   DevLevels L = p.dlv;
   const double2* w = fwd ? p.d_w : p.d_winv;
   void* args[] = {&data, &L, (void*)&w};
   if ((nsub << ls) > 0x7fffffffL) return fail(CFFT_ERR_INVALID_SIZE, "batch too large");
   const int grid = (int)(nsub << ls);
-  return launch_kernel_cluster(fn, grid, threads, 1 << ls, args, smem, stream, true);
+  return launch_kernel_cluster(fn, grid, threads, 1 << ls, args, spread_smem(fn, grid, threads, 1 << ls, smem),
+                               stream, true);
 }
 
 cfft_status launch_level(bool fwd, double2* data, long total, int log2r, int log2nl, const double2* wl, int nsm,

@@ -237,6 +237,39 @@ struct Core<16, FWD, E> {  // src/dif16.rs:650-779
   }
 };
 
+// Half of a radix-2 or radix-4 core: the outputs k with k % 2 == H, by the
+// same operations on the same operands as Core<R> (whose other outputs use
+// disjoint intermediate values, so no operation is repeated).  Two threads
+// then share one butterfly, which doubles the threads a pass can use.
+// y[j] = output 2j + H.
+template <int R, bool FWD, int H>
+struct CoreHalf;
+
+template <bool FWD, int H>
+struct CoreHalf<2, FWD, H> {
+  __device__ __forceinline__ static void run(const c64* x, c64* y) { y[0] = H == 0 ? cadd(x[0], x[1]) : csub(x[0], x[1]); }
+};
+
+template <bool FWD>
+struct CoreHalf<4, FWD, 0> {
+  __device__ __forceinline__ static void run(const c64* x, c64* y) {
+    const c64 apc = cadd(x[0], x[2]);
+    const c64 bpd = cadd(x[1], x[3]);
+    y[0] = cadd(apc, bpd);
+    y[1] = csub(apc, bpd);
+  }
+};
+
+template <bool FWD>
+struct CoreHalf<4, FWD, 1> {
+  __device__ __forceinline__ static void run(const c64* x, c64* y) {
+    const c64 amc = csub(x[0], x[2]);
+    const c64 jbmd = mul_j<FWD>(csub(x[1], x[3]));
+    y[0] = csub(amc, jbmd);
+    y[1] = cadd(amc, jbmd);
+  }
+};
+
 // ----------------------------------------------------------------------------
 // Exact integer <-> double conversions on the integer pipe.  On GB300 the
 // I2F.F64/F2I.F64 conversions issue on the (narrow) FP64 pipe, so the product

@@ -57,6 +57,10 @@ cfft_status ensure_smem(const void* fn, size_t smem);
 cfft_status launch_kernel_cluster(const void* fn, int grid, int block, int cluster, void** args, size_t smem,
                                   cudaStream_t stream, bool pdl = false);
 int max_blocks_per_sm(const void* fn, int block, size_t smem);
+// Dynamic shared memory for a launch that spreads a one-wave grid evenly over
+// the SMs (ceil(grid / SMs) CTAs per SM); `smem` itself when the grid takes
+// several waves, already spreads, or the padded shape would not hold it.
+size_t spread_smem(const void* fn, int grid, int block, int cluster, size_t smem);
 
 // kernel<<<grid, block, smem, stream>>>(args...) as a programmatic dependent
 // launch (the kernel calls grid_dependency_wait() before its first global access).

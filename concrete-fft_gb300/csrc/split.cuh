@@ -11,14 +11,14 @@
 //
 // The S CTAs of a transform form a thread-block cluster.
 //
-// "First" kernels: every CTA reads the whole transform from global memory,
-// computes the outputs of the first step that fall in its own part --
-// selected at compile time, so the arithmetic of the other outputs is dropped
-// -- then finishes its part alone and stores it.  The transform is updated in
-// place, so a CTA stores only after every CTA of its cluster has read (a
-// cluster barrier split into an arrive after the reads and a wait before the
-// stores).  Used for DIF-structured transforms (ordered DIF algorithms, the
-// unordered base with no outer levels).
+// "First" kernels: the first step's butterflies are shared out, 1/S per CTA;
+// each CTA reads its butterflies' inputs from global memory and stores every
+// output into the part that holds its residue class (distributed shared
+// memory), so no arithmetic is repeated; then each CTA finishes its part alone
+// and stores it.  The transform is updated in place, and the cluster barrier
+// after the first step also orders every read of it before any store.  Used
+// for DIF-structured transforms (ordered DIF algorithms, the unordered base
+// with no outer levels).
 //
 // The forward unordered transform with levels exchanges once instead: each
 // CTA loads its own part, and level 0 takes 1/S of the butterflies per CTA,
@@ -38,25 +38,6 @@
 #include "stockham.cuh"
 
 namespace cfft {
-
-template <int V>
-struct IntC {
-  static constexpr int value = V;
-};
-
-// Cluster barrier in two halves: arrive (releasing this thread's prior memory
-// operations) and wait (acquiring the other threads').
-__device__ __forceinline__ void cluster_arrive() { asm volatile("barrier.cluster.arrive.release.aligned;\n" ::: "memory"); }
-__device__ __forceinline__ void cluster_wait() { asm volatile("barrier.cluster.wait.acquire.aligned;\n" ::: "memory"); }
-
-// Calls f(IntC<c>{}) for the runtime rank c < 2^LS.
-template <int LS, int C = 0, class F>
-__device__ __forceinline__ void with_rank(int c, F&& f) {
-  if constexpr (C < (1 << LS)) {
-    if (c == C) f(IntC<C>{});
-    else with_rank<LS, C + 1>(c, f);
-  }
-}
 
 // Passes 1 .. npass-1 and the end butterfly of a DIF transform of 2^log2n
 // points, run on one residue class mod 2^LS compacted to 2^(log2n - LS) points.
@@ -153,6 +134,59 @@ __device__ __forceinline__ void level0_last(double2* g, int lm, double2* const* 
   }
 }
 
+// The first (s = 1) pass of a DIF transform over its cluster: CTA c takes the
+// butterflies [c*per, (c+1)*per) in full -- no output is computed twice --
+// reading their inputs from global memory, and stores each output into the
+// part of its residue class mod S (distributed shared memory), compacted.
+// With twice as many threads as butterflies (a multiple of 32), radix 2 and 4
+// butterflies are split into halves as in stockham_pass.
+template <int R, bool FWD, int LS>
+__device__ __forceinline__ void dif_first_scatter(const double2* g, int lper, int c, double2* const* part,
+                                                  const double2* __restrict__ wb, int tid, int nth) {
+  constexpr int LR = Log2<R>::v;
+  constexpr int S = 1 << LS;
+  const int per = (1 << lper) >> LS;
+  const int p0 = c * per;
+  if constexpr (R == 2 || R == 4) {
+    if (nth >= 2 * per && (per & 31) == 0) {
+      if (tid < 2 * per) {
+        const int h = tid >= per ? 1 : 0;
+        const int p = p0 + tid - h * per;
+        c64 v[R];
+#pragma unroll
+        for (int k = 0; k < R; ++k) v[k] = ld(g + (k << lper) + p);
+        const double2* tw = wb + (p << LR);
+        c64 y[R / 2];
+        if (h == 0) {
+          CoreHalf<R, FWD, 0>::run(v, y);
+          st(part[0] + ((p << LR) >> LS), y[0]);
+#pragma unroll
+          for (int j = 1; j < R / 2; ++j)
+            st(part[(2 * j) & (S - 1)] + (((p << LR) + 2 * j) >> LS), cmul(ldg(tw + 2 * j), y[j]));
+        } else {
+          CoreHalf<R, FWD, 1>::run(v, y);
+#pragma unroll
+          for (int j = 0; j < R / 2; ++j)
+            st(part[(2 * j + 1) & (S - 1)] + (((p << LR) + 2 * j + 1) >> LS), cmul(ldg(tw + 2 * j + 1), y[j]));
+        }
+      }
+      return;
+    }
+  }
+  for (int p = p0 + tid; p < p0 + per; p += nth) {
+    c64 v[R];
+#pragma unroll
+    for (int k = 0; k < R; ++k) v[k] = ld(g + (k << lper) + p);
+    Core<R, FWD, 0>::run(v);
+    const double2* tw = wb + (p << LR);
+#pragma unroll
+    for (int k = 0; k < R; ++k) {
+      const c64 o = k == 0 ? v[0] : cmul(ldg(tw + k), v[k]);
+      st(part[k & (S - 1)] + (((p << LR) + k) >> LS), o);
+    }
+  }
+}
+
 // MODE 0: the plan has no outer levels (ordered plan, or unordered with
 // n = base_n); the base algorithm's structure decides (DIF: first, DIT: last).
 // MODE 1: unordered with outer levels (forward: first, inverse: last).
@@ -178,28 +212,17 @@ __global__ void __launch_bounds__(256) c64_split_kernel(double2* data, DevLevels
   const double2* wb = FWD ? w + L.w_off[L.nlevels] + (1 << log2base) : w + (1 << log2base);
 
   if constexpr (MODE == 0 && !LAST) {
-    // DIF: pass 0 (s = 1) from global, own residue class only.
-    const int lper = log2n - LR;
-    with_rank<LS>(c, [&](auto C) {
-      for (int p = tid; p < (1 << lper); p += nth) {
-        c64 v[R];
+    // DIF: pass 0 (s = 1) over the cluster, 1/S of the butterflies per CTA, each
+    // output stored into the part of its residue class; then this class alone.
+    namespace cg = cooperative_groups;
+    cg::cluster_group cl = cg::this_cluster();
+    double2* part[S];
 #pragma unroll
-        for (int k = 0; k < R; ++k) v[k] = ld(g + (k << lper) + p);
-        Core<R, FWD, 0>::run(v);
-        const double2* tw = wb + (p << LR);
-#pragma unroll
-        for (int k = 0; k < R; ++k) {
-          if ((k & (S - 1)) == decltype(C)::value) {
-            const c64 o = k == 0 ? v[0] : cmul(ldg(tw + k), v[k]);
-            st(xs + (((p << LR) + k) >> LS), o);
-          }
-        }
-      }
-    });
-    __syncthreads();
-    cluster_arrive();
+    for (int j = 0; j < S; ++j) part[j] = cl.map_shared_rank(xs, (unsigned)j);
+    cl.sync();  // every CTA of the cluster is running before its shared memory is written
+    dif_first_scatter<R, FWD, LS>(g, log2n - LR, c, part, wb, tid, nth);
+    cl.sync();  // every part is complete, and every read of the transform in global memory is done
     const FlatBuf r = dif_after_first<R, FWD>(log2n, LS, FlatBuf{xs}, FlatBuf{ys}, wb, tid, nth);
-    cluster_wait();
     for (int j = tid; j < (1 << log2c); j += nth) g[(j << LS) + c] = r.p[j];
   } else if constexpr (MODE == 0 && LAST) {
     // DIT: own residue class through every pass but the last, then the s = 1

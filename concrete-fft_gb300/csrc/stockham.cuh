@@ -51,6 +51,13 @@ struct CtaSync {
 // twlog: the pass runs on one residue class mod 2^twlog of a transform 2^twlog
 // times larger, compacted (see split.cuh); its twiddles are those of the full
 // transform's stride s * 2^twlog.  0 for a whole transform.
+//
+// Half butterflies: when the CTA has at least twice as many threads as the
+// pass has butterflies (a multiple of 32), a DIF radix-2/4 pass gives each
+// butterfly two threads, the first `total` threads computing its even outputs
+// and the next `total` its odd ones (CoreHalf: the same operations, none
+// repeated), so whole warps take one half.  Twiddles multiply the outputs
+// after the core, so each half twiddles its own.
 template <int R, bool FWD, bool DIT, int E, class B>
 __device__ __forceinline__ void stockham_pass(int log2n, int log2s, int nchunks, B src, B dst,
                                               const double2* __restrict__ w, int tid, int nth, int twlog = 0) {
@@ -58,6 +65,35 @@ __device__ __forceinline__ void stockham_pass(int log2n, int log2s, int nchunks,
   const int lper = log2n - LR;  // log2(n / R): butterflies per chunk
   const int total = nchunks << lper;
   const int smask = (1 << log2s) - 1;
+  if constexpr (!DIT && E == 0 && (R == 2 || R == 4)) {
+    if (nth >= 2 * total && (total & 31) == 0) {
+      if (tid < 2 * total) {
+        const int h = tid >= total ? 1 : 0;
+        const int b = tid - h * total;
+        const int base = (b >> lper) << log2n;
+        const int bb = b & ((1 << lper) - 1);
+        const int p = bb >> log2s;
+        const int q = bb & smask;
+        const double2* tw = w + (p << (log2s + twlog + LR));
+        c64 v[R];
+#pragma unroll
+        for (int k = 0; k < R; ++k) v[k] = ld(src.at(base + (k << lper) + (p << log2s) + q));
+        const int o = base + (p << (log2s + LR)) + q;
+        c64 y[R / 2];
+        if (h == 0) {
+          CoreHalf<R, FWD, 0>::run(v, y);
+          st(dst.at(o), y[0]);
+#pragma unroll
+          for (int j = 1; j < R / 2; ++j) st(dst.at(o + ((2 * j) << log2s)), cmul(ldg(tw + 2 * j), y[j]));
+        } else {
+          CoreHalf<R, FWD, 1>::run(v, y);
+#pragma unroll
+          for (int j = 0; j < R / 2; ++j) st(dst.at(o + ((2 * j + 1) << log2s)), cmul(ldg(tw + 2 * j + 1), y[j]));
+        }
+      }
+      return;
+    }
+  }
   for (int b = tid; b < total; b += nth) {
     const int base = (b >> lper) << log2n;
     const int bb = b & ((1 << lper) - 1);
@@ -86,12 +122,37 @@ __device__ __forceinline__ void stockham_pass(int log2n, int log2s, int nchunks,
 }
 
 // End butterfly of size M at stride n/M, in place (src/dif4.rs:195-244 and twins).
+// Radix 2 and 4 split into half butterflies as stockham_pass does; being in
+// place, every half loads its inputs before a CTA barrier and stores after it
+// (every thread of the CTA calls this function).
 template <int M, bool FWD, int E, class B>
 __device__ __forceinline__ void end_pass(int log2n, int nchunks, B x, int tid, int nth) {
   constexpr int LM = Log2<M>::v;
   const int log2s = log2n - LM;
   const int total = nchunks << log2s;
   const int smask = (1 << log2s) - 1;
+  if constexpr (E == 0 && (M == 2 || M == 4)) {
+    if (nth >= 2 * total && (total & 31) == 0) {
+      const bool act = tid < 2 * total;
+      const int h = tid >= total ? 1 : 0;
+      const int g = tid - h * total;
+      const int base = act ? ((g >> log2s) << log2n) + (g & smask) : 0;
+      c64 v[M];
+      if (act) {
+#pragma unroll
+        for (int k = 0; k < M; ++k) v[k] = ld(x.at(base + (k << log2s)));
+      }
+      __syncthreads();
+      if (act) {
+        c64 y[M / 2];
+        if (h == 0) CoreHalf<M, FWD, 0>::run(v, y);
+        else CoreHalf<M, FWD, 1>::run(v, y);
+#pragma unroll
+        for (int j = 0; j < M / 2; ++j) st(x.at(base + ((2 * j + h) << log2s)), y[j]);
+      }
+      return;
+    }
+  }
   for (int g = tid; g < total; g += nth) {
     const int base = ((g >> log2s) << log2n) + (g & smask);
     c64 v[M];

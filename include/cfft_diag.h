@@ -41,6 +41,11 @@ cfft_status cfft_diag_host_mapping(const void* p, size_t bytes, void** device_ad
  * library's default).  Process-wide; for measurement. */
 cfft_status cfft_diag_set_cluster_policy(int policy);
 
+/* Even spreading of one-wave grids over the SMs (the c64 transform kernels pad
+ * their shared memory so that ceil(grid / SMs) CTAs fit an SM): 1 on (the
+ * default), 0 off.  Process-wide; for measurement. */
+cfft_status cfft_diag_set_spread(int on);
+
 #ifdef __cplusplus
 }
 #endif

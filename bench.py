@@ -1308,6 +1308,8 @@ def run_product_sum(args):
     ops = groups * (T * (fp64_ops_per_transform(n, 1024, 2) + 4 * n + 4 * n + 2 * n) - 2 * n
                     + fp64_ops_per_transform(n, 1024, 2) + 4 * n)
     peak = fp64_peak(cf)
+    peaks, peak_kind = measured_peaks()
+    alg_bytes = groups * T * N * 8 + groups * T * n * 16 + groups * N * 8  # A and Bhat read, sums written
     if rank != 0:
         return
     print(json.dumps({
@@ -1316,7 +1318,11 @@ def run_product_sum(args):
         "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded numpy PCG64)",
         "config": {"workload": "1024 groups x 8 products, one inverse per group"},
-        "roofline": {"fp64": {"achieved_ops_per_s": ops / per, "peak_ops_per_s": peak, "frac": ops / per / peak}},
+        "roofline": {"bound": "hbm", "achieved": alg_bytes / per / 1e9, "peak": peaks["hbm_gbs"], "unit": "GB/s",
+                     "frac": alg_bytes / per / 1e9 / peaks["hbm_gbs"], "peak_kind": peak_kind,
+                     "traffic": (profiled_traffic("u64_product_sum_n2048") or {}).get("dram_bytes_per_launch"),
+                     "algorithmic_bytes_per_launch": alg_bytes,
+                     "fp64": {"achieved_ops_per_s": ops / per, "peak_ops_per_s": peak, "frac": ops / per / peak}},
         "clocks": clocks, "gpu_launches": args.steps,
     }))
 

@@ -1222,12 +1222,63 @@ def print_line(entry, world, data="synthetic (seeded)"):
     print(json.dumps(line))
 
 
+def autotune_check(torch, cf, schedule, local, world, points=1 << 24):
+    """Whether the persistent kernel's per-size schedule (Dif4 / Dif8, bases 512 / 1024) is the best
+    of every candidate the reference's Method::Measure considers: per size, the standalone plan
+    of each (algorithm, base) times forward+inverse over 2^24 points of that size, and the best
+    is compared with the algorithm and base the mixed batch scheduled (same FP64 work per
+    transform, so the standalone ranking carries over)."""
+    rows = {}
+    for k in range(8, 17):
+        n = 1 << k
+        batch = points // n
+        x = torch.empty((batch, n, 2), dtype=torch.float64, device="cuda")
+        cands = {}
+        bases = [n] if n <= 512 else [bb for bb in (512, 1024) if bb <= n]
+        for base in bases:
+            for a in range(8):
+                algo = cf.FftAlgo(a)
+                plan = cf.unordered.Plan(n, cf.unordered.Method.UserProvided(algo, base))
+                x.uniform_(-1, 1)  # six forward+inverse steps grow the data by at most n^6 <= 2^96
+
+                def step():
+                    plan.fwd(x)
+                    plan.inv(x)
+                ms, _ = timed(torch, step, 4, 2, local, world)
+                cands["%s/%d" % (algo.name, base)] = ms * 1e3 / 4 / (2 * batch)
+        best = min(cands, key=cands.get)
+        sched = schedule.get("u%d" % k)
+        sname = "%s/%d" % (sched[0], sched[1]) if sched else None
+        rows[n] = {"best": best, "best_us_per_transform": round(cands[best], 4), "scheduled": sname,
+                   "scheduled_us_per_transform": round(cands[sname], 4) if sname in cands else None,
+                   "gap_pct": round(100 * (cands[sname] / cands[best] - 1), 2) if sname in cands else None,
+                   "fp64_ops_per_point": {c: fp64_ops_per_transform(n, int(c.split("/")[1]),
+                                                                    int(cf.FftAlgo[c.split("/")[0]])) / n
+                                          for c in (best, sname) if c},
+                   "fastest_candidates_us": {c: round(v, 4) for c, v in sorted(cands.items(), key=lambda kv: kv[1])[:6]}}
+        del x
+    return rows
+
+
 def run_mixed(args):
-    """The mixed-size batch (100,000 items) as its own JSON line."""
+    """The mixed-size batch (100,000 items) as its own JSON line, with the check of the
+    persistent kernel's per-size schedule against every Method::Measure candidate."""
     torch, cf, rank, world, local = gpu_setup()
+    if args.profile_case:  # for ncu: two persistent launches over --mixed-items items of the same mix
+        items, log2n, kind, sizes, offs, rng = mixed_items(cf, args.mixed_items, 3)
+        b = cf.batch.Batch(items, tune_seconds=args.tune_seconds)
+        total = int(sizes.sum())
+        data = torch.rand((total, 2), dtype=torch.float64, device="cuda") * 2 - 1
+        for _ in range(2):
+            b.run(data)
+        torch.cuda.synchronize()
+        print(json.dumps({"profile_case": "mixed batch x2", "items": args.mixed_items, "points": total}))
+        return
     entry = measure_mixed(torch, cf, args.steps, args.warmup, local, world, count=args.mixed_items,
                           tune_seconds=args.tune_seconds, seed=3 + rank, cpu=not args.no_cpu_baseline and rank == 0,
                           cpu_seconds=args.cpu_seconds)
+    torch.cuda.empty_cache()
+    entry["autotune_check"] = autotune_check(torch, cf, entry["config"]["schedule"], local, world)
     if rank == 0:
         print_line(entry, world)
 

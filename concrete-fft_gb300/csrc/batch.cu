@@ -265,7 +265,31 @@ cfft_status finalize(cfft_batch* b) {
   return st;
 }
 
+// FP64 instructions (DADD/DMUL/DFMA) of one unordered transform of 2^log2n points
+// with the given base: the outer levels' radix-r butterflies plus r - 1 twiddle
+// products each, the base's radix-R passes likewise, and its end butterfly.
+double fp64_ops_per_point(int log2n, int base_log2, int algo) {
+  auto core = [](int r) { return r == 2 ? 4.0 : r == 4 ? 16.0 : r == 8 ? 56.0 : 168.0; };
+  const LevelDesc lv = make_levels(size_t(1) << log2n, size_t(1) << base_log2);
+  double ops = 0;
+  for (int l = 0; l < lv.nlevels; ++l) {
+    const int r = 1 << lv.log2r[l];
+    ops += (core(r) + 4.0 * (r - 1)) / r;
+  }
+  const int lr = ilog2((size_t)algo_radix(algo));
+  int rem = base_log2;
+  while (rem > lr) {
+    rem -= lr;
+    ops += (core(1 << lr) + 4.0 * ((1 << lr) - 1)) / (1 << lr);
+  }
+  if (rem > 0) ops += core(1 << rem) / (1 << rem);
+  return ops;
+}
+
 // Times candidate schedules of one size class on a synthetic homogeneous batch.
+// The class runs at the FP64 roof, so among candidates timed within 3% of the
+// fastest (short timings are that noisy) the one with the fewest FP64
+// instructions per point wins, and the time decides between equal counts.
 cfft_status tune_class(cfft_batch* b, size_t ci, double seconds) {
   ClassHost& c = b->classes[ci];
   const int log2n = c.key.log2n;
@@ -296,8 +320,7 @@ cfft_status tune_class(cfft_batch* b, size_t ci, double seconds) {
   cudaEvent_t e0, e1;
   cudaEventCreate(&e0);
   cudaEventCreate(&e1);
-  double best = 1e30;
-  auto bestc = cands.front();
+  std::vector<double> times;
   cfft_status st = CFFT_OK;
   for (auto cand : cands) {
     ClassHost t;
@@ -325,10 +348,7 @@ cfft_status tune_class(cfft_batch* b, size_t ci, double seconds) {
       reps *= 2;
     }
     free_tables(tb.classes[0]);
-    if (per < best) {
-      best = per;
-      bestc = cand;
-    }
+    times.push_back(per);
   }
   free_batch_device(&tb);
   cudaFree(tb.d_head);
@@ -337,7 +357,18 @@ cfft_status tune_class(cfft_batch* b, size_t ci, double seconds) {
   cudaStreamDestroy(s);
   cudaFree(buf);
   if (st != CFFT_OK) return st;
-  std::tie(c.algo, c.base_log2, c.tpc) = bestc;
+  const double fastest = *std::min_element(times.begin(), times.end());
+  size_t pick = 0;
+  double pick_ops = 1e30;
+  for (size_t i = 0; i < cands.size(); ++i) {
+    if (times[i] > 1.03 * fastest) continue;
+    const double ops = fp64_ops_per_point(log2n, std::get<1>(cands[i]), std::get<0>(cands[i]));
+    if (ops < pick_ops - 1e-9 || (ops < pick_ops + 1e-9 && times[i] < times[pick])) {
+      pick = i;
+      pick_ops = ops;
+    }
+  }
+  std::tie(c.algo, c.base_log2, c.tpc) = cands[pick];
   return CFFT_OK;
 }
 

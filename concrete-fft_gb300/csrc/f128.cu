@@ -347,7 +347,11 @@ cfft_status run_f128_tw(size_t n, const F128Tw& tw, double* re0, double* re1, do
   const int grid = product_grid(fwd ? (const void*)f128_smem_kernel<true> : (const void*)f128_smem_kernel<false>,
                                 threads, smem, (nblocks + (1L << log2t) - 1) >> log2t);
   const long total = (long)batch << (log2n - 1);
-  const int sgrid = (int)std::min<long>((total + 255) / 256, (long)sm_count() * 16);
+  // global stages: 256-thread CTAs; a stage of fewer butterflies than one such CTA per SM
+  // takes 128-thread CTAs, so that its warps land on twice as many SM sub-partitions (a
+  // warp issues FP64 on one sub-partition, and one butterfly is ~100 dependent FP64 steps)
+  const int sthreads = total < 256L * sm_count() ? 128 : 256;
+  const int sgrid = (int)std::min<long>((total + sthreads - 1) / sthreads, (long)sm_count() * 16);
   // programmatic dependent launches: each kernel is launched as the previous one's CTAs exit
   F128Tw t = tw;
   long tot = total, nb = nblocks;
@@ -355,7 +359,7 @@ cfft_status run_f128_tw(size_t n, const F128Tw& tw, double* re0, double* re1, do
   auto stage = [&](int lt) {
     void* args[] = {&g, &ln, &lt, &tot, &t};
     return launch_kernel(fwd ? (const void*)f128_stage_kernel<true> : (const void*)f128_stage_kernel<false>, sgrid,
-                         256, args, 0, stream, true);
+                         sthreads, args, 0, stream, true);
   };
   void* sargs[] = {&g, &ln, &lc, &nb, &t, &log2t};
   const void* sfn = fwd ? (const void*)f128_smem_kernel<true> : (const void*)f128_smem_kernel<false>;

@@ -214,7 +214,7 @@ def run_reference(args):
     import pyoracle
     import numpy as np
     algo, base = cpu_fastest_algo(threads)
-    sample = max(256, 32 * threads)
+    sample = 256 * threads  # large enough per step that thread start-up does not show in the rate
     a, b = make_inputs(sample, BASE_SEED)
     bhat = pyoracle.u64_prepare(N_POLY, algo, base, b)
     for _ in range(args.warmup):

@@ -420,7 +420,8 @@ def run_gb300(args):
         for name, fn in (("ordered_c64_n1024", lambda: measure_ordered(torch, cf, 50, 3, local, world)),
                          ("u128_product", lambda: measure_u128(torch, cf, 10, 3, local, world)),
                          ("mixed_batch_100k", lambda: measure_mixed(torch, cf, 3, 3, local, world)),
-                         ("serving_20k_req_s", lambda: measure_serving(torch, cf, local, world))):
+                         ("serving_20k_req_s", lambda: measure_serving(torch, cf, local, world)),
+                         ("reference_bench_cases", lambda: measure_reference_cases(torch, cf, local, world))):
             t_cfg = time.perf_counter()
             try:
                 configs[name] = fn()
@@ -1111,6 +1112,122 @@ def measure_u128(torch, cf, steps, warmup, local, world, full=False, cpu_seconds
     return entry
 
 
+# ---------------------------------------------------------------- the reference's own bench cases
+def reference_case_tables(torch, cf, local, world, cpu=True, cpu_seconds=0.04):
+    """The cases of the reference's benches/fft.rs, one call each as criterion times them:
+    ordered fwd (n <= 1024), unordered fwd, unordered inv and fwd_monomial for n = 2^8..2^16
+    (plans from Method::Measure), and fft128 negacyclic fwd/inv for n = 64..16384.  Per case:
+    the GPU's device time per call (20 calls of one transform replayed from a CUDA graph, so no
+    host call sits between them), the time per call through the host-slice entry point on a
+    pageable buffer (what a caller of the slice API pays, Python's call overhead included),
+    the GPU's batched rate (2^22 points per call), and the restated reference's time per call
+    on one host core with the algorithm its Method::Measure picks there."""
+    import numpy as np
+    po = _oracle()
+    stream = torch.cuda.current_stream()
+
+    def events_ms(fn, steps, warmup):  # CUDA events on the launching stream (clocks: the configs' samplers)
+        for _ in range(warmup):
+            fn()
+        torch.cuda.synchronize()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(steps):
+            fn()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1)
+
+    def device_us(call):
+        call()  # first call outside the capture (one-time kernel attributes and launch shapes)
+        torch.cuda.synchronize()
+        graph = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(graph):
+            for _ in range(20):
+                call()
+        return events_ms(graph.replay, 10, 2) * 1e3 / 200
+
+    def host_us(call, reps=20):
+        call()
+        t0 = time.perf_counter()
+        for _ in range(reps):
+            call()
+        return (time.perf_counter() - t0) * 1e6 / reps
+
+    def batched_per_s(call, count):
+        return count * 5 / (events_ms(call, 5, 2) * 1e-3)
+
+    rows = {}
+    rng = np.random.default_rng(13)
+    for k in range(8, 17):
+        n = 1 << k
+        batch = max(1, (1 << 22) // n)
+        one = torch.from_numpy(rng.uniform(-1, 1, (1, n)) + 1j * rng.uniform(-1, 1, (1, n))).cuda()
+        many = torch.empty((batch, n), dtype=torch.complex128, device="cuda").normal_()
+        host = (rng.uniform(-1, 1, (1, n)) + 1j * rng.uniform(-1, 1, (1, n))).astype(np.complex128)
+        up = cf.unordered.Plan(n, cf.unordered.Method.Measure(0.002))
+        ua, ub = up.algo()
+        row = {"gpu_unordered_plan": "%s/%d" % (ua.name, ub)}
+        cases = [("unordered_fwd", lambda b: up.fwd(b)), ("unordered_inv", lambda b: up.inv(b)),
+                 ("fwd_monomial", lambda b: up.fwd_monomial(n // 3, b))]
+        if n <= 1024:
+            op = cf.ordered.Plan(n, cf.ordered.Method.Measure(0.002))
+            row["gpu_ordered_plan"] = op.algo().name
+            cases.insert(0, ("ordered_fwd", lambda b: op.fwd(b)))
+        for name, fn in cases:
+            r = {"gpu_device_us": round(device_us(lambda: fn(one)), 3),
+                 "host_slice_api_us": round(host_us(lambda: fn(host)), 2)}
+            if name != "fwd_monomial":
+                r["gpu_batched_transforms_per_s"] = batched_per_s(lambda: fn(many), batch)
+            rows.setdefault(n, row)[name] = r
+        if cpu and world == 1:
+            ca, cb = cpu_measure_unordered(po, n)
+            row["cpu_unordered_plan"] = "%s/%d" % (ALGO_NAMES[ca], cb)
+            row["unordered_fwd"]["cpu_one_core_us"] = round(po.bench_call(1, n, ca, cb, cpu_seconds) * 1e6, 2)
+            row["unordered_inv"]["cpu_one_core_us"] = round(po.bench_call(2, n, ca, cb, cpu_seconds) * 1e6, 2)
+            row["fwd_monomial"]["cpu_one_core_us"] = round(po.bench_call(3, n, 0, cb, cpu_seconds) * 1e6, 3)
+            if n <= 1024:
+                oa = cpu_measure_ordered(po, n)
+                row["cpu_ordered_plan"] = ALGO_NAMES[oa]
+                row["ordered_fwd"]["cpu_one_core_us"] = round(po.bench_call(0, n, oa, 0, cpu_seconds) * 1e6, 2)
+        rows[n] = row
+        del one, many
+    f128rows = {}
+    for k in range(6, 15):
+        n = 1 << k
+        batch = max(1, (1 << 20) // n)
+        fp = cf.fft128.Plan(n)
+        one = [torch.rand((1, n), dtype=torch.float64, device="cuda") for _ in range(4)]
+        many = [torch.rand((batch, n), dtype=torch.float64, device="cuda") for _ in range(4)]
+        host = [np.random.default_rng(k).uniform(-1, 1, (1, n)) for _ in range(4)]
+        row = {}
+        for name, fn in (("fwd", fp.fwd), ("inv", fp.inv)):
+            row[name] = {"gpu_device_us": round(device_us(lambda: fn(*one)), 3),
+                         "host_slice_api_us": round(host_us(lambda: fn(*host)), 2),
+                         "gpu_batched_transforms_per_s": batched_per_s(lambda: fn(*many), batch)}
+            if cpu and world == 1:
+                row[name]["cpu_one_core_us"] = round(po.bench_call(4 if name == "fwd" else 5, n, 0, 0, cpu_seconds)
+                                                     * 1e6, 2)
+        f128rows[n] = row
+        del one, many
+    return rows, f128rows
+
+
+def measure_reference_cases(torch, cf, local, world, cpu=True, cpu_seconds=0.04):
+    """reference_case_tables under an nvidia-smi clock sampler."""
+    with ClockSampler(local) as clk:
+        t0 = time.time()
+        rows, f128rows = reference_case_tables(torch, cf, local, world, cpu, cpu_seconds)
+        clk.mark(t0, time.time())
+    return {"c64": rows, "fft128": f128rows, "clocks": clk.summary(),
+            "cpu": "restated reference, one host thread, scalar (the reference's own Scalar backend on this Arm "
+                   "host), each call timed in a loop in C as criterion does",
+            "gpu_device": "20 calls of one transform in a CUDA graph, replayed 10 times, CUDA events",
+            "host_slice_api": "cfft_*_fwd_host / _inv_host / fwd_monomial_host on a pageable numpy buffer, from "
+                              "Python (staged copies in and out)"}
+
+
 # ---------------------------------------------------------------- config 5: serving
 SERVE_SIZES = [10, 11, 12, 13, 14]
 
@@ -1524,7 +1641,7 @@ def main():
     ap.add_argument("--serve-seconds", type=float, default=1.0)
     ap.add_argument("--operand-gb", type=int, default=8)
     ap.add_argument("--workload", choices=["u64_product", "mixed", "ordered", "u128_product", "serving", "product_sum", "serde",
-                             "u64_large"],
+                             "u64_large", "reference_cases"],
                     default="u64_product",
                     help="u64_product (default headline) or one of the other benchmark configurations")
     ap.add_argument("--mixed-items", type=int, default=100000)
@@ -1551,6 +1668,11 @@ def main():
         run_serving(args)
     elif args.workload == "product_sum":
         run_product_sum(args)
+    elif args.workload == "reference_cases":
+        torch, cf, rank, world, local = gpu_setup()
+        res = measure_reference_cases(torch, cf, local, world, cpu=not args.no_cpu_baseline)
+        if rank == 0:
+            print(json.dumps({"workload": "reference bench cases (benches/fft.rs)", "results": res}))
     else:
         run_gb300(args)
 

@@ -8,6 +8,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <cstring>
 #include <mutex>
 #include <vector>
 
@@ -416,10 +417,31 @@ cfft_status run_f128_host(const cfft_f128_plan* p, double* re0, double* re1, dou
       return CFFT_OK;
     }
   }
+  double* hh[4] = {re0, re1, im0, im1};
+  // pageable arrays of up to 4 MiB in all: CPU copies into the thread's page-locked
+  // bounce buffer and one DMA copy each way (a pageable cudaMemcpy costs ~10 us of
+  // driver time, and there would be eight), with the device path in between, which
+  // spreads a small batch over many SMs
+  if (batch > 0 && 4 * bytes <= kHostBounceMax) {
+    void *hb = nullptr, *db = nullptr;
+    cfft_status st = host_bounce(4 * bytes, &hb, &db);
+    if (st != CFFT_OK) return st;
+    st = host_staging(4 * bytes, &d, &s);
+    if (st != CFFT_OK) return st;
+    for (int i = 0; i < 4; ++i) std::memcpy((char*)hb + i * bytes, hh[i], bytes);
+    CFFT_CUDA_TRY(cudaMemcpyAsync(d, hb, 4 * bytes, cudaMemcpyHostToDevice, s));
+    double* m[4];
+    for (int i = 0; i < 4; ++i) m[i] = (double*)((char*)d + i * bytes);
+    st = run_f128(p, m[0], m[1], m[2], m[3], batch, fwd, s);
+    if (st != CFFT_OK) return st;
+    CFFT_CUDA_TRY(cudaMemcpyAsync(hb, d, 4 * bytes, cudaMemcpyDeviceToHost, s));
+    CFFT_CUDA_TRY(cudaStreamSynchronize(s));
+    for (int i = 0; i < 4; ++i) std::memcpy(hh[i], (char*)hb + i * bytes, bytes);
+    return CFFT_OK;
+  }
   cfft_status st = host_staging(4 * bytes, &d, &s);
   if (st != CFFT_OK) return st;
   double* dd[4];
-  double* hh[4] = {re0, re1, im0, im1};
   for (int i = 0; i < 4; ++i) {
     dd[i] = (double*)((char*)d + i * bytes);
     CFFT_CUDA_TRY(cudaMemcpyAsync(dd[i], hh[i], bytes, cudaMemcpyHostToDevice, s));

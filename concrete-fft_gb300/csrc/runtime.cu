@@ -70,6 +70,37 @@ cfft_status host_staging(size_t bytes, void** dev_ptr, cudaStream_t* stream) {
 }
 
 namespace {
+struct Bounce {
+  void* host = nullptr;
+  size_t cap = 0;
+  ~Bounce() {
+    if (host) cudaFreeHost(host);
+  }
+};
+thread_local Bounce t_bounce;
+}  // namespace
+
+// Page-locked, device-mapped host buffer of the calling thread for the *_host
+// entry points on pageable memory (grown on demand up to kHostBounceMax, never
+// shrunk).  A pageable cudaMemcpy costs ~10 us of fixed driver time each way;
+// a CPU memcpy into this buffer costs about a microsecond for a small transform.
+cfft_status host_bounce(size_t bytes, void** host_ptr, void** dev_ptr) {
+  if (bytes > kHostBounceMax) return fail(CFFT_ERR_INVALID_SIZE, "host bounce buffer request too large");
+  Bounce& b = t_bounce;
+  if (bytes > b.cap) {
+    if (b.host) CFFT_CUDA_TRY(cudaFreeHost(b.host));
+    b.host = nullptr;
+    b.cap = 0;
+    const size_t cap = std::max<size_t>(bytes, 64 << 10);
+    CFFT_CUDA_TRY(cudaHostAlloc(&b.host, cap, cudaHostAllocMapped | cudaHostAllocPortable));
+    b.cap = cap;
+  }
+  CFFT_CUDA_TRY(cudaHostGetDevicePointer(dev_ptr, b.host, 0));
+  *host_ptr = b.host;
+  return CFFT_OK;
+}
+
+namespace {
 std::mutex g_attr_mu;
 struct AttrEntry {
   const void* fn;

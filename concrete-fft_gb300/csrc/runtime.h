@@ -82,6 +82,11 @@ cudaError_t launch_dependent(void (*kernel)(Params...), int grid, int block, siz
 
 // Persistent scratch for the *_host convenience entry points (one per thread).
 cfft_status host_staging(size_t bytes, void** dev_ptr, cudaStream_t* stream);
+// Page-locked, device-mapped bounce buffer of the calling thread (at most
+// kHostBounceMax bytes) for small host calls on pageable memory: host address
+// and the address kernels use.
+constexpr size_t kHostBounceMax = size_t(4) << 20;
+cfft_status host_bounce(size_t bytes, void** host_ptr, void** dev_ptr);
 
 // Copy/compute pipeline of the *_host product entry points: `nslots` device
 // buffers of `bytes` each, one stream per slot (per thread, grown on demand).

@@ -14,6 +14,7 @@
 #include "cfft_oracle.h"
 
 #include <algorithm>
+#include <chrono>
 #include <cmath>
 #include <cstring>
 #include <thread>
@@ -1335,6 +1336,94 @@ int oracle_schoolbook_batch(int words, size_t N, size_t count, const uint64_t* a
     }
   });
   return bad ? -1 : 0;
+}
+
+// Per-call CPU time of the restated reference, single-threaded, for the timed
+// CPU baseline of the reference's own benchmark cases (benches/fft.rs): the
+// call repeated `reps` times on one buffer, as a criterion loop does.
+//   kind 0: ordered fwd (algo), 1: unordered fwd, 2: unordered inv (algo, base_n),
+//   3: fwd_monomial (base_n; degree cycling as in the reference bench),
+//   4: fft128 negacyclic fwd, 5: fft128 negacyclic inv.
+int oracle_bench_call(int kind, int algo, size_t n, size_t base_n, size_t reps, double* ns_per_call) {
+  if (!ns_per_call || !is_pow2(n) || reps == 0) return -1;
+  if ((kind == 1 || kind == 2 || kind == 3) && !unordered_args_ok(n, base_n)) return -1;
+  if (kind <= 2 && (algo < 0 || algo > 7)) return -1;
+  if (kind == 0 && log2u(n) > 10) return -1;
+  if (kind >= 4 && n < 2) return -1;
+  std::vector<c64> buf(n, c64{0.0, 0.0}), scratch(std::max(n, base_n) + 1);
+  for (size_t i = 0; i < n; ++i) buf[i] = c64{std::sin(0.1 * (double)i), std::cos(0.3 * (double)i)};
+  std::vector<c64> w, wi;
+  std::vector<double> f[4], t[4];
+  std::vector<size_t> indices;
+  std::vector<c64> mono;
+  if (kind == 0) {
+    w.assign(2 * n, c64{0, 0});
+    wi.assign(2 * n, c64{0, 0});
+    init_wt(radix_of(algo), n, w.data(), wi.data());
+  } else if (kind <= 2) {
+    w.assign(n + base_n, c64{0, 0});
+    wi.assign(n + base_n, c64{0, 0});
+    unordered_twiddles(n, base_n, radix_of(algo), w.data(), wi.data(), n + base_n);
+  } else if (kind == 3) {
+    mono.resize(n);
+    const double theta = -2.0 / (double)n;
+    for (size_t i = 0; i < n; ++i) {
+      double sn, cs;
+      sincospi64(theta * (double)i, &sn, &cs);
+      mono[i] = c64{cs, sn};
+    }
+    indices.resize(n);
+    for (size_t j = 0; j < n; ++j) indices[j] = oracle_bit_rev_twice_inv(log2u(n), log2u(base_n), j);
+  } else {
+    for (int k = 0; k < 4; ++k) {
+      f[k].assign(n, 0.0);
+      t[k].assign(n, 0.0);
+    }
+    for (size_t i = 0; i < n; ++i) {
+      f[0][i] = std::sin(0.1 * (double)i);
+      f[2][i] = std::cos(0.3 * (double)i);
+    }
+    f128_twiddles(n, t[0].data(), t[1].data(), t[2].data(), t[3].data());
+  }
+  const size_t mask = n - 1, ratio = n / (base_n ? base_n : n);
+  size_t degree = 0;
+  const auto t0 = std::chrono::steady_clock::now();
+  for (size_t r = 0; r < reps; ++r) {
+    switch (kind) {
+      case 0: ordered_transform(algo, true, n, buf.data(), scratch.data(), w.data() + n); break;
+      case 1: fwd_depth(n, buf.data(), w.data(), algo, base_n, scratch.data()); break;
+      case 2: inv_depth(n, buf.data(), wi.data(), n + base_n, algo, base_n, scratch.data()); break;
+      case 3:
+        degree = degree + 1 == n ? 0 : degree + 1;
+        if (ratio == 1) {
+          for (size_t i = 0; i < n; ++i) buf[i] = mono[(i * degree) & mask];
+        } else if (ratio == 2) {
+          for (size_t i = 0; i < n / 2; ++i) {
+            buf[i] = mono[((2 * i) * degree) & mask];
+            buf[i + n / 2] = mono[((2 * i + 1) * degree) & mask];
+          }
+        } else {
+          for (size_t j = 0; j < n; ++j) buf[j] = mono[(indices[j] * degree) & mask];
+        }
+        break;
+      case 4: f128_fwd(n, f[0].data(), f[1].data(), f[2].data(), f[3].data(), t[0].data(), t[1].data(), t[2].data(), t[3].data()); break;
+      default: f128_inv(n, f[0].data(), f[1].data(), f[2].data(), f[3].data(), t[0].data(), t[1].data(), t[2].data(), t[3].data()); break;
+    }
+    // every 16 calls, bring the values back to magnitude ~1 (an exact power-of-two
+    // scaling): repeated unnormalised transforms would otherwise overflow
+    if (kind <= 2 && (r & 15) == 15) {
+      double m = 0.0;
+      for (size_t i = 0; i < n; ++i) m = std::max(m, std::max(std::fabs(buf[i].re), std::fabs(buf[i].im)));
+      if (m > 0.0 && std::isfinite(m)) {
+        int e = 0;
+        std::frexp(m, &e);
+        for (size_t i = 0; i < n; ++i) buf[i] = c64{std::ldexp(buf[i].re, -e), std::ldexp(buf[i].im, -e)};
+      }
+    }
+  }
+  const auto t1 = std::chrono::steady_clock::now();
+  *ns_per_call = std::chrono::duration<double, std::nano>(t1 - t0).count() / (double)reps;
+  return 0;
 }
 
 }  // extern "C"

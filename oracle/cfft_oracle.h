@@ -103,6 +103,10 @@ int oracle_unordered_batch(int fwd, int base_algo, size_t n, size_t base_n, size
 int oracle_f128_batch(int fwd, size_t n, size_t count, double* re0, double* re1, double* im0, double* im1,
                       const double* t_re0, const double* t_re1, const double* t_im0, const double* t_im1,
                       int nthreads);
+/* single-threaded per-call CPU time of the restated reference (the reference's own
+ * benchmark cases): kind 0 ordered fwd, 1 unordered fwd, 2 unordered inv,
+ * 3 fwd_monomial, 4 fft128 fwd, 5 fft128 inv; `reps` calls on one buffer */
+int oracle_bench_call(int kind, int algo, size_t n, size_t base_n, size_t reps, double* ns_per_call);
 /* exact schoolbook products over a batch (words = 1: u64, words = 2: u128 as lo/hi u64 pairs), threaded */
 int oracle_schoolbook_batch(int words, size_t N, size_t count, const uint64_t* a, const int64_t* b, uint64_t* out,
                             int nthreads);

@@ -292,3 +292,16 @@ def schoolbook_batch(a, b, nthreads=0):
     out = np.zeros_like(a)
     _ok(lib().oracle_schoolbook_batch(words, S(N), S(b.size // N), P(a), P(b), P(out), nthreads))
     return out
+
+
+def bench_call(kind, n, algo=0, base_n=0, seconds=0.05):
+    """Single-threaded per-call CPU time (seconds) of the restated reference; see
+    oracle_bench_call in cfft_oracle.h for `kind`.  The repetition count grows until the
+    loop runs at least `seconds`."""
+    ns = ctypes.c_double()
+    reps = 1
+    while True:
+        _ok(lib().oracle_bench_call(int(kind), int(algo), S(n), S(base_n or n), S(reps), ctypes.byref(ns)))
+        if ns.value * reps * 1e-9 >= seconds or reps >= 1 << 24:
+            return ns.value * 1e-9
+        reps *= 4

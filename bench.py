@@ -1242,7 +1242,7 @@ def measure_serving(torch, cf, local, world, rate=20000.0, seconds=1.0, operand_
     t0 = time.perf_counter()
     srv = cf.serving.Server(eng, SERVE_SIZES, operand_bytes=operand_gb << 30, seed=seed)
     setup_s = time.perf_counter() - t0
-    srv.run(srv.config(rate=rate, duration_s=0.05))  # warm-up
+    srv.run(srv.config(rate=rate, duration_s=0.5))  # warm-up: a process's first runs show a longer tail
     record_every = 50
     cfg = srv.config(rate=rate, duration_s=seconds, record_every=record_every)
     with ClockSampler(local) as clk:
@@ -1256,6 +1256,10 @@ def measure_serving(torch, cf, local, world, rate=20000.0, seconds=1.0, operand_
         extra["batched_without_clusters"] = srv.run(srv.config(rate=rate, duration_s=seconds, cluster_log2N=32))
         extra["batched_staged_io"] = srv.run(srv.config(rate=rate, duration_s=seconds, staged_io=True))
         extra["batched_via_queue"] = srv.run(srv.config(rate=rate, duration_s=seconds, via_queue=True))
+        # the memory gate on a fixed stand-in budget instead of cudaMemGetInfo readings (its cost)
+        extra["batched_gate_without_readings"] = srv.run(srv.config(rate=rate, duration_s=seconds,
+                                                                    mem_free_override=1 << 50))
+        extra["batched_repeat"] = srv.run(srv.config(rate=rate, duration_s=seconds))  # the first run, again
         sweep = {}
         for r in (50000.0, 100000.0, 150000.0, 200000.0):
             st = srv.run(srv.config(rate=r, duration_s=0.5))

@@ -5,6 +5,7 @@
 #include <atomic>
 #include <mutex>
 #include <string>
+#include <unordered_map>
 #include <vector>
 
 #include "cfft_internal.h"
@@ -213,8 +214,18 @@ struct SpreadKey {
            smem == o.smem;
   }
 };
+struct SpreadKeyHash {
+  size_t operator()(const SpreadKey& k) const {
+    size_t h = std::hash<const void*>()(k.fn);
+    for (size_t v : {(size_t)k.grid, (size_t)k.block, (size_t)k.cluster, (size_t)k.dev, k.smem})
+      h = h * 0x9e3779b97f4a7c15ull + v;
+    return h;
+  }
+};
 std::mutex g_spread_mu;
-std::vector<std::pair<SpreadKey, size_t>> g_spread_cache;
+// launch shapes seen so far (one entry per kernel, grid, block, cluster, device and
+// shared-memory size); cleared when it reaches 65536 entries
+std::unordered_map<SpreadKey, size_t, SpreadKeyHash> g_spread_cache;
 
 size_t compute_spread(const void* fn, int grid, int block, int cluster, size_t smem, int dev) {
   const int nsm = sm_count();
@@ -262,12 +273,13 @@ size_t spread_smem(const void* fn, int grid, int block, int cluster, size_t smem
   const SpreadKey key{fn, grid, block, cluster, dev, smem};
   {
     std::lock_guard<std::mutex> lk(g_spread_mu);
-    for (const auto& e : g_spread_cache)
-      if (e.first == key) return e.second;
+    const auto it = g_spread_cache.find(key);
+    if (it != g_spread_cache.end()) return it->second;
   }
   const size_t v = compute_spread(fn, grid, block, cluster, smem, dev);
   std::lock_guard<std::mutex> lk(g_spread_mu);
-  if (g_spread_cache.size() < 4096) g_spread_cache.push_back({key, v});
+  if (g_spread_cache.size() >= 65536) g_spread_cache.clear();
+  g_spread_cache.emplace(key, v);
   return v;
 }
 

@@ -410,8 +410,8 @@ typedef struct cfft_serve_config {
                             each request submitted on arrival, its ticket polled */
   uint64_t mem_reserve_bytes; /* batched mode, device memory gate: the output bytes of admitted,
                                  unfinished requests stay within the device's free memory less
-                                 this reserve, read with cudaMemGetInfo at most once per
-                                 millisecond during the run (a request is always admitted when
+                                 this reserve, read with cudaMemGetInfo by a reader thread every
+                                 20 ms during the run (a request is always admitted when
                                  nothing is in flight, so the stream makes progress) */
   uint64_t mem_free_override; /* nonzero: stands in for cudaMemGetInfo's free bytes (tests) */
 } cfft_serve_config;

@@ -217,8 +217,8 @@ def run_reference(args):
     sample = 256 * threads  # large enough per step that thread start-up does not show in the rate
     a, b = make_inputs(sample, BASE_SEED)
     bhat = pyoracle.u64_prepare(N_POLY, algo, base, b)
-    for _ in range(args.warmup):
-        pyoracle.u64_product(N_POLY, algo, base, a[:threads], bhat[:threads], nthreads=threads)
+    for _ in range(args.warmup):  # full-size steps, so that caches and clocks settle as in the timed ones
+        pyoracle.u64_product(N_POLY, algo, base, a, bhat, nthreads=threads)
     t0 = time.perf_counter()
     for _ in range(args.steps):
         pyoracle.u64_product(N_POLY, algo, base, a, bhat, nthreads=threads)

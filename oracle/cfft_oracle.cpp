@@ -14,9 +14,13 @@
 #include "cfft_oracle.h"
 
 #include <algorithm>
+#include <atomic>
 #include <chrono>
 #include <cmath>
+#include <condition_variable>
 #include <cstring>
+#include <functional>
+#include <mutex>
 #include <thread>
 #include <vector>
 
@@ -925,6 +929,85 @@ void u128_product_one(const U128Pipeline& P, const uint64_t* a, const double* bh
   }
 }
 
+// A persistent pool of host threads for the batched calls (the CPU baseline runs
+// many short batches; starting threads per call cost milliseconds).  One parallel
+// region at a time: concurrent callers wait for the pool.  The work is cut into
+// chunks that the caller and the workers take from a shared counter.
+class HostPool {
+ public:
+  static HostPool& get() {
+    static HostPool pool;
+    return pool;
+  }
+  void run(size_t count, int nthreads, const std::function<void(size_t, size_t)>& f) {
+    std::lock_guard<std::mutex> region(region_mu_);
+    ensure_workers(nthreads - 1);
+    const size_t nchunks = std::min<size_t>(count, (size_t)nthreads * 4);
+    {
+      std::lock_guard<std::mutex> lk(mu_);
+      fn_ = &f;
+      count_ = count;
+      nchunks_ = nchunks;
+      next_.store(0);
+      active_ = (int)std::min<size_t>(workers_.size(), (size_t)nthreads - 1);
+      pending_ = active_;
+      ++generation_;
+    }
+    cv_.notify_all();
+    work();
+    std::unique_lock<std::mutex> lk(mu_);
+    done_cv_.wait(lk, [&] { return pending_ == 0; });
+    fn_ = nullptr;
+  }
+  ~HostPool() {
+    {
+      std::lock_guard<std::mutex> lk(mu_);
+      quit_ = true;
+    }
+    cv_.notify_all();
+    for (auto& t : workers_) t.join();
+  }
+
+ private:
+  void work() {
+    for (;;) {
+      const size_t c = next_.fetch_add(1);
+      if (c >= nchunks_) return;
+      const size_t b = count_ * c / nchunks_, e = count_ * (c + 1) / nchunks_;
+      if (b < e) (*fn_)(b, e);
+    }
+  }
+  void ensure_workers(int n) {
+    while ((int)workers_.size() < n) {
+      const int id = (int)workers_.size();
+      workers_.emplace_back([this, id] {
+        uint64_t seen = 0;
+        for (;;) {
+          {
+            std::unique_lock<std::mutex> lk(mu_);
+            cv_.wait(lk, [&] { return quit_ || generation_ != seen; });
+            if (quit_) return;
+            seen = generation_;
+            if (id >= active_) continue;
+          }
+          work();
+          std::lock_guard<std::mutex> lk(mu_);
+          if (--pending_ == 0) done_cv_.notify_all();
+        }
+      });
+    }
+  }
+  std::mutex region_mu_, mu_;
+  std::condition_variable cv_, done_cv_;
+  std::vector<std::thread> workers_;
+  const std::function<void(size_t, size_t)>* fn_ = nullptr;
+  size_t count_ = 0, nchunks_ = 0;
+  std::atomic<size_t> next_{0};
+  int active_ = 0, pending_ = 0;
+  uint64_t generation_ = 0;
+  bool quit_ = false;
+};
+
 template <class F>
 void parallel_for(size_t count, int nthreads, F f) {
   if (nthreads <= 0) nthreads = (int)std::max(1u, std::thread::hardware_concurrency());
@@ -933,14 +1016,8 @@ void parallel_for(size_t count, int nthreads, F f) {
     f(0, count);
     return;
   }
-  std::vector<std::thread> th;
-  const size_t per = (count + nthreads - 1) / nthreads;
-  for (int t = 0; t < nthreads; ++t) {
-    const size_t b = (size_t)t * per, e = std::min(count, b + per);
-    if (b >= e) break;
-    th.emplace_back([=] { f(b, e); });
-  }
-  for (auto& t : th) t.join();
+  const std::function<void(size_t, size_t)> fn = f;
+  HostPool::get().run(count, nthreads, fn);
 }
 
 // ------------------------------------------------ rand 0.8 StdRng restatement

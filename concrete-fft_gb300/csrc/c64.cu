@@ -268,9 +268,9 @@ cfft_status launch_split(const C64Plan& p, bool fwd, int ls, int mode, long nsub
   const size_t part = p.n >> ls;
   const size_t smem = 2 * part * sizeof(double2);
   // one thread per butterfly of a pass over the part (more would idle at the barriers);
-  // two for the DIF radix-2/4 algorithms, whose passes split each butterfly into halves
+  // two for the DIF algorithms, whose passes split each butterfly into halves
   const int R = algo_radix(p.base_algo);
-  const bool halves = (p.base_algo & 1) == 0 && R <= 4;
+  const bool halves = (p.base_algo & 1) == 0;
   const int threads = (int)std::min<size_t>(256, std::max<size_t>(32, (halves ? 2 : 1) * part / (size_t)R));
   DevLevels L = p.dlv;
   const double2* w = fwd ? p.d_w : p.d_winv;

@@ -237,11 +237,11 @@ struct Core<16, FWD, E> {  // src/dif16.rs:650-779
   }
 };
 
-// Half of a radix-2 or radix-4 core: the outputs k with k % 2 == H, by the
-// same operations on the same operands as Core<R> (whose other outputs use
-// disjoint intermediate values, so no operation is repeated).  Two threads
-// then share one butterfly, which doubles the threads a pass can use.
-// y[j] = output 2j + H.
+// Half of a radix-R core: the outputs k with k % 2 == H, by the same
+// operations on the same operands as Core<R>.  The even outputs depend only on
+// the sums x_k + x_{k+R/2} and the odd outputs only on the differences, so no
+// operation is repeated.  Two threads then share one butterfly, which doubles
+// the threads a pass can use.  y[j] = output 2j + H.
 template <int R, bool FWD, int H>
 struct CoreHalf;
 
@@ -267,6 +267,121 @@ struct CoreHalf<4, FWD, 1> {
     const c64 jbmd = mul_j<FWD>(csub(x[1], x[3]));
     y[0] = csub(amc, jbmd);
     y[1] = cadd(amc, jbmd);
+  }
+};
+
+// Radix 8: the even outputs use the sums x_k + x_{k+4}, the odd outputs the
+// differences (src/dif8.rs:311-352, as Core<8>).
+template <bool FWD>
+struct CoreHalf<8, FWD, 0> {
+  __device__ __forceinline__ static void run(const c64* x, c64* y) {
+    const c64 a04 = cadd(x[0], x[4]);
+    const c64 a26 = cadd(x[2], x[6]);
+    const c64 a15 = cadd(x[1], x[5]);
+    const c64 a37 = cadd(x[3], x[7]);
+    const c64 a04_p1_a26 = cadd(a04, a26);
+    const c64 a04_m1_a26 = csub(a04, a26);
+    const c64 a15_p1_a37 = cadd(a15, a37);
+    const c64 j_a15_m1_a37 = mul_j<FWD>(csub(a15, a37));
+    y[0] = cadd(a04_p1_a26, a15_p1_a37);
+    y[1] = csub(a04_m1_a26, j_a15_m1_a37);
+    y[2] = csub(a04_p1_a26, a15_p1_a37);
+    y[3] = cadd(a04_m1_a26, j_a15_m1_a37);
+  }
+};
+
+template <bool FWD>
+struct CoreHalf<8, FWD, 1> {
+  __device__ __forceinline__ static void run(const c64* x, c64* y) {
+    const c64 s04 = csub(x[0], x[4]);
+    const c64 js26 = mul_j<FWD>(csub(x[2], x[6]));
+    const c64 s15 = csub(x[1], x[5]);
+    const c64 js37 = mul_j<FWD>(csub(x[3], x[7]));
+    const c64 s04_mj_s26 = csub(s04, js26);
+    const c64 s04_pj_s26 = cadd(s04, js26);
+    const c64 w8_s15_mj_s37 = mul_exp_neg_pi_over_8<FWD>(csub(s15, js37));
+    const c64 v8_s15_pj_s37 = mul_exp_pi_over_8<FWD>(cadd(s15, js37));
+    y[0] = cadd(s04_mj_s26, w8_s15_mj_s37);
+    y[1] = csub(s04_pj_s26, v8_s15_pj_s37);
+    y[2] = csub(s04_mj_s26, w8_s15_mj_s37);
+    y[3] = cadd(s04_pj_s26, v8_s15_pj_s37);
+  }
+};
+
+// Radix 16 (src/dif16.rs:650-779, as Core<16>): the even outputs use the sums
+// x_k + x_{k+8}, the odd outputs the differences.
+template <bool FWD>
+struct CoreHalf<16, FWD, 0> {
+  __device__ __forceinline__ static void run(const c64* x, c64* y) {
+    const c64 a08 = cadd(x[0], x[8]), a4c = cadd(x[4], x[12]);
+    const c64 a2a = cadd(x[2], x[10]), a6e = cadd(x[6], x[14]);
+    const c64 a19 = cadd(x[1], x[9]), a5d = cadd(x[5], x[13]);
+    const c64 a3b = cadd(x[3], x[11]), a7f = cadd(x[7], x[15]);
+    const c64 a08p1a4c = cadd(a08, a4c), a08m1a4c = csub(a08, a4c);
+    const c64 a2ap1a6e = cadd(a2a, a6e), a2am1a6e = csub(a2a, a6e);
+    const c64 a19p1a5d = cadd(a19, a5d), a19m1a5d = csub(a19, a5d);
+    const c64 a3bp1a7f = cadd(a3b, a7f), a3bm1a7f = csub(a3b, a7f);
+    const c64 j_a2am1a6e = mul_j<FWD>(a2am1a6e);
+    const c64 e0 = cadd(a08p1a4c, a2ap1a6e);
+    const c64 e2 = csub(a08m1a4c, j_a2am1a6e);
+    const c64 e4 = csub(a08p1a4c, a2ap1a6e);
+    const c64 e6 = cadd(a08m1a4c, j_a2am1a6e);
+    const c64 j_a3bm1a7f = mul_j<FWD>(a3bm1a7f);
+    const c64 f0 = cadd(a19p1a5d, a3bp1a7f);
+    const c64 f2 = csub(a19m1a5d, j_a3bm1a7f);
+    const c64 f4 = csub(a19p1a5d, a3bp1a7f);
+    const c64 f6 = cadd(a19m1a5d, j_a3bm1a7f);
+    const c64 w8 = mul_exp_neg_pi_over_8<FWD>(f2);
+    const c64 j4 = mul_j<FWD>(f4);
+    const c64 v8 = mul_exp_pi_over_8<FWD>(f6);
+    y[0] = cadd(e0, f0);
+    y[1] = cadd(e2, w8);
+    y[2] = csub(e4, j4);
+    y[3] = csub(e6, v8);
+    y[4] = csub(e0, f0);
+    y[5] = csub(e2, w8);
+    y[6] = cadd(e4, j4);
+    y[7] = cadd(e6, v8);
+  }
+};
+
+template <bool FWD>
+struct CoreHalf<16, FWD, 1> {
+  __device__ __forceinline__ static void run(const c64* x, c64* y) {
+    const c64 s08 = csub(x[0], x[8]), s4c = csub(x[4], x[12]);
+    const c64 s2a = csub(x[2], x[10]), s6e = csub(x[6], x[14]);
+    const c64 s19 = csub(x[1], x[9]), s5d = csub(x[5], x[13]);
+    const c64 s3b = csub(x[3], x[11]), s7f = csub(x[7], x[15]);
+    const c64 js4c = mul_j<FWD>(s4c), js6e = mul_j<FWD>(s6e);
+    const c64 js5d = mul_j<FWD>(s5d), js7f = mul_j<FWD>(s7f);
+    const c64 s08mjs4c = csub(s08, js4c), s08pjs4c = cadd(s08, js4c);
+    const c64 s2amjs6e = csub(s2a, js6e), s2apjs6e = cadd(s2a, js6e);
+    const c64 s19mjs5d = csub(s19, js5d), s19pjs5d = cadd(s19, js5d);
+    const c64 s3bmjs7f = csub(s3b, js7f), s3bpjs7f = cadd(s3b, js7f);
+    const c64 w8_s2amjs6e = mul_exp_neg_pi_over_8<FWD>(s2amjs6e);
+    const c64 v8_s2apjs6e = mul_exp_pi_over_8<FWD>(s2apjs6e);
+    const c64 e1 = cadd(s08mjs4c, w8_s2amjs6e);
+    const c64 e3 = csub(s08pjs4c, v8_s2apjs6e);
+    const c64 e5 = csub(s08mjs4c, w8_s2amjs6e);
+    const c64 e7 = cadd(s08pjs4c, v8_s2apjs6e);
+    const c64 w8_s3bmjs7f = mul_exp_neg_pi_over_8<FWD>(s3bmjs7f);
+    const c64 v8_s3bpjs7f = mul_exp_pi_over_8<FWD>(s3bpjs7f);
+    const c64 f1 = cadd(s19mjs5d, w8_s3bmjs7f);
+    const c64 f3 = csub(s19pjs5d, v8_s3bpjs7f);
+    const c64 f5 = csub(s19mjs5d, w8_s3bmjs7f);
+    const c64 f7 = cadd(s19pjs5d, v8_s3bpjs7f);
+    const c64 h1 = mul_exp_pi_over_16<FWD>(f1);
+    const c64 h3 = mul_exp_17pi_over_16<FWD>(f3);
+    const c64 hd = mul_exp_17pi_over_16<!FWD>(f5);
+    const c64 hf = mul_exp_pi_over_16<!FWD>(f7);
+    y[0] = cadd(e1, h1);
+    y[1] = cadd(e3, h3);
+    y[2] = csub(e5, hd);
+    y[3] = csub(e7, hf);
+    y[4] = csub(e1, h1);
+    y[5] = csub(e3, h3);
+    y[6] = cadd(e5, hd);
+    y[7] = cadd(e7, hf);
   }
 };
 

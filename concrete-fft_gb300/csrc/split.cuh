@@ -53,13 +53,13 @@ __device__ __forceinline__ FlatBuf dif_after_first(int log2n, int ls, FlatBuf x,
   const int log2c = log2n - ls;
   FlatBuf cur = x, oth = y;
   for (int i = 1; i < npass; ++i) {
-    stockham_pass<R, FWD, false, 0>(log2c, i * LR - ls, 1, cur, oth, wb, tid, nth, ls);
+    stockham_pass<R, FWD, false, 0, true>(log2c, i * LR - ls, 1, cur, oth, wb, tid, nth, ls);
     __syncthreads();
     const FlatBuf t = cur;
     cur = oth;
     oth = t;
   }
-  end_dispatch<R, FWD, 0>(lm, log2c, 1, cur, tid, nth);
+  end_dispatch<R, FWD, 0, true>(lm, log2c, 1, cur, tid, nth);
   __syncthreads();
   return cur;
 }
@@ -138,7 +138,7 @@ __device__ __forceinline__ void level0_last(double2* g, int lm, double2* const* 
 // butterflies [c*per, (c+1)*per) in full -- no output is computed twice --
 // reading their inputs from global memory, and stores each output into the
 // part of its residue class mod S (distributed shared memory), compacted.
-// With twice as many threads as butterflies (a multiple of 32), radix 2 and 4
+// With twice as many threads as butterflies (a multiple of 32), the
 // butterflies are split into halves as in stockham_pass.
 template <int R, bool FWD, int LS>
 __device__ __forceinline__ void dif_first_scatter(const double2* g, int lper, int c, double2* const* part,
@@ -147,7 +147,7 @@ __device__ __forceinline__ void dif_first_scatter(const double2* g, int lper, in
   constexpr int S = 1 << LS;
   const int per = (1 << lper) >> LS;
   const int p0 = c * per;
-  if constexpr (R == 2 || R == 4) {
+  {
     if (nth >= 2 * per && (per & 31) == 0) {
       if (tid < 2 * per) {
         const int h = tid >= per ? 1 : 0;

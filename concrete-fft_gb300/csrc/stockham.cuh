@@ -52,20 +52,21 @@ struct CtaSync {
 // times larger, compacted (see split.cuh); its twiddles are those of the full
 // transform's stride s * 2^twlog.  0 for a whole transform.
 //
-// Half butterflies: when the CTA has at least twice as many threads as the
-// pass has butterflies (a multiple of 32), a DIF radix-2/4 pass gives each
+// Half butterflies (HALF, compiled into the split kernels only): when the CTA
+// has at least twice as many threads as the pass has butterflies (a multiple
+// of 32), a DIF pass gives each
 // butterfly two threads, the first `total` threads computing its even outputs
 // and the next `total` its odd ones (CoreHalf: the same operations, none
 // repeated), so whole warps take one half.  Twiddles multiply the outputs
 // after the core, so each half twiddles its own.
-template <int R, bool FWD, bool DIT, int E, class B>
+template <int R, bool FWD, bool DIT, int E, bool HALF = false, class B>
 __device__ __forceinline__ void stockham_pass(int log2n, int log2s, int nchunks, B src, B dst,
                                               const double2* __restrict__ w, int tid, int nth, int twlog = 0) {
   constexpr int LR = Log2<R>::v;
   const int lper = log2n - LR;  // log2(n / R): butterflies per chunk
   const int total = nchunks << lper;
   const int smask = (1 << log2s) - 1;
-  if constexpr (!DIT && E == 0 && (R == 2 || R == 4)) {
+  if constexpr (HALF && !DIT && E == 0) {
     if (nth >= 2 * total && (total & 31) == 0) {
       if (tid < 2 * total) {
         const int h = tid >= total ? 1 : 0;
@@ -122,16 +123,16 @@ __device__ __forceinline__ void stockham_pass(int log2n, int log2s, int nchunks,
 }
 
 // End butterfly of size M at stride n/M, in place (src/dif4.rs:195-244 and twins).
-// Radix 2 and 4 split into half butterflies as stockham_pass does; being in
+// It splits into half butterflies as stockham_pass does; being in
 // place, every half loads its inputs before a CTA barrier and stores after it
 // (every thread of the CTA calls this function).
-template <int M, bool FWD, int E, class B>
+template <int M, bool FWD, int E, bool HALF = false, class B>
 __device__ __forceinline__ void end_pass(int log2n, int nchunks, B x, int tid, int nth) {
   constexpr int LM = Log2<M>::v;
   const int log2s = log2n - LM;
   const int total = nchunks << log2s;
   const int smask = (1 << log2s) - 1;
-  if constexpr (E == 0 && (M == 2 || M == 4)) {
+  if constexpr (HALF && E == 0) {
     if (nth >= 2 * total && (total & 31) == 0) {
       const bool act = tid < 2 * total;
       const int h = tid >= total ? 1 : 0;
@@ -164,17 +165,17 @@ __device__ __forceinline__ void end_pass(int log2n, int nchunks, B x, int tid, i
   }
 }
 
-template <int R, bool FWD, int E, class B>
+template <int R, bool FWD, int E, bool HALF = false, class B>
 __device__ __forceinline__ void end_dispatch(int lm, int log2n, int nchunks, B x, int tid, int nth) {
-  if (lm == 1) end_pass<2, FWD, E>(log2n, nchunks, x, tid, nth);
+  if (lm == 1) end_pass<2, FWD, E, HALF>(log2n, nchunks, x, tid, nth);
   if constexpr (R >= 4) {
-    if (lm == 2) end_pass<4, FWD, E>(log2n, nchunks, x, tid, nth);
+    if (lm == 2) end_pass<4, FWD, E, HALF>(log2n, nchunks, x, tid, nth);
   }
   if constexpr (R >= 8) {
-    if (lm == 3) end_pass<8, FWD, E>(log2n, nchunks, x, tid, nth);
+    if (lm == 3) end_pass<8, FWD, E, HALF>(log2n, nchunks, x, tid, nth);
   }
   if constexpr (R >= 16) {
-    if (lm == 4) end_pass<16, FWD, E>(log2n, nchunks, x, tid, nth);
+    if (lm == 4) end_pass<16, FWD, E, HALF>(log2n, nchunks, x, tid, nth);
   }
 }
 

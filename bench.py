@@ -361,11 +361,21 @@ def run_gb300(args):
         for i in range(sample):
             plan.product_unfused(a[i:i + 1], bhat[i:i + 1], out_plain[i:i + 1], z[i:i + 1])
     ms_pp, _ = timed(torch, per_product, 2, 1, local, world)
+    # device time of one product (20 calls in a CUDA graph): the automatic path (a cluster of
+    # CTAs on the base's residue classes), one CTA, the five launches
+    one_dev = {"auto": graph_device_us(torch, lambda: plan.product(a1, bh1, o1))}
+    plan.set_cluster_size(1)
+    one_dev["one_cta"] = graph_device_us(torch, lambda: plan.product(a1, bh1, o1))
+    plan.set_cluster_size(0)
+    one_dev["five_launches"] = graph_device_us(torch, lambda: plan.product_unfused(a1, bh1, o1, z1))
     plain = {"batched_5_launches_products_per_s": world * count * plain_steps / (ms_pb * 1e-3),
              "per_product_5_launches_products_per_s": world * sample * 2 / (ms_pp * 1e-3),
              "per_product_sample": sample, "matches_fused_result": plain_ok,
              "one_product_us": round(ms_one_auto * 1e3 / 50, 2), "one_product_us_fused": round(ms_one * 1e3 / 50, 2),
-             "one_product_us_5_launches": round(ms_one_u * 1e3 / 50, 2)}
+             "one_product_us_5_launches": round(ms_one_u * 1e3 / 50, 2),
+             "one_product_device_us": {k: round(v, 2) for k, v in one_dev.items()},
+             "one_product_note": "one_product_us*: 50 calls from Python between CUDA events (host launch cost "
+                                 "included); one_product_device_us: 20 calls in a CUDA graph"}
 
     # end to end: pinned host A in, pinned host result out, through the C ABI host entry point
     # (A crosses by copy; the kernels store the results into the page-locked `hout` over the link)
@@ -513,6 +523,28 @@ def timed(torch, fn, steps, warmup, local, world):
         clk.mark(t0, time.time())
     from concrete_fft import replicas
     return replicas.max_over_ranks(e0.elapsed_time(e1), "cuda"), clk.summary()
+
+
+def graph_device_us(torch, call, calls=20, replays=10):
+    """Device time of one call: `calls` calls captured in a CUDA graph, replayed `replays`
+    times between CUDA events (no host launch cost between the calls)."""
+    call()  # outside the capture: one-time kernel attributes and launch shapes
+    torch.cuda.synchronize()
+    graph = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(graph):
+        for _ in range(calls):
+            call()
+    graph.replay()
+    torch.cuda.synchronize()
+    stream = torch.cuda.current_stream()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(replays):
+        graph.replay()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    return e0.elapsed_time(e1) * 1e3 / (calls * replays)
 
 
 def fp64_rates(cf):

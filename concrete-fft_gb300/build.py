@@ -21,7 +21,7 @@ CSRC = os.path.join(PKG, "csrc")
 BUILD = os.path.join(PKG, "_build")
 LIB = os.path.join(PKG, "lib", "libcfft_gb300.so")
 
-CUDA_SOURCES = ["c64.cu", "product_u64.cu", "f128.cu", "runtime.cu", "batch.cu", "product_engine.cu", "server.cu", "queue.cu", "kinst_c64_e0.cu", "kinst_c64_emu.cu", "kinst_prod_e0.cu", "kinst_prod_emu.cu", "kinst_split_01.cu", "kinst_split_23.cu", "kinst_split_45.cu", "kinst_split_67.cu", "kinst_split_prod_0123.cu", "kinst_split_prod_4567.cu"]
+CUDA_SOURCES = ["c64.cu", "product_u64.cu", "f128.cu", "runtime.cu", "batch.cu", "product_engine.cu", "server.cu", "queue.cu", "kinst_c64_e0.cu", "kinst_c64_emu.cu", "kinst_prod_e0.cu", "kinst_prod_emu.cu", "kinst_split_01.cu", "kinst_split_23.cu", "kinst_split_45.cu", "kinst_split_67.cu", "kinst_split_prod_01.cu", "kinst_split_prod_23.cu", "kinst_split_prod_45.cu", "kinst_split_prod_67.cu"]
 CXX_SOURCES = ["twiddles.cpp", "tune_cache.cpp"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 

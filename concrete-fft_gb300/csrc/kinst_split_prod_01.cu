@@ -1,0 +1,20 @@
+// u64 products split over a cluster (split_product.cuh) for base algorithms
+// 0 and 1; one translation unit per pair so that they compile in parallel.
+#include "split_product.cuh"
+
+namespace cfft {
+const void* u64_product_split_ptr_01(int algo, int ls, bool big) {
+  switch (algo) {
+    case 0: return split_product_ptr<0>(ls, big);
+    case 1: return split_product_ptr<1>(ls, big);
+    default: return nullptr;
+  }
+}
+const void* u64_product_split0_ptr_01(int algo, int ls) {
+  switch (algo) {
+    case 0: return split0_product_ptr<0>(ls);
+    case 1: return split0_product_ptr<1>(ls);
+    default: return nullptr;
+  }
+}
+}  // namespace cfft

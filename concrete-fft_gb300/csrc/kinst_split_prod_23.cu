@@ -1,0 +1,20 @@
+// u64 products split over a cluster (split_product.cuh) for base algorithms
+// 2 and 3; one translation unit per pair so that they compile in parallel.
+#include "split_product.cuh"
+
+namespace cfft {
+const void* u64_product_split_ptr_23(int algo, int ls, bool big) {
+  switch (algo) {
+    case 2: return split_product_ptr<2>(ls, big);
+    case 3: return split_product_ptr<3>(ls, big);
+    default: return nullptr;
+  }
+}
+const void* u64_product_split0_ptr_23(int algo, int ls) {
+  switch (algo) {
+    case 2: return split0_product_ptr<2>(ls);
+    case 3: return split0_product_ptr<3>(ls);
+    default: return nullptr;
+  }
+}
+}  // namespace cfft

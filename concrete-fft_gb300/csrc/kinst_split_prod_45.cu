@@ -1,0 +1,20 @@
+// u64 products split over a cluster (split_product.cuh) for base algorithms
+// 4 and 5; one translation unit per pair so that they compile in parallel.
+#include "split_product.cuh"
+
+namespace cfft {
+const void* u64_product_split_ptr_45(int algo, int ls, bool big) {
+  switch (algo) {
+    case 4: return split_product_ptr<4>(ls, big);
+    case 5: return split_product_ptr<5>(ls, big);
+    default: return nullptr;
+  }
+}
+const void* u64_product_split0_ptr_45(int algo, int ls) {
+  switch (algo) {
+    case 4: return split0_product_ptr<4>(ls);
+    case 5: return split0_product_ptr<5>(ls);
+    default: return nullptr;
+  }
+}
+}  // namespace cfft

@@ -217,8 +217,7 @@ cfft_status launch_split_product(const cfft_u64_product_plan* plan, int ls, cons
                                  const cfft_product_item* items = nullptr, int terms = 1) {
   const size_t part = plan->n >> ls;
   const bool big = part > 2048;  // 4096 points per CTA: one CTA per SM, 512 threads
-  const void* fn = plan->base_algo < 4 ? u64_product_split_ptr_0123(plan->base_algo, ls, big)
-                                       : u64_product_split_ptr_4567(plan->base_algo, ls, big);
+  const void* fn = u64_product_split_ptr(plan->base_algo, ls, big);
   const size_t smem = 2 * (plan->n >> ls) * sizeof(double2);
   if ((count << ls) > 0x7fffffffUL) return fail(CFFT_ERR_INVALID_SIZE, "batch too large");
   DevLevels L = plan->dlv;
@@ -229,7 +228,52 @@ cfft_status launch_split_product(const cfft_u64_product_plan* plan, int ls, cons
   // 128 threads (several CTAs per SM) for parts up to 1024 points, 256 for 2048
   // (shared memory allows 3 CTAs per SM), 512 for 4096 (one CTA per SM)
   const int threads = part <= 1024 ? 128 : (part <= 2048 ? kSplitProdThreads : kSplitProdThreadsBig);
-  return launch_kernel_cluster(fn, (int)(count << ls), threads, 1 << ls, args, smem, stream);
+  const int grid = (int)(count << ls);
+  return launch_kernel_cluster(fn, grid, threads, 1 << ls, args, spread_smem(fn, grid, threads, 1 << ls, smem),
+                               stream);
+}
+
+// CTAs per product as a log2 for plans without an outer level (n = base_n;
+// u64_product_split0_kernel): S <= the base radix R and S <= 8, with at least
+// 64 points per CTA.  `fast` also keeps at least 32 butterflies in each of a
+// class's passes (64 for DIT, one thread per butterfly): with fewer, a lone
+// product measured slower than on fewer CTAs (N = 2048, Dif8: 23.4 us on 8
+// CTAs, 16.0 on 4; Dif16: 36.8 on 8, 25.0 on 2; Dit16 on 2: 45.9 against
+// 39.8 for the five launches).  0 when the plan has levels or no S >= 2 fits.
+int split0_log2(const cfft_u64_product_plan* p, bool fast = true) {
+  if (p->lv.nlevels != 0) return 0;
+  const int lr = p->base_algo / 2 + 1;
+  const int log2n = ilog2(p->n);
+  const int min_lb = !fast ? 0 : ((p->base_algo & 1) ? 6 : 5);
+  int ls = std::min(3, lr);
+  while (ls > 0 && (log2n - ls < 6 || log2n - ls - lr < min_lb)) --ls;
+  return ls;
+}
+
+cfft_status launch_split0_product(const cfft_u64_product_plan* plan, int ls, const uint64_t* a, const double* bhat,
+                                  size_t bhat_stride, uint64_t* out, size_t count, cudaStream_t stream,
+                                  const cfft_product_item* items = nullptr) {
+  const int algo = plan->base_algo;
+  const void* fn = u64_product_split0_ptr(algo, ls);
+  if (!fn) return fail(CFFT_ERR_INVALID_SIZE, "no cluster product kernel for this base and cluster size");
+  if ((count << ls) > 0x7fffffffUL) return fail(CFFT_ERR_INVALID_SIZE, "batch too large");
+  const size_t part = plan->n >> ls;
+  const size_t radix = size_t(2) << (algo / 2);
+  // DIF: two threads per butterfly of a pass (half butterflies), DIT: one; at
+  // least a thread per two points for the elementwise steps (radix 16 has few
+  // butterflies per pass)
+  const size_t pass_threads = ((algo & 1) ? 1 : 2) * part / radix;
+  const int threads = (int)std::min<size_t>(256, std::max<size_t>(32, std::max(pass_threads, part / 2)));
+  const size_t smem = 3 * part * sizeof(double2);
+  const int grid = (int)(count << ls);
+  DevLevels L = plan->dlv;
+  long stride = (long)bhat_stride;
+  const double2* bh = (const double2*)bhat;
+  void* args[] = {(void*)&a, (void*)&bh, &stride, (void*)&out, (void*)&items, &L, (void*)&plan->d_w,
+                  (void*)&plan->d_winv, (void*)&plan->d_tw, (void*)&plan->d_itw};
+  // a few products: every CTA on an SM of its own
+  return launch_kernel_cluster(fn, grid, threads, 1 << ls, args, spread_smem(fn, grid, threads, 1 << ls, smem),
+                               stream);
 }
 
 }  // namespace
@@ -237,7 +281,8 @@ cfft_status launch_split_product(const cfft_u64_product_plan* plan, int ls, cons
 // Products given as device items (all of the plan's N) on the largest cluster
 // the plan allows, for latency: the serving loop's large products.
 bool cfft::u64_product_splittable(const cfft_u64_product_plan* plan) {
-  const int max_ls = plan->lv.nlevels >= 1 ? std::min(3, plan->lv.log2r[0]) : 0;
+  if (plan->lv.nlevels == 0) return split0_log2(plan) >= 1;
+  const int max_ls = std::min(3, plan->lv.log2r[0]);
   const int min_ls = std::max(0, ilog2(plan->n) - kSmemLog2Max);
   return max_ls >= 1 && min_ls <= max_ls;
 }
@@ -246,6 +291,9 @@ cfft_status cfft::u64_product_split_items(const cfft_u64_product_plan* plan, con
                                           size_t count, void* stream) {
   if (!u64_product_splittable(plan)) return fail(CFFT_ERR_INVALID_SIZE, "product size cannot be split over a cluster");
   if (count == 0) return CFFT_OK;
+  if (plan->lv.nlevels == 0)
+    return launch_split0_product(plan, split0_log2(plan), nullptr, nullptr, 0, nullptr, count, (cudaStream_t)stream,
+                                 items);
   const int max_ls = std::min(3, plan->lv.log2r[0]);
   return launch_split_product(plan, max_ls, nullptr, nullptr, 0, nullptr, count, (cudaStream_t)stream, items);
 }
@@ -437,10 +485,18 @@ cfft_status cfft_u64_product(const cfft_u64_product_plan* plan, const uint64_t* 
   // (no cluster holds it), and large batches of N >= 32768, where it measured faster
   // than one cluster per product (304 vs 280 k products/s at 32768, 129 vs 102 k at 65536)
   const bool many = (long)count >= (long)sm_count() / 2 && plan->cluster == 0;
-  // A few products whose transform has no outer level (n = base_n), so no cluster
-  // can split the fused kernel, also take the five launches: their transforms
-  // split over 2-8 CTAs each, and the launches follow one another without gaps
-  // (one product at N = 2048, base 1024: 20 vs 31 us; 76 products: 26 vs 31 us)
+  // Fewer than SMs/2 products whose transform has no outer level (n = base_n): one
+  // cluster per product on the base's residue classes (u64_product_split0_kernel), as
+  // does a plan forced to a cluster size.  Device time per call at N = 2048, Dif4, 4
+  // CTAs: 11.7 us for one product (one CTA: 32.2, the five launches: 13.7), 16.7 for
+  // 38 (one CTA: 34.9, five launches: 19.4)
+  if (plan->cluster >= 2 && split0_log2(plan, false) >= 1)
+    return launch_split0_product(plan, std::min(split0_log2(plan, false), ilog2((size_t)plan->cluster)), a, bhat,
+                                 bhat_stride, out, count, (cudaStream_t)stream);
+  if (plan->cluster == 0 && plan->N >= 512 && !many && split0_log2(plan) >= 1)
+    return launch_split0_product(plan, split0_log2(plan), a, bhat, bhat_stride, out, count, (cudaStream_t)stream);
+  // otherwise (no cluster kernel for the base) the five launches, whose transforms
+  // split over 2-8 CTAs each
   const bool few_unsplit = ls == 0 && plan->cluster == 0 && plan->N >= 2048 && !many;
   // Fewer than SMs/4 products of N = 4096 or 8192 as well (one product: 34 vs 37 us at
   // 4096, 37 vs 39 us at 8192; from SMs/4 products of N = 8192 the cluster kernel is faster)

@@ -134,49 +134,47 @@ __device__ __forceinline__ void level0_last(double2* g, int lm, double2* const* 
   }
 }
 
-// The first (s = 1) pass of a DIF transform over its cluster: CTA c takes the
-// butterflies [c*per, (c+1)*per) in full -- no output is computed twice --
-// reading their inputs from global memory, and stores each output into the
-// part of its residue class mod S (distributed shared memory), compacted.
-// With twice as many threads as butterflies (a multiple of 32), the
-// butterflies are split into halves as in stockham_pass.
-template <int R, bool FWD, int LS>
-__device__ __forceinline__ void dif_first_scatter(const double2* g, int lper, int c, double2* const* part,
-                                                  const double2* __restrict__ wb, int tid, int nth) {
+// The first (s = 1) pass of a DIF transform over its cluster, for `per`
+// butterflies: butterfly b is p = p0 + b * pstep, load(k, b, p) gives its
+// input k (of R), and each output (p*R + k) is stored into the part of its
+// residue class mod S (distributed shared memory), compacted.  With twice as
+// many threads as butterflies (a multiple of 32), the butterflies are split
+// into halves as in stockham_pass.
+template <int R, bool FWD, int LS, class Load>
+__device__ __forceinline__ void first_pass_scatter(Load load, int per, int p0, int pstep, double2* const* part,
+                                                   const double2* __restrict__ wb, int tid, int nth) {
   constexpr int LR = Log2<R>::v;
   constexpr int S = 1 << LS;
-  const int per = (1 << lper) >> LS;
-  const int p0 = c * per;
-  {
-    if (nth >= 2 * per && (per & 31) == 0) {
-      if (tid < 2 * per) {
-        const int h = tid >= per ? 1 : 0;
-        const int p = p0 + tid - h * per;
-        c64 v[R];
+  if (nth >= 2 * per && (per & 31) == 0) {
+    if (tid < 2 * per) {
+      const int h = tid >= per ? 1 : 0;
+      const int b = tid - h * per;
+      const int p = p0 + b * pstep;
+      c64 v[R];
 #pragma unroll
-        for (int k = 0; k < R; ++k) v[k] = ld(g + (k << lper) + p);
-        const double2* tw = wb + (p << LR);
-        c64 y[R / 2];
-        if (h == 0) {
-          CoreHalf<R, FWD, 0>::run(v, y);
-          st(part[0] + ((p << LR) >> LS), y[0]);
+      for (int k = 0; k < R; ++k) v[k] = load(k, b, p);
+      const double2* tw = wb + (p << LR);
+      c64 y[R / 2];
+      if (h == 0) {
+        CoreHalf<R, FWD, 0>::run(v, y);
+        st(part[0] + ((p << LR) >> LS), y[0]);
 #pragma unroll
-          for (int j = 1; j < R / 2; ++j)
-            st(part[(2 * j) & (S - 1)] + (((p << LR) + 2 * j) >> LS), cmul(ldg(tw + 2 * j), y[j]));
-        } else {
-          CoreHalf<R, FWD, 1>::run(v, y);
+        for (int j = 1; j < R / 2; ++j)
+          st(part[(2 * j) & (S - 1)] + (((p << LR) + 2 * j) >> LS), cmul(ldg(tw + 2 * j), y[j]));
+      } else {
+        CoreHalf<R, FWD, 1>::run(v, y);
 #pragma unroll
-          for (int j = 0; j < R / 2; ++j)
-            st(part[(2 * j + 1) & (S - 1)] + (((p << LR) + 2 * j + 1) >> LS), cmul(ldg(tw + 2 * j + 1), y[j]));
-        }
+        for (int j = 0; j < R / 2; ++j)
+          st(part[(2 * j + 1) & (S - 1)] + (((p << LR) + 2 * j + 1) >> LS), cmul(ldg(tw + 2 * j + 1), y[j]));
       }
-      return;
     }
+    return;
   }
-  for (int p = p0 + tid; p < p0 + per; p += nth) {
+  for (int b = tid; b < per; b += nth) {
+    const int p = p0 + b * pstep;
     c64 v[R];
 #pragma unroll
-    for (int k = 0; k < R; ++k) v[k] = ld(g + (k << lper) + p);
+    for (int k = 0; k < R; ++k) v[k] = load(k, b, p);
     Core<R, FWD, 0>::run(v);
     const double2* tw = wb + (p << LR);
 #pragma unroll
@@ -185,6 +183,17 @@ __device__ __forceinline__ void dif_first_scatter(const double2* g, int lper, in
       st(part[k & (S - 1)] + (((p << LR) + k) >> LS), o);
     }
   }
+}
+
+// The first pass of a DIF transform held in global memory: CTA c takes the
+// butterflies [c*per, (c+1)*per) in full -- no output is computed twice --
+// reading their inputs from g.
+template <int R, bool FWD, int LS>
+__device__ __forceinline__ void dif_first_scatter(const double2* g, int lper, int c, double2* const* part,
+                                                  const double2* __restrict__ wb, int tid, int nth) {
+  const int per = (1 << lper) >> LS;
+  first_pass_scatter<R, FWD, LS>([&](int k, int, int p) { return ld(g + (k << lper) + p); }, per, c * per, 1, part,
+                                 wb, tid, nth);
 }
 
 // MODE 0: the plan has no outer levels (ordered plan, or unordered with

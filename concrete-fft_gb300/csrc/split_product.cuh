@@ -1,7 +1,9 @@
 // split_product.cuh -- one negacyclic u64 product (or one Fourier-domain sum
 // of products) spread over a thread-block cluster of S = 2^LS CTAs, for
 // products whose N/2-point transform does not fit one CTA's shared memory
-// (N > 8192) and for small batches.
+// (N > 8192) and for small batches.  Two kernels: u64_product_split_kernel
+// for plans with an unordered outer level (below) and
+// u64_product_split0_kernel for plans without one (n = base_n).
 //
 // The transform of n = N/2 points has at least one unordered outer level; its
 // level 0 of radix R0 >= S splits it into R0 contiguous slices of m = n/R0
@@ -178,18 +180,192 @@ __global__ void __launch_bounds__(MAXT) u64_product_split_kernel(
   cl.sync();  // no CTA exits while a peer reads its shared memory
 }
 
-// kernel pointers by base algorithm (kinst_split_prod_*.cu)
-// (big: the 512-thread variant, S = 8 only)
-const void* u64_product_split_ptr_0123(int algo, int ls, bool big);
-const void* u64_product_split_ptr_4567(int algo, int ls, bool big);
+// One product per cluster of S = 2^LS CTAs (S <= the base radix R) when the
+// N/2-point transform has no outer level (n = base_n, e.g. N = 2048 on a
+// 1024-point base), for latency: a few products then run on S SMs each
+// instead of one.  The residue classes mod S of the base algorithm's passes
+// (split.cuh) are the parts: CTA c holds the points j*S + c of the transform,
+// compacted to j.
+// DIF base: the forward's first pass is shared out (CTA c folds and twists the
+// inputs of its butterflies into y, then stores each output into the part of
+// its class through distributed shared memory); after a cluster barrier every
+// later pass, the pointwise product and the inverse's first pass are local to
+// the class -- the inverse's first-pass butterfly p reads the points k*n/R + p,
+// all of class p mod S -- and the inverse's first-pass outputs go to the parts
+// of their classes (a third buffer z, which no CTA uses before); after a
+// second barrier the rest of the inverse, the untwist and the rounding are
+// local.
+// DIT base: CTA c folds and twists its class, runs every forward pass but the
+// last alone, and takes the last pass's butterflies p = c + b*S, whose inputs
+// come from every part and whose outputs (the points k*n/R + p) all belong to
+// class c: the pointwise product is applied as they are stored into z.  Every
+// inverse pass but the last is local; the last reads every part and its
+// outputs are untwisted, rounded and stored.
+// Every butterfly and elementwise step does the operations of the one-CTA
+// product kernel on the same values, so results are bit-identical to it.
+// Shared memory: three buffers of n/S points.  Requires L.nlevels == 0,
+// S <= R and n >= R*S.
+template <int ALGO, int LS>
+__global__ void __launch_bounds__(256) u64_product_split0_kernel(
+    const uint64_t* __restrict__ a, const double2* __restrict__ bhat, long bhat_stride, uint64_t* __restrict__ out,
+    const cfft_product_item* __restrict__ items, DevLevels L, const double2* __restrict__ w,
+    const double2* __restrict__ winv, const double2* __restrict__ tw, const double2* __restrict__ itw) {
+  constexpr int R = AlgoInfo<ALGO>::R;
+  constexpr int LR = Log2<R>::v;
+  constexpr int S = 1 << LS;
+  namespace cg = cooperative_groups;
+  cg::cluster_group cl = cg::this_cluster();
+  extern __shared__ double2 smem[];
+  const int log2n = L.log2n[0];
+  const int log2c = log2n - LS;
+  const int n = 1 << log2n;
+  const int c = (int)(blockIdx.x & (S - 1));
+  const long g = (long)(blockIdx.x >> LS);
+  double2* x = smem;
+  double2* y = smem + (1 << log2c);
+  double2* z = smem + (2 << log2c);
+  const int tid = threadIdx.x, nth = blockDim.x;
+  const int lper = log2n - LR;          // log2(n/R)
+  const int lpc = lper - LS;            // log2 of the first/last-pass butterflies per CTA
+  const int per = 1 << lpc;
+  const uint64_t* ap = items ? items[g].a : a + (g << (log2n + 1));
+  const double2* bp = items ? (const double2*)items[g].bhat : bhat + g * bhat_stride;
+  uint64_t* op = items ? items[g].out : out + (g << (log2n + 1));
+  const double2* wf = w + L.w_off[0] + n;  // the base's forward and inverse tables
+  const double2* wi = winv + n;
+
+  if constexpr (!AlgoInfo<ALGO>::DIT) {
+    double2* peer_x[S];
+    double2* peer_z[S];
+#pragma unroll
+    for (int j = 0; j < S; ++j) {
+      peer_x[j] = cl.map_shared_rank(x, (unsigned)j);
+      peer_z[j] = cl.map_shared_rank(z, (unsigned)j);
+    }
+    auto token = cl.barrier_arrive();  // every CTA runs before a peer's memory is written
+    // input k of first-pass butterfly c*per + b, folded and twisted, at y[k*per + b]
+    for (int t = tid; t < (R << lpc); t += nth) {
+      const int j = ((t >> lpc) << lper) + c * per + (t & (per - 1));
+      const c64 v{i64_to_f64_rne((int64_t)__ldcs(ap + j)), i64_to_f64_rne((int64_t)__ldcs(ap + j + n))};
+      st(y + t, cmul(ldg(tw + j), v));
+    }
+    __syncthreads();
+    cl.barrier_wait(std::move(token));
+    first_pass_scatter<R, true, LS>([&](int k, int b, int) { return ld(y + (k << lpc) + b); }, per, c * per, 1,
+                                    peer_x, wf, tid, nth);
+    cl.sync();  // every part's x is complete
+    const FlatBuf r = dif_after_first<R, true>(log2n, LS, FlatBuf{x}, FlatBuf{y}, wf, tid, nth);
+    for (int j = tid; j < (1 << log2c); j += nth) st(r.p + j, cmul(ldg(bp + (j << LS) + c), ld(r.p + j)));
+    __syncthreads();
+    first_pass_scatter<R, false, LS>([&](int k, int b, int) { return ld(r.p + (k << lpc) + b); }, per, c, S, peer_z,
+                                     wi, tid, nth);
+    cl.sync();  // every part's z is complete (no peer memory is touched after this)
+    const FlatBuf s = dif_after_first<R, false>(log2n, LS, FlatBuf{z}, FlatBuf{x}, wi, tid, nth);
+    for (int j = tid; j < (1 << log2c); j += nth) {
+      const int jg = (j << LS) + c;
+      const c64 t = cmul(ldg(itw + jg), ld(s.p + j));
+      __stcs(op + jg, round_half_up_mod64(t.re));
+      __stcs(op + jg + n, round_half_up_mod64(t.im));
+    }
+  } else {
+    for (int j = tid; j < (1 << log2c); j += nth) {
+      const int jg = (j << LS) + c;
+      const c64 v{i64_to_f64_rne((int64_t)__ldcs(ap + jg)), i64_to_f64_rne((int64_t)__ldcs(ap + jg + n))};
+      st(x + j, cmul(ldg(tw + jg), v));
+    }
+    __syncthreads();
+    const FlatBuf r = dit_before_last<R, true>(log2n, LS, FlatBuf{x}, FlatBuf{y}, wf, tid, nth);
+    double2* peer[S];
+#pragma unroll
+    for (int j = 0; j < S; ++j) peer[j] = cl.map_shared_rank(r.p, (unsigned)j);
+    cl.sync();  // every part's forward passes are done
+    // last forward pass, butterflies p = c + b*S: output k (the point k*n/R + p) times
+    // the operand, into z[k*per + b]
+    for (int b = tid; b < per; b += nth) {
+      const int p = c + (b << LS);
+      const int lo = p << (LR - LS);
+      const double2* twp = wf + (p << LR);
+      c64 v[R];
+      v[0] = ld(peer[0] + lo);
+#pragma unroll
+      for (int k = 1; k < R; ++k) v[k] = cmul(ldg(twp + k), ld(peer[k & (S - 1)] + lo + (k >> LS)));
+      Core<R, true, 0>::run(v);
+#pragma unroll
+      for (int k = 0; k < R; ++k) st(z + (k << lpc) + b, cmul(ldg(bp + (k << lper) + p), v[k]));
+    }
+    __syncthreads();
+    // the inverse ping-pongs between z and the buffer that no peer reads
+    const FlatBuf s = dit_before_last<R, false>(log2n, LS, FlatBuf{z}, FlatBuf{r.p == x ? y : x}, wi, tid, nth);
+#pragma unroll
+    for (int j = 0; j < S; ++j) peer[j] = cl.map_shared_rank(s.p, (unsigned)j);
+    cl.sync();  // every part's inverse passes are done
+    for (int p = c * per + tid; p < (c + 1) * per; p += nth) {
+      const int lo = p << (LR - LS);
+      const double2* twp = wi + (p << LR);
+      c64 v[R];
+      v[0] = ld(peer[0] + lo);
+#pragma unroll
+      for (int k = 1; k < R; ++k) v[k] = cmul(ldg(twp + k), ld(peer[k & (S - 1)] + lo + (k >> LS)));
+      Core<R, false, 0>::run(v);
+#pragma unroll
+      for (int k = 0; k < R; ++k) {
+        const int jg = (k << lper) + p;
+        const c64 t = cmul(ldg(itw + jg), v[k]);
+        __stcs(op + jg, round_half_up_mod64(t.re));
+        __stcs(op + jg + n, round_half_up_mod64(t.im));
+      }
+    }
+    cl.sync();  // no CTA exits while a peer reads its shared memory
+  }
+}
+
+// kernel pointers by base algorithm (kinst_split_prod_*.cu, one unit per pair)
+// (big: the 512-thread variant, for parts of 4096 points)
+const void* u64_product_split_ptr_01(int algo, int ls, bool big);
+const void* u64_product_split_ptr_23(int algo, int ls, bool big);
+const void* u64_product_split_ptr_45(int algo, int ls, bool big);
+const void* u64_product_split_ptr_67(int algo, int ls, bool big);
+inline const void* u64_product_split_ptr(int algo, int ls, bool big) {
+  return algo < 2 ? u64_product_split_ptr_01(algo, ls, big)
+                  : algo < 4 ? u64_product_split_ptr_23(algo, ls, big)
+                             : algo < 6 ? u64_product_split_ptr_45(algo, ls, big) : u64_product_split_ptr_67(algo, ls, big);
+}
+// the kernel for plans without an outer level; nullptr where S = 2^ls exceeds the radix
+const void* u64_product_split0_ptr_01(int algo, int ls);
+const void* u64_product_split0_ptr_23(int algo, int ls);
+const void* u64_product_split0_ptr_45(int algo, int ls);
+const void* u64_product_split0_ptr_67(int algo, int ls);
+inline const void* u64_product_split0_ptr(int algo, int ls) {
+  return algo < 2 ? u64_product_split0_ptr_01(algo, ls)
+                  : algo < 4 ? u64_product_split0_ptr_23(algo, ls)
+                             : algo < 6 ? u64_product_split0_ptr_45(algo, ls) : u64_product_split0_ptr_67(algo, ls);
+}
 
 template <int A>
 const void* split_product_ptr(int ls, bool big) {
-  if (big) return ls == 3 ? (const void*)u64_product_split_kernel<A, 3, kSplitProdThreadsBig> : nullptr;
+  if (big) {
+    switch (ls) {
+      case 1: return (const void*)u64_product_split_kernel<A, 1, kSplitProdThreadsBig>;
+      case 2: return (const void*)u64_product_split_kernel<A, 2, kSplitProdThreadsBig>;
+      case 3: return (const void*)u64_product_split_kernel<A, 3, kSplitProdThreadsBig>;
+      default: return nullptr;
+    }
+  }
   switch (ls) {
     case 1: return (const void*)u64_product_split_kernel<A, 1, kSplitProdThreads>;
     case 2: return (const void*)u64_product_split_kernel<A, 2, kSplitProdThreads>;
     case 3: return (const void*)u64_product_split_kernel<A, 3, kSplitProdThreads>;
+    default: return nullptr;
+  }
+}
+
+template <int A>
+const void* split0_product_ptr(int ls) {
+  constexpr int LRA = Log2<AlgoInfo<A>::R>::v;
+  switch (ls) {
+    case 1: return (const void*)u64_product_split0_kernel<A, 1>;
+    case 2: if constexpr (LRA >= 2) return (const void*)u64_product_split0_kernel<A, 2>; else return nullptr;
+    case 3: if constexpr (LRA >= 3) return (const void*)u64_product_split0_kernel<A, 3>; else return nullptr;
     default: return nullptr;
   }
 }

@@ -294,6 +294,31 @@ def test_u64_product_cluster_sizes_bit_identical(cuda, N, base):
             assert torch.equal(out, ref), (N, base, algo, ctas)
 
 
+@pytest.mark.parametrize("N,base", [(2048, 1024), (1024, 512), (256, 128)])
+def test_u64_product_no_level_clusters_bit_exact(cuda, oracle, N, base):
+    """Plans whose transform has no outer level (n = base_n) on clusters of 2/4/8 CTAs
+    (the residue classes of the base algorithm's passes), for all eight base
+    algorithms, DIF and DIT: the oracle's bits at every cluster size."""
+    import concrete_fft as cf
+    torch = cuda
+    count = 3
+    for algo in range(8):
+        plan = cf.product.U64ProductPlan(N, algo, base)
+        assert plan.algo() == (algo, base)
+        a = RNG.integers(0, 2 ** 64, (count, N), dtype=np.uint64)
+        b = RNG.integers(-2 ** 7, 2 ** 7, (count, N))
+        bhat = torch.empty((count, N // 2), dtype=torch.complex128, device="cuda")
+        plan.prepare_operand(torch.from_numpy(b).cuda(), bhat)
+        want_bhat = oracle.u64_prepare(N, algo, base, b)
+        want = oracle.u64_product(N, algo, base, a, want_bhat, nthreads=0)
+        da = torch.from_numpy(a.view(np.int64)).cuda()
+        for ctas in (1, 2, 4, 8, 0):
+            plan.set_cluster_size(ctas)
+            out = torch.zeros_like(da)
+            plan.product(da, bhat, out)
+            assert np.array_equal(out.cpu().numpy().view(np.uint64), want), (N, algo, ctas)
+
+
 @pytest.mark.parametrize("N", [16384, 32768, 1 << 21])
 def test_u128_product_large_N(cuda, oracle, N):
     """N > 8192: five launches around the fft128 plan, bit-exact against the CPU pipeline

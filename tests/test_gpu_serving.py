@@ -77,14 +77,18 @@ def test_unfused_pipeline_equals_fused(cuda, oracle, engine, lN):
     assert np.array_equal(out.cpu().numpy().view(np.uint64), want)
 
 
-@pytest.mark.parametrize("staged_io,via_queue", [(False, False), (True, False), (False, True)])
-def test_server_results_same_alone_and_in_the_mix(cuda, oracle, engine, staged_io, via_queue):
+@pytest.mark.parametrize("staged_io,via_queue,cluster_log2N", [(False, False, 0), (True, False, 0), (False, True, 0),
+                                                               (False, False, 10), (False, True, 10)])
+def test_server_results_same_alone_and_in_the_mix(cuda, oracle, engine, staged_io, via_queue, cluster_log2N):
     """Every recorded result of the batched loop equals the request run alone, with the
     kernels reading item records from and storing results into page-locked host memory
-    (default) and with per-launch copies (staged_io)."""
+    (default) and with per-launch copies (staged_io); cluster_log2N = 10 puts every size
+    on thread-block clusters (N = 1024 and 2048, whose plans have no outer level,
+    included)."""
     import concrete_fft as cf
     srv = cf.serving.Server(engine, SIZES, operand_bytes=64 << 20, ring_bytes=256 << 20, seed=9)
-    cfg = srv.config(rate=20000, duration_s=0.05, record_every=1, staged_io=staged_io, via_queue=via_queue)
+    cfg = srv.config(rate=20000, duration_s=0.05, record_every=1, staged_io=staged_io, via_queue=via_queue,
+                     cluster_log2N=cluster_log2N)
     stats = srv.run(cfg)
     assert stats["requests"] > 100 and stats["launches"] < stats["requests"]  # batching happened (the
     # queue counts its own launches: 0 here)

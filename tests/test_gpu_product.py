@@ -272,7 +272,7 @@ def test_u64_product_large_N(cuda, oracle, N, algo, base):
         assert np.array_equal(out1.cpu().numpy().view(np.uint64), exact)
 
 
-@pytest.mark.parametrize("N,base", [(4096, 1024), (8192, 1024), (8192, 256), (2048, 64)])
+@pytest.mark.parametrize("N,base", [(4096, 1024), (8192, 1024), (8192, 256), (2048, 64), (16384, 1024)])
 def test_u64_product_cluster_sizes_bit_identical(cuda, N, base):
     """Small batches on clusters of 2/4/8 CTAs give the one-CTA kernel's bits."""
     import concrete_fft as cf

@@ -47,6 +47,7 @@ _SIGS = [
     ("cfft_diag_host_mapping", c_int, [vp, c_size, vp]),
     ("cfft_diag_set_cluster_policy", c_int, [c_int]),
     ("cfft_diag_set_spread", c_int, [c_int]),
+    ("cfft_diag_set_host_chunks", c_int, [c_int, c_int, c_int, c_int]),
     ("cfft_ordered_plan_create", c_int, [c_size, c_int, pp]),
     ("cfft_ordered_plan_create_measure", c_int, [c_size, c_dbl, pp]),
     ("cfft_ordered_plan_destroy", None, [vp]),

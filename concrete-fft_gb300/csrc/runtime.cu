@@ -319,6 +319,15 @@ cfft_status host_pipeline(int nslots, size_t bytes, PipeSlot* slots) {
   return CFFT_OK;
 }
 
+namespace {
+std::atomic<int> g_hc_chunks{24}, g_hc_slots{4}, g_hc_first{0}, g_hc_last{0};
+}
+
+HostChunks host_chunks() {
+  return HostChunks{g_hc_chunks.load(std::memory_order_relaxed), g_hc_slots.load(std::memory_order_relaxed),
+                    g_hc_first.load(std::memory_order_relaxed), g_hc_last.load(std::memory_order_relaxed)};
+}
+
 void bind_device_context() {
   // a thread's first runtime call does not always make the device's primary
   // context current, and pointer queries then miss page-locked host memory;
@@ -564,6 +573,16 @@ extern "C" cfft_status cfft_diag_dadd_int_rate(double* adds_per_second) {
 extern "C" cfft_status cfft_diag_host_mapping(const void* p, size_t bytes, void** device_address) {
   if (!device_address) return cfft::fail(CFFT_ERR_INVALID_ARGUMENT, "null output pointer");
   *device_address = cfft::mapped_host_range(p, bytes);
+  return CFFT_OK;
+}
+
+extern "C" cfft_status cfft_diag_set_host_chunks(int chunks, int slots, int first, int last) {
+  if (chunks < 0 || chunks > 1024 || slots < 0 || slots > 8 || first < 0 || last < 0)
+    return cfft::fail(CFFT_ERR_INVALID_ARGUMENT, "chunks 0..1024, slots 0..8, first and last >= 0");
+  cfft::g_hc_chunks.store(chunks ? chunks : 24, std::memory_order_relaxed);
+  cfft::g_hc_slots.store(slots ? slots : 4, std::memory_order_relaxed);
+  cfft::g_hc_first.store(first, std::memory_order_relaxed);
+  cfft::g_hc_last.store(last, std::memory_order_relaxed);
   return CFFT_OK;
 }
 

@@ -95,6 +95,13 @@ struct PipeSlot {
   cudaStream_t stream;
 };
 cfft_status host_pipeline(int nslots, size_t bytes, PipeSlot* slots);
+// The schedule of the host product entry points' pipeline (cfft_diag_set_host_chunks):
+// `chunks` equal chunks on `slots` streams, after a first chunk of `first` products and
+// before a last one of `last` (0: none).
+struct HostChunks {
+  int chunks, slots, first, last;
+};
+HostChunks host_chunks();
 
 // The device address of `bytes` of page-locked host memory starting at p, or
 // nullptr when the range is not one page-locked, device-mapped allocation

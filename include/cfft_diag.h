@@ -46,6 +46,14 @@ cfft_status cfft_diag_set_cluster_policy(int policy);
  * default), 0 off.  Process-wide; for measurement. */
 cfft_status cfft_diag_set_spread(int on);
 
+/* Schedule of the u64 product's host entry point (cfft_u64_product_host): the
+ * batch is copied in and multiplied in `chunks` equal chunks (default 24, at
+ * least two products per SM each) over `slots` streams (default 4, at most 8),
+ * after a first chunk of `first` products and before a last one of `last`
+ * (0: none, the default).  0 for chunks or slots restores its default.
+ * Process-wide; for measurement. */
+cfft_status cfft_diag_set_host_chunks(int chunks, int slots, int first, int last);
+
 #ifdef __cplusplus
 }
 #endif

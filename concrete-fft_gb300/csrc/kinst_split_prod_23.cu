@@ -17,4 +17,11 @@ const void* u64_product_split0_ptr_23(int algo, int ls) {
     default: return nullptr;
   }
 }
+const void* u64_product_split2_ptr_23(int algo, int ls0, int ls1) {
+  switch (algo) {
+    case 2: return split2_product_ptr<2>(ls0, ls1);
+    case 3: return split2_product_ptr<3>(ls0, ls1);
+    default: return nullptr;
+  }
+}
 }  // namespace cfft

@@ -17,4 +17,11 @@ const void* u64_product_split0_ptr_45(int algo, int ls) {
     default: return nullptr;
   }
 }
+const void* u64_product_split2_ptr_45(int algo, int ls0, int ls1) {
+  switch (algo) {
+    case 4: return split2_product_ptr<4>(ls0, ls1);
+    case 5: return split2_product_ptr<5>(ls0, ls1);
+    default: return nullptr;
+  }
+}
 }  // namespace cfft

@@ -17,4 +17,11 @@ const void* u64_product_split0_ptr_67(int algo, int ls) {
     default: return nullptr;
   }
 }
+const void* u64_product_split2_ptr_67(int algo, int ls0, int ls1) {
+  switch (algo) {
+    case 6: return split2_product_ptr<6>(ls0, ls1);
+    case 7: return split2_product_ptr<7>(ls0, ls1);
+    default: return nullptr;
+  }
+}
 }  // namespace cfft

@@ -276,6 +276,46 @@ cfft_status launch_split0_product(const cfft_u64_product_plan* plan, int ls, con
                                stream);
 }
 
+// The shape of u64_product_split2_kernel for a plan, as log2s: one outer level
+// of radix R0 = 2^ls0 <= 4 over a DIF base of m points, S1 = 2^ls1 classes of
+// the base with S1 <= R, R0 * S1 <= 8, at least 64 points per CTA and at least
+// 32 butterflies in each of a class's passes (as split0_log2).  Not for a
+// radix-2 base under a radix-4 level: N = 4096 on Dif2/512 measured slower than
+// the five launches from 16 products (29.7 against 24.9 us).  false when the
+// plan has another shape.
+bool split2_shape(const cfft_u64_product_plan* p, int* ls0, int* ls1) {
+  if (p->lv.nlevels != 1 || (p->base_algo & 1) || p->lv.log2r[0] > 2) return false;
+  const int lr = p->base_algo / 2 + 1;
+  if (lr == 1 && p->lv.log2r[0] > 1) return false;
+  const int log2m = ilog2(p->base_n);
+  *ls0 = p->lv.log2r[0];
+  int l1 = std::min(3 - *ls0, lr);
+  while (l1 > 0 && (log2m - l1 < 6 || log2m - l1 - lr < 5)) --l1;
+  *ls1 = l1;
+  return l1 >= 1;
+}
+
+cfft_status launch_split2_product(const cfft_u64_product_plan* plan, int ls0, int ls1, const uint64_t* a,
+                                  const double* bhat, size_t bhat_stride, uint64_t* out, size_t count,
+                                  cudaStream_t stream, const cfft_product_item* items = nullptr) {
+  const void* fn = u64_product_split2_ptr(plan->base_algo, ls0, ls1);
+  if (!fn) return fail(CFFT_ERR_INVALID_SIZE, "no one-level cluster product kernel for this shape");
+  const int ls = ls0 + ls1;
+  if ((count << ls) > 0x7fffffffUL) return fail(CFFT_ERR_INVALID_SIZE, "batch too large");
+  const size_t part = plan->base_n >> ls1;
+  const size_t radix = size_t(2) << (plan->base_algo / 2);
+  const int threads = (int)std::min<size_t>(256, std::max<size_t>(32, std::max(2 * part / radix, part / 2)));
+  const size_t smem = 3 * part * sizeof(double2);
+  const int grid = (int)(count << ls);
+  DevLevels L = plan->dlv;
+  long stride = (long)bhat_stride;
+  const double2* bh = (const double2*)bhat;
+  void* args[] = {(void*)&a, (void*)&bh, &stride, (void*)&out, (void*)&items, &L, (void*)&plan->d_w,
+                  (void*)&plan->d_winv, (void*)&plan->d_tw, (void*)&plan->d_itw};
+  return launch_kernel_cluster(fn, grid, threads, 1 << ls, args, spread_smem(fn, grid, threads, 1 << ls, smem),
+                               stream);
+}
+
 }  // namespace
 
 // Products given as device items (all of the plan's N) on the largest cluster
@@ -495,6 +535,13 @@ cfft_status cfft_u64_product(const cfft_u64_product_plan* plan, const uint64_t* 
                                  bhat_stride, out, count, (cudaStream_t)stream);
   if (plan->cluster == 0 && plan->N >= 512 && !many && split0_log2(plan) >= 1)
     return launch_split0_product(plan, split0_log2(plan), a, bhat, bhat_stride, out, count, (cudaStream_t)stream);
+  // Likewise a plan with one outer level of radix 2 or 4 over a DIF base: level 0's
+  // slices times classes of the base (u64_product_split2_kernel).  One product, Dif4
+  // on 1024 points: 13.7 us at N = 4096 (five launches 32.1), 20.9 at 8192 (34.2);
+  // 38 products: 23.3 (33.5) and 44.7 (58.8)
+  int ls0 = 0, ls1 = 0;
+  if (plan->cluster == 0 && !many && split2_shape(plan, &ls0, &ls1))
+    return launch_split2_product(plan, ls0, ls1, a, bhat, bhat_stride, out, count, (cudaStream_t)stream);
   // otherwise (no cluster kernel for the base) the five launches, whose transforms
   // split over 2-8 CTAs each
   const bool few_unsplit = ls == 0 && plan->cluster == 0 && plan->N >= 2048 && !many;

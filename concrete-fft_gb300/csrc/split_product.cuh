@@ -319,6 +319,155 @@ __global__ void __launch_bounds__(256) u64_product_split0_kernel(
   }
 }
 
+// One product per cluster of S = R0 x S1 CTAs when the N/2-point transform has
+// exactly one unordered outer level, of radix R0 = 2^LS0 <= 4, over a DIF base of
+// m points (e.g. N = 4096 on a 1024-point base: R0 = 2, S1 = 4): for latency, a
+// few products then run on up to 8 SMs each, where u64_product_split_kernel
+// gives each CTA a whole base transform.  Level 0 splits the transform into R0
+// slices of m points; CTA c = s0 * S1 + c1 holds class c1 (mod S1) of slice
+// s0, i.e. the slice points j * S1 + c1 after the base's first pass.
+//   1. Level 0 forward: CTA c takes the butterflies [c*m/S, (c+1)*m/S),
+//      reading its inputs folded and twisted from the product's coefficients;
+//      output k (slice slot(k), point i) is stored into the staging buffer y of
+//      the CTA of that slice that computes the base's first-pass butterfly
+//      i mod (m/R), through distributed shared memory.
+//   2. Cluster barrier.  The base's first pass on the slice, 1/S1 of the
+//      butterflies per CTA, each output into the part of its class (as in
+//      u64_product_split0_kernel).
+//   3. Cluster barrier.  The later passes, the pointwise product and the
+//      inverse's first pass are local to the class; the inverse's first-pass
+//      outputs go to the parts of their classes (buffer z).
+//   4. Cluster barrier.  The rest of the base inverse, locally.
+//   5. Cluster barrier.  Level 0 inverse: CTA c takes the butterflies
+//      [c*m/S, (c+1)*m/S), reading point i of every slice from the CTA that
+//      holds its class, and untwists, rounds and stores the outputs; a last
+//      cluster barrier keeps every CTA alive while a peer reads its memory.
+// Every butterfly and elementwise step does the operations of the one-CTA
+// product kernel on the same values, so results are bit-identical to it.
+// Shared memory: three buffers of m/S1 points.  Requires L.nlevels == 1,
+// 2^L.log2r[0] == R0, S1 <= the base radix R and m >= R*S1.
+template <int ALGO, int LS0, int LS1>
+__global__ void __launch_bounds__(256) u64_product_split2_kernel(
+    const uint64_t* __restrict__ a, const double2* __restrict__ bhat, long bhat_stride, uint64_t* __restrict__ out,
+    const cfft_product_item* __restrict__ items, DevLevels L, const double2* __restrict__ w,
+    const double2* __restrict__ winv, const double2* __restrict__ tw, const double2* __restrict__ itw) {
+  constexpr int R = AlgoInfo<ALGO>::R;
+  constexpr int LR = Log2<R>::v;
+  constexpr int R0 = 1 << LS0;
+  constexpr int S1 = 1 << LS1;
+  constexpr int LS = LS0 + LS1;
+  constexpr int S = 1 << LS;
+  static_assert(!AlgoInfo<ALGO>::DIT, "DIF base algorithms only");
+  namespace cg = cooperative_groups;
+  cg::cluster_group cl = cg::this_cluster();
+  extern __shared__ double2 smem[];
+  const int log2n = L.log2n[0];
+  const int log2m = L.log2n[1];
+  const int n = 1 << log2n, m = 1 << log2m;
+  const int log2c = log2m - LS1;  // points per CTA
+  const int c = (int)(blockIdx.x & (S - 1));
+  const long g = (long)(blockIdx.x >> LS);
+  const int s0 = c >> LS1, c1 = c & (S1 - 1);
+  double2* x = smem;
+  double2* y = smem + (1 << log2c);
+  double2* z = smem + (2 << log2c);
+  const int tid = threadIdx.x, nth = blockDim.x;
+  const int lq = log2m - LR;  // log2(m/R): the base's first-pass stride
+  const int lpp = lq - LS1;   // log2 of the first-pass butterflies per CTA
+  const int pp = 1 << lpp;
+  const uint64_t* ap = items ? items[g].a : a + (g << (log2n + 1));
+  const double2* bp = items ? (const double2*)items[g].bhat : bhat + g * bhat_stride;
+  uint64_t* op = items ? items[g].out : out + (g << (log2n + 1));
+  const double2* wl = w + L.w_off[0];
+  const double2* wli = winv + L.winv_off[0];
+  const double2* wf = w + L.w_off[1] + m;  // the base's forward and inverse tables
+  const double2* wi = winv + m;
+  double2* peer_x[S1];
+  double2* peer_z[S1];
+#pragma unroll
+  for (int j = 0; j < S1; ++j) {
+    peer_x[j] = cl.map_shared_rank(x, (unsigned)((s0 << LS1) + j));
+    peer_z[j] = cl.map_shared_rank(z, (unsigned)((s0 << LS1) + j));
+  }
+  auto token = cl.barrier_arrive();  // every CTA runs before a peer's memory is written
+
+  // 1. level 0 forward on butterflies [c*m/S, (c+1)*m/S)
+  const int cnt = m >> LS;
+  const int i0 = c * cnt;
+  auto load_l0 = [&](int i, c64* v) {
+#pragma unroll
+    for (int k = 0; k < R0; ++k) {
+      const int j = (k << log2m) + i;
+      const c64 u{i64_to_f64_rne((int64_t)__ldcs(ap + j)), i64_to_f64_rne((int64_t)__ldcs(ap + j + n))};
+      v[k] = cmul(ldg(tw + j), u);
+    }
+  };
+  c64 v0[R0];
+  if (tid < cnt) load_l0(i0 + tid, v0);
+  cl.barrier_wait(std::move(token));
+  for (int b = tid; b < cnt; b += nth) {
+    const int i = i0 + b;
+    c64 v[R0];
+    if (b == tid) {
+#pragma unroll
+      for (int k = 0; k < R0; ++k) v[k] = v0[k];
+    } else {
+      load_l0(i, v);
+    }
+    Core<R0, true, 0>::run(v);
+    const double2* twl = wl + (R0 - 1) * i - 1;
+    const int p = i & ((1 << lq) - 1);
+    const int dst = (((i >> lq) << lpp) + (p & (pp - 1)));
+    const int cls = p >> lpp;
+#pragma unroll
+    for (int k = 0; k < R0; ++k) {
+      const c64 o = k == 0 ? v[0] : cmul(ldg(twl + k), v[k]);
+      st(cl.map_shared_rank(y, (unsigned)((slot<R0>(k) << LS1) + cls)) + dst, o);
+    }
+  }
+  cl.sync();  // every staging buffer is complete
+
+  // 2. the base's first pass on this slice, butterflies [c1*pp, (c1+1)*pp)
+  first_pass_scatter<R, true, LS1>([&](int k, int b, int) { return ld(y + (k << lpp) + b); }, pp, c1 * pp, 1, peer_x,
+                                   wf, tid, nth);
+  cl.sync();  // every part's x is complete
+
+  // 3. the later passes, the pointwise product, the inverse's first pass
+  const FlatBuf r = dif_after_first<R, true>(log2m, LS1, FlatBuf{x}, FlatBuf{y}, wf, tid, nth);
+  const double2* bs = bp + ((long)s0 << log2m) + c1;
+  for (int j = tid; j < (1 << log2c); j += nth) st(r.p + j, cmul(ldg(bs + (j << LS1)), ld(r.p + j)));
+  __syncthreads();
+  first_pass_scatter<R, false, LS1>([&](int k, int b, int) { return ld(r.p + (k << lpp) + b); }, pp, c1, S1, peer_z,
+                                    wi, tid, nth);
+  cl.sync();  // every part's z is complete
+
+  // 4. the rest of the base inverse
+  const FlatBuf sv = dif_after_first<R, false>(log2m, LS1, FlatBuf{z}, FlatBuf{x}, wi, tid, nth);
+  cl.sync();  // every slice's inverse is complete
+
+  // 5. level 0 inverse on butterflies [c*m/S, (c+1)*m/S), untwisted and rounded
+  for (int b = tid; b < cnt; b += nth) {
+    const int i = i0 + b;
+    const int cls = i & (S1 - 1);
+    const int at = i >> LS1;
+    const double2* twl = wli + (R0 - 1) * i - 1;
+    c64 v[R0];
+    v[0] = ld(cl.map_shared_rank(sv.p, (unsigned)cls) + at);
+#pragma unroll
+    for (int k = 1; k < R0; ++k)
+      v[k] = cmul(ldg(twl + k), ld(cl.map_shared_rank(sv.p, (unsigned)((slot<R0>(k) << LS1) + cls)) + at));
+    Core<R0, false, 0>::run(v);
+#pragma unroll
+    for (int k = 0; k < R0; ++k) {
+      const int j = (k << log2m) + i;
+      const c64 t = cmul(ldg(itw + j), v[k]);
+      __stcs(op + j, round_half_up_mod64(t.re));
+      __stcs(op + j + n, round_half_up_mod64(t.im));
+    }
+  }
+  cl.sync();  // no CTA exits while a peer reads its shared memory
+}
+
 // kernel pointers by base algorithm (kinst_split_prod_*.cu, one unit per pair)
 // (big: the 512-thread variant, for parts of 4096 points)
 const void* u64_product_split_ptr_01(int algo, int ls, bool big);
@@ -335,6 +484,17 @@ const void* u64_product_split0_ptr_01(int algo, int ls);
 const void* u64_product_split0_ptr_23(int algo, int ls);
 const void* u64_product_split0_ptr_45(int algo, int ls);
 const void* u64_product_split0_ptr_67(int algo, int ls);
+// the one-level kernel (DIF bases only); nullptr where the shape is not instantiated
+const void* u64_product_split2_ptr_01(int algo, int ls0, int ls1);
+const void* u64_product_split2_ptr_23(int algo, int ls0, int ls1);
+const void* u64_product_split2_ptr_45(int algo, int ls0, int ls1);
+const void* u64_product_split2_ptr_67(int algo, int ls0, int ls1);
+inline const void* u64_product_split2_ptr(int algo, int ls0, int ls1) {
+  return algo < 2 ? u64_product_split2_ptr_01(algo, ls0, ls1)
+                  : algo < 4 ? u64_product_split2_ptr_23(algo, ls0, ls1)
+                             : algo < 6 ? u64_product_split2_ptr_45(algo, ls0, ls1)
+                                        : u64_product_split2_ptr_67(algo, ls0, ls1);
+}
 inline const void* u64_product_split0_ptr(int algo, int ls) {
   return algo < 2 ? u64_product_split0_ptr_01(algo, ls)
                   : algo < 4 ? u64_product_split0_ptr_23(algo, ls)
@@ -367,6 +527,22 @@ const void* split0_product_ptr(int ls) {
     case 2: if constexpr (LRA >= 2) return (const void*)u64_product_split0_kernel<A, 2>; else return nullptr;
     case 3: if constexpr (LRA >= 3) return (const void*)u64_product_split0_kernel<A, 3>; else return nullptr;
     default: return nullptr;
+  }
+}
+
+// (R0, S1) = (2, 2), (2, 4), (4, 2) for DIF bases with S1 <= R
+template <int A>
+const void* split2_product_ptr(int ls0, int ls1) {
+  if constexpr (AlgoInfo<A>::DIT) {
+    return nullptr;
+  } else {
+    constexpr int LRA = Log2<AlgoInfo<A>::R>::v;
+    if (ls0 == 1 && ls1 == 1) return (const void*)u64_product_split2_kernel<A, 1, 1>;
+    if constexpr (LRA >= 2) {
+      if (ls0 == 1 && ls1 == 2) return (const void*)u64_product_split2_kernel<A, 1, 2>;
+    }
+    if (ls0 == 2 && ls1 == 1) return (const void*)u64_product_split2_kernel<A, 2, 1>;
+    return nullptr;
   }
 }
 

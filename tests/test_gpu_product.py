@@ -319,6 +319,29 @@ def test_u64_product_no_level_clusters_bit_exact(cuda, oracle, N, base):
             assert np.array_equal(out.cpu().numpy().view(np.uint64), want), (N, algo, ctas)
 
 
+@pytest.mark.parametrize("N,base", [(4096, 1024), (8192, 1024), (4096, 512), (2048, 512)])
+def test_u64_product_one_level_clusters_bit_exact(cuda, oracle, N, base):
+    """A few products of a plan with one outer level (radix 2 or 4) run on a cluster of
+    level-0 slices times classes of the base (DIF bases; DIT bases take another path):
+    the oracle's bits, and the same bits on one CTA per product."""
+    import concrete_fft as cf
+    torch = cuda
+    count = 3
+    for algo in range(8):
+        plan = cf.product.U64ProductPlan(N, algo, base)
+        a = RNG.integers(0, 2 ** 64, (count, N), dtype=np.uint64)
+        b = RNG.integers(-2 ** 7, 2 ** 7, (count, N))
+        bhat = torch.empty((count, N // 2), dtype=torch.complex128, device="cuda")
+        plan.prepare_operand(torch.from_numpy(b).cuda(), bhat)
+        want = oracle.u64_product(N, algo, base, a, oracle.u64_prepare(N, algo, base, b), nthreads=0)
+        da = torch.from_numpy(a.view(np.int64)).cuda()
+        for ctas in (0, 1):
+            plan.set_cluster_size(ctas)
+            out = torch.zeros_like(da)
+            plan.product(da, bhat, out)
+            assert np.array_equal(out.cpu().numpy().view(np.uint64), want), (N, base, algo, ctas)
+
+
 @pytest.mark.parametrize("N", [16384, 32768, 1 << 21])
 def test_u128_product_large_N(cuda, oracle, N):
     """N > 8192: five launches around the fft128 plan, bit-exact against the CPU pipeline

@@ -232,7 +232,9 @@ cfft_status build_plan(C64Plan& p, size_t n, size_t base_n, int algo, bool unord
 // split over S = 2^ls CTAs (split.cuh) when the batch is too small to give
 // every SM work, or as the plan forces.  Only plans whose transform fits one
 // CTA whole (d0 == 0).  S is bounded by the radix of the step that is split
-// (the base radix without outer levels, level 0's radix with them) and by 8.
+// (the base radix without outer levels, level 0's radix with them) and by 8;
+// with one outer level of radix 2 or 4 over a DIF base, by level 0's radix
+// times the base classes (mode 2 for radix 2, 3 for radix 4).
 int split_log2(const C64Plan& p, long batch, int* mode) {
   if (p.cluster == 1) return 0;
   const int log2n = p.lv.log2n[0];
@@ -248,14 +250,50 @@ int split_log2(const C64Plan& p, long batch, int* mode) {
     min_ls = std::max(0, log2n - kSmemLog2Max);
   }
   if (log2n < 6 || max_ls < 1 || min_ls > max_ls) return 0;
-  if (p.cluster >= 2) return std::max(min_ls, std::min(max_ls, ilog2((size_t)p.cluster)));
+  // one outer level of radix 2 or 4 over a DIF base: level 0's slices times
+  // S1 = 2^ls1 classes of the base (c64_split2_kernel, modes 2 and 3), with at
+  // least 64 points per CTA and 32 butterflies per class pass, and not a radix-2
+  // base under a radix-4 level
+  int ls1 = 0;
+  const int ls0 = p.lv.nlevels == 1 ? p.lv.log2r[0] : 0;
+  if (p.lv.nlevels == 1 && ls0 <= 2 && !(p.base_algo & 1) && min_ls == 0) {
+    const int lr = ilog2((size_t)algo_radix(p.base_algo));
+    const int log2m = p.lv.log2n[1];
+    if (!(lr == 1 && ls0 > 1)) {
+      ls1 = std::min(3 - ls0, lr);
+      while (ls1 > 0 && (log2m - ls1 < 6 || log2m - ls1 - lr < 5)) --ls1;
+    }
+  }
   const long target = 4L * sm_count();
+  if (p.cluster >= 2) {
+    const int want = ilog2((size_t)p.cluster);
+    if (want > max_ls && ls1 >= 1) {
+      *mode = 1 + ls0;
+      return ls0 + std::min(ls1, want - ls0);
+    }
+    return std::max(min_ls, std::min(max_ls, want));
+  }
+  // a small batch, up to 2 CTAs per SM: the most CTAs per transform.  fwd+inv of
+  // 2048 points on Dif4/1024: batch 1 12.8 us on 8 CTAs, 28.1 on 2; batch 16 17.8 and
+  // 28.1.  From 4 CTAs per SM it lost (4096 points, batch 64: 55.8 against 52.3 on 4)
+  if (ls1 >= 1 && (batch << (ls0 + ls1)) <= 2L * sm_count()) {
+    *mode = 1 + ls0;
+    return ls0 + ls1;
+  }
   if (min_ls > 0) {
     // transforms above one CTA's shared memory: a cluster of 8 SMs beats the global-level
     // path (all SMs, several launches) only up to 8192 points and for small batches
     // (measured, batch 1 fwd+inv: 37 vs 47 us at 8192, 70 vs 72 at 16384, 131 vs 123 at 32768)
     if (log2n > 13 || (batch << max_ls) >= target) return 0;
     return max_ls;
+  }
+  // without levels, keep at least 32 butterflies in each of a class's passes (64 for
+  // DIT, one thread per butterfly): with fewer the CTAs idle (fwd+inv of 512 points on
+  // Dif8: 12.8 us on 2 CTAs, 19.2 on 8; 1024 points on Dif16: 24.9 on 2, 36.3 on 8)
+  if (*mode == 0) {
+    const int lr = ilog2((size_t)algo_radix(p.base_algo));
+    const int min_lb = (p.base_algo & 1) ? 6 : 5;
+    while (max_ls > 0 && log2n - max_ls - lr < min_lb) --max_ls;
   }
   int ls = 0;
   while (ls < max_ls && (batch << ls) < target) ++ls;

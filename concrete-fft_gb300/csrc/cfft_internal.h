@@ -58,12 +58,17 @@ LevelDesc make_levels(size_t n, size_t base_n);
 
 void set_error(const std::string& msg);
 
-// Device tables of a u64 product plan (forward/inverse FFT tables, twist, untwist).
 // Products from a device item array (one plan's N) on a thread-block cluster
 // each (split_product.cuh), the largest the plan allows.
 cfft_status u64_product_split_items(const cfft_u64_product_plan* plan, const cfft_product_item* items, size_t count,
                                     void* stream);
 bool u64_product_splittable(const cfft_u64_product_plan* plan);
+// The serving loop and the work queue, with an automatic cluster threshold: a launch
+// of at most this many products runs every product whose plan has a cluster kernel on
+// a cluster (up to 8 CTAs each, so the launch still has an SM per CTA); a larger one
+// only the products of N >= 8192.
+constexpr size_t kClusterAllItems = 12;
+// Device tables of a u64 product plan (forward/inverse FFT tables, twist, untwist).
 void u64_product_tables(const cfft_u64_product_plan* p, const void** w, const void** winv, const void** tw,
                         const void** itw);
 

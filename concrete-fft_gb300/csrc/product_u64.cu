@@ -334,6 +334,9 @@ cfft_status cfft::u64_product_split_items(const cfft_u64_product_plan* plan, con
   if (plan->lv.nlevels == 0)
     return launch_split0_product(plan, split0_log2(plan), nullptr, nullptr, 0, nullptr, count, (cudaStream_t)stream,
                                  items);
+  int ls0 = 0, ls1 = 0;
+  if (split2_shape(plan, &ls0, &ls1))
+    return launch_split2_product(plan, ls0, ls1, nullptr, nullptr, 0, nullptr, count, (cudaStream_t)stream, items);
   const int max_ls = std::min(3, plan->lv.log2r[0]);
   return launch_split_product(plan, max_ls, nullptr, nullptr, 0, nullptr, count, (cudaStream_t)stream, items);
 }

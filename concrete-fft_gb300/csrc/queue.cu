@@ -52,7 +52,8 @@ struct cfft_product_queue {
   const cfft_product_engine* engine = nullptr;
   int device = 0;
   int nslots = 3;
-  bool on_cluster[32] = {};
+  bool on_cluster[32] = {};      // launches of more than kClusterAllItems products
+  bool on_cluster_all[32] = {};  // smaller launches
   QSlot slots[kMaxQueueSlots];
   std::mutex mu;
   std::condition_variable cv_work, cv_done;
@@ -81,16 +82,17 @@ cfft_status grow_items(QSlot& sl, size_t n) {
 cfft_status launch_slot(cfft_product_queue* q, QSlot& sl, const std::vector<Pending>& batch) {
   size_t nitems = 0;
   for (const auto& p : batch) nitems += p.items.size();
+  const bool* on_cluster = nitems <= kClusterAllItems ? q->on_cluster_all : q->on_cluster;
   cfft_status st = grow_items(sl, nitems);
   if (st != CFFT_OK) return st;
   size_t at = 0;
   for (const auto& p : batch)
     for (const auto& it : p.items)
-      if (!q->on_cluster[it.log2N]) sl.h_items[at++] = it;
+      if (!on_cluster[it.log2N]) sl.h_items[at++] = it;
   const size_t nsmall = at;
   size_t first[32] = {}, count[32] = {};
   for (uint32_t lN = 0; lN < 32; ++lN) {
-    if (!q->on_cluster[lN]) continue;
+    if (!on_cluster[lN]) continue;
     first[lN] = at;
     for (const auto& p : batch)
       for (const auto& it : p.items)
@@ -246,7 +248,9 @@ cfft_status cfft_product_queue_create(const cfft_product_engine* engine, const c
   if (cudaGetDevice(&q->device) != cudaSuccess) st = fail(CFFT_ERR_CUDA, "no CUDA device");
   for (uint32_t lN = 0; lN < 32 && st == CFFT_OK; ++lN) {
     const cfft_u64_product_plan* p = lN <= 17 ? cfft_product_engine_plan(engine, lN) : nullptr;
-    q->on_cluster[lN] = p && lN >= big && u64_product_splittable(p);
+    const bool split = p && u64_product_splittable(p);
+    q->on_cluster[lN] = split && lN >= big;
+    q->on_cluster_all[lN] = config && config->cluster_log2N ? q->on_cluster[lN] : split;
   }
   const size_t ws = cfft_product_engine_workspace_bytes(engine);
   for (int k = 0; k < q->nslots && st == CFFT_OK; ++k) {

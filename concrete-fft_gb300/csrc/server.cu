@@ -408,13 +408,17 @@ cfft_status cfft_server_run(cfft_server* s, const cfft_serve_config* cfg, cfft_s
   if (!c.plain) gate.start();
   const auto t0 = std::chrono::steady_clock::now();
   const uint32_t nslots = std::max<uint32_t>(1, std::min<uint32_t>(c.max_inflight ? c.max_inflight : kSlots, kSlots));
-  // products of at least this size run one per thread-block cluster (only sizes whose
-  // plan has an unordered outer level can)
+  // products of at least this size run one per thread-block cluster (sizes whose plan
+  // has a cluster kernel); automatic (cluster_log2N = 0): N >= 8192, and every size in
+  // a launch of at most kClusterAllItems products, whose products would otherwise each
+  // take one SM of a mostly idle GPU
   const uint32_t big_log2N = c.cluster_log2N ? c.cluster_log2N : 13;
-  bool on_cluster[18] = {};
-  for (uint32_t lN = big_log2N; lN <= 17; ++lN) {
+  bool on_cluster_big[18] = {}, on_cluster_all[18] = {};
+  for (uint32_t lN = 0; lN <= 17; ++lN) {
     const cfft_u64_product_plan* p = cfft_product_engine_plan(s->engine, lN);
-    on_cluster[lN] = p && u64_product_splittable(p);
+    const bool split = p && u64_product_splittable(p);
+    on_cluster_big[lN] = split && lN >= big_log2N;
+    on_cluster_all[lN] = c.cluster_log2N ? on_cluster_big[lN] : split;
   }
   size_t done_count = 0;
 
@@ -467,7 +471,7 @@ cfft_status cfft_server_run(cfft_server* s, const cfft_serve_config* cfg, cfft_s
   } else if (c.via_queue) {
     // the same stream through the public work queue: each admitted request is
     // submitted on arrival; its ticket is polled until done
-    cfft_product_queue_config qc{std::min<uint32_t>(nslots, 4), big_log2N};
+    cfft_product_queue_config qc{std::min<uint32_t>(nslots, 4), c.cluster_log2N};
     cfft_product_queue* q = nullptr;
     cfft_status st = cfft_product_queue_create(s->engine, &qc, &q);
     if (st != CFFT_OK) return st;
@@ -557,6 +561,7 @@ cfft_status cfft_server_run(cfft_server* s, const cfft_serve_config* cfg, cfft_s
           if (sl.busy) continue;
           size_t nitems = 0;
           for (size_t ri : batch) nitems += reqs[ri].d.nprod;
+          const bool* on_cluster = nitems <= kClusterAllItems ? on_cluster_all : on_cluster_big;
           cfft_status st = ensure_items(sl, nitems);
           if (st != CFFT_OK) return st;
           // item records: the engine's products first, then the large ones grouped by N

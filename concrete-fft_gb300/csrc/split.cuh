@@ -319,6 +319,119 @@ __global__ void __launch_bounds__(256) c64_split_kernel(double2* data, DevLevels
   }
 }
 
+// An unordered transform with exactly one outer level, of radix R0 = 2^LS0 <= 4,
+// over a DIF base of m points, on a cluster of S = R0 x S1 CTAs (S1 = 2^LS1
+// classes of the base, S <= 8): CTA c = s0 * S1 + c1 holds class c1 (mod S1)
+// of slice s0, i.e. the slice's points j * S1 + c1 after the base's first pass.
+// Forward: CTA c takes 1/S of level 0's butterflies from global memory and
+// stores output k (slice slot(k), point i) into the staging buffer of the CTA
+// of that slice that computes the base's first-pass butterfly i mod (m/R);
+// after a cluster barrier the CTAs of a slice share out its first pass, each
+// output into the part of its class; after a second barrier the rest is local.
+// Inverse: each CTA loads its class, whose inverse first-pass butterflies
+// (p = c1 + b*S1) read only that class, stores each output into the part of its
+// class, finishes the base inverse locally, and after a barrier takes 1/S of
+// level 0's butterflies, reading point i of every slice from the CTA that
+// holds its class.  The same operations on the same values as the one-CTA
+// kernel, in place.
+template <int ALGO, bool FWD, int LS0, int LS1>
+__global__ void __launch_bounds__(256) c64_split2_kernel(double2* data, DevLevels L, const double2* __restrict__ w) {
+  constexpr int R = AlgoInfo<ALGO>::R;
+  constexpr int LR = Log2<R>::v;
+  constexpr int R0 = 1 << LS0;
+  constexpr int S1 = 1 << LS1;
+  constexpr int LS = LS0 + LS1;
+  constexpr int S = 1 << LS;
+  static_assert(!AlgoInfo<ALGO>::DIT, "DIF base algorithms only");
+  namespace cg = cooperative_groups;
+  cg::cluster_group cl = cg::this_cluster();
+  extern __shared__ double2 smem[];
+  grid_dependency_wait();
+  const int log2n = L.log2n[0];
+  const int log2m = L.log2n[1];
+  const int m = 1 << log2m;
+  const int log2c = log2m - LS1;
+  const int c = (int)(blockIdx.x & (S - 1));
+  const long t = blockIdx.x >> LS;
+  const int s0 = c >> LS1, c1 = c & (S1 - 1);
+  double2* g = data + (t << log2n);
+  double2* xs = smem;
+  double2* ys = smem + (1 << log2c);
+  const int tid = threadIdx.x, nth = blockDim.x;
+  const int lq = log2m - LR;
+  const int lpp = lq - LS1;
+  const int pp = 1 << lpp;
+  const int cnt = m >> LS;  // level-0 butterflies per CTA
+  const int i0 = c * cnt;
+  double2* part[S1];
+  if constexpr (FWD) {
+    const double2* wl = w + L.w_off[0];
+    const double2* wb = w + L.w_off[1] + m;
+#pragma unroll
+    for (int j = 0; j < S1; ++j) part[j] = cl.map_shared_rank(xs, (unsigned)((s0 << LS1) + j));
+    auto token = cl.barrier_arrive();  // every CTA runs before a peer's memory is written
+    c64 v0[R0];
+    if (tid < cnt) {
+#pragma unroll
+      for (int k = 0; k < R0; ++k) v0[k] = ld(g + (k << log2m) + i0 + tid);
+    }
+    cl.barrier_wait(std::move(token));
+    for (int b = tid; b < cnt; b += nth) {
+      const int i = i0 + b;
+      c64 v[R0];
+#pragma unroll
+      for (int k = 0; k < R0; ++k) v[k] = b == tid ? v0[k] : ld(g + (k << log2m) + i);
+      Core<R0, true, 0>::run(v);
+      const double2* twl = wl + (R0 - 1) * i - 1;
+      const int p = i & ((1 << lq) - 1);
+      const int dst = ((i >> lq) << lpp) + (p & (pp - 1));
+      const int cls = p >> lpp;
+#pragma unroll
+      for (int k = 0; k < R0; ++k) {
+        const c64 o = k == 0 ? v[0] : cmul(ldg(twl + k), v[k]);
+        st(cl.map_shared_rank(ys, (unsigned)((slot<R0>(k) << LS1) + cls)) + dst, o);
+      }
+    }
+    cl.sync();  // every staging buffer is complete; every read of the transform is done
+    first_pass_scatter<R, true, LS1>([&](int k, int b, int) { return ld(ys + (k << lpp) + b); }, pp, c1 * pp, 1,
+                                     part, wb, tid, nth);
+    cl.sync();  // every part is complete
+    const FlatBuf r = dif_after_first<R, true>(log2m, LS1, FlatBuf{xs}, FlatBuf{ys}, wb, tid, nth);
+    double2* gs = g + ((long)s0 << log2m) + c1;
+    for (int j = tid; j < (1 << log2c); j += nth) gs[j << LS1] = r.p[j];
+  } else {
+    const double2* wl = w + L.winv_off[0];
+    const double2* wb = w + m;
+#pragma unroll
+    for (int j = 0; j < S1; ++j) part[j] = cl.map_shared_rank(ys, (unsigned)((s0 << LS1) + j));
+    auto token = cl.barrier_arrive();
+    const double2* gs = g + ((long)s0 << log2m) + c1;
+    for (int j = tid; j < (1 << log2c); j += nth) xs[j] = gs[j << LS1];
+    __syncthreads();
+    cl.barrier_wait(std::move(token));
+    first_pass_scatter<R, false, LS1>([&](int k, int b, int) { return ld(xs + (k << lpp) + b); }, pp, c1, S1, part,
+                                      wb, tid, nth);
+    cl.sync();  // every part is complete; every read of the transform is done
+    const FlatBuf sv = dif_after_first<R, false>(log2m, LS1, FlatBuf{ys}, FlatBuf{xs}, wb, tid, nth);
+    cl.sync();  // every slice is complete
+    for (int b = tid; b < cnt; b += nth) {
+      const int i = i0 + b;
+      const int cls = i & (S1 - 1);
+      const int at = i >> LS1;
+      const double2* twl = wl + (R0 - 1) * i - 1;
+      c64 v[R0];
+      v[0] = ld(cl.map_shared_rank(sv.p, (unsigned)cls) + at);
+#pragma unroll
+      for (int k = 1; k < R0; ++k)
+        v[k] = cmul(ldg(twl + k), ld(cl.map_shared_rank(sv.p, (unsigned)((slot<R0>(k) << LS1) + cls)) + at));
+      Core<R0, false, 0>::run(v);
+#pragma unroll
+      for (int k = 0; k < R0; ++k) st(g + (k << log2m) + i, v[k]);
+    }
+    cl.sync();  // no CTA exits while a peer reads its shared memory
+  }
+}
+
 // Kernel pointer for (ALGO, direction, LS, MODE); nullptr where S = 2^LS
 // exceeds the radix that is split.
 template <int A, int LS>
@@ -331,8 +444,27 @@ const void* split_ptr_ls(bool fwd, int mode) {
   }
   return fwd ? (const void*)c64_split_kernel<A, true, LS, 1> : (const void*)c64_split_kernel<A, false, LS, 1>;
 }
+// Mode 2 (R0 = 2) and 3 (R0 = 4): c64_split2_kernel with S1 = 2^ls / R0, for DIF
+// bases with S1 <= R and R0 * S1 <= 8.
+template <int A, int LS0>
+const void* split2_ptr(bool fwd, int ls) {
+  if constexpr (AlgoInfo<A>::DIT) {
+    return nullptr;
+  } else {
+    constexpr int LRA = Log2<AlgoInfo<A>::R>::v;
+    const int ls1 = ls - LS0;
+    if (ls1 == 1) return fwd ? (const void*)c64_split2_kernel<A, true, LS0, 1> : (const void*)c64_split2_kernel<A, false, LS0, 1>;
+    if constexpr (LS0 == 1 && LRA >= 2) {
+      if (ls1 == 2)
+        return fwd ? (const void*)c64_split2_kernel<A, true, 1, 2> : (const void*)c64_split2_kernel<A, false, 1, 2>;
+    }
+    return nullptr;
+  }
+}
 template <int A>
 const void* split_ptr(bool fwd, int ls, int mode) {
+  if (mode == 2) return split2_ptr<A, 1>(fwd, ls);
+  if (mode == 3) return split2_ptr<A, 2>(fwd, ls);
   switch (ls) {
     case 1: return split_ptr_ls<A, 1>(fwd, mode);
     case 2: return split_ptr_ls<A, 2>(fwd, mode);

@@ -353,7 +353,8 @@ cfft_status cfft_product_engine_run(const cfft_product_engine* engine, const cff
 typedef struct cfft_product_queue_config {
   uint32_t max_inflight;  /* concurrent launches, 1..4 (0: 3) */
   uint32_t cluster_log2N; /* products with N >= 2^cluster_log2N run one per thread-block cluster
-                             (0: 13; > 17: never) */
+                             (> 17: never; 0: automatic, N >= 8192, and every size that has a
+                             cluster kernel in a launch of at most 12 products) */
 } cfft_product_queue_config;
 typedef struct cfft_product_queue cfft_product_queue;
 cfft_status cfft_product_queue_create(const cfft_product_engine* engine, const cfft_product_queue_config* config,
@@ -406,7 +407,9 @@ typedef struct cfft_serve_config {
   uint32_t max_inflight; /* concurrent launches, 1..3 */
   uint32_t record_every; /* keep the outputs of every k-th request (0: none) */
   uint32_t cluster_log2N; /* batched mode: products with N >= 2^cluster_log2N run one per
-                             thread-block cluster beside the engine launch (0: 13; > 17: never) */
+                             thread-block cluster beside the engine launch (> 17: never; 0:
+                             automatic, N >= 8192, and every size that has a cluster kernel in
+                             a launch of at most 12 products) */
   uint32_t staged_io;    /* batched mode: 0 = the kernels read the item records from and store
                             the results into page-locked host memory; 1 = item records copied
                             in and results copied out per launch */

@@ -250,8 +250,11 @@ def test_cluster_sizes_bit_exact(cuda, oracle, ctas):
             plan.inv(d)
             want = oracle.ordered_inv(algo, want)
             assert np.array_equal(bits(d.cpu().numpy()), bits(want)), (algo, n, ctas)
-    for n, base in [(256, 32), (1024, 64), (2048, 1024), (4096, 512), (8192, 1024), (16384, 512), (32768, 1024)]:
-        for algo in (2, 7):
+    # with one outer level of radix 2 or 4 over a DIF base, clusters of up to 8 CTAs
+    # take level 0's slices times the base's classes
+    for n, base in [(256, 32), (1024, 64), (2048, 1024), (2048, 512), (4096, 1024), (4096, 512), (8192, 1024),
+                    (16384, 512), (32768, 1024)]:
+        for algo in ((0, 2, 4, 6, 7) if n in (2048, 4096) else (2, 7)):
             plan = cf.unordered.Plan(n, cf.unordered.Method.UserProvided(algo, base))
             plan.set_cluster_size(ctas)
             x = rand_c64(2, n)

@@ -288,12 +288,14 @@ int split_log2(const C64Plan& p, long batch, int* mode) {
     return max_ls;
   }
   // without levels, keep at least 32 butterflies in each of a class's passes (64 for
-  // DIT, one thread per butterfly): with fewer the CTAs idle (fwd+inv of 512 points on
-  // Dif8: 12.8 us on 2 CTAs, 19.2 on 8; 1024 points on Dif16: 24.9 on 2, 36.3 on 8)
+  // DIT, one thread per butterfly), but split at least in two: with fewer butterflies
+  // the CTAs idle (fwd+inv of 512 points on Dif8: 12.8 us on 2 CTAs, 19.2 on 8; 1024
+  // points on Dif16: 24.9 on 2, 36.3 on 8), while the one-CTA kernel packs several
+  // small transforms per CTA (256 points on Dit4, batch 16: 20.8 us, 12.9 on 2 CTAs)
   if (*mode == 0) {
     const int lr = ilog2((size_t)algo_radix(p.base_algo));
     const int min_lb = (p.base_algo & 1) ? 6 : 5;
-    while (max_ls > 0 && log2n - max_ls - lr < min_lb) --max_ls;
+    while (max_ls > 1 && log2n - max_ls - lr < min_lb) --max_ls;
   }
   int ls = 0;
   while (ls < max_ls && (batch << ls) < target) ++ls;

@@ -137,16 +137,24 @@ __device__ __forceinline__ void level0_last(double2* g, int lm, double2* const* 
 // The first (s = 1) pass of a DIF transform over its cluster, for `per`
 // butterflies: butterfly b is p = p0 + b * pstep, load(k, b, p) gives its
 // input k (of R), and each output (p*R + k) is stored into the part of its
-// residue class mod S (distributed shared memory), compacted.  With twice as
-// many threads as butterflies (a multiple of 32), the butterflies are split
-// into halves as in stockham_pass.
-template <int R, bool FWD, int LS, class Load>
+// residue class mod S (distributed shared memory), compacted.  Every thread
+// calls before_store() once, before its first store (warp-uniformly): a
+// cluster barrier's wait there overlaps the barrier with the loads.  With
+// twice as many threads as butterflies (a multiple of 32), the butterflies are
+// split into halves as in stockham_pass.
+struct NoWait {
+  __device__ void operator()() const {}
+};
+template <int R, bool FWD, int LS, class Load, class Wait = NoWait>
 __device__ __forceinline__ void first_pass_scatter(Load load, int per, int p0, int pstep, double2* const* part,
-                                                   const double2* __restrict__ wb, int tid, int nth) {
+                                                   const double2* __restrict__ wb, int tid, int nth,
+                                                   Wait before_store = Wait{}) {
   constexpr int LR = Log2<R>::v;
   constexpr int S = 1 << LS;
   if (nth >= 2 * per && (per & 31) == 0) {
-    if (tid < 2 * per) {
+    if (tid >= 2 * per) {
+      before_store();
+    } else {
       const int h = tid >= per ? 1 : 0;
       const int b = tid - h * per;
       const int p = p0 + b * pstep;
@@ -155,6 +163,7 @@ __device__ __forceinline__ void first_pass_scatter(Load load, int per, int p0, i
       for (int k = 0; k < R; ++k) v[k] = load(k, b, p);
       const double2* tw = wb + (p << LR);
       c64 y[R / 2];
+      before_store();
       if (h == 0) {
         CoreHalf<R, FWD, 0>::run(v, y);
         st(part[0] + ((p << LR) >> LS), y[0]);
@@ -170,6 +179,7 @@ __device__ __forceinline__ void first_pass_scatter(Load load, int per, int p0, i
     }
     return;
   }
+  before_store();
   for (int b = tid; b < per; b += nth) {
     const int p = p0 + b * pstep;
     c64 v[R];
@@ -188,12 +198,13 @@ __device__ __forceinline__ void first_pass_scatter(Load load, int per, int p0, i
 // The first pass of a DIF transform held in global memory: CTA c takes the
 // butterflies [c*per, (c+1)*per) in full -- no output is computed twice --
 // reading their inputs from g.
-template <int R, bool FWD, int LS>
+template <int R, bool FWD, int LS, class Wait>
 __device__ __forceinline__ void dif_first_scatter(const double2* g, int lper, int c, double2* const* part,
-                                                  const double2* __restrict__ wb, int tid, int nth) {
+                                                  const double2* __restrict__ wb, int tid, int nth,
+                                                  Wait before_store) {
   const int per = (1 << lper) >> LS;
   first_pass_scatter<R, FWD, LS>([&](int k, int, int p) { return ld(g + (k << lper) + p); }, per, c * per, 1, part,
-                                 wb, tid, nth);
+                                 wb, tid, nth, before_store);
 }
 
 // MODE 0: the plan has no outer levels (ordered plan, or unordered with
@@ -228,8 +239,11 @@ __global__ void __launch_bounds__(256) c64_split_kernel(double2* data, DevLevels
     double2* part[S];
 #pragma unroll
     for (int j = 0; j < S; ++j) part[j] = cl.map_shared_rank(xs, (unsigned)j);
-    cl.sync();  // every CTA of the cluster is running before its shared memory is written
-    dif_first_scatter<R, FWD, LS>(g, log2n - LR, c, part, wb, tid, nth);
+    // every CTA of the cluster runs before its shared memory is written: the barrier's
+    // wait comes after the first pass's loads
+    auto token = cl.barrier_arrive();
+    dif_first_scatter<R, FWD, LS>(g, log2n - LR, c, part, wb, tid, nth,
+                                  [&] { cl.barrier_wait(std::move(token)); });
     cl.sync();  // every part is complete, and every read of the transform in global memory is done
     const FlatBuf r = dif_after_first<R, FWD>(log2n, LS, FlatBuf{xs}, FlatBuf{ys}, wb, tid, nth);
     for (int j = tid; j < (1 << log2c); j += nth) g[(j << LS) + c] = r.p[j];

@@ -126,6 +126,68 @@ __device__ __forceinline__ void f128_inv_bfly(F128Arrays d, long j, long t, cons
   d.im1[j + t] = mi.lo;
 }
 
+// One radix-2 stage of double-double butterflies with two warps per 32
+// butterflies: warp 2k computes the real parts of both outputs of butterflies
+// 32k .. 32k+31, warp 2k+1 their imaginary parts.  The real and imaginary
+// parts of a butterfly share no operation (cplx_mul, cplx_mul_conj), so each
+// half does exactly the operations of its outputs and the results are the
+// one-thread butterfly's bits; the inverse's conjugate product needs the other
+// half's difference, which passes through xs (4 doubles per butterfly of an
+// iteration).  A barrier separates every read of an iteration's elements from
+// the stores.  Warp-uniform halves keep each warp on one instruction stream.
+// map(b, qa, qb, widx) gives butterfly b's elements and twiddle index; nb
+// butterflies; every thread of the CTA calls it.
+template <bool FWD, class Map>
+__device__ __forceinline__ void f128_half_stage(F128Arrays s, double* xs, int nb, Map map, const F128Tw& tw,
+                                                int tid, int nth) {
+  const int h = (tid >> 5) & 1;
+  const int bi = ((tid >> 6) << 5) + (tid & 31);
+  const int step = nth >> 1;
+  double* d0 = h ? s.im0 : s.re0;
+  double* d1 = h ? s.im1 : s.re1;
+  for (int b0 = 0; b0 < nb; b0 += step) {
+    const int b = b0 + bi;
+    const bool act = b < nb;
+    int qa = 0, qb = 0;
+    f128 u{0, 0}, v{0, 0}, dd{0, 0}, wr{0, 0}, wi{0, 0};
+    if (act) {
+      long widx;
+      map(b, qa, qb, widx);
+      wr = f128{__ldg(tw.re0 + widx), __ldg(tw.re1 + widx)};
+      wi = f128{__ldg(tw.im0 + widx), __ldg(tw.im1 + widx)};
+      const f128 z0{d0[qa], d1[qa]};
+      if (FWD) {
+        const f128 z1r{s.re0[qb], s.re1[qb]}, z1i{s.im0[qb], s.im1[qb]};
+        // real: mul(z1r, wr) - mul(z1i, wi); imaginary: mul(z1i, wr) + mul(z1r, wi)
+        const f128 z = h ? add_est(mul(z1i, wr), mul(z1r, wi)) : sub_est(mul(z1r, wr), mul(z1i, wi));
+        u = add_est(z0, z);
+        v = sub_est(z0, z);
+      } else {
+        const f128 z1{d0[qb], d1[qb]};
+        dd = sub_est(z0, z1);  // dr (h = 0) or di (h = 1)
+        u = add_est(z0, z1);
+        double* x = xs + (((b - b0) << 1) + h) * 2;
+        x[0] = dd.hi;
+        x[1] = dd.lo;
+      }
+    }
+    __syncthreads();  // every read of this iteration's elements is done
+    if (act) {
+      if (!FWD) {
+        const double* x = xs + (((b - b0) << 1) + (h ^ 1)) * 2;
+        const f128 od{x[0], x[1]};
+        // real: mul(dr, wr) + mul(di, wi); imaginary: mul(di, wr) - mul(dr, wi)
+        v = h ? sub_est(mul(dd, wr), mul(od, wi)) : add_est(mul(dd, wr), mul(od, wi));
+      }
+      d0[qa] = u.hi;
+      d1[qa] = u.lo;
+      d0[qb] = v.hi;
+      d1[qb] = v.lo;
+    }
+    __syncthreads();  // the stores are done before the next reads
+  }
+}
+
 // Stages of a transform of 2^log2n points restricted to one sub-block of
 // 2^log2c points (sub-block index sb), all in shared memory.  Forward runs
 // t = 2^(log2c-1) .. 1 (src/fft128/mod.rs:363-401), inverse t = 1 .. 2^(log2c-1)

@@ -431,7 +431,8 @@ def run_gb300(args):
                          ("u128_product", lambda: measure_u128(torch, cf, 10, 3, local, world)),
                          ("mixed_batch_100k", lambda: measure_mixed(torch, cf, 3, 3, local, world)),
                          ("serving_20k_req_s", lambda: measure_serving(torch, cf, local, world)),
-                         ("reference_bench_cases", lambda: measure_reference_cases(torch, cf, local, world))):
+                         ("reference_bench_cases", lambda: measure_reference_cases(torch, cf, local, world)),
+                         ("one_call_latency", lambda: measure_latency(torch, cf, local, world))):
             t_cfg = time.perf_counter()
             try:
                 configs[name] = fn()
@@ -1548,6 +1549,85 @@ def run_serving(args):
         print_line(entry, world, data="synthetic (seeded Poisson stream, resident operands %d GiB)" % args.operand_gb)
 
 
+def measure_latency(torch, cf, local, world, cpu=True, cpu_seconds=0.5, profile_case=False):
+    """One call at a time on device-resident data, device time per call (20 calls in a CUDA
+    graph): u64 products of N = 2048, 4096, 8192 (Method::Measure plans) on the automatic path
+    (a cluster over the base's residue classes for a few products), on one CTA and as five
+    launches; a u128 product of N = 1024; fft128 and unordered transforms.  Beside them the
+    restated reference pipeline on one host core."""
+    import numpy as np
+    po = _oracle() if cpu and world == 1 else None
+    rng = np.random.default_rng(21)
+    if profile_case:
+        # ncu case: 20 lone products of N = 2048 (Dif4, base 1024) and 20 fft128 forwards of 512
+        plan = cf.product.U64ProductPlan(2048, cf.FftAlgo.Dif4, 1024)
+        a = torch.from_numpy(rng.integers(0, 2 ** 64, (1, 2048), dtype=np.uint64).view(np.int64)).cuda()
+        bh = torch.empty((1, 1024), dtype=torch.complex128, device="cuda")
+        plan.prepare_operand(torch.from_numpy(rng.integers(-128, 128, (1, 2048))).cuda(), bh)
+        out = torch.empty_like(a)
+        fp = cf.fft128.Plan(512)
+        arrs = [torch.rand((1, 512), dtype=torch.float64, device="cuda") for _ in range(4)]
+        for _ in range(20):
+            plan.product(a, bh, out)
+            fp.fwd(*arrs)
+        torch.cuda.synchronize()
+        return {"profile_case": "20 lone u64 products N=2048 (Dif4/1024) and 20 fft128 forwards n=512"}
+    rows = {}
+    with ClockSampler(local) as clk:
+        t0 = time.time()
+        for N in (2048, 4096, 8192):
+            plan = cf.product.U64ProductPlan(N, measure_seconds=0.002)
+            algo, base = plan.algo()
+            a_np = rng.integers(0, 2 ** 64, (1, N), dtype=np.uint64)
+            b_np = rng.integers(-128, 128, (1, N))
+            a = torch.from_numpy(a_np.view(np.int64)).cuda()
+            bh = torch.empty((1, N // 2), dtype=torch.complex128, device="cuda")
+            plan.prepare_operand(torch.from_numpy(b_np).cuda(), bh)
+            out = torch.empty_like(a)
+            z = torch.empty((1, N // 2), dtype=torch.complex128, device="cuda")
+            row = {"plan": "%s/%d" % (ALGO_NAMES[int(algo)], base),
+                   "auto_us": graph_device_us(torch, lambda: plan.product(a, bh, out))}
+            ok = out.clone()
+            plan.set_cluster_size(1)
+            row["one_cta_us"] = graph_device_us(torch, lambda: plan.product(a, bh, out))
+            plan.set_cluster_size(0)
+            row["five_launches_us"] = graph_device_us(torch, lambda: plan.product_unfused(a, bh, out, z))
+            row["paths_agree"] = bool(torch.equal(out, ok))
+            if po is not None:  # per product, over calls of 32 (the plan's set-up spread over them)
+                ca = rng.integers(0, 2 ** 64, (32, N), dtype=np.uint64)
+                wb = po.u64_prepare(N, int(algo), base, rng.integers(-128, 128, (32, N)))
+                reps, el = cpu_loop(lambda: po.u64_product(N, int(algo), base, ca, wb, nthreads=1), cpu_seconds)
+                row["cpu_one_core_us"] = el / (32 * reps) * 1e6
+            rows["u64_product_N%d" % N] = {k: (round(v, 2) if isinstance(v, float) else v) for k, v in row.items()}
+        # u128 product N = 1024
+        p128 = cf.product.U128ProductPlan(1024)
+        a_np = rng.integers(0, 2 ** 64, (1, 1024, 2), dtype=np.uint64)
+        b_np = rng.integers(-2 ** 15, 2 ** 15, (1, 1024))
+        a = torch.from_numpy(a_np.view(np.int64)).cuda()
+        bh = torch.empty((1, 4, 512), dtype=torch.float64, device="cuda")
+        p128.prepare_operand(torch.from_numpy(b_np).cuda(), bh)
+        out = torch.empty_like(a)
+        row = {"auto_us": round(graph_device_us(torch, lambda: p128.product(a, bh, out)), 2)}
+        if po is not None:
+            ca = rng.integers(0, 2 ** 64, (8, 1024, 2), dtype=np.uint64)
+            wb = po.u128_prepare(1024, rng.integers(-2 ** 15, 2 ** 15, (8, 1024)))
+            reps, el = cpu_loop(lambda: po.u128_product(1024, ca, wb, nthreads=1), cpu_seconds)
+            row["cpu_one_core_us"] = round(el / (8 * reps) * 1e6, 2)
+        rows["u128_product_N1024"] = row
+        clk.mark(t0, time.time())
+    return {"rows": rows, "clocks": clk.summary(),
+            "gpu": "device time per call: 20 calls captured in a CUDA graph, replayed 10 times, CUDA events",
+            "cpu": "the restated reference pipeline on one host core with the plan's algorithm, per product over "
+                   "calls of 32 products (8 for u128), so that the plan's set-up is spread as for a prepared plan"}
+
+
+def run_latency(args):
+    torch, cf, rank, world, local = gpu_setup()
+    res = measure_latency(torch, cf, local, world, cpu=not args.no_cpu_baseline, profile_case=args.profile_case)
+    if rank == 0:
+        print(json.dumps({"workload": "one call at a time (latency)", "results": res}))
+
+
 def run_u64_large(args):
     """Fused u64 products from N = 8192 (one product per thread-block cluster) against the
     plain five-launch path on the same products: N = 8192 (also against one CTA per
@@ -1677,7 +1757,7 @@ def main():
     ap.add_argument("--serve-seconds", type=float, default=1.0)
     ap.add_argument("--operand-gb", type=int, default=8)
     ap.add_argument("--workload", choices=["u64_product", "mixed", "ordered", "u128_product", "serving", "product_sum", "serde",
-                             "u64_large", "reference_cases"],
+                             "u64_large", "reference_cases", "latency"],
                     default="u64_product",
                     help="u64_product (default headline) or one of the other benchmark configurations")
     ap.add_argument("--mixed-items", type=int, default=100000)
@@ -1704,6 +1784,8 @@ def main():
         run_serving(args)
     elif args.workload == "product_sum":
         run_product_sum(args)
+    elif args.workload == "latency":
+        run_latency(args)
     elif args.workload == "reference_cases":
         torch, cf, rank, world, local = gpu_setup()
         res = measure_reference_cases(torch, cf, local, world, cpu=not args.no_cpu_baseline)

@@ -215,6 +215,7 @@ extern "C" {
     pub fn cfft_u64_product_plan_destroy(plan: *mut cfft_u64_product_plan);
     pub fn cfft_u64_product_poly_size(plan: *const cfft_u64_product_plan) -> usize;
     pub fn cfft_u64_product_algo(plan: *const cfft_u64_product_plan, base_algo: *mut c_int, base_n: *mut usize);
+    pub fn cfft_u64_product_set_cluster_size(plan: *mut cfft_u64_product_plan, ctas: c_int) -> c_int;
     pub fn cfft_u64_prepare_operand(
         plan: *const cfft_u64_product_plan,
         b: *const i64,

@@ -147,7 +147,8 @@ impl crate::fft128::Plan {
 }
 
 struct RawU64(*mut ffi::cfft_u64_product_plan);
-// SAFETY: immutable after creation (include/cfft.h).
+// SAFETY: immutable after creation (include/cfft.h) but for the CTAs-per-product
+// setting, an int read at each launch that changes speed only (set_cluster_size).
 unsafe impl Send for RawU64 {}
 unsafe impl Sync for RawU64 {}
 impl Drop for RawU64 {
@@ -194,6 +195,15 @@ impl U64ProductPlan {
         // SAFETY: live plan, valid out-pointers.
         unsafe { ffi::cfft_u64_product_algo(self.raw.0, &mut a, &mut b) };
         (FftAlgo::from_c(a), b)
+    }
+
+    /// CTAs per product: 0 automatic (a thread-block cluster for a few products or a
+    /// large N), 1 one CTA, 2/4/8 a cluster of that size, capped at what the plan
+    /// allows.  Changes speed only, never results.  The setting belongs to the plan,
+    /// so it applies to every clone; set it before the plan is shared across threads.
+    pub fn set_cluster_size(&mut self, ctas: i32) -> Result<(), GpuError> {
+        // SAFETY: live plan; `&mut self` orders this call after this handle's launches.
+        ffi::status(unsafe { ffi::cfft_u64_product_set_cluster_size(self.raw.0, ctas) })
     }
 
     /// Fourier operands of `count` signed-digit polynomials: `b` holds count * N i64,

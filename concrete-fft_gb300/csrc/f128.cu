@@ -65,17 +65,69 @@ __global__ void __launch_bounds__(256) f128_smem_kernel(F128Arrays g, int log2n,
   }
 }
 
+// Cluster layouts of one transform of 2^log2n points over S = 2^LS CTAs: a
+// stage of half-size t >= S pairs points of one residue class mod S, a stage
+// of t < S points of one block of n/S.  CTA c holds class c (the points
+// j*S + c, compacted to j) in A for the wide stages and block c (the points
+// c*n/S ..) in B for the narrow ones; two warps per 32 butterflies
+// (f128_half_stage).  The butterflies and twiddles are those of the one-CTA
+// kernel, so the results are bit-identical.
+template <bool FWD, int LS>
+__device__ __forceinline__ void f128_wide_stage(const F128Arrays& A, double* xs, int log2n, int c, int log2t,
+                                                const F128Tw& tw, int tid, int nth) {
+  const int lt = log2t - LS;
+  const long m = 1L << (log2n - 1 - log2t);
+  f128_half_stage<FWD>(A, xs, 1 << (log2n - LS - 1), [&](int b, int& qa, int& qb, long& widx) {
+    qa = ((b >> lt) << (lt + 1)) + (b & ((1 << lt) - 1));
+    qb = qa + (1 << lt);
+    widx = m + ((((long)qa << LS) + c) >> (log2t + 1));
+  }, tw, tid, nth);
+}
+template <bool FWD, int LS>
+__device__ __forceinline__ void f128_narrow_stage(const F128Arrays& B, double* xs, int log2n, int c, int log2t,
+                                                  const F128Tw& tw, int tid, int nth) {
+  const int lnp = log2n - LS;
+  const long m = 1L << (log2n - 1 - log2t);
+  f128_half_stage<FWD>(B, xs, 1 << (lnp - 1), [&](int b, int& qa, int& qb, long& widx) {
+    qa = ((b >> log2t) << (log2t + 1)) + (b & ((1 << log2t) - 1));
+    qb = qa + (1 << log2t);
+    widx = m + ((((long)c << lnp) + qa) >> (log2t + 1));
+  }, tw, tid, nth);
+}
+// class c (A) -> the blocks (B) of the cluster, through distributed shared memory
+template <int LS, class Cluster>
+__device__ __forceinline__ void f128_classes_to_blocks(Cluster& cl, const F128Arrays& A, const F128Arrays& B, int lnp,
+                                                       int c, int tid, int nth) {
+  for (int q = tid; q < (1 << lnp); q += nth) {
+    const int p = (q << LS) + c;
+    const unsigned o = (unsigned)(p >> lnp);
+    const int at = p & ((1 << lnp) - 1);
+    cl.map_shared_rank(B.re0, o)[at] = A.re0[q];
+    cl.map_shared_rank(B.re1, o)[at] = A.re1[q];
+    cl.map_shared_rank(B.im0, o)[at] = A.im0[q];
+    cl.map_shared_rank(B.im1, o)[at] = A.im1[q];
+  }
+}
+// block c (B) -> the classes (A) of the cluster
+template <int LS, class Cluster>
+__device__ __forceinline__ void f128_blocks_to_classes(Cluster& cl, const F128Arrays& A, const F128Arrays& B, int lnp,
+                                                       int c, int tid, int nth) {
+  for (int q = tid; q < (1 << lnp); q += nth) {
+    const int p = (c << lnp) + q;
+    const unsigned o = (unsigned)(p & ((1 << LS) - 1));
+    const int at = p >> LS;
+    cl.map_shared_rank(A.re0, o)[at] = B.re0[q];
+    cl.map_shared_rank(A.re1, o)[at] = B.re1[q];
+    cl.map_shared_rank(A.im0, o)[at] = B.im0[q];
+    cl.map_shared_rank(A.im1, o)[at] = B.im1[q];
+  }
+}
+
 // One transform of 2^log2n points (64 <= n <= 4096) per cluster of S = 2^LS CTAs,
-// for small batches: two warps per 32 butterflies (f128_half_stage) and S SMs
-// per transform.  A stage of half-size t >= S pairs points of one residue class
-// mod S, a stage of t < S points of one block of n/S: CTA c holds class c (the
-// points j*S + c, compacted to j) for the wide stages and block c (points
-// c*n/S ..) for the narrow ones, with one exchange between them through
-// distributed shared memory.  Forward: t = n/2 .. 1 (class, exchange, block);
-// inverse: t = 1 .. n/2 (block, exchange, class).  The butterflies and
-// twiddles are those of the one-CTA kernel, so the results are bit-identical.
-// Shared memory: the class and block copies of n/S points, and the exchange of
-// the inverse's differences.
+// for small batches (S SMs per transform).  Forward: t = n/2 .. 1 (wide stages,
+// exchange, narrow stages); inverse: t = 1 .. n/2 (narrow, exchange, wide).
+// Shared memory: A and B of n/S points each, and the exchange of the inverse's
+// differences.
 template <bool FWD, int LS>
 __global__ void __launch_bounds__(256) f128_cluster_kernel(F128Arrays g, int log2n, F128Tw tw) {
   constexpr int S = 1 << LS;
@@ -88,29 +140,9 @@ __global__ void __launch_bounds__(256) f128_cluster_kernel(F128Arrays g, int log
   const int c = (int)(blockIdx.x & (S - 1));
   const long base = (long)(blockIdx.x >> LS) << log2n;
   const int tid = threadIdx.x, nth = blockDim.x;
-  const F128Arrays A{sm, sm + np, sm + 2 * np, sm + 3 * np};               // class c
-  const F128Arrays B{sm + 4 * np, sm + 5 * np, sm + 6 * np, sm + 7 * np};  // block c
+  const F128Arrays A{sm, sm + np, sm + 2 * np, sm + 3 * np};
+  const F128Arrays B{sm + 4 * np, sm + 5 * np, sm + 6 * np, sm + 7 * np};
   double* xs = sm + 8 * np;
-  const int nb = np >> 1;  // butterflies per CTA and stage
-  // wide stage (log2t >= LS) on the class copy
-  auto wide = [&](int log2t) {
-    const int lt = log2t - LS;
-    const long m = 1L << (log2n - 1 - log2t);
-    f128_half_stage<FWD>(A, xs, nb, [&](int b, int& qa, int& qb, long& widx) {
-      qa = ((b >> lt) << (lt + 1)) + (b & ((1 << lt) - 1));
-      qb = qa + (1 << lt);
-      widx = m + ((((long)qa << LS) + c) >> (log2t + 1));
-    }, tw, tid, nth);
-  };
-  // narrow stage (log2t < LS) on the block copy
-  auto narrow = [&](int log2t) {
-    const long m = 1L << (log2n - 1 - log2t);
-    f128_half_stage<FWD>(B, xs, nb, [&](int b, int& qa, int& qb, long& widx) {
-      qa = ((b >> log2t) << (log2t + 1)) + (b & ((1 << log2t) - 1));
-      qb = qa + (1 << log2t);
-      widx = m + ((((long)c << lnp) + qa) >> (log2t + 1));
-    }, tw, tid, nth);
-  };
   auto token = cl.barrier_arrive();  // every CTA runs before a peer's memory is written
   if constexpr (FWD) {
     for (int q = tid; q < np; q += nth) {
@@ -121,20 +153,11 @@ __global__ void __launch_bounds__(256) f128_cluster_kernel(F128Arrays g, int log
       A.im1[q] = g.im1[p];
     }
     __syncthreads();
-    for (int lt = log2n - 1; lt >= LS; --lt) wide(lt);
+    for (int lt = log2n - 1; lt >= LS; --lt) f128_wide_stage<true, LS>(A, xs, log2n, c, lt, tw, tid, nth);
     cl.barrier_wait(std::move(token));
-    // class -> blocks: point (q << LS) + c to block ((q << LS) + c) >> lnp
-    for (int q = tid; q < np; q += nth) {
-      const int p = (q << LS) + c;
-      const unsigned o = (unsigned)(p >> lnp);
-      const int at = p & (np - 1);
-      cl.map_shared_rank(B.re0, o)[at] = A.re0[q];
-      cl.map_shared_rank(B.re1, o)[at] = A.re1[q];
-      cl.map_shared_rank(B.im0, o)[at] = A.im0[q];
-      cl.map_shared_rank(B.im1, o)[at] = A.im1[q];
-    }
+    f128_classes_to_blocks<LS>(cl, A, B, lnp, c, tid, nth);
     cl.sync();  // every block is complete (no peer memory is touched after this)
-    for (int lt = LS - 1; lt >= 0; --lt) narrow(lt);
+    for (int lt = LS - 1; lt >= 0; --lt) f128_narrow_stage<true, LS>(B, xs, log2n, c, lt, tw, tid, nth);
     for (int q = tid; q < np; q += nth) {
       const long p = base + ((long)c << lnp) + q;
       g.re0[p] = B.re0[q];
@@ -151,20 +174,11 @@ __global__ void __launch_bounds__(256) f128_cluster_kernel(F128Arrays g, int log
       B.im1[q] = g.im1[p];
     }
     __syncthreads();
-    for (int lt = 0; lt < LS; ++lt) narrow(lt);
+    for (int lt = 0; lt < LS; ++lt) f128_narrow_stage<false, LS>(B, xs, log2n, c, lt, tw, tid, nth);
     cl.barrier_wait(std::move(token));
-    // blocks -> classes: point (c << lnp) + q to class ((c << lnp) + q) & (S - 1)
-    for (int q = tid; q < np; q += nth) {
-      const int p = (c << lnp) + q;
-      const unsigned o = (unsigned)(p & (S - 1));
-      const int at = p >> LS;
-      cl.map_shared_rank(A.re0, o)[at] = B.re0[q];
-      cl.map_shared_rank(A.re1, o)[at] = B.re1[q];
-      cl.map_shared_rank(A.im0, o)[at] = B.im0[q];
-      cl.map_shared_rank(A.im1, o)[at] = B.im1[q];
-    }
+    f128_blocks_to_classes<LS>(cl, A, B, lnp, c, tid, nth);
     cl.sync();  // every class is complete
-    for (int lt = LS; lt <= log2n - 1; ++lt) wide(lt);
+    for (int lt = LS; lt <= log2n - 1; ++lt) f128_wide_stage<false, LS>(A, xs, log2n, c, lt, tw, tid, nth);
     for (int q = tid; q < np; q += nth) {
       const long p = base + ((long)q << LS) + c;
       g.re0[p] = A.re0[q];
@@ -190,6 +204,18 @@ __global__ void __launch_bounds__(256) f128_stage_kernel(F128Arrays g, int log2n
   }
 }
 
+// One u128 coefficient (lo, hi, read as i128) -> f128: hi = the nearest double, lo =
+// the nearest double to the remainder (src/fft128/mod.rs:2006-2016 pattern).
+__device__ __forceinline__ void u128_to_f128(uint64_t lo, uint64_t hi, double& xh, double& xl) {
+  xh = i128_to_f64_rne(lo, hi);
+  uint64_t tl, th;
+  double fr;
+  trunc_mod128(xh, tl, th, fr);
+  const uint64_t rl = lo - tl;
+  const uint64_t rh = hi - th - (lo < tl ? 1 : 0);
+  xl = i128_to_f64_rne(rl, rh);
+}
+
 // u128 product: the fft128 pipeline of src/fft128/mod.rs:1998-2058 fused.
 // a, out: N coefficients as (lo, hi) u64 pairs; bhat: 4 arrays of n = N/2 f64.
 __global__ void __launch_bounds__(256) u128_product_kernel(const uint64_t* __restrict__ a,
@@ -204,14 +230,8 @@ __global__ void __launch_bounds__(256) u128_product_kernel(const uint64_t* __res
     const uint64_t* ap = a + prod * 4L * n;
     for (int j = tid; j < 2 * n; j += nth) {
       // coefficient j -> re (j < n) or im (j >= n) of point j mod n
-      const uint64_t lo = __ldcs(ap + 2 * j), hi = __ldcs(ap + 2 * j + 1);
-      const double xh = i128_to_f64_rne(lo, hi);
-      uint64_t tl, th;
-      double fr;
-      trunc_mod128(xh, tl, th, fr);
-      const uint64_t rl = lo - tl;
-      const uint64_t rh = hi - th - (lo < tl ? 1 : 0);
-      const double xl = i128_to_f64_rne(rl, rh);
+      double xh, xl;
+      u128_to_f128(__ldcs(ap + 2 * j), __ldcs(ap + 2 * j + 1), xh, xl);
       if (j < n) {
         s.re0[j] = xh;
         s.re1[j] = xl;
@@ -243,6 +263,81 @@ __global__ void __launch_bounds__(256) u128_product_kernel(const uint64_t* __res
       __stcs(op + 2 * j + 1, rh);
     }
     __syncthreads();
+  }
+}
+
+// One u128 product of N = 2n coefficients (64 <= n <= 1024) per cluster of S = 2^LS
+// CTAs, for a few products: the steps of u128_product_kernel on the cluster
+// layouts of f128_cluster_kernel.  CTA c folds the coefficients of class c into
+// A, runs the wide forward stages, sends its class to the blocks, runs the
+// narrow forward stages, the pointwise product (the operand at the block's
+// points) and the narrow inverse stages on its block, sends the block to the
+// classes, runs the wide inverse stages and rounds class c.  The same operations
+// on the same values as the one-CTA kernel, so the results are bit-identical.
+template <int LS>
+__global__ void __launch_bounds__(256) u128_product_cluster_kernel(const uint64_t* __restrict__ a,
+                                                                  const double* __restrict__ bhat, long bhat_stride,
+                                                                  uint64_t* __restrict__ out, int log2n, F128Tw tw,
+                                                                  double factor) {
+  constexpr int S = 1 << LS;
+  namespace cg = cooperative_groups;
+  cg::cluster_group cl = cg::this_cluster();
+  extern __shared__ double sm[];
+  const int lnp = log2n - LS;
+  const int np = 1 << lnp;
+  const int n = 1 << log2n;
+  const int c = (int)(blockIdx.x & (S - 1));
+  const long prod = (long)(blockIdx.x >> LS);
+  const int tid = threadIdx.x, nth = blockDim.x;
+  const F128Arrays A{sm, sm + np, sm + 2 * np, sm + 3 * np};
+  const F128Arrays B{sm + 4 * np, sm + 5 * np, sm + 6 * np, sm + 7 * np};
+  double* xs = sm + 8 * np;
+  const uint64_t* ap = a + prod * 4L * n;
+  auto token = cl.barrier_arrive();  // every CTA runs before a peer's memory is written
+  // coefficient p of class c -> re of point p, coefficient p + n -> im of point p
+  for (int t = tid; t < 2 * np; t += nth) {
+    const int q = t & (np - 1);
+    const int j = ((q << LS) + c) + (t >= np ? n : 0);
+    double xh, xl;
+    u128_to_f128(__ldcs(ap + 2 * j), __ldcs(ap + 2 * j + 1), xh, xl);
+    if (t < np) {
+      A.re0[q] = xh;
+      A.re1[q] = xl;
+    } else {
+      A.im0[q] = xh;
+      A.im1[q] = xl;
+    }
+  }
+  __syncthreads();
+  for (int lt = log2n - 1; lt >= LS; --lt) f128_wide_stage<true, LS>(A, xs, log2n, c, lt, tw, tid, nth);
+  cl.barrier_wait(std::move(token));
+  f128_classes_to_blocks<LS>(cl, A, B, lnp, c, tid, nth);
+  cl.sync();  // every block is complete; every CTA is done with its class copy
+  for (int lt = LS - 1; lt >= 0; --lt) f128_narrow_stage<true, LS>(B, xs, log2n, c, lt, tw, tid, nth);
+  const double* bp = bhat + prod * bhat_stride + ((long)c << lnp);
+  for (int q = tid; q < np; q += nth) {
+    f128 pr, pi;
+    cplx_mul(f128{B.re0[q], B.re1[q]}, f128{B.im0[q], B.im1[q]}, f128{__ldg(bp + q), __ldg(bp + n + q)},
+             f128{__ldg(bp + 2 * n + q), __ldg(bp + 3 * n + q)}, pr, pi);
+    B.re0[q] = __dmul_rn(pr.hi, factor);
+    B.re1[q] = __dmul_rn(pr.lo, factor);
+    B.im0[q] = __dmul_rn(pi.hi, factor);
+    B.im1[q] = __dmul_rn(pi.lo, factor);
+  }
+  __syncthreads();
+  for (int lt = 0; lt < LS; ++lt) f128_narrow_stage<false, LS>(B, xs, log2n, c, lt, tw, tid, nth);
+  f128_blocks_to_classes<LS>(cl, A, B, lnp, c, tid, nth);
+  cl.sync();  // every class is complete (no peer memory is touched after this)
+  for (int lt = LS; lt <= log2n - 1; ++lt) f128_wide_stage<false, LS>(A, xs, log2n, c, lt, tw, tid, nth);
+  uint64_t* op = out + prod * 4L * n;
+  for (int t = tid; t < 2 * np; t += nth) {
+    const int q = t & (np - 1);
+    const int j = ((q << LS) + c) + (t >= np ? n : 0);
+    uint64_t rl, rh;
+    if (t < np) round_half_up_mod128(A.re0[q], A.re1[q], rl, rh);
+    else round_half_up_mod128(A.im0[q], A.im1[q], rl, rh);
+    __stcs(op + 2 * j, rl);
+    __stcs(op + 2 * j + 1, rh);
   }
 }
 
@@ -288,14 +383,8 @@ __global__ void __launch_bounds__(256) u128_fold_kernel(const uint64_t* __restri
   for (long g = (long)blockIdx.x * blockDim.x + threadIdx.x; g < total; g += (long)gridDim.x * blockDim.x) {
     const long p = g >> (log2n + 1), j = g & (2 * n - 1);
     const uint64_t* ap = a + p * 4 * n;
-    const uint64_t lo = __ldcs(ap + 2 * j), hi = __ldcs(ap + 2 * j + 1);
-    const double xh = i128_to_f64_rne(lo, hi);
-    uint64_t tl, th;
-    double fr;
-    trunc_mod128(xh, tl, th, fr);
-    const uint64_t rl = lo - tl;
-    const uint64_t rh = hi - th - (lo < tl ? 1 : 0);
-    const double xl = i128_to_f64_rne(rl, rh);
+    double xh, xl;
+    u128_to_f128(__ldcs(ap + 2 * j), __ldcs(ap + 2 * j + 1), xh, xl);
     if (j < n) {
       z.re0[p * n + j] = xh;
       z.re1[p * n + j] = xl;
@@ -780,10 +869,33 @@ cfft_status cfft_u128_product(const cfft_u128_product_plan* p, const uint64_t* a
   if (bhat_stride != 0 && bhat_stride != 2 * p->N)
     return fail(CFFT_ERR_INVALID_ARGUMENT, "bhat_stride must be 0 or 2N");
   if (count == 0) return CFFT_OK;
+  const bool few = (long)count < (long)sm_count() / 2;
+  // A few products of N = 128..2048: one product per cluster of up to 8 CTAs of 128
+  // points (u128_product_cluster_kernel), two warps per 32 butterflies
+  {
+    const int log2n = ilog2(p->f.n);
+    const int ls = std::max(0, log2n - 7);
+    if (log2n >= 6 && log2n <= 10 && ((long)count << ls) <= (long)sm_count() / 2) {
+      static const void* const kfn[4] = {
+          (const void*)u128_product_cluster_kernel<0>, (const void*)u128_product_cluster_kernel<1>,
+          (const void*)u128_product_cluster_kernel<2>, (const void*)u128_product_cluster_kernel<3>};
+      const void* fn = kfn[ls];
+      const int np = 1 << (log2n - ls);
+      const int threads = std::min(256, np);
+      const size_t smem = (8 * (size_t)np + 2 * (size_t)threads) * sizeof(double);
+      const int grid = (int)((long)count << ls);
+      long stride = (long)bhat_stride;
+      int ln = log2n;
+      F128Tw t = p->f.tw();
+      double factor = 2.0 / (double)p->N;
+      void* args[] = {(void*)&a, (void*)&bhat4, &stride, (void*)&out, &ln, &t, &factor};
+      return launch_kernel_cluster(fn, grid, threads, 1 << ls, args, spread_smem(fn, grid, threads, 1 << ls, smem),
+                                   (cudaStream_t)stream);
+    }
+  }
   // Above N = 8192, and for a few products of N >= 1024 (their transforms then spread
   // over many SMs instead of one CTA each): fold, forward, pointwise, inverse, round
   // as five launches around the plan's transform.  Bit-identical to the fused kernel.
-  const bool few = (long)count < (long)sm_count() / 2;
   if (ilog2(p->f.n) > kF128SmemLog2 || (few && p->f.n >= 512)) {
     cudaStream_t s = (cudaStream_t)stream;
     const int log2n = ilog2(p->f.n);

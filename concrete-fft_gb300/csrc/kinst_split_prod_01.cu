@@ -10,10 +10,10 @@ const void* u64_product_split_ptr_01(int algo, int ls, bool big) {
     default: return nullptr;
   }
 }
-const void* u64_product_split0_ptr_01(int algo, int ls) {
+const void* u64_product_split0_ptr_01(int algo, int ls, bool sum) {
   switch (algo) {
-    case 0: return split0_product_ptr<0>(ls);
-    case 1: return split0_product_ptr<1>(ls);
+    case 0: return split0_product_ptr<0>(ls, sum);
+    case 1: return split0_product_ptr<1>(ls, sum);
     default: return nullptr;
   }
 }

@@ -10,10 +10,10 @@ const void* u64_product_split_ptr_23(int algo, int ls, bool big) {
     default: return nullptr;
   }
 }
-const void* u64_product_split0_ptr_23(int algo, int ls) {
+const void* u64_product_split0_ptr_23(int algo, int ls, bool sum) {
   switch (algo) {
-    case 2: return split0_product_ptr<2>(ls);
-    case 3: return split0_product_ptr<3>(ls);
+    case 2: return split0_product_ptr<2>(ls, sum);
+    case 3: return split0_product_ptr<3>(ls, sum);
     default: return nullptr;
   }
 }

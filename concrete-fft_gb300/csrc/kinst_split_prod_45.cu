@@ -10,10 +10,10 @@ const void* u64_product_split_ptr_45(int algo, int ls, bool big) {
     default: return nullptr;
   }
 }
-const void* u64_product_split0_ptr_45(int algo, int ls) {
+const void* u64_product_split0_ptr_45(int algo, int ls, bool sum) {
   switch (algo) {
-    case 4: return split0_product_ptr<4>(ls);
-    case 5: return split0_product_ptr<5>(ls);
+    case 4: return split0_product_ptr<4>(ls, sum);
+    case 5: return split0_product_ptr<5>(ls, sum);
     default: return nullptr;
   }
 }

@@ -10,10 +10,10 @@ const void* u64_product_split_ptr_67(int algo, int ls, bool big) {
     default: return nullptr;
   }
 }
-const void* u64_product_split0_ptr_67(int algo, int ls) {
+const void* u64_product_split0_ptr_67(int algo, int ls, bool sum) {
   switch (algo) {
-    case 6: return split0_product_ptr<6>(ls);
-    case 7: return split0_product_ptr<7>(ls);
+    case 6: return split0_product_ptr<6>(ls, sum);
+    case 7: return split0_product_ptr<7>(ls, sum);
     default: return nullptr;
   }
 }

@@ -252,9 +252,9 @@ int split0_log2(const cfft_u64_product_plan* p, bool fast = true) {
 
 cfft_status launch_split0_product(const cfft_u64_product_plan* plan, int ls, const uint64_t* a, const double* bhat,
                                   size_t bhat_stride, uint64_t* out, size_t count, cudaStream_t stream,
-                                  const cfft_product_item* items = nullptr) {
+                                  const cfft_product_item* items = nullptr, int terms = 1) {
   const int algo = plan->base_algo;
-  const void* fn = u64_product_split0_ptr(algo, ls);
+  const void* fn = u64_product_split0_ptr(algo, ls, terms > 1);
   if (!fn) return fail(CFFT_ERR_INVALID_SIZE, "no cluster product kernel for this base and cluster size");
   if ((count << ls) > 0x7fffffffUL) return fail(CFFT_ERR_INVALID_SIZE, "batch too large");
   const size_t part = plan->n >> ls;
@@ -269,7 +269,7 @@ cfft_status launch_split0_product(const cfft_u64_product_plan* plan, int ls, con
   DevLevels L = plan->dlv;
   long stride = (long)bhat_stride;
   const double2* bh = (const double2*)bhat;
-  void* args[] = {(void*)&a, (void*)&bh, &stride, (void*)&out, (void*)&items, &L, (void*)&plan->d_w,
+  void* args[] = {(void*)&a, (void*)&bh, &stride, (void*)&out, &terms, (void*)&items, &L, (void*)&plan->d_w,
                   (void*)&plan->d_winv, (void*)&plan->d_tw, (void*)&plan->d_itw};
   // a few products: every CTA on an SM of its own
   return launch_kernel_cluster(fn, grid, threads, 1 << ls, args, spread_smem(fn, grid, threads, 1 << ls, smem),
@@ -419,6 +419,12 @@ cfft_status cfft_u64_product_sum(const cfft_u64_product_plan* plan, const uint64
                                   (int)terms);
   }
   if (count == 0) return CFFT_OK;
+  // a few outputs of a plan without an outer level on a DIF base (the external
+  // product of a blind-rotation step): one cluster per output, as the products
+  const int ls0 = split0_log2(plan);
+  if (ls0 >= 1 && !(plan->base_algo & 1) && (long)count < (long)sm_count() / 2 && plan->cluster == 0 &&
+      (plan->n >> ls0) <= (size_t)kSplit0Acc * 256)
+    return launch_split0_product(plan, ls0, a, bhat, plan->n, out, count, (cudaStream_t)stream, nullptr, (int)terms);
   const bool reg_acc = plan->n <= (size_t)(kSumRegAcc * kProdThreads);
   const void* fn = u64_product_sum_kernel_ptr(plan->base_algo, reg_acc);
   const size_t smem = (reg_acc ? 2 : 3) * plan->n * sizeof(double2);

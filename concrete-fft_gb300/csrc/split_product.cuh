@@ -71,6 +71,9 @@ __device__ __forceinline__ void level0_inv_untwist(double2* const* src, int lm, 
 // Accumulator entries per thread: the CTA sizes keep a part at most 8 entries
 // per thread (1024 points / 128 threads, 2048 / 256, 4096 / 512).
 constexpr int kSplitAcc = 8;
+// The same for u64_product_split0_kernel, whose launches give at least one
+// thread per two points of a part.
+constexpr int kSplit0Acc = 2;
 
 // One output per cluster of S CTAs (blockIdx.x >> LS): the sum over `terms`
 // products a_t * B_t, accumulated in the Fourier domain in term order, then
@@ -201,14 +204,17 @@ __global__ void __launch_bounds__(MAXT) u64_product_split_kernel(
 // class c: the pointwise product is applied as they are stored into z.  Every
 // inverse pass but the last is local; the last reads every part and its
 // outputs are untwisted, rounded and stored.
+// SUM (DIF bases): one output is the Fourier-domain sum of `terms` products:
+// each term runs the forward steps and is multiplied and added into a register
+// accumulator in term order, as in u64_product_sum_kernel, then one inverse.
 // Every butterfly and elementwise step does the operations of the one-CTA
 // product kernel on the same values, so results are bit-identical to it.
 // Shared memory: three buffers of n/S points.  Requires L.nlevels == 0,
-// S <= R and n >= R*S.
-template <int ALGO, int LS>
+// S <= R, n >= R*S and, for SUM, n/S <= kSplit0Acc x blockDim.x.
+template <int ALGO, int LS, bool SUM>
 __global__ void __launch_bounds__(256) u64_product_split0_kernel(
     const uint64_t* __restrict__ a, const double2* __restrict__ bhat, long bhat_stride, uint64_t* __restrict__ out,
-    const cfft_product_item* __restrict__ items, DevLevels L, const double2* __restrict__ w,
+    int terms, const cfft_product_item* __restrict__ items, DevLevels L, const double2* __restrict__ w,
     const double2* __restrict__ winv, const double2* __restrict__ tw, const double2* __restrict__ itw) {
   constexpr int R = AlgoInfo<ALGO>::R;
   constexpr int LR = Log2<R>::v;
@@ -242,22 +248,58 @@ __global__ void __launch_bounds__(256) u64_product_split0_kernel(
       peer_x[j] = cl.map_shared_rank(x, (unsigned)j);
       peer_z[j] = cl.map_shared_rank(z, (unsigned)j);
     }
-    auto token = cl.barrier_arrive();  // every CTA runs before a peer's memory is written
-    // input k of first-pass butterfly c*per + b, folded and twisted, at y[k*per + b]
-    for (int t = tid; t < (R << lpc); t += nth) {
-      const int j = ((t >> lpc) << lper) + c * per + (t & (per - 1));
-      const c64 v{i64_to_f64_rne((int64_t)__ldcs(ap + j)), i64_to_f64_rne((int64_t)__ldcs(ap + j + n))};
-      st(y + t, cmul(ldg(tw + j), v));
+    // SUM: a sum of `terms` products (terms of an output consecutive in a and bhat,
+    // bhat at stride bhat_stride): each term forward and multiplied, added into
+    // registers in term order, one inverse.  Otherwise one product (terms = 1).
+    c64 acc[SUM ? kSplit0Acc : 1];
+    const double2* src = x;  // input of the inverse's first pass
+    const int nterms = SUM ? terms : 1;
+#pragma unroll 1
+    for (int t = 0; t < nterms; ++t) {
+      const long term = g * nterms + t;
+      const uint64_t* tap = SUM ? a + (term << (log2n + 1)) : ap;
+      const double2* tbp = SUM ? bhat + term * bhat_stride : bp;
+      // every CTA runs, and is done with its x from the previous term, before a peer
+      // writes its x
+      auto token = cl.barrier_arrive();
+      if (t > 0) __syncthreads();  // this CTA is done with y
+      // input k of first-pass butterfly c*per + b, folded and twisted, at y[k*per + b]
+      for (int q = tid; q < (R << lpc); q += nth) {
+        const int j = ((q >> lpc) << lper) + c * per + (q & (per - 1));
+        const c64 v{i64_to_f64_rne((int64_t)__ldcs(tap + j)), i64_to_f64_rne((int64_t)__ldcs(tap + j + n))};
+        st(y + q, cmul(ldg(tw + j), v));
+      }
+      __syncthreads();
+      cl.barrier_wait(std::move(token));
+      first_pass_scatter<R, true, LS>([&](int k, int b, int) { return ld(y + (k << lpc) + b); }, per, c * per, 1,
+                                      peer_x, wf, tid, nth);
+      cl.sync();  // every part's x is complete
+      const FlatBuf r = dif_after_first<R, true>(log2n, LS, FlatBuf{x}, FlatBuf{y}, wf, tid, nth);
+      if constexpr (!SUM) {
+        for (int j = tid; j < (1 << log2c); j += nth) st(r.p + j, cmul(ldg(tbp + (j << LS) + c), ld(r.p + j)));
+        src = r.p;
+      } else {
+#pragma unroll
+        for (int k = 0; k < kSplit0Acc; ++k) {
+          const int j = tid + k * nth;
+          if (j < (1 << log2c)) {
+            const c64 p = cmul(ldg(tbp + (j << LS) + c), ld(r.p + j));
+            acc[k] = t == 0 ? p : cadd(acc[k], p);
+          }
+        }
+      }
+    }
+    if constexpr (SUM) {
+      __syncthreads();  // every read of the last term's buffers is done
+#pragma unroll
+      for (int k = 0; k < kSplit0Acc; ++k) {
+        const int j = tid + k * nth;
+        if (j < (1 << log2c)) st(y + j, acc[k]);
+      }
+      src = y;
     }
     __syncthreads();
-    cl.barrier_wait(std::move(token));
-    first_pass_scatter<R, true, LS>([&](int k, int b, int) { return ld(y + (k << lpc) + b); }, per, c * per, 1,
-                                    peer_x, wf, tid, nth);
-    cl.sync();  // every part's x is complete
-    const FlatBuf r = dif_after_first<R, true>(log2n, LS, FlatBuf{x}, FlatBuf{y}, wf, tid, nth);
-    for (int j = tid; j < (1 << log2c); j += nth) st(r.p + j, cmul(ldg(bp + (j << LS) + c), ld(r.p + j)));
-    __syncthreads();
-    first_pass_scatter<R, false, LS>([&](int k, int b, int) { return ld(r.p + (k << lpc) + b); }, per, c, S, peer_z,
+    first_pass_scatter<R, false, LS>([&](int k, int b, int) { return ld(src + (k << lpc) + b); }, per, c, S, peer_z,
                                      wi, tid, nth);
     cl.sync();  // every part's z is complete (no peer memory is touched after this)
     const FlatBuf s = dif_after_first<R, false>(log2n, LS, FlatBuf{z}, FlatBuf{x}, wi, tid, nth);
@@ -479,11 +521,12 @@ inline const void* u64_product_split_ptr(int algo, int ls, bool big) {
                   : algo < 4 ? u64_product_split_ptr_23(algo, ls, big)
                              : algo < 6 ? u64_product_split_ptr_45(algo, ls, big) : u64_product_split_ptr_67(algo, ls, big);
 }
-// the kernel for plans without an outer level; nullptr where S = 2^ls exceeds the radix
-const void* u64_product_split0_ptr_01(int algo, int ls);
-const void* u64_product_split0_ptr_23(int algo, int ls);
-const void* u64_product_split0_ptr_45(int algo, int ls);
-const void* u64_product_split0_ptr_67(int algo, int ls);
+// the kernel for plans without an outer level (sum: its Fourier-domain sum
+// variant); nullptr where S = 2^ls exceeds the radix, or a sum on a DIT base
+const void* u64_product_split0_ptr_01(int algo, int ls, bool sum);
+const void* u64_product_split0_ptr_23(int algo, int ls, bool sum);
+const void* u64_product_split0_ptr_45(int algo, int ls, bool sum);
+const void* u64_product_split0_ptr_67(int algo, int ls, bool sum);
 // the one-level kernel (DIF bases only); nullptr where the shape is not instantiated
 const void* u64_product_split2_ptr_01(int algo, int ls0, int ls1);
 const void* u64_product_split2_ptr_23(int algo, int ls0, int ls1);
@@ -495,10 +538,11 @@ inline const void* u64_product_split2_ptr(int algo, int ls0, int ls1) {
                              : algo < 6 ? u64_product_split2_ptr_45(algo, ls0, ls1)
                                         : u64_product_split2_ptr_67(algo, ls0, ls1);
 }
-inline const void* u64_product_split0_ptr(int algo, int ls) {
-  return algo < 2 ? u64_product_split0_ptr_01(algo, ls)
-                  : algo < 4 ? u64_product_split0_ptr_23(algo, ls)
-                             : algo < 6 ? u64_product_split0_ptr_45(algo, ls) : u64_product_split0_ptr_67(algo, ls);
+inline const void* u64_product_split0_ptr(int algo, int ls, bool sum) {
+  return algo < 2 ? u64_product_split0_ptr_01(algo, ls, sum)
+                  : algo < 4 ? u64_product_split0_ptr_23(algo, ls, sum)
+                             : algo < 6 ? u64_product_split0_ptr_45(algo, ls, sum)
+                                        : u64_product_split0_ptr_67(algo, ls, sum);
 }
 
 template <int A>
@@ -519,15 +563,22 @@ const void* split_product_ptr(int ls, bool big) {
   }
 }
 
-template <int A>
-const void* split0_product_ptr(int ls) {
+template <int A, bool SUM>
+const void* split0_product_ptr_t(int ls) {
   constexpr int LRA = Log2<AlgoInfo<A>::R>::v;
   switch (ls) {
-    case 1: return (const void*)u64_product_split0_kernel<A, 1>;
-    case 2: if constexpr (LRA >= 2) return (const void*)u64_product_split0_kernel<A, 2>; else return nullptr;
-    case 3: if constexpr (LRA >= 3) return (const void*)u64_product_split0_kernel<A, 3>; else return nullptr;
+    case 1: return (const void*)u64_product_split0_kernel<A, 1, SUM>;
+    case 2: if constexpr (LRA >= 2) return (const void*)u64_product_split0_kernel<A, 2, SUM>; else return nullptr;
+    case 3: if constexpr (LRA >= 3) return (const void*)u64_product_split0_kernel<A, 3, SUM>; else return nullptr;
     default: return nullptr;
   }
+}
+// sum: the Fourier-domain sum variant (DIF bases only)
+template <int A>
+const void* split0_product_ptr(int ls, bool sum) {
+  if (!sum) return split0_product_ptr_t<A, false>(ls);
+  if constexpr (AlgoInfo<A>::DIT) return nullptr;
+  else return split0_product_ptr_t<A, true>(ls);
 }
 
 // (R0, S1) = (2, 2), (2, 4), (4, 2) for DIF bases with S1 <= R

@@ -286,9 +286,10 @@ cfft_status cfft_u64_product_host(const cfft_u64_product_plan* plan, const uint6
  * mod (X^N + 1), every term transformed forward, multiplied and accumulated
  * in term order, then one inverse per group instead of one per term.
  * a: count * terms * N u64; bhat: count * terms * N/2 c64; out: count * N u64.
- * N <= 2^29: one output per CTA up to 8192, per thread-block cluster up to
- * 65536, and above that the unfused steps on a stream-ordered workspace of at
- * most 1 GiB (groups in chunks). */
+ * N <= 2^29: one output per CTA up to 8192 (fewer than SMs/2 outputs of a plan
+ * without an outer level on a DIF base: one thread-block cluster each), per
+ * thread-block cluster up to 65536, and above that the unfused steps on a
+ * stream-ordered workspace of at most 1 GiB (groups in chunks). */
 cfft_status cfft_u64_product_sum(const cfft_u64_product_plan* plan, const uint64_t* a, const double* bhat,
                                  size_t terms, uint64_t* out, size_t count, void* stream);
 

@@ -1600,28 +1600,30 @@ def measure_latency(torch, cf, local, world, cpu=True, cpu_seconds=0.5, profile_
                 row["cpu_one_core_us"] = el / (32 * reps) * 1e6
             rows["u64_product_N%d" % N] = {k: (round(v, 2) if isinstance(v, float) else v) for k, v in row.items()}
         # one external product of a blind-rotation step: 2 outputs, each the Fourier-domain
-        # sum of 4 products (k + 1 = 2, l = 2), N = 2048
-        plan = cf.product.U64ProductPlan(2048, measure_seconds=0.002)
-        algo, base = plan.algo()
-        a_np = rng.integers(0, 2 ** 64, (2, 4, 2048), dtype=np.uint64)
-        b_np = rng.integers(-128, 128, (8, 2048))
-        a = torch.from_numpy(a_np.view(np.int64)).cuda()
-        bh = torch.empty((2, 4, 1024), dtype=torch.complex128, device="cuda")
-        plan.prepare_operand(torch.from_numpy(b_np).cuda(), bh)
-        out = torch.empty((2, 2048), dtype=torch.int64, device="cuda")
-        row = {"plan": "%s/%d" % (ALGO_NAMES[int(algo)], base),
-               "auto_us": graph_device_us(torch, lambda: plan.product_sum(a, bh, out))}
-        ok = out.clone()
-        plan.set_cluster_size(1)
-        row["one_cta_per_output_us"] = graph_device_us(torch, lambda: plan.product_sum(a, bh, out))
-        plan.set_cluster_size(0)
-        row["paths_agree"] = bool(torch.equal(out, ok))
-        if po is not None:  # per external product, over calls of 16 (32 outputs of 4 terms)
-            ca = rng.integers(0, 2 ** 64, (32, 4, 2048), dtype=np.uint64)
-            wb = po.u64_prepare(2048, int(algo), base, rng.integers(-128, 128, (128, 2048))).reshape(32, 4, 1024)
-            reps, el = cpu_loop(lambda: po.u64_product_sum(2048, int(algo), base, ca, wb, nthreads=1), cpu_seconds)
-            row["cpu_one_core_us"] = el / (16 * reps) * 1e6
-        rows["external_product_N2048_2x4"] = {k: (round(v, 2) if isinstance(v, float) else v) for k, v in row.items()}
+        # sum of 4 products (k + 1 = 2, l = 2), N = 2048 and 4096
+        for N in (2048, 4096):
+            plan = cf.product.U64ProductPlan(N, measure_seconds=0.002)
+            algo, base = plan.algo()
+            a_np = rng.integers(0, 2 ** 64, (2, 4, N), dtype=np.uint64)
+            b_np = rng.integers(-128, 128, (8, N))
+            a = torch.from_numpy(a_np.view(np.int64)).cuda()
+            bh = torch.empty((2, 4, N // 2), dtype=torch.complex128, device="cuda")
+            plan.prepare_operand(torch.from_numpy(b_np).cuda(), bh)
+            out = torch.empty((2, N), dtype=torch.int64, device="cuda")
+            row = {"plan": "%s/%d" % (ALGO_NAMES[int(algo)], base),
+                   "auto_us": graph_device_us(torch, lambda: plan.product_sum(a, bh, out))}
+            ok = out.clone()
+            plan.set_cluster_size(1)
+            row["one_cta_per_output_us"] = graph_device_us(torch, lambda: plan.product_sum(a, bh, out))
+            plan.set_cluster_size(0)
+            row["paths_agree"] = bool(torch.equal(out, ok))
+            if po is not None:  # per external product, over calls of 16 (32 outputs of 4 terms)
+                ca = rng.integers(0, 2 ** 64, (32, 4, N), dtype=np.uint64)
+                wb = po.u64_prepare(N, int(algo), base, rng.integers(-128, 128, (128, N))).reshape(32, 4, N // 2)
+                reps, el = cpu_loop(lambda: po.u64_product_sum(N, int(algo), base, ca, wb, nthreads=1), cpu_seconds)
+                row["cpu_one_core_us"] = el / (16 * reps) * 1e6
+            rows["external_product_N%d_2x4" % N] = {k: (round(v, 2) if isinstance(v, float) else v)
+                                                    for k, v in row.items()}
         # u128 product N = 1024
         p128 = cf.product.U128ProductPlan(1024)
         a_np = rng.integers(0, 2 ** 64, (1, 1024, 2), dtype=np.uint64)

@@ -17,10 +17,10 @@ const void* u64_product_split0_ptr_01(int algo, int ls, bool sum) {
     default: return nullptr;
   }
 }
-const void* u64_product_split2_ptr_01(int algo, int ls0, int ls1) {
+const void* u64_product_split2_ptr_01(int algo, int ls0, int ls1, bool sum) {
   switch (algo) {
-    case 0: return split2_product_ptr<0>(ls0, ls1);
-    case 1: return split2_product_ptr<1>(ls0, ls1);
+    case 0: return split2_product_ptr<0>(ls0, ls1, sum);
+    case 1: return split2_product_ptr<1>(ls0, ls1, sum);
     default: return nullptr;
   }
 }

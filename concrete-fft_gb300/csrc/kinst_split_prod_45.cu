@@ -17,10 +17,10 @@ const void* u64_product_split0_ptr_45(int algo, int ls, bool sum) {
     default: return nullptr;
   }
 }
-const void* u64_product_split2_ptr_45(int algo, int ls0, int ls1) {
+const void* u64_product_split2_ptr_45(int algo, int ls0, int ls1, bool sum) {
   switch (algo) {
-    case 4: return split2_product_ptr<4>(ls0, ls1);
-    case 5: return split2_product_ptr<5>(ls0, ls1);
+    case 4: return split2_product_ptr<4>(ls0, ls1, sum);
+    case 5: return split2_product_ptr<5>(ls0, ls1, sum);
     default: return nullptr;
   }
 }

@@ -17,10 +17,10 @@ const void* u64_product_split0_ptr_67(int algo, int ls, bool sum) {
     default: return nullptr;
   }
 }
-const void* u64_product_split2_ptr_67(int algo, int ls0, int ls1) {
+const void* u64_product_split2_ptr_67(int algo, int ls0, int ls1, bool sum) {
   switch (algo) {
-    case 6: return split2_product_ptr<6>(ls0, ls1);
-    case 7: return split2_product_ptr<7>(ls0, ls1);
+    case 6: return split2_product_ptr<6>(ls0, ls1, sum);
+    case 7: return split2_product_ptr<7>(ls0, ls1, sum);
     default: return nullptr;
   }
 }

@@ -297,8 +297,8 @@ bool split2_shape(const cfft_u64_product_plan* p, int* ls0, int* ls1) {
 
 cfft_status launch_split2_product(const cfft_u64_product_plan* plan, int ls0, int ls1, const uint64_t* a,
                                   const double* bhat, size_t bhat_stride, uint64_t* out, size_t count,
-                                  cudaStream_t stream, const cfft_product_item* items = nullptr) {
-  const void* fn = u64_product_split2_ptr(plan->base_algo, ls0, ls1);
+                                  cudaStream_t stream, const cfft_product_item* items = nullptr, int terms = 1) {
+  const void* fn = u64_product_split2_ptr(plan->base_algo, ls0, ls1, terms > 1);
   if (!fn) return fail(CFFT_ERR_INVALID_SIZE, "no one-level cluster product kernel for this shape");
   const int ls = ls0 + ls1;
   if ((count << ls) > 0x7fffffffUL) return fail(CFFT_ERR_INVALID_SIZE, "batch too large");
@@ -310,7 +310,7 @@ cfft_status launch_split2_product(const cfft_u64_product_plan* plan, int ls0, in
   DevLevels L = plan->dlv;
   long stride = (long)bhat_stride;
   const double2* bh = (const double2*)bhat;
-  void* args[] = {(void*)&a, (void*)&bh, &stride, (void*)&out, (void*)&items, &L, (void*)&plan->d_w,
+  void* args[] = {(void*)&a, (void*)&bh, &stride, (void*)&out, &terms, (void*)&items, &L, (void*)&plan->d_w,
                   (void*)&plan->d_winv, (void*)&plan->d_tw, (void*)&plan->d_itw};
   return launch_kernel_cluster(fn, grid, threads, 1 << ls, args, spread_smem(fn, grid, threads, 1 << ls, smem),
                                stream);
@@ -409,6 +409,12 @@ cfft_status cfft_u64_product_sum(const cfft_u64_product_plan* plan, const uint64
                                  size_t terms, uint64_t* out, size_t count, void* stream) {
   if (!plan || !a || !bhat || !out) return fail(CFFT_ERR_INVALID_ARGUMENT, "null argument");
   if (terms == 0 || terms > 0x7fffffff) return fail(CFFT_ERR_INVALID_ARGUMENT, "terms must be at least 1");
+  // a few outputs of a plan with one outer level of radix 2 or 4 over a DIF base: one
+  // cluster of level-0 slices times base classes per output, as the products
+  int l0 = 0, l1 = 0;
+  if (count > 0 && (long)count < (long)sm_count() / 2 && plan->cluster == 0 && split2_shape(plan, &l0, &l1))
+    return launch_split2_product(plan, l0, l1, a, bhat, plan->n, out, count, (cudaStream_t)stream, nullptr,
+                                 (int)terms);
   if (plan->N > (size_t(2) << kBlockLog2Auto)) {  // one output per thread-block cluster (N = 8192: by default)
     bool ok = true;
     const int ls = product_split_log2(plan, count, &ok);

@@ -386,12 +386,15 @@ __global__ void __launch_bounds__(256) u64_product_split0_kernel(
 //      cluster barrier keeps every CTA alive while a peer reads its memory.
 // Every butterfly and elementwise step does the operations of the one-CTA
 // product kernel on the same values, so results are bit-identical to it.
+// SUM: one output is the Fourier-domain sum of `terms` products (steps 1-3 per
+// term, added into a register accumulator in term order, then one inverse).
 // Shared memory: three buffers of m/S1 points.  Requires L.nlevels == 1,
-// 2^L.log2r[0] == R0, S1 <= the base radix R and m >= R*S1.
-template <int ALGO, int LS0, int LS1>
+// 2^L.log2r[0] == R0, S1 <= the base radix R, m >= R*S1 and, for SUM,
+// m/S1 <= kSplit0Acc x blockDim.x.
+template <int ALGO, int LS0, int LS1, bool SUM>
 __global__ void __launch_bounds__(256) u64_product_split2_kernel(
     const uint64_t* __restrict__ a, const double2* __restrict__ bhat, long bhat_stride, uint64_t* __restrict__ out,
-    const cfft_product_item* __restrict__ items, DevLevels L, const double2* __restrict__ w,
+    int terms, const cfft_product_item* __restrict__ items, DevLevels L, const double2* __restrict__ w,
     const double2* __restrict__ winv, const double2* __restrict__ tw, const double2* __restrict__ itw) {
   constexpr int R = AlgoInfo<ALGO>::R;
   constexpr int LR = Log2<R>::v;
@@ -431,16 +434,29 @@ __global__ void __launch_bounds__(256) u64_product_split2_kernel(
     peer_x[j] = cl.map_shared_rank(x, (unsigned)((s0 << LS1) + j));
     peer_z[j] = cl.map_shared_rank(z, (unsigned)((s0 << LS1) + j));
   }
-  auto token = cl.barrier_arrive();  // every CTA runs before a peer's memory is written
-
-  // 1. level 0 forward on butterflies [c*m/S, (c+1)*m/S)
   const int cnt = m >> LS;
   const int i0 = c * cnt;
+  // SUM: a sum of `terms` products (terms of an output consecutive in a and bhat,
+  // bhat at stride bhat_stride), steps 1-3 per term, each product added into a
+  // register accumulator in term order, one inverse.  Otherwise one product.
+  c64 acc[SUM ? kSplit0Acc : 1];
+  const double2* src = nullptr;  // input of the inverse's first pass
+  const int nterms = SUM ? terms : 1;
+#pragma unroll 1
+  for (int t = 0; t < nterms; ++t) {
+  const long term = g * nterms + t;
+  const uint64_t* tap = SUM ? a + (term << (log2n + 1)) : ap;
+  const double2* tbp = SUM ? bhat + term * bhat_stride : bp;
+  // every CTA runs, and is done with its buffers of the previous term, before a
+  // peer writes them
+  auto token = cl.barrier_arrive();
+
+  // 1. level 0 forward on butterflies [c*m/S, (c+1)*m/S)
   auto load_l0 = [&](int i, c64* v) {
 #pragma unroll
     for (int k = 0; k < R0; ++k) {
       const int j = (k << log2m) + i;
-      const c64 u{i64_to_f64_rne((int64_t)__ldcs(ap + j)), i64_to_f64_rne((int64_t)__ldcs(ap + j + n))};
+      const c64 u{i64_to_f64_rne((int64_t)__ldcs(tap + j)), i64_to_f64_rne((int64_t)__ldcs(tap + j + n))};
       v[k] = cmul(ldg(tw + j), u);
     }
   };
@@ -476,10 +492,32 @@ __global__ void __launch_bounds__(256) u64_product_split2_kernel(
 
   // 3. the later passes, the pointwise product, the inverse's first pass
   const FlatBuf r = dif_after_first<R, true>(log2m, LS1, FlatBuf{x}, FlatBuf{y}, wf, tid, nth);
-  const double2* bs = bp + ((long)s0 << log2m) + c1;
-  for (int j = tid; j < (1 << log2c); j += nth) st(r.p + j, cmul(ldg(bs + (j << LS1)), ld(r.p + j)));
+  const double2* bs = tbp + ((long)s0 << log2m) + c1;
+  if constexpr (!SUM) {
+    for (int j = tid; j < (1 << log2c); j += nth) st(r.p + j, cmul(ldg(bs + (j << LS1)), ld(r.p + j)));
+    src = r.p;
+  } else {
+#pragma unroll
+    for (int k = 0; k < kSplit0Acc; ++k) {
+      const int j = tid + k * nth;
+      if (j < (1 << log2c)) {
+        const c64 p = cmul(ldg(bs + (j << LS1)), ld(r.p + j));
+        acc[k] = t == 0 ? p : cadd(acc[k], p);
+      }
+    }
+  }
+  }
+  if constexpr (SUM) {
+    __syncthreads();  // every read of the last term's buffers is done
+#pragma unroll
+    for (int k = 0; k < kSplit0Acc; ++k) {
+      const int j = tid + k * nth;
+      if (j < (1 << log2c)) st(y + j, acc[k]);
+    }
+    src = y;
+  }
   __syncthreads();
-  first_pass_scatter<R, false, LS1>([&](int k, int b, int) { return ld(r.p + (k << lpp) + b); }, pp, c1, S1, peer_z,
+  first_pass_scatter<R, false, LS1>([&](int k, int b, int) { return ld(src + (k << lpp) + b); }, pp, c1, S1, peer_z,
                                     wi, tid, nth);
   cl.sync();  // every part's z is complete
 
@@ -527,16 +565,17 @@ const void* u64_product_split0_ptr_01(int algo, int ls, bool sum);
 const void* u64_product_split0_ptr_23(int algo, int ls, bool sum);
 const void* u64_product_split0_ptr_45(int algo, int ls, bool sum);
 const void* u64_product_split0_ptr_67(int algo, int ls, bool sum);
-// the one-level kernel (DIF bases only); nullptr where the shape is not instantiated
-const void* u64_product_split2_ptr_01(int algo, int ls0, int ls1);
-const void* u64_product_split2_ptr_23(int algo, int ls0, int ls1);
-const void* u64_product_split2_ptr_45(int algo, int ls0, int ls1);
-const void* u64_product_split2_ptr_67(int algo, int ls0, int ls1);
-inline const void* u64_product_split2_ptr(int algo, int ls0, int ls1) {
-  return algo < 2 ? u64_product_split2_ptr_01(algo, ls0, ls1)
-                  : algo < 4 ? u64_product_split2_ptr_23(algo, ls0, ls1)
-                             : algo < 6 ? u64_product_split2_ptr_45(algo, ls0, ls1)
-                                        : u64_product_split2_ptr_67(algo, ls0, ls1);
+// the one-level kernel (DIF bases only; sum: its Fourier-domain sum variant);
+// nullptr where the shape is not instantiated
+const void* u64_product_split2_ptr_01(int algo, int ls0, int ls1, bool sum);
+const void* u64_product_split2_ptr_23(int algo, int ls0, int ls1, bool sum);
+const void* u64_product_split2_ptr_45(int algo, int ls0, int ls1, bool sum);
+const void* u64_product_split2_ptr_67(int algo, int ls0, int ls1, bool sum);
+inline const void* u64_product_split2_ptr(int algo, int ls0, int ls1, bool sum) {
+  return algo < 2 ? u64_product_split2_ptr_01(algo, ls0, ls1, sum)
+                  : algo < 4 ? u64_product_split2_ptr_23(algo, ls0, ls1, sum)
+                             : algo < 6 ? u64_product_split2_ptr_45(algo, ls0, ls1, sum)
+                                        : u64_product_split2_ptr_67(algo, ls0, ls1, sum);
 }
 inline const void* u64_product_split0_ptr(int algo, int ls, bool sum) {
   return algo < 2 ? u64_product_split0_ptr_01(algo, ls, sum)
@@ -582,19 +621,24 @@ const void* split0_product_ptr(int ls, bool sum) {
 }
 
 // (R0, S1) = (2, 2), (2, 4), (4, 2) for DIF bases with S1 <= R
-template <int A>
-const void* split2_product_ptr(int ls0, int ls1) {
+template <int A, bool SUM>
+const void* split2_product_ptr_t(int ls0, int ls1) {
   if constexpr (AlgoInfo<A>::DIT) {
     return nullptr;
   } else {
     constexpr int LRA = Log2<AlgoInfo<A>::R>::v;
-    if (ls0 == 1 && ls1 == 1) return (const void*)u64_product_split2_kernel<A, 1, 1>;
+    if (ls0 == 1 && ls1 == 1) return (const void*)u64_product_split2_kernel<A, 1, 1, SUM>;
     if constexpr (LRA >= 2) {
-      if (ls0 == 1 && ls1 == 2) return (const void*)u64_product_split2_kernel<A, 1, 2>;
+      if (ls0 == 1 && ls1 == 2) return (const void*)u64_product_split2_kernel<A, 1, 2, SUM>;
     }
-    if (ls0 == 2 && ls1 == 1) return (const void*)u64_product_split2_kernel<A, 2, 1>;
+    if (ls0 == 2 && ls1 == 1) return (const void*)u64_product_split2_kernel<A, 2, 1, SUM>;
     return nullptr;
   }
+}
+// sum: the Fourier-domain sum variant
+template <int A>
+const void* split2_product_ptr(int ls0, int ls1, bool sum) {
+  return sum ? split2_product_ptr_t<A, true>(ls0, ls1) : split2_product_ptr_t<A, false>(ls0, ls1);
 }
 
 }  // namespace cfft

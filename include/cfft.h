@@ -287,7 +287,8 @@ cfft_status cfft_u64_product_host(const cfft_u64_product_plan* plan, const uint6
  * in term order, then one inverse per group instead of one per term.
  * a: count * terms * N u64; bhat: count * terms * N/2 c64; out: count * N u64.
  * N <= 2^29: one output per CTA up to 8192 (fewer than SMs/2 outputs of a plan
- * without an outer level on a DIF base: one thread-block cluster each), per
+ * on a DIF base without an outer level or with one of radix 2 or 4: one
+ * thread-block cluster each), per
  * thread-block cluster up to 65536, and above that the unfused steps on a
  * stream-ordered workspace of at most 1 GiB (groups in chunks). */
 cfft_status cfft_u64_product_sum(const cfft_u64_product_plan* plan, const uint64_t* a, const double* bhat,

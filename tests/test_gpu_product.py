@@ -395,10 +395,12 @@ def test_u128_product_host_pipeline(cuda, oracle):
 @pytest.mark.parametrize("N,algo,base,terms", [(2048, 2, 1024, 8), (1024, 4, 512, 3), (4096, 6, 1024, 1),
                                                (8192, 3, 1024, 2), (16384, 2, 1024, 3), (32768, 6, 1024, 2),
                                                (1 << 18, 2, 1024, 3), (2048, 6, 1024, 4), (2048, 0, 1024, 2),
-                                               (2048, 3, 1024, 3), (512, 2, 256, 2)])
+                                               (2048, 3, 1024, 3), (512, 2, 256, 2), (4096, 2, 1024, 3),
+                                               (8192, 4, 1024, 2), (4096, 0, 1024, 2), (8192, 6, 1024, 2)])
 def test_u64_product_sum_bit_exact(cuda, oracle, N, algo, base, terms):
     """Fourier-domain accumulation of `terms` products, one inverse per group (4 groups:
-    a cluster per group for plans without an outer level on a DIF base)."""
+    a cluster per group for plans on a DIF base without an outer level or with one of
+    radix 2 or 4)."""
     import concrete_fft as cf
     torch = cuda
     count = 4

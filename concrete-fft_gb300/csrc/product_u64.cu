@@ -540,15 +540,19 @@ cfft_status cfft_u64_product(const cfft_u64_product_plan* plan, const uint64_t* 
   // (no cluster holds it), and large batches of N >= 32768, where it measured faster
   // than one cluster per product (304 vs 280 k products/s at 32768, 129 vs 102 k at 65536)
   const bool many = (long)count >= (long)sm_count() / 2 && plan->cluster == 0;
-  // Fewer than SMs/2 products whose transform has no outer level (n = base_n): one
-  // cluster per product on the base's residue classes (u64_product_split0_kernel), as
-  // does a plan forced to a cluster size.  Device time per call at N = 2048, Dif4, 4
+  // A few products whose transform has no outer level (n = base_n): one cluster per
+  // product on the base's residue classes (u64_product_split0_kernel), as does a plan
+  // forced to a cluster size.  Device time per call at N = 2048, Dif4, 4
   // CTAs: 11.7 us for one product (one CTA: 32.2, the five launches: 13.7), 16.7 for
   // 38 (one CTA: 34.9, five launches: 19.4)
   if (plan->cluster >= 2 && split0_log2(plan, false) >= 1)
     return launch_split0_product(plan, std::min(split0_log2(plan, false), ilog2((size_t)plan->cluster)), a, bhat,
                                  bhat_stride, out, count, (cudaStream_t)stream);
-  if (plan->cluster == 0 && plan->N >= 512 && !many && split0_log2(plan) >= 1)
+  // Base radix >= 4: up to one product per SM (N = 2048, 152 products: 25.5 us on Dif4
+  // clusters, 33.9 on one CTA each; Dif8 28.9 against 35.0); radix 2 lost there (Dif2,
+  // N = 1024, 152 products: 24.9 against 20.5 us) and keeps the SMs/2 limit.
+  const long split0_max = (plan->base_algo >= 2) ? (long)sm_count() : (long)sm_count() / 2 - 1;
+  if (plan->cluster == 0 && plan->N >= 512 && (long)count <= split0_max && split0_log2(plan) >= 1)
     return launch_split0_product(plan, split0_log2(plan), a, bhat, bhat_stride, out, count, (cudaStream_t)stream);
   // Likewise a plan with one outer level of radix 2 or 4 over a DIF base: level 0's
   // slices times classes of the base (u64_product_split2_kernel).  One product, Dif4

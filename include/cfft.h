@@ -263,9 +263,10 @@ cfft_status cfft_u64_product_set_int_adds(cfft_u64_product_plan* plan, int eight
 int cfft_u64_product_int_adds(const cfft_u64_product_plan* plan);
 /* CTAs per product (no counterpart in the reference): 0 chooses per call (a
  * cluster when N > 8192, which needs one, or when the batch is too small to
- * give every SM a product; fewer than SMs/2 products of a plan without an
- * outer level, N/2 = base_n, or with one of radix 2 or 4 over a DIF base, on a
- * cluster over the base algorithm's residue classes), 1 one CTA (N <= 8192),
+ * give every SM a product; a few products of a plan without an outer level,
+ * N/2 = base_n (up to one per SM; radix-2 bases fewer than SMs/2), or with one
+ * of radix 2 or 4 over a DIF base (fewer than SMs/2), on a cluster over the
+ * base algorithm's residue classes), 1 one CTA (N <= 8192),
  * 2/4/8 force a cluster of that size, capped
  * at what the plan allows (level 0's radix, or the base radix without levels,
  * with at least 64 points per CTA; N > 8192 also needs N/2/S <= 4096).

@@ -321,6 +321,27 @@ def test_u64_product_no_level_clusters_bit_exact(cuda, oracle, N, base):
             assert np.array_equal(out.cpu().numpy().view(np.uint64), want), (N, algo, ctas)
 
 
+def test_u64_product_no_level_clusters_up_to_one_per_sm(cuda):
+    """Up to one product per SM on a radix-4 base runs on clusters by default: the
+    same bits as one CTA per product, at 120 and 152 products."""
+    import concrete_fft as cf
+    torch = cuda
+    plan = cf.product.U64ProductPlan(2048, 2, 1024)
+    for count in (120, 152):
+        a = torch.from_numpy(RNG.integers(0, 2 ** 64, (count, 2048), dtype=np.uint64).view(np.int64)).cuda()
+        b = torch.from_numpy(RNG.integers(-2 ** 7, 2 ** 7, (count, 2048))).cuda()
+        bhat = torch.empty((count, 1024), dtype=torch.complex128, device="cuda")
+        plan.prepare_operand(b, bhat)
+        out0 = torch.zeros_like(a)
+        plan.set_cluster_size(0)
+        plan.product(a, bhat, out0)
+        out1 = torch.zeros_like(a)
+        plan.set_cluster_size(1)
+        plan.product(a, bhat, out1)
+        plan.set_cluster_size(0)
+        assert torch.equal(out0, out1), count
+
+
 @pytest.mark.parametrize("N,base", [(4096, 1024), (8192, 1024), (4096, 512), (2048, 512)])
 def test_u64_product_one_level_clusters_bit_exact(cuda, oracle, N, base):
     """A few products of a plan with one outer level (radix 2 or 4) run on a cluster of

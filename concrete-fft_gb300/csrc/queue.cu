@@ -12,6 +12,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <chrono>
 #include <condition_variable>
 #include <deque>
 #include <mutex>
@@ -121,9 +122,15 @@ void finish(cfft_product_queue* q, const std::vector<uint64_t>& tickets, int res
   for (uint64_t t : tickets) q->state[t] = result;
 }
 
+// After its last launch completes the worker keeps polling for this long before it
+// blocks on the condition variable: a request that arrives meanwhile is launched
+// without the scheduler's wake-up latency (tens of microseconds).
+constexpr auto kQueueSpin = std::chrono::microseconds(200);
+
 void worker_main(cfft_product_queue* q) {
   cudaSetDevice(q->device);
   std::unique_lock<std::mutex> lk(q->mu);
+  auto idle_since = std::chrono::steady_clock::now();
   for (;;) {
     int free_slot = -1;
     bool any_busy = false;
@@ -158,7 +165,14 @@ void worker_main(cfft_product_queue* q) {
     }
     if (!any_busy) {
       if (q->stop && q->pending.empty()) break;
+      if (std::chrono::steady_clock::now() - idle_since < kQueueSpin) {
+        lk.unlock();
+        std::this_thread::yield();
+        lk.lock();
+        continue;
+      }
       q->cv_work.wait(lk);
+      idle_since = std::chrono::steady_clock::now();
       continue;
     }
     // launches in flight: look at their events without holding the lock
@@ -186,6 +200,7 @@ void worker_main(cfft_product_queue* q) {
     finish(q, sl.tickets, err == cudaSuccess ? 1 : (int)CFFT_ERR_CUDA);
     sl.tickets.clear();
     sl.busy = false;
+    idle_since = std::chrono::steady_clock::now();
     q->cv_done.notify_all();
   }
 }

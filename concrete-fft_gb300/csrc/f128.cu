@@ -525,24 +525,27 @@ cfft_status run_f128_tw(size_t n, const F128Tw& tw, double* re0, double* re1, do
   cfft_status ast = f128_attrs();
   if (ast != CFFT_OK) return ast;
   const int log2n = ilog2(n);
-  // a small batch of 64..1024 points: one transform per cluster of up to 8 CTAs of
-  // 128 points, two warps per 32 butterflies, every CTA on an SM of its own.  fwd+inv,
-  // one transform: 24.9 us at 64 points (one CTA, a thread per butterfly: 43.6), 42.1
-  // at 512 (75.8), 46.7 at 1024 (85.2).  Larger transforms spread over more SMs through
-  // the global stages (4096 points: 105 us against 197 on a cluster of 8), and from
-  // SMs/2 CTAs on the block path is as fast
-  if (!one_kernel && block_log2 == 0 && log2n >= 6 && log2n <= 10) {
-    const int ls = std::max(0, log2n - 7);
-    if (((long)batch << ls) <= (long)sm_count() / 2) {
-      static const void* const kfn[2][4] = {
-          {(const void*)f128_cluster_kernel<false, 0>, (const void*)f128_cluster_kernel<false, 1>,
-           (const void*)f128_cluster_kernel<false, 2>, (const void*)f128_cluster_kernel<false, 3>},
-          {(const void*)f128_cluster_kernel<true, 0>, (const void*)f128_cluster_kernel<true, 1>,
-           (const void*)f128_cluster_kernel<true, 2>, (const void*)f128_cluster_kernel<true, 3>}};
-      const void* fn = kfn[fwd ? 1 : 0][ls];
-      const int np = 1 << (log2n - ls);
-      const int threads = std::min(256, np);
-      const size_t smem = (8 * (size_t)np + 2 * (size_t)threads) * sizeof(double);
+  // a small batch of 64..4096 points: one transform per cluster, two warps per 32
+  // butterflies, every CTA on an SM of its own: up to 8 CTAs of 128 points up to 1024
+  // points, 16 CTAs (a non-portable cluster size, when such a cluster fits) at 2048 and
+  // 4096.  fwd+inv, one transform: 24.9 us at 64 points (one CTA, a thread per
+  // butterfly: 43.6), 42.1 at 512 (75.8), 46.7 at 1024 (85.2), 51.7 at 2048 (93.6 over
+  // global stages), 102.6 at 4096 (104.4; 197 on a cluster of 8).  From SMs/2 CTAs on
+  // the block path is as fast
+  if (!one_kernel && block_log2 == 0 && log2n >= 6 && log2n <= 12) {
+    const int ls = log2n <= 10 ? std::max(0, log2n - 7) : 4;
+    static const void* const kfn[2][5] = {
+        {(const void*)f128_cluster_kernel<false, 0>, (const void*)f128_cluster_kernel<false, 1>,
+         (const void*)f128_cluster_kernel<false, 2>, (const void*)f128_cluster_kernel<false, 3>,
+         (const void*)f128_cluster_kernel<false, 4>},
+        {(const void*)f128_cluster_kernel<true, 0>, (const void*)f128_cluster_kernel<true, 1>,
+         (const void*)f128_cluster_kernel<true, 2>, (const void*)f128_cluster_kernel<true, 3>,
+         (const void*)f128_cluster_kernel<true, 4>}};
+    const void* fn = kfn[fwd ? 1 : 0][ls];
+    const int np = 1 << (log2n - ls);
+    const int threads = std::min(256, np);
+    const size_t smem = (8 * (size_t)np + 2 * (size_t)threads) * sizeof(double);
+    if (((long)batch << ls) <= (long)sm_count() / 2 && (ls <= 3 || cluster_fits(fn, threads, 1 << ls, smem))) {
       const int grid = (int)((long)batch << ls);
       F128Arrays g{re0, re1, im0, im1};
       F128Tw t = tw;
@@ -870,19 +873,22 @@ cfft_status cfft_u128_product(const cfft_u128_product_plan* p, const uint64_t* a
     return fail(CFFT_ERR_INVALID_ARGUMENT, "bhat_stride must be 0 or 2N");
   if (count == 0) return CFFT_OK;
   const bool few = (long)count < (long)sm_count() / 2;
-  // A few products of N = 128..2048: one product per cluster of up to 8 CTAs of 128
-  // points (u128_product_cluster_kernel), two warps per 32 butterflies
+  // A few products of N = 128..8192: one product per cluster of up to 8 CTAs of 128
+  // points, 16 CTAs at N = 4096 and 8192 (u128_product_cluster_kernel), two warps
+  // per 32 butterflies
   {
     const int log2n = ilog2(p->f.n);
-    const int ls = std::max(0, log2n - 7);
-    if (log2n >= 6 && log2n <= 10 && ((long)count << ls) <= (long)sm_count() / 2) {
-      static const void* const kfn[4] = {
-          (const void*)u128_product_cluster_kernel<0>, (const void*)u128_product_cluster_kernel<1>,
-          (const void*)u128_product_cluster_kernel<2>, (const void*)u128_product_cluster_kernel<3>};
-      const void* fn = kfn[ls];
-      const int np = 1 << (log2n - ls);
-      const int threads = std::min(256, np);
-      const size_t smem = (8 * (size_t)np + 2 * (size_t)threads) * sizeof(double);
+    const int ls = log2n <= 10 ? std::max(0, log2n - 7) : 4;
+    static const void* const kfn[5] = {
+        (const void*)u128_product_cluster_kernel<0>, (const void*)u128_product_cluster_kernel<1>,
+        (const void*)u128_product_cluster_kernel<2>, (const void*)u128_product_cluster_kernel<3>,
+        (const void*)u128_product_cluster_kernel<4>};
+    const void* fn = kfn[ls];
+    const int np = 1 << (log2n - ls);
+    const int threads = std::min(256, np);
+    const size_t smem = (8 * (size_t)np + 2 * (size_t)threads) * sizeof(double);
+    if (log2n >= 6 && log2n <= 12 && ((long)count << ls) <= (long)sm_count() / 2 &&
+        (ls <= 3 || cluster_fits(fn, threads, 1 << ls, smem))) {
       const int grid = (int)((long)count << ls);
       long stride = (long)bhat_stride;
       int ln = log2n;

@@ -150,10 +150,49 @@ cfft_status launch_kernel(const void* fn, int grid, int block, void** args, size
 // with the driver's default; the split transforms are unchanged).
 static std::atomic<int> g_cluster_policy{(int)cudaClusterSchedulingPolicyLoadBalancing};
 
+cfft_status allow_cluster16(const void* fn) {
+  static std::mutex mu;
+  static std::vector<std::pair<const void*, int>> done;
+  int dev = 0;
+  CFFT_CUDA_TRY(cudaGetDevice(&dev));
+  std::lock_guard<std::mutex> lk(mu);
+  for (const auto& e : done)
+    if (e.first == fn && e.second == dev) return CFFT_OK;
+  CFFT_CUDA_TRY(cudaFuncSetAttribute(fn, cudaFuncAttributeNonPortableClusterSizeAllowed, 1));
+  done.emplace_back(fn, dev);
+  return CFFT_OK;
+}
+
+bool cluster_fits(const void* fn, int block, int cluster, size_t smem) {
+  if (ensure_smem_attr(fn, smem) != CFFT_OK) return false;
+  if (cluster > 8 && allow_cluster16(fn) != CFFT_OK) return false;
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3((unsigned)cluster);
+  cfg.blockDim = dim3((unsigned)block);
+  cfg.dynamicSmemBytes = smem;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeClusterDimension;
+  attr[0].val.clusterDim.x = (unsigned)cluster;
+  attr[0].val.clusterDim.y = 1;
+  attr[0].val.clusterDim.z = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  int clusters = 0;
+  if (cudaOccupancyMaxActiveClusters(&clusters, fn, &cfg) != cudaSuccess) {
+    cudaGetLastError();
+    return false;
+  }
+  return clusters >= 1;
+}
+
 cfft_status launch_kernel_cluster(const void* fn, int grid, int block, int cluster, void** args, size_t smem,
                                   cudaStream_t stream, bool pdl) {
   if (!fn) return fail(CFFT_ERR_INVALID_ARGUMENT, "no kernel instantiated for this configuration");
-  if (cluster < 1 || cluster > 8 || grid % cluster != 0) return fail(CFFT_ERR_INVALID_ARGUMENT, "bad cluster shape");
+  if (cluster < 1 || cluster > 16 || grid % cluster != 0) return fail(CFFT_ERR_INVALID_ARGUMENT, "bad cluster shape");
+  if (cluster > 8) {
+    cfft_status a = allow_cluster16(fn);
+    if (a != CFFT_OK) return a;
+  }
   cfft_status st = ensure_smem_attr(fn, smem);
   if (st != CFFT_OK) return st;
   cudaLaunchConfig_t cfg = {};
@@ -245,6 +284,7 @@ size_t compute_spread(const void* fn, int grid, int block, int cluster, size_t s
   size_t padded = std::min<size_t>((size_t)per_block & ~(size_t)127, (size_t)max_block - fa.sharedSizeBytes);
   if (padded <= smem || max_blocks_per_sm(fn, block, padded) != need) return smem;
   if (cluster > 1) {  // every cluster of the grid must still be resident at once
+    if (cluster > 8 && allow_cluster16(fn) != CFFT_OK) return smem;
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = dim3((unsigned)grid);
     cfg.blockDim = dim3((unsigned)block);

@@ -61,6 +61,10 @@ int max_blocks_per_sm(const void* fn, int block, size_t smem);
 // the SMs (ceil(grid / SMs) CTAs per SM); `smem` itself when the grid takes
 // several waves, already spreads, or the padded shape would not hold it.
 size_t spread_smem(const void* fn, int grid, int block, int cluster, size_t smem);
+// Clusters of 9-16 CTAs (non-portable sizes) for fn; launch_kernel_cluster calls it.
+cfft_status allow_cluster16(const void* fn);
+// Whether one cluster of `cluster` CTAs of fn with this shape can be resident.
+bool cluster_fits(const void* fn, int block, int cluster, size_t smem);
 
 // kernel<<<grid, block, smem, stream>>>(args...) as a programmatic dependent
 // launch (the kernel calls grid_dependency_wait() before its first global access).

@@ -456,10 +456,10 @@ cfft_status cfft_server_run_alone(cfft_server* server, const cfft_serve_config* 
 /* u128: coefficients as little-endian (lo, hi) u64 pairs read as i128,
  * double-double arithmetic around fft128::Plan(N/2), floor(x + 1/2) mod 2^128.
  * 64 <= N <= 2^25: one fused kernel up to N = 8192 (a few products of
- * N = 128..2048: one thread-block cluster each); above, and for a few products
- * of N = 4096 or 8192, five launches around the plan's transform on a
- * workspace from the stream-ordered allocator (2N f64 per product, freed on
- * the stream).  bhat holds 4 arrays of N/2 f64
+ * N = 128..8192: one thread-block cluster each, of 16 CTAs at N = 4096 and
+ * 8192 where the device fits one); above, five launches around the plan's
+ * transform on a workspace from the stream-ordered allocator (2N f64 per
+ * product, freed on the stream).  bhat holds 4 arrays of N/2 f64
  * (re0, re1, im0, im1) per operand; bhat_stride is 0 or 2N (doubles). */
 typedef struct cfft_u128_product_plan cfft_u128_product_plan;
 cfft_status cfft_u128_product_plan_create(size_t N, cfft_u128_product_plan** out);

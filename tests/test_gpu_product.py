@@ -197,10 +197,11 @@ def test_u64_measure_plan(cuda, oracle):
     assert base in (512, 1024) and 0 <= int(algo) <= 7
 
 
-@pytest.mark.parametrize("N", [64, 128, 256, 512, 1024, 2048, 4096])
+@pytest.mark.parametrize("N", [64, 128, 256, 512, 1024, 2048, 4096, 8192])
 def test_u128_product_bit_exact(cuda, oracle, N):
     """A few products: the one-CTA kernel (N = 64), a cluster of 1-8 CTAs
-    (N = 128..2048), five launches (N = 4096); the oracle's bits."""
+    (N = 128..2048) or of 16 (N = 4096, 8192; five launches where such a cluster
+    does not fit); the oracle's bits."""
     import concrete_fft as cf
     torch = cuda
     count = 3

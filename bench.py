@@ -1557,7 +1557,7 @@ def run_serving(args):
 
 def measure_latency(torch, cf, local, world, cpu=True, cpu_seconds=0.5, profile_case=False):
     """One call at a time on device-resident data, device time per call (20 calls in a CUDA
-    graph): u64 products of N = 2048, 4096, 8192 (Method::Measure plans) on the automatic path
+    graph): u64 products of N = 2048 to 16384 (Method::Measure plans) on the automatic path
     (a cluster over the base's residue classes for a few products), on one CTA and as five
     launches; a u128 product of N = 1024; fft128 and unordered transforms.  Beside them the
     restated reference pipeline on one host core."""
@@ -1581,7 +1581,7 @@ def measure_latency(torch, cf, local, world, cpu=True, cpu_seconds=0.5, profile_
     rows = {}
     with ClockSampler(local) as clk:
         t0 = time.time()
-        for N in (2048, 4096, 8192):
+        for N in (2048, 4096, 8192, 16384):
             plan = cf.product.U64ProductPlan(N, measure_seconds=0.002)
             algo, base = plan.algo()
             a_np = rng.integers(0, 2 ** 64, (1, N), dtype=np.uint64)
@@ -1598,6 +1598,10 @@ def measure_latency(torch, cf, local, world, cpu=True, cpu_seconds=0.5, profile_
             row["one_cta_us"] = graph_device_us(torch, lambda: plan.product(a, bh, out))
             plan.set_cluster_size(0)
             row["five_launches_us"] = graph_device_us(torch, lambda: plan.product_unfused(a, bh, out, z))
+            if N >= 16384:  # the kernel with level-0 slices only, on 8 CTAs
+                plan.set_cluster_size(8)
+                row["level_slices_8_ctas_us"] = graph_device_us(torch, lambda: plan.product(a, bh, out))
+                plan.set_cluster_size(0)
             row["paths_agree"] = bool(torch.equal(out, ok))
             if po is not None:  # per product, over calls of 32 (the plan's set-up spread over them)
                 ca = rng.integers(0, 2 ** 64, (32, N), dtype=np.uint64)

@@ -276,23 +276,48 @@ cfft_status launch_split0_product(const cfft_u64_product_plan* plan, int ls, con
                                stream);
 }
 
+// Launch shape of u64_product_split2_kernel with 2^ls1 classes: threads per CTA
+// and shared memory (three buffers of the CTA's part of the base).
+void split2_launch_shape(const cfft_u64_product_plan* p, int ls1, int* threads, size_t* smem) {
+  const size_t part = p->base_n >> ls1;
+  const size_t radix = size_t(2) << (p->base_algo / 2);
+  *threads = (int)std::min<size_t>(256, std::max<size_t>(32, std::max(2 * part / radix, part / 2)));
+  *smem = 3 * part * sizeof(double2);
+}
+
 // The shape of u64_product_split2_kernel for a plan, as log2s: one outer level
-// of radix R0 = 2^ls0 <= 4 over a DIF base of m points, S1 = 2^ls1 classes of
-// the base with S1 <= R, R0 * S1 <= 8, at least 64 points per CTA and at least
-// 32 butterflies in each of a class's passes (as split0_log2).  Not for a
-// radix-2 base under a radix-4 level: N = 4096 on Dif2/512 measured slower than
-// the five launches from 16 products (29.7 against 24.9 us).  false when the
-// plan has another shape.
-bool split2_shape(const cfft_u64_product_plan* p, int* ls0, int* ls1) {
-  if (p->lv.nlevels != 1 || (p->base_algo & 1) || p->lv.log2r[0] > 2) return false;
+// of radix R0 = 2^ls0 <= 8 over a DIF base of m points and S1 = 2^ls1 >= 2
+// classes of the base, with S1 <= R, at least 64 points per CTA and at least 32
+// butterflies in each of a class's passes (as split0_log2).  R0 * S1 is at most
+// 16 for `count` products (or sums) of 16 CTAs that fit the SMs one CTA each, where
+// one 16-CTA cluster (a non-portable size) of that kernel fits the device; else at
+// most 8.  Not for a radix-2 base under a radix-4 level: N = 4096
+// on Dif2/512 measured slower than the five launches from 16 products (29.7
+// against 24.9 us).  false when the plan has another shape.
+bool split2_shape(const cfft_u64_product_plan* p, size_t count, int* ls0, int* ls1, bool sum = false,
+                  bool allow16 = true) {
+  if (p->lv.nlevels != 1 || (p->base_algo & 1) || p->lv.log2r[0] > 3) return false;
   const int lr = p->base_algo / 2 + 1;
   if (lr == 1 && p->lv.log2r[0] > 1) return false;
   const int log2m = ilog2(p->base_n);
-  *ls0 = p->lv.log2r[0];
-  int l1 = std::min(3 - *ls0, lr);
-  while (l1 > 0 && (log2m - l1 < 6 || log2m - l1 - lr < 5)) --l1;
-  *ls1 = l1;
-  return l1 >= 1;
+  const int l0 = p->lv.log2r[0];
+  for (int max_ls = allow16 && (count << 4) <= (size_t)sm_count() ? 4 : 3; max_ls >= 3; --max_ls) {
+    int l1 = std::min(max_ls - l0, lr);
+    while (l1 > 0 && (log2m - l1 < 6 || log2m - l1 - lr < 5)) --l1;
+    if (l1 < 1) return false;
+    const void* fn = u64_product_split2_ptr(p->base_algo, l0, l1, sum);
+    if (!fn) continue;
+    if (l0 + l1 > 3) {
+      int threads = 0;
+      size_t smem = 0;
+      split2_launch_shape(p, l1, &threads, &smem);
+      if (!cluster_fits(fn, threads, 1 << (l0 + l1), smem)) continue;
+    }
+    *ls0 = l0;
+    *ls1 = l1;
+    return true;
+  }
+  return false;
 }
 
 cfft_status launch_split2_product(const cfft_u64_product_plan* plan, int ls0, int ls1, const uint64_t* a,
@@ -302,10 +327,9 @@ cfft_status launch_split2_product(const cfft_u64_product_plan* plan, int ls0, in
   if (!fn) return fail(CFFT_ERR_INVALID_SIZE, "no one-level cluster product kernel for this shape");
   const int ls = ls0 + ls1;
   if ((count << ls) > 0x7fffffffUL) return fail(CFFT_ERR_INVALID_SIZE, "batch too large");
-  const size_t part = plan->base_n >> ls1;
-  const size_t radix = size_t(2) << (plan->base_algo / 2);
-  const int threads = (int)std::min<size_t>(256, std::max<size_t>(32, std::max(2 * part / radix, part / 2)));
-  const size_t smem = 3 * part * sizeof(double2);
+  int threads = 0;
+  size_t smem = 0;
+  split2_launch_shape(plan, ls1, &threads, &smem);
   const int grid = (int)(count << ls);
   DevLevels L = plan->dlv;
   long stride = (long)bhat_stride;
@@ -334,8 +358,10 @@ cfft_status cfft::u64_product_split_items(const cfft_u64_product_plan* plan, con
   if (plan->lv.nlevels == 0)
     return launch_split0_product(plan, split0_log2(plan), nullptr, nullptr, 0, nullptr, count, (cudaStream_t)stream,
                                  items);
+  // At most 8 CTAs per product here: the serving loop and the work queue keep several
+  // launches in flight, and a 16-CTA cluster waits for 16 free SMs of one GPC
   int ls0 = 0, ls1 = 0;
-  if (split2_shape(plan, &ls0, &ls1))
+  if (split2_shape(plan, count, &ls0, &ls1, false, false))
     return launch_split2_product(plan, ls0, ls1, nullptr, nullptr, 0, nullptr, count, (cudaStream_t)stream, items);
   const int max_ls = std::min(3, plan->lv.log2r[0]);
   return launch_split_product(plan, max_ls, nullptr, nullptr, 0, nullptr, count, (cudaStream_t)stream, items);
@@ -412,7 +438,8 @@ cfft_status cfft_u64_product_sum(const cfft_u64_product_plan* plan, const uint64
   // a few outputs of a plan with one outer level of radix 2 or 4 over a DIF base: one
   // cluster of level-0 slices times base classes per output, as the products
   int l0 = 0, l1 = 0;
-  if (count > 0 && (long)count < (long)sm_count() / 2 && plan->cluster == 0 && split2_shape(plan, &l0, &l1))
+  if (count > 0 && (long)count < (long)sm_count() / 2 && plan->cluster == 0 &&
+      split2_shape(plan, count, &l0, &l1, terms > 1))
     return launch_split2_product(plan, l0, l1, a, bhat, plan->n, out, count, (cudaStream_t)stream, nullptr,
                                  (int)terms);
   if (plan->N > (size_t(2) << kBlockLog2Auto)) {  // one output per thread-block cluster (N = 8192: by default)
@@ -554,12 +581,12 @@ cfft_status cfft_u64_product(const cfft_u64_product_plan* plan, const uint64_t* 
   const long split0_max = (plan->base_algo >= 2) ? (long)sm_count() : (long)sm_count() / 2 - 1;
   if (plan->cluster == 0 && plan->N >= 512 && (long)count <= split0_max && split0_log2(plan) >= 1)
     return launch_split0_product(plan, split0_log2(plan), a, bhat, bhat_stride, out, count, (cudaStream_t)stream);
-  // Likewise a plan with one outer level of radix 2 or 4 over a DIF base: level 0's
+  // Likewise a plan with one outer level of radix 2, 4 or 8 over a DIF base: level 0's
   // slices times classes of the base (u64_product_split2_kernel).  One product, Dif4
   // on 1024 points: 13.7 us at N = 4096 (five launches 32.1), 20.9 at 8192 (34.2);
   // 38 products: 23.3 (33.5) and 44.7 (58.8)
   int ls0 = 0, ls1 = 0;
-  if (plan->cluster == 0 && !many && split2_shape(plan, &ls0, &ls1))
+  if (plan->cluster == 0 && !many && split2_shape(plan, count, &ls0, &ls1))
     return launch_split2_product(plan, ls0, ls1, a, bhat, bhat_stride, out, count, (cudaStream_t)stream);
   // otherwise (no cluster kernel for the base) the five launches, whose transforms
   // split over 2-8 CTAs each

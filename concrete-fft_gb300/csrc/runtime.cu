@@ -150,6 +150,8 @@ cfft_status launch_kernel(const void* fn, int grid, int block, void** args, size
 // with the driver's default; the split transforms are unchanged).
 static std::atomic<int> g_cluster_policy{(int)cudaClusterSchedulingPolicyLoadBalancing};
 
+bool cluster_fits_query(const void* fn, int block, int cluster, size_t smem);
+
 cfft_status allow_cluster16(const void* fn) {
   static std::mutex mu;
   static std::vector<std::pair<const void*, int>> done;
@@ -164,6 +166,34 @@ cfft_status allow_cluster16(const void* fn) {
 }
 
 bool cluster_fits(const void* fn, int block, int cluster, size_t smem) {
+  // answers are kept per device, kernel and shape: the query costs microseconds and
+  // the launchers ask before every small-batch launch
+  struct Key {
+    const void* fn;
+    int dev, block, cluster;
+    size_t smem;
+  };
+  static std::mutex mu;
+  static std::vector<std::pair<Key, bool>> known;
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) {
+    cudaGetLastError();
+    return false;
+  }
+  {
+    std::lock_guard<std::mutex> lk(mu);
+    for (const auto& e : known)
+      if (e.first.fn == fn && e.first.dev == dev && e.first.block == block && e.first.cluster == cluster &&
+          e.first.smem == smem)
+        return e.second;
+  }
+  const bool fits = cluster_fits_query(fn, block, cluster, smem);
+  std::lock_guard<std::mutex> lk(mu);
+  known.push_back({Key{fn, dev, block, cluster, smem}, fits});
+  return fits;
+}
+
+bool cluster_fits_query(const void* fn, int block, int cluster, size_t smem) {
   if (ensure_smem_attr(fn, smem) != CFFT_OK) return false;
   if (cluster > 8 && allow_cluster16(fn) != CFFT_OK) return false;
   cudaLaunchConfig_t cfg = {};

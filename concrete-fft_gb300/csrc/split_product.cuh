@@ -628,10 +628,13 @@ const void* split2_product_ptr_t(int ls0, int ls1) {
   } else {
     constexpr int LRA = Log2<AlgoInfo<A>::R>::v;
     if (ls0 == 1 && ls1 == 1) return (const void*)u64_product_split2_kernel<A, 1, 1, SUM>;
+    if (ls0 == 2 && ls1 == 1) return (const void*)u64_product_split2_kernel<A, 2, 1, SUM>;
     if constexpr (LRA >= 2) {
       if (ls0 == 1 && ls1 == 2) return (const void*)u64_product_split2_kernel<A, 1, 2, SUM>;
+      // 16-CTA clusters
+      if (ls0 == 2 && ls1 == 2) return (const void*)u64_product_split2_kernel<A, 2, 2, SUM>;
+      if (ls0 == 3 && ls1 == 1) return (const void*)u64_product_split2_kernel<A, 3, 1, SUM>;
     }
-    if (ls0 == 2 && ls1 == 1) return (const void*)u64_product_split2_kernel<A, 2, 1, SUM>;
     return nullptr;
   }
 }

@@ -343,11 +343,12 @@ def test_u64_product_no_level_clusters_up_to_one_per_sm(cuda):
         assert torch.equal(out0, out1), count
 
 
-@pytest.mark.parametrize("N,base", [(4096, 1024), (8192, 1024), (4096, 512), (2048, 512)])
+@pytest.mark.parametrize("N,base", [(4096, 1024), (8192, 1024), (4096, 512), (2048, 512), (16384, 1024)])
 def test_u64_product_one_level_clusters_bit_exact(cuda, oracle, N, base):
-    """A few products of a plan with one outer level (radix 2 or 4) run on a cluster of
-    level-0 slices times classes of the base (DIF bases; DIT bases take another path):
-    the oracle's bits, and the same bits on one CTA per product."""
+    """A few products of a plan with one outer level (radix 2, 4 or 8) run on a cluster
+    of level-0 slices times classes of the base, 16 CTAs where such a cluster fits
+    (DIF bases; DIT bases take another path): the oracle's bits, and the same bits on
+    one CTA per product."""
     import concrete_fft as cf
     torch = cuda
     count = 3
@@ -418,11 +419,12 @@ def test_u128_product_host_pipeline(cuda, oracle):
                                                (8192, 3, 1024, 2), (16384, 2, 1024, 3), (32768, 6, 1024, 2),
                                                (1 << 18, 2, 1024, 3), (2048, 6, 1024, 4), (2048, 0, 1024, 2),
                                                (2048, 3, 1024, 3), (512, 2, 256, 2), (4096, 2, 1024, 3),
-                                               (8192, 4, 1024, 2), (4096, 0, 1024, 2), (8192, 6, 1024, 2)])
+                                               (8192, 4, 1024, 2), (4096, 0, 1024, 2), (8192, 6, 1024, 2),
+                                               (16384, 4, 1024, 2), (16384, 6, 1024, 2), (8192, 2, 1024, 3)])
 def test_u64_product_sum_bit_exact(cuda, oracle, N, algo, base, terms):
     """Fourier-domain accumulation of `terms` products, one inverse per group (4 groups:
     a cluster per group for plans on a DIF base without an outer level or with one of
-    radix 2 or 4)."""
+    radix 2, 4 or 8)."""
     import concrete_fft as cf
     torch = cuda
     count = 4

@@ -233,8 +233,9 @@ cfft_status build_plan(C64Plan& p, size_t n, size_t base_n, int algo, bool unord
 // every SM work, or as the plan forces.  Only plans whose transform fits one
 // CTA whole (d0 == 0).  S is bounded by the radix of the step that is split
 // (the base radix without outer levels, level 0's radix with them) and by 8;
-// with one outer level of radix 2 or 4 over a DIF base, by level 0's radix
-// times the base classes (mode 2 for radix 2, 3 for radix 4).
+// with one outer level of radix 2, 4 or 8 over a DIF base, by level 0's radix
+// times the base classes (modes 2, 3 and 4), up to 16 CTAs for a batch whose
+// CTAs fit the SMs one each, where one 16-CTA cluster fits the device.
 int split_log2(const C64Plan& p, long batch, int* mode) {
   if (p.cluster == 1) return 0;
   const int log2n = p.lv.log2n[0];
@@ -250,18 +251,30 @@ int split_log2(const C64Plan& p, long batch, int* mode) {
     min_ls = std::max(0, log2n - kSmemLog2Max);
   }
   if (log2n < 6 || max_ls < 1 || min_ls > max_ls) return 0;
-  // one outer level of radix 2 or 4 over a DIF base: level 0's slices times
-  // S1 = 2^ls1 classes of the base (c64_split2_kernel, modes 2 and 3), with at
+  // one outer level of radix 2, 4 or 8 over a DIF base: level 0's slices times
+  // S1 = 2^ls1 classes of the base (c64_split2_kernel, modes 2, 3 and 4), with at
   // least 64 points per CTA and 32 butterflies per class pass, and not a radix-2
   // base under a radix-4 level
   int ls1 = 0;
   const int ls0 = p.lv.nlevels == 1 ? p.lv.log2r[0] : 0;
-  if (p.lv.nlevels == 1 && ls0 <= 2 && !(p.base_algo & 1) && min_ls == 0) {
+  // (a part is at most half the base, so it fits one CTA at every size)
+  if (p.lv.nlevels == 1 && ls0 <= 3 && !(p.base_algo & 1)) {
     const int lr = ilog2((size_t)algo_radix(p.base_algo));
     const int log2m = p.lv.log2n[1];
     if (!(lr == 1 && ls0 > 1)) {
-      ls1 = std::min(3 - ls0, lr);
-      while (ls1 > 0 && (log2m - ls1 < 6 || log2m - ls1 - lr < 5)) --ls1;
+      for (int max_total = p.cluster == 0 && (batch << 4) <= (long)sm_count() ? 4 : 3; max_total >= 3; --max_total) {
+        ls1 = std::max(0, std::min(max_total - ls0, lr));
+        while (ls1 > 0 && (log2m - ls1 < 6 || log2m - ls1 - lr < 5)) --ls1;
+        if (ls1 < 1 || ls0 + ls1 <= 3) break;
+        // 16 CTAs: both directions' kernels must fit one cluster of that size
+        const size_t part = p.n >> (ls0 + ls1);
+        const int threads = (int)std::min<size_t>(256, std::max<size_t>(32, 2 * part / (size_t)(1 << lr)));
+        const size_t smem = 2 * part * sizeof(double2);
+        const void* f = c64_split_kernel_ptr(p.base_algo, true, ls0 + ls1, 1 + ls0);
+        const void* i = c64_split_kernel_ptr(p.base_algo, false, ls0 + ls1, 1 + ls0);
+        if (f && i && cluster_fits(f, threads, 16, smem) && cluster_fits(i, threads, 16, smem)) break;
+        ls1 = 0;
+      }
     }
   }
   const long target = 4L * sm_count();

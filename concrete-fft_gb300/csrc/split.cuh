@@ -458,8 +458,8 @@ const void* split_ptr_ls(bool fwd, int mode) {
   }
   return fwd ? (const void*)c64_split_kernel<A, true, LS, 1> : (const void*)c64_split_kernel<A, false, LS, 1>;
 }
-// Mode 2 (R0 = 2) and 3 (R0 = 4): c64_split2_kernel with S1 = 2^ls / R0, for DIF
-// bases with S1 <= R and R0 * S1 <= 8.
+// Mode 2 (R0 = 2), 3 (R0 = 4) and 4 (R0 = 8): c64_split2_kernel with S1 = 2^ls / R0,
+// for DIF bases with S1 <= R and R0 * S1 <= 8, or 16 (4 x 4 and 8 x 2).
 template <int A, int LS0>
 const void* split2_ptr(bool fwd, int ls) {
   if constexpr (AlgoInfo<A>::DIT) {
@@ -467,10 +467,15 @@ const void* split2_ptr(bool fwd, int ls) {
   } else {
     constexpr int LRA = Log2<AlgoInfo<A>::R>::v;
     const int ls1 = ls - LS0;
-    if (ls1 == 1) return fwd ? (const void*)c64_split2_kernel<A, true, LS0, 1> : (const void*)c64_split2_kernel<A, false, LS0, 1>;
-    if constexpr (LS0 == 1 && LRA >= 2) {
+    if constexpr (LS0 == 3 && LRA < 2) {
+      return nullptr;
+    } else {
+      if (ls1 == 1)
+        return fwd ? (const void*)c64_split2_kernel<A, true, LS0, 1> : (const void*)c64_split2_kernel<A, false, LS0, 1>;
+    }
+    if constexpr (LS0 <= 2 && LRA >= 2) {
       if (ls1 == 2)
-        return fwd ? (const void*)c64_split2_kernel<A, true, 1, 2> : (const void*)c64_split2_kernel<A, false, 1, 2>;
+        return fwd ? (const void*)c64_split2_kernel<A, true, LS0, 2> : (const void*)c64_split2_kernel<A, false, LS0, 2>;
     }
     return nullptr;
   }
@@ -479,6 +484,7 @@ template <int A>
 const void* split_ptr(bool fwd, int ls, int mode) {
   if (mode == 2) return split2_ptr<A, 1>(fwd, ls);
   if (mode == 3) return split2_ptr<A, 2>(fwd, ls);
+  if (mode == 4) return split2_ptr<A, 3>(fwd, ls);
   switch (ls) {
     case 1: return split_ptr_ls<A, 1>(fwd, mode);
     case 2: return split_ptr_ls<A, 2>(fwd, mode);

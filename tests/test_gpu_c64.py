@@ -250,11 +250,11 @@ def test_cluster_sizes_bit_exact(cuda, oracle, ctas):
             plan.inv(d)
             want = oracle.ordered_inv(algo, want)
             assert np.array_equal(bits(d.cpu().numpy()), bits(want)), (algo, n, ctas)
-    # with one outer level of radix 2 or 4 over a DIF base, clusters of up to 8 CTAs
-    # take level 0's slices times the base's classes
+    # with one outer level of radix 2, 4 or 8 over a DIF base, clusters of up to 16 CTAs
+    # (automatic, for a small batch) take level 0's slices times the base's classes
     for n, base in [(256, 32), (1024, 64), (2048, 1024), (2048, 512), (4096, 1024), (4096, 512), (8192, 1024),
                     (16384, 512), (32768, 1024)]:
-        for algo in ((0, 2, 4, 6, 7) if n in (2048, 4096) else (2, 7)):
+        for algo in ((0, 2, 4, 6, 7) if n in (2048, 4096, 8192) else (2, 7)):
             plan = cf.unordered.Plan(n, cf.unordered.Method.UserProvided(algo, base))
             plan.set_cluster_size(ctas)
             x = rand_c64(2, n)

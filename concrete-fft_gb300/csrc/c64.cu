@@ -266,13 +266,13 @@ int split_log2(const C64Plan& p, long batch, int* mode) {
         ls1 = std::max(0, std::min(max_total - ls0, lr));
         while (ls1 > 0 && (log2m - ls1 < 6 || log2m - ls1 - lr < 5)) --ls1;
         if (ls1 < 1 || ls0 + ls1 <= 3) break;
-        // 16 CTAs: both directions' kernels must fit one cluster of that size
+        // 16 CTAs: every transform's cluster resident at once, one CTA per SM, in
+        // both directions (with one cluster more than fit, some SMs run two CTAs)
         const size_t part = p.n >> (ls0 + ls1);
         const int threads = (int)std::min<size_t>(256, std::max<size_t>(32, 2 * part / (size_t)(1 << lr)));
-        const size_t smem = 2 * part * sizeof(double2);
         const void* f = c64_split_kernel_ptr(p.base_algo, true, ls0 + ls1, 1 + ls0);
         const void* i = c64_split_kernel_ptr(p.base_algo, false, ls0 + ls1, 1 + ls0);
-        if (f && i && cluster_fits(f, threads, 16, smem) && cluster_fits(i, threads, 16, smem)) break;
+        if (f && i && batch <= spread_clusters(f, threads, 16) && batch <= spread_clusters(i, threads, 16)) break;
         ls1 = 0;
       }
     }
@@ -336,10 +336,36 @@ cfft_status launch_split(const C64Plan& p, bool fwd, int ls, int mode, long nsub
 
 cfft_status launch_level(bool fwd, double2* data, long total, int log2r, int log2nl, const double2* wl, int nsm,
                          cudaStream_t stream) {
-  const int grid = (int)std::min<long>((total + 255) / 256, (long)nsm * 16);
+  // fewer butterflies than 256 per SM: smaller CTAs, so that the level's FP64 work
+  // spreads over the SMs (one forward of 16384 points on Dif8/512, a radix-8 level
+  // in global memory, then 8 sub-transforms on clusters: 15.2 us with 256-thread
+  // level CTAs, 12.3 us with 32-thread ones)
+  int threads = 256;
+  while (threads > 32 && (total + threads - 1) / threads < nsm) threads >>= 1;
+  const int grid = (int)std::min<long>((total + threads - 1) / threads, (long)nsm * 16);
   void* args[] = {&data, &total, &log2r, &log2nl, (void*)&wl};
   const void* fn = fwd ? (const void*)c64_level_kernel<true> : (const void*)c64_level_kernel<false>;
-  return launch_kernel(fn, grid, 256, args, 0, stream, true);
+  return launch_kernel(fn, grid, threads, args, 0, stream, true);
+}
+
+// The plan of the sub-transforms from level e on (levels e..L-1 over the same
+// base), on the same device tables: after levels 0..e-1 every block of 2^log2n[e]
+// consecutive points is one such transform.
+C64Plan sub_plan(const C64Plan& p, int e) {
+  C64Plan s = p;
+  s.n = size_t(1) << p.lv.log2n[e];
+  s.lv.nlevels = p.lv.nlevels - e;
+  for (int i = 0; i <= kMaxLevels; ++i) {
+    s.lv.log2n[i] = i + e <= kMaxLevels ? p.lv.log2n[i + e] : 0;
+    s.lv.w_off[i] = i + e <= kMaxLevels ? p.lv.w_off[i + e] : 0;
+  }
+  for (int i = 0; i < kMaxLevels; ++i) {
+    s.lv.log2r[i] = i + e < kMaxLevels ? p.lv.log2r[i + e] : 0;
+    s.lv.winv_off[i] = i + e < kMaxLevels ? p.lv.winv_off[i + e] : 0;
+  }
+  s.dlv = to_dev(s.lv);
+  s.d0 = 0;
+  return s;
 }
 
 cfft_status run_plan(const C64Plan& plan, double* buf, size_t batch, bool fwd, cudaStream_t stream,
@@ -353,6 +379,53 @@ cfft_status run_plan(const C64Plan& plan, double* buf, size_t batch, bool fwd, c
   const int ls = allow_split ? split_log2(plan, (long)batch, &mode) : 0;
   if (ls > 0) return launch_split(plan, fwd, ls, mode, (long)batch, stream, data);
   const int nsm = sm_count();
+  // Two or more levels over a DIF base and a small batch: the levels above the last
+  // in global memory over all SMs, then every sub-transform (the last level over the
+  // base) on a cluster, of its level-0 slices times the base's classes
+  // (c64_split2_kernel) or of its slices, as split_log2 gives it (the levels take
+  // small CTAs, spread over the SMs: launch_level)
+  if (allow_split && plan.cluster == 0 && !plan.block_set && plan.lv.nlevels >= 2 && !(plan.base_algo & 1)) {
+    int e = plan.lv.nlevels - 1;
+    long nsub = (long)batch << (log2n - plan.lv.log2n[e]);
+    C64Plan sub = sub_plan(plan, e);
+    int smode = 0;
+    int sls = split_log2(sub, nsub, &smode);
+    {
+      // or every level in global memory and the bases on clusters of their classes,
+      // where that runs on more CTAs (one transform, fwd: 32768 points on Dif4/1024
+      // 11.8 us against 13.3, 65536 points 16.1 against 20.9; 16384 points on
+      // Dif8/512, 64 CTAs either way: 12.2 us with the sub-transforms' clusters,
+      // 12.9 with the bases')
+      const int eb = plan.lv.nlevels;
+      const long nb = (long)batch << (log2n - plan.lv.log2n[eb]);
+      const C64Plan bsub = sub_plan(plan, eb);
+      int bmode = 0;
+      const int bls = split_log2(bsub, nb, &bmode);
+      if (bls > 0 && (sls == 0 || (nb << bls) > (nsub << sls))) {
+        e = eb;
+        nsub = nb;
+        sub = bsub;
+        smode = bmode;
+        sls = bls;
+      }
+    }
+    if (sls > 0) {
+      if (!fwd) {
+        cfft_status st = launch_split(sub, false, sls, smode, nsub, stream, data);
+        if (st != CFFT_OK) return st;
+      }
+      for (int k = 0; k < e; ++k) {
+        const int l = fwd ? k : e - 1 - k;
+        cfft_status st = launch_level(fwd, data, ((long)batch << log2n) >> plan.lv.log2r[l], plan.lv.log2r[l],
+                                      plan.lv.log2n[l],
+                                      fwd ? plan.d_w + plan.lv.w_off[l] : plan.d_winv + plan.lv.winv_off[l], nsm,
+                                      stream);
+        if (st != CFFT_OK) return st;
+      }
+      if (fwd) return launch_split(sub, true, sls, smode, nsub, stream, data);
+      return CFFT_OK;
+    }
+  }
   // A plan with levels in global memory and a batch whose blocks would cover
   // fewer than half the SMs takes smaller blocks for this call (one more level
   // in global memory, blocks of at least 512 points): one transform of 16384

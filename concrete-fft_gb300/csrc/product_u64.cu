@@ -289,9 +289,8 @@ void split2_launch_shape(const cfft_u64_product_plan* p, int ls1, int* threads, 
 // of radix R0 = 2^ls0 <= 8 over a DIF base of m points and S1 = 2^ls1 >= 2
 // classes of the base, with S1 <= R, at least 64 points per CTA and at least 32
 // butterflies in each of a class's passes (as split0_log2).  R0 * S1 is at most
-// 16 for `count` products (or sums) of 16 CTAs that fit the SMs one CTA each, where
-// one 16-CTA cluster (a non-portable size) of that kernel fits the device; else at
-// most 8.  Not for a radix-2 base under a radix-4 level: N = 4096
+// 16 where the `count` products' (or sums') 16-CTA clusters (a non-portable size)
+// are resident at once with one CTA per SM; else at most 8.  Not for a radix-2 base under a radix-4 level: N = 4096
 // on Dif2/512 measured slower than the five launches from 16 products (29.7
 // against 24.9 us).  false when the plan has another shape.
 bool split2_shape(const cfft_u64_product_plan* p, size_t count, int* ls0, int* ls1, bool sum = false,
@@ -307,11 +306,11 @@ bool split2_shape(const cfft_u64_product_plan* p, size_t count, int* ls0, int* l
     if (l1 < 1) return false;
     const void* fn = u64_product_split2_ptr(p->base_algo, l0, l1, sum);
     if (!fn) continue;
-    if (l0 + l1 > 3) {
+    if (l0 + l1 > 3) {  // every product's 16-CTA cluster resident at once, one CTA per SM
       int threads = 0;
       size_t smem = 0;
       split2_launch_shape(p, l1, &threads, &smem);
-      if (!cluster_fits(fn, threads, 1 << (l0 + l1), smem)) continue;
+      if ((long)count > (long)spread_clusters(fn, threads, 16)) continue;
     }
     *ls0 = l0;
     *ls1 = l1;

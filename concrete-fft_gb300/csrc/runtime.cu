@@ -150,7 +150,7 @@ cfft_status launch_kernel(const void* fn, int grid, int block, void** args, size
 // with the driver's default; the split transforms are unchanged).
 static std::atomic<int> g_cluster_policy{(int)cudaClusterSchedulingPolicyLoadBalancing};
 
-bool cluster_fits_query(const void* fn, int block, int cluster, size_t smem);
+int cluster_count_query(const void* fn, int block, int cluster, size_t smem);
 
 cfft_status allow_cluster16(const void* fn) {
   static std::mutex mu;
@@ -165,7 +165,7 @@ cfft_status allow_cluster16(const void* fn) {
   return CFFT_OK;
 }
 
-bool cluster_fits(const void* fn, int block, int cluster, size_t smem) {
+int cluster_count(const void* fn, int block, int cluster, size_t smem) {
   // answers are kept per device, kernel and shape: the query costs microseconds and
   // the launchers ask before every small-batch launch
   struct Key {
@@ -174,11 +174,11 @@ bool cluster_fits(const void* fn, int block, int cluster, size_t smem) {
     size_t smem;
   };
   static std::mutex mu;
-  static std::vector<std::pair<Key, bool>> known;
+  static std::vector<std::pair<Key, int>> known;
   int dev = 0;
   if (cudaGetDevice(&dev) != cudaSuccess) {
     cudaGetLastError();
-    return false;
+    return 0;
   }
   {
     std::lock_guard<std::mutex> lk(mu);
@@ -187,15 +187,31 @@ bool cluster_fits(const void* fn, int block, int cluster, size_t smem) {
           e.first.smem == smem)
         return e.second;
   }
-  const bool fits = cluster_fits_query(fn, block, cluster, smem);
+  const int count = cluster_count_query(fn, block, cluster, smem);
   std::lock_guard<std::mutex> lk(mu);
-  known.push_back({Key{fn, dev, block, cluster, smem}, fits});
-  return fits;
+  known.push_back({Key{fn, dev, block, cluster, smem}, count});
+  return count;
 }
 
-bool cluster_fits_query(const void* fn, int block, int cluster, size_t smem) {
-  if (ensure_smem_attr(fn, smem) != CFFT_OK) return false;
-  if (cluster > 8 && allow_cluster16(fn) != CFFT_OK) return false;
+bool cluster_fits(const void* fn, int block, int cluster, size_t smem) {
+  return cluster_count(fn, block, cluster, smem) >= 1;
+}
+
+int spread_clusters(const void* fn, int block, int cluster) {
+  int dev = 0, max_block = 0;
+  cudaFuncAttributes fa{};
+  if (cudaGetDevice(&dev) != cudaSuccess ||
+      cudaDeviceGetAttribute(&max_block, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev) != cudaSuccess ||
+      cudaFuncGetAttributes(&fa, fn) != cudaSuccess || (size_t)max_block <= fa.sharedSizeBytes) {
+    cudaGetLastError();
+    return 0;
+  }
+  return cluster_count(fn, block, cluster, (size_t)max_block - fa.sharedSizeBytes);
+}
+
+int cluster_count_query(const void* fn, int block, int cluster, size_t smem) {
+  if (ensure_smem_attr(fn, smem) != CFFT_OK) return 0;
+  if (cluster > 8 && allow_cluster16(fn) != CFFT_OK) return 0;
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = dim3((unsigned)cluster);
   cfg.blockDim = dim3((unsigned)block);
@@ -210,9 +226,9 @@ bool cluster_fits_query(const void* fn, int block, int cluster, size_t smem) {
   int clusters = 0;
   if (cudaOccupancyMaxActiveClusters(&clusters, fn, &cfg) != cudaSuccess) {
     cudaGetLastError();
-    return false;
+    return 0;
   }
-  return clusters >= 1;
+  return clusters;
 }
 
 cfft_status launch_kernel_cluster(const void* fn, int grid, int block, int cluster, void** args, size_t smem,

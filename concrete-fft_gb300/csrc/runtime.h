@@ -63,8 +63,15 @@ int max_blocks_per_sm(const void* fn, int block, size_t smem);
 size_t spread_smem(const void* fn, int grid, int block, int cluster, size_t smem);
 // Clusters of 9-16 CTAs (non-portable sizes) for fn; launch_kernel_cluster calls it.
 cfft_status allow_cluster16(const void* fn);
+// Clusters of `cluster` CTAs of fn with this shape resident at once
+// (cudaOccupancyMaxActiveClusters, kept per device, kernel and shape).
+int cluster_count(const void* fn, int block, int cluster, size_t smem);
 // Whether one cluster of `cluster` CTAs of fn with this shape can be resident.
 bool cluster_fits(const void* fn, int block, int cluster, size_t smem);
+// Clusters of `cluster` CTAs of fn resident at once with one CTA per SM (dynamic
+// shared memory padded to the per-block limit).  A 16-CTA cluster needs 16 SMs of
+// one GPC: a 152-SM GB300 holds 7 such clusters, and 15 of 8 CTAs.
+int spread_clusters(const void* fn, int block, int cluster);
 
 // kernel<<<grid, block, smem, stream>>>(args...) as a programmatic dependent
 // launch (the kernel calls grid_dependency_wait() before its first global access).

@@ -267,6 +267,26 @@ def test_cluster_sizes_bit_exact(cuda, oracle, ctas):
             assert np.array_equal(bits(d.cpu().numpy()), bits(want)), (n, base, algo, ctas)
 
 
+@pytest.mark.parametrize("n,base", [(16384, 1024), (16384, 512), (32768, 1024), (65536, 1024), (1 << 17, 1024)])
+def test_levels_then_clusters_bit_exact(cuda, oracle, n, base):
+    """A few transforms with two or more outer levels over a DIF base: the levels above
+    the last in global memory, then every sub-transform on a cluster of level-0 slices
+    times base classes.  Bits equal the oracle's, in both directions."""
+    import concrete_fft as cf
+    torch = cuda
+    for algo in (0, 2, 4, 6):
+        plan = cf.unordered.Plan(n, cf.unordered.Method.UserProvided(algo, base))
+        for batch in (1, 3):
+            x = rand_c64(batch, n)
+            d = on_gpu(torch, x)
+            plan.fwd(d)
+            want = oracle.unordered_fwd(algo, base, x, nthreads=0)
+            assert np.array_equal(bits(d.cpu().numpy()), bits(want)), (n, base, algo, batch)
+            plan.inv(d)
+            want = oracle.unordered_inv(algo, base, want, nthreads=0)
+            assert np.array_equal(bits(d.cpu().numpy()), bits(want)), (n, base, algo, batch)
+
+
 @pytest.mark.parametrize("batch", [1, 256])
 def test_plan_calls_capture_into_a_cuda_graph(cuda, oracle, batch):
     """fwd and inv enqueue only kernels on the caller's stream, so a caller can capture

@@ -445,7 +445,9 @@ cfft_status cfft_u64_product_sum(const cfft_u64_product_plan* plan, const uint64
     bool ok = true;
     const int ls = product_split_log2(plan, count, &ok);
     if (count == 0) return CFFT_OK;
-    if (!ok) return product_sum_unfused(plan, a, bhat, terms, out, count, (cudaStream_t)stream);
+    // from N = 32768 the unfused sum, as the products take five launches there
+    if (!ok || (plan->N >= 32768 && plan->cluster == 0))
+      return product_sum_unfused(plan, a, bhat, terms, out, count, (cudaStream_t)stream);
     if (ls > 0)
       return launch_split_product(plan, ls, a, bhat, plan->n, out, count, (cudaStream_t)stream, nullptr,
                                   (int)terms);
@@ -563,8 +565,10 @@ cfft_status cfft_u64_product(const cfft_u64_product_plan* plan, const uint64_t* 
   const int ls = product_split_log2(plan, count, &ok);
   if (count == 0) return CFFT_OK;
   // The five-launch path on a workspace from the stream-ordered allocator: N > 65536
-  // (no cluster holds it), and large batches of N >= 32768, where it measured faster
-  // than one cluster per product (304 vs 280 k products/s at 32768, 129 vs 102 k at 65536)
+  // (no cluster holds it), and N >= 32768 at every batch, where it measured faster
+  // than one cluster per product (Dif8/512, CUDA events: one product 30.5 vs 74.4 us
+  // at 32768, 35.8 vs 142 at 65536; 38 products 134 vs 212 and 274 vs 423; large
+  // batches 304 vs 280 k products/s at 32768, 129 vs 102 k at 65536)
   const bool many = (long)count >= (long)sm_count() / 2 && plan->cluster == 0;
   // A few products whose transform has no outer level (n = base_n): one cluster per
   // product on the base's residue classes (u64_product_split0_kernel), as does a plan
@@ -594,7 +598,7 @@ cfft_status cfft_u64_product(const cfft_u64_product_plan* plan, const uint64_t* 
   // 4096, 37 vs 39 us at 8192; from SMs/4 products of N = 8192 the cluster kernel is faster)
   const bool few_mid = plan->cluster == 0 && plan->N >= 4096 && plan->N <= 8192 &&
                        (long)count < (long)sm_count() / 4;
-  if (!ok || (plan->N >= 32768 && many) || few_unsplit || few_mid) {
+  if (!ok || (plan->N >= 32768 && plan->cluster == 0) || few_unsplit || few_mid) {
     cudaStream_t s = (cudaStream_t)stream;
     void* z = nullptr;
     if (cudaMallocAsync(&z, count * plan->n * sizeof(double2), s) != cudaSuccess)

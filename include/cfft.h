@@ -247,9 +247,10 @@ cfft_status cfft_f128_sincospi(double x_hi, double x_lo, double* sin_out2, doubl
  *
  * u64: coefficients are read as i64, rounded with floor(x + 1/2) and reduced
  * mod 2^64.  N a power of two, 64 <= N <= 2^29: one CTA per product up to
- * N = 8192, a thread-block cluster of 2..8 CTAs per product up to 65536 (and
- * for small batches, see cfft_u64_product_set_cluster_size), and above 65536
- * the five-launch path on a workspace from the stream-ordered allocator.  bhat
+ * N = 8192, a thread-block cluster of 2..16 CTAs per product up to 16384 (and
+ * for small batches, see cfft_u64_product_set_cluster_size), and from 32768
+ * the five-launch path on a workspace from the stream-ordered allocator (a
+ * forced cluster size keeps clusters up to 65536).  bhat
  * holds N/2 c64 per operand in the plan's permuted order; `bhat_stride` is 0
  * (one operand shared by all products) or N/2 (one operand per product). */
 typedef struct cfft_u64_product_plan cfft_u64_product_plan;
@@ -288,10 +289,11 @@ cfft_status cfft_u64_product_host(const cfft_u64_product_plan* plan, const uint6
  * in term order, then one inverse per group instead of one per term.
  * a: count * terms * N u64; bhat: count * terms * N/2 c64; out: count * N u64.
  * N <= 2^29: one output per CTA up to 8192 (fewer than SMs/2 outputs of a plan
- * on a DIF base without an outer level or with one of radix 2 or 4: one
+ * on a DIF base without an outer level or with one of radix 2, 4 or 8: one
  * thread-block cluster each), per
- * thread-block cluster up to 65536, and above that the unfused steps on a
- * stream-ordered workspace of at most 1 GiB (groups in chunks). */
+ * thread-block cluster up to 16384 (65536 with a forced cluster size), and
+ * from 32768 the unfused steps on a stream-ordered workspace of at most 1 GiB
+ * (groups in chunks). */
 cfft_status cfft_u64_product_sum(const cfft_u64_product_plan* plan, const uint64_t* a, const double* bhat,
                                  size_t terms, uint64_t* out, size_t count, void* stream);
 

@@ -1559,7 +1559,7 @@ def measure_latency(torch, cf, local, world, cpu=True, cpu_seconds=0.5, profile_
     """One call at a time on device-resident data, device time per call (20 calls in a CUDA
     graph): u64 products of N = 2048 to 65536 (Method::Measure plans) on the automatic path
     (a cluster over the base's residue classes for a few products), on one CTA and as five
-    launches; a u128 product of N = 1024; fft128 and unordered transforms.  Beside them the
+    launches; u128 products of N = 1024 and 8192; fft128 and unordered transforms.  Beside them the
     restated reference pipeline on one host core."""
     import numpy as np
     po = _oracle() if cpu and world == 1 else None
@@ -1634,21 +1634,22 @@ def measure_latency(torch, cf, local, world, cpu=True, cpu_seconds=0.5, profile_
                 row["cpu_one_core_us"] = el / (16 * reps) * 1e6
             rows["external_product_N%d_2x4" % N] = {k: (round(v, 2) if isinstance(v, float) else v)
                                                     for k, v in row.items()}
-        # u128 product N = 1024
-        p128 = cf.product.U128ProductPlan(1024)
-        a_np = rng.integers(0, 2 ** 64, (1, 1024, 2), dtype=np.uint64)
-        b_np = rng.integers(-2 ** 15, 2 ** 15, (1, 1024))
-        a = torch.from_numpy(a_np.view(np.int64)).cuda()
-        bh = torch.empty((1, 4, 512), dtype=torch.float64, device="cuda")
-        p128.prepare_operand(torch.from_numpy(b_np).cuda(), bh)
-        out = torch.empty_like(a)
-        row = {"auto_us": round(graph_device_us(torch, lambda: p128.product(a, bh, out)), 2)}
-        if po is not None:
-            ca = rng.integers(0, 2 ** 64, (8, 1024, 2), dtype=np.uint64)
-            wb = po.u128_prepare(1024, rng.integers(-2 ** 15, 2 ** 15, (8, 1024)))
-            reps, el = cpu_loop(lambda: po.u128_product(1024, ca, wb, nthreads=1), cpu_seconds)
-            row["cpu_one_core_us"] = round(el / (8 * reps) * 1e6, 2)
-        rows["u128_product_N1024"] = row
+        # u128 products N = 1024 and 8192
+        for N in (1024, 8192):
+            p128 = cf.product.U128ProductPlan(N)
+            a_np = rng.integers(0, 2 ** 64, (1, N, 2), dtype=np.uint64)
+            b_np = rng.integers(-2 ** 15, 2 ** 15, (1, N))
+            a = torch.from_numpy(a_np.view(np.int64)).cuda()
+            bh = torch.empty((1, 4, N // 2), dtype=torch.float64, device="cuda")
+            p128.prepare_operand(torch.from_numpy(b_np).cuda(), bh)
+            out = torch.empty_like(a)
+            row = {"auto_us": round(graph_device_us(torch, lambda: p128.product(a, bh, out)), 2)}
+            if po is not None:
+                ca = rng.integers(0, 2 ** 64, (8, N, 2), dtype=np.uint64)
+                wb = po.u128_prepare(N, rng.integers(-2 ** 15, 2 ** 15, (8, N)))
+                reps, el = cpu_loop(lambda: po.u128_product(N, ca, wb, nthreads=1), cpu_seconds)
+                row["cpu_one_core_us"] = round(el / (8 * reps) * 1e6, 2)
+            rows["u128_product_N%d" % N] = row
         clk.mark(t0, time.time())
     return {"rows": rows, "clocks": clk.summary(),
             "gpu": "device time per call: 20 calls captured in a CUDA graph, replayed 10 times, CUDA events",

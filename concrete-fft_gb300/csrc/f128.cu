@@ -204,6 +204,70 @@ __global__ void __launch_bounds__(256) f128_stage_kernel(F128Arrays g, int log2n
   }
 }
 
+// Small batches: one stage over every transform of the batch in global memory with
+// two warps per 32 butterflies (real and imaginary halves, f128_half_stage), 32
+// butterflies per 64-thread CTA, so that a stage of a few thousand butterflies
+// keeps twice as many SM sub-partitions' FP64 pipes busy as one thread per
+// butterfly.  The butterflies and twiddles of f128_stage_kernel; total < 2^31
+// points in the batch.
+template <bool FWD>
+__global__ void __launch_bounds__(64) f128_half_stage_kernel(F128Arrays g, int log2n, int log2t, long total,
+                                                             F128Tw tw) {
+  __shared__ double xs[128];  // the inverse's differences: 4 doubles per butterfly
+  const long m = 1L << (log2n - 1 - log2t);
+  const long first = (long)blockIdx.x * 32;
+  const int nb = (int)(total - first < 32 ? total - first : 32);
+  grid_dependency_wait();
+  f128_half_stage<FWD>(g, xs, nb, [&](int b, int& qa, int& qb, long& widx) {
+    const long gb = first + b;
+    const long tr = gb >> (log2n - 1);               // transform index
+    const long bb = gb & ((1L << (log2n - 1)) - 1);  // butterfly within transform
+    const long i = bb >> log2t;
+    const long j = (tr << log2n) + (i << (log2t + 1)) + (bb & ((1L << log2t) - 1));
+    qa = (int)j;
+    qb = (int)(j + (1L << log2t));
+    widx = m + i;
+  }, tw, threadIdx.x, 64);
+}
+
+// Small batches: the stages of one sub-block of 2^log2c points (log2c <= 8) per CTA
+// in shared memory, two warps per 32 butterflies (f128_half_stage); the
+// butterflies and twiddles of f128_stages_smem.  2^log2c threads per CTA.
+template <bool FWD>
+__global__ void __launch_bounds__(256) f128_smem_half_kernel(F128Arrays g, int log2n, int log2c, F128Tw tw) {
+  __shared__ double sm[4 * 256 + 2 * 256];
+  const int c = 1 << log2c;
+  const F128Arrays s{sm, sm + c, sm + 2 * c, sm + 3 * c};
+  double* xs = sm + 4 * c;
+  const int tid = threadIdx.x, nth = blockDim.x;
+  const long off = (long)blockIdx.x << log2c;
+  const long sb = (long)blockIdx.x & ((1L << (log2n - log2c)) - 1);  // sub-block inside its transform
+  grid_dependency_wait();
+  for (int i = tid; i < c; i += nth) {
+    s.re0[i] = g.re0[off + i];
+    s.re1[i] = g.re1[off + i];
+    s.im0[i] = g.im0[off + i];
+    s.im1[i] = g.im1[off + i];
+  }
+  __syncthreads();
+  for (int st = 0; st < log2c; ++st) {
+    const int log2t = FWD ? (log2c - 1 - st) : st;
+    const long m = 1L << (log2n - 1 - log2t);
+    f128_half_stage<FWD>(s, xs, c >> 1, [&](int b, int& qa, int& qb, long& widx) {
+      const int il = b >> log2t;
+      qa = (il << (log2t + 1)) + (b & ((1 << log2t) - 1));
+      qb = qa + (1 << log2t);
+      widx = m + (sb << (log2c - 1 - log2t)) + il;
+    }, tw, tid, nth);
+  }
+  for (int i = tid; i < c; i += nth) {
+    g.re0[off + i] = s.re0[i];
+    g.re1[off + i] = s.re1[i];
+    g.im0[off + i] = s.im0[i];
+    g.im1[off + i] = s.im1[i];
+  }
+}
+
 // One u128 coefficient (lo, hi, read as i128) -> f128: hi = the nearest double, lo =
 // the nearest double to the remainder (src/fft128/mod.rs:2006-2016 pattern).
 __device__ __forceinline__ void u128_to_f128(uint64_t lo, uint64_t hi, double& xh, double& xl) {
@@ -525,14 +589,14 @@ cfft_status run_f128_tw(size_t n, const F128Tw& tw, double* re0, double* re1, do
   cfft_status ast = f128_attrs();
   if (ast != CFFT_OK) return ast;
   const int log2n = ilog2(n);
-  // a small batch of 64..4096 points: one transform per cluster, two warps per 32
+  // a small batch of 64..2048 points: one transform per cluster, two warps per 32
   // butterflies, every CTA on an SM of its own: up to 8 CTAs of 128 points up to 1024
-  // points, 16 CTAs (a non-portable cluster size, when such a cluster fits) at 2048 and
-  // 4096.  fwd+inv, one transform: 24.9 us at 64 points (one CTA, a thread per
+  // points, 16 CTAs (a non-portable cluster size, when such a cluster fits) at 2048.  fwd+inv, one transform: 24.9 us at 64 points (one CTA, a thread per
   // butterfly: 43.6), 42.1 at 512 (75.8), 46.7 at 1024 (85.2), 51.7 at 2048 (93.6 over
-  // global stages), 102.6 at 4096 (104.4; 197 on a cluster of 8).  From SMs/2 CTAs on
-  // the block path is as fast
-  if (!one_kernel && block_log2 == 0 && log2n >= 6 && log2n <= 12) {
+  // global stages).  From SMs/2 CTAs on the block path is as fast.  4096 points take
+  // the half-butterfly stages below (one forward 51.9 us on a 16-CTA cluster, whose 16
+  // SMs' FP64 pipes bind it)
+  if (!one_kernel && block_log2 == 0 && log2n >= 6 && log2n <= 11) {
     const int ls = log2n <= 10 ? std::max(0, log2n - 7) : 4;
     static const void* const kfn[2][5] = {
         {(const void*)f128_cluster_kernel<false, 0>, (const void*)f128_cluster_kernel<false, 1>,
@@ -553,6 +617,38 @@ cfft_status run_f128_tw(size_t n, const F128Tw& tw, double* re0, double* re1, do
       void* args[] = {&g, &ln, &t};
       return launch_kernel_cluster(fn, grid, threads, 1 << ls, args, spread_smem(fn, grid, threads, 1 << ls, smem),
                                    stream, true);
+    }
+  }
+  // a small batch of larger transforms (or more transforms than the cluster rule above
+  // takes): every stage above 128- or 256-point blocks in global memory, then the
+  // blocks in shared memory, one per CTA, all with two warps per 32 butterflies
+  // (f128_half_stage_kernel, f128_smem_half_kernel), at most one block per SM
+  if (!one_kernel && block_log2 == 0 && log2n >= 8 && ((long)batch << log2n) < (1L << 31)) {
+    int log2c = 7;
+    while (log2c < 8 && ((long)batch << (log2n - log2c)) > (long)sm_count()) ++log2c;
+    if (((long)batch << (log2n - log2c)) <= (long)sm_count()) {
+      F128Arrays g{re0, re1, im0, im1};
+      F128Tw t = tw;
+      int ln = log2n, lc = log2c;
+      long total = (long)batch << (log2n - 1);
+      const int sgrid = (int)((total + 31) / 32);
+      const int bgrid = (int)((long)batch << (log2n - log2c));
+      const void* sfn = fwd ? (const void*)f128_half_stage_kernel<true> : (const void*)f128_half_stage_kernel<false>;
+      const void* bfn = fwd ? (const void*)f128_smem_half_kernel<true> : (const void*)f128_smem_half_kernel<false>;
+      auto stage = [&](int lt) {
+        void* args[] = {&g, &ln, &lt, &total, &t};
+        return launch_kernel(sfn, sgrid, 64, args, 0, stream, true);
+      };
+      void* bargs[] = {&g, &ln, &lc, &t};
+      cfft_status st = CFFT_OK;
+      if (fwd) {
+        for (int lt = log2n - 1; lt >= log2c && st == CFFT_OK; --lt) st = stage(lt);
+        if (st == CFFT_OK) st = launch_kernel(bfn, bgrid, 1 << log2c, bargs, 0, stream, true);
+      } else {
+        st = launch_kernel(bfn, bgrid, 1 << log2c, bargs, 0, stream, true);
+        for (int lt = log2c; lt <= log2n - 1 && st == CFFT_OK; ++lt) st = stage(lt);
+      }
+      return st;
     }
   }
   int log2c = std::min(log2n, block_log2 > 0 ? block_log2 : kF128SmemLog2);
@@ -873,9 +969,10 @@ cfft_status cfft_u128_product(const cfft_u128_product_plan* p, const uint64_t* a
     return fail(CFFT_ERR_INVALID_ARGUMENT, "bhat_stride must be 0 or 2N");
   if (count == 0) return CFFT_OK;
   const bool few = (long)count < (long)sm_count() / 2;
-  // A few products of N = 128..8192: one product per cluster of up to 8 CTAs of 128
-  // points, 16 CTAs at N = 4096 and 8192 (u128_product_cluster_kernel), two warps
-  // per 32 butterflies
+  // A few products of N = 128..4096: one product per cluster of up to 8 CTAs of 128
+  // points, 16 CTAs at N = 4096 (u128_product_cluster_kernel), two warps per 32
+  // butterflies.  N = 8192 takes the five launches, whose transforms run the
+  // half-butterfly stages over more SMs
   {
     const int log2n = ilog2(p->f.n);
     const int ls = log2n <= 10 ? std::max(0, log2n - 7) : 4;
@@ -887,7 +984,7 @@ cfft_status cfft_u128_product(const cfft_u128_product_plan* p, const uint64_t* a
     const int np = 1 << (log2n - ls);
     const int threads = std::min(256, np);
     const size_t smem = (8 * (size_t)np + 2 * (size_t)threads) * sizeof(double);
-    if (log2n >= 6 && log2n <= 12 && ((long)count << ls) <= (long)sm_count() / 2 &&
+    if (log2n >= 6 && log2n <= 11 && ((long)count << ls) <= (long)sm_count() / 2 &&
         (ls <= 3 || cluster_fits(fn, threads, 1 << ls, smem))) {
       const int grid = (int)((long)count << ls);
       long stride = (long)bhat_stride;

@@ -8,7 +8,7 @@ pytestmark = pytest.mark.gpu
 RNG = np.random.default_rng(11)
 
 
-@pytest.mark.parametrize("n", [32, 64, 128, 256, 512, 1024, 2048, 4096, 8192, 32768, 1 << 20])
+@pytest.mark.parametrize("n", [32, 64, 128, 256, 512, 1024, 2048, 4096, 8192, 16384, 32768, 1 << 20])
 def test_f128_fwd_inv_bit_exact(cuda, oracle, n):
     import concrete_fft as cf
     torch = cuda

@@ -1565,7 +1565,8 @@ def measure_latency(torch, cf, local, world, cpu=True, cpu_seconds=0.5, profile_
     po = _oracle() if cpu and world == 1 else None
     rng = np.random.default_rng(21)
     if profile_case:
-        # ncu case: 20 lone products of N = 2048 (Dif4, base 1024) and 20 fft128 forwards of 512
+        # ncu case: 20 lone products of N = 2048 (Dif4, base 1024) and 20 fft128 forwards of 512,
+        # then 20 fft128 forwards of 16384
         plan = cf.product.U64ProductPlan(2048, cf.FftAlgo.Dif4, 1024)
         a = torch.from_numpy(rng.integers(0, 2 ** 64, (1, 2048), dtype=np.uint64).view(np.int64)).cuda()
         bh = torch.empty((1, 1024), dtype=torch.complex128, device="cuda")
@@ -1576,8 +1577,14 @@ def measure_latency(torch, cf, local, world, cpu=True, cpu_seconds=0.5, profile_
         for _ in range(20):
             plan.product(a, bh, out)
             fp.fwd(*arrs)
+        # then 20 fft128 forwards of 16384 points, batch 1 (half-butterfly stages and blocks)
+        fb = cf.fft128.Plan(16384)
+        big = [torch.rand((1, 16384), dtype=torch.float64, device="cuda") for _ in range(4)]
+        for _ in range(20):
+            fb.fwd(*big)
         torch.cuda.synchronize()
-        return {"profile_case": "20 lone u64 products N=2048 (Dif4/1024) and 20 fft128 forwards n=512"}
+        return {"profile_case": "20 lone u64 products N=2048 (Dif4/1024) and 20 fft128 forwards n=512, "
+                                "then 20 fft128 forwards n=16384"}
     rows = {}
     with ClockSampler(local) as clk:
         t0 = time.time()

@@ -198,15 +198,33 @@ bool cluster_fits(const void* fn, int block, int cluster, size_t smem) {
 }
 
 int spread_clusters(const void* fn, int block, int cluster) {
-  int dev = 0, max_block = 0;
-  cudaFuncAttributes fa{};
-  if (cudaGetDevice(&dev) != cudaSuccess ||
-      cudaDeviceGetAttribute(&max_block, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev) != cudaSuccess ||
-      cudaFuncGetAttributes(&fa, fn) != cudaSuccess || (size_t)max_block <= fa.sharedSizeBytes) {
+  // the padded size per device and kernel (the attribute queries are driver calls)
+  static std::mutex mu;
+  static std::vector<std::pair<std::pair<const void*, int>, size_t>> padded;
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) {
     cudaGetLastError();
     return 0;
   }
-  return cluster_count(fn, block, cluster, (size_t)max_block - fa.sharedSizeBytes);
+  size_t smem = 0;
+  {
+    std::lock_guard<std::mutex> lk(mu);
+    for (const auto& e : padded)
+      if (e.first.first == fn && e.first.second == dev) smem = e.second;
+  }
+  if (smem == 0) {
+    int max_block = 0;
+    cudaFuncAttributes fa{};
+    if (cudaDeviceGetAttribute(&max_block, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev) != cudaSuccess ||
+        cudaFuncGetAttributes(&fa, fn) != cudaSuccess || (size_t)max_block <= fa.sharedSizeBytes) {
+      cudaGetLastError();
+      return 0;
+    }
+    smem = (size_t)max_block - fa.sharedSizeBytes;
+    std::lock_guard<std::mutex> lk(mu);
+    padded.push_back({{fn, dev}, smem});
+  }
+  return cluster_count(fn, block, cluster, smem);
 }
 
 int cluster_count_query(const void* fn, int block, int cluster, size_t smem) {

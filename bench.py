@@ -1276,7 +1276,9 @@ def measure_serving(torch, cf, local, world, rate=20000.0, seconds=1.0, operand_
     t0 = time.perf_counter()
     srv = cf.serving.Server(eng, SERVE_SIZES, operand_bytes=operand_gb << 30, seed=seed)
     setup_s = time.perf_counter() - t0
-    srv.run(srv.config(rate=rate, duration_s=0.5))  # warm-up: a process's first runs show a longer tail
+    # warm-up as long as the timed run: a process's first runs show a longer tail, and the
+    # timed run's results then land in output-ring pages the device has written before
+    srv.run(srv.config(rate=rate, duration_s=seconds))
     cfg = srv.config(rate=rate, duration_s=seconds)
     with ClockSampler(local, interval_ms=1000) as clk:
         time.sleep(0.5)  # the sampler's start-up (a process on the host) stays out of the timed run

@@ -401,7 +401,7 @@ cfft_status run_plan(const C64Plan& plan, double* buf, size_t batch, bool fwd, c
       const C64Plan bsub = sub_plan(plan, eb);
       int bmode = 0;
       const int bls = split_log2(bsub, nb, &bmode);
-      if (bls > 0 && (sls == 0 || (nb << bls) > (nsub << sls))) {
+      if (bls > 0 && (nb << bls) <= 2L * nsm && (sls == 0 || (nb << bls) > (nsub << sls))) {
         e = eb;
         nsub = nb;
         sub = bsub;
@@ -409,7 +409,8 @@ cfft_status run_plan(const C64Plan& plan, double* buf, size_t batch, bool fwd, c
         sls = bls;
       }
     }
-    if (sls > 0) {
+    // up to 2 CTAs per SM (one wave); larger batches keep the block path below
+    if (sls > 0 && (nsub << sls) <= 2L * nsm) {
       if (!fwd) {
         cfft_status st = launch_split(sub, false, sls, smode, nsub, stream, data);
         if (st != CFFT_OK) return st;

@@ -401,7 +401,8 @@ cfft_status run_plan(const C64Plan& plan, double* buf, size_t batch, bool fwd, c
       const C64Plan bsub = sub_plan(plan, eb);
       int bmode = 0;
       const int bls = split_log2(bsub, nb, &bmode);
-      if (bls > 0 && (nb << bls) <= 2L * nsm && (sls == 0 || (nb << bls) > (nsub << sls))) {
+      const bool sub_ok = sls > 0 && (nsub << sls) <= 2L * nsm;
+      if (bls > 0 && (nb << bls) <= 2L * nsm && (!sub_ok || (nb << bls) > (nsub << sls))) {
         e = eb;
         nsub = nb;
         sub = bsub;
